@@ -1,0 +1,142 @@
+"""ctypes wrapper around ``oracle/sr_oracle.c``, the CPU restatement of the
+reference's expression-fitting path.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
+bench.py's CPU-baseline leg, never by the package.  The shared library is built
+by :func:`build` (gcc, OpenMP, ``-ffp-contract=off``) into ``oracle/``.
+
+All arrays use the reference's user-facing layouts: X (N,nx), Ops (B,M),
+Ch (B,M,2), C (B,M), cache (B,M,N), Y (B,N).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "sr_oracle.c")
+LIB = os.path.join(HERE, "libsr_oracle.so")
+
+ERR_MESSAGES = {
+    101: "Validation failed: A child's index is greater than or equal to its parent's.",
+    102: "Validation failed: Operator arity does not match the number of children.",
+    201: "Backward pass error: A non-zero gradient was passed to a NO_OP node.",
+    204: "Backward pass error: Gradient for a/b where b = 0.",
+}
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library (no-op when it is up to date)."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-std=gnu11", SRC, "-o", LIB + ".tmp", "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        i64, vp, dbl = ctypes.c_int64, ctypes.c_void_p, ctypes.c_double
+        L.sro_validate.argtypes = [vp, vp, i64, i64, i64, i64, i64, i64]
+        L.sro_validate.restype = ctypes.c_int
+        for suf in ("f32", "f64"):
+            f = getattr(L, "sro_eval_fwd_" + suf)
+            f.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp]
+            f.restype = None
+            g = getattr(L, "sro_eval_bwd_" + suf)
+            g.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, vp]
+            g.restype = ctypes.c_int
+        L.sro_optimize_f32.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, i64, ctypes.c_int, ctypes.c_int,
+                                       dbl, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
+        L.sro_optimize_f32.restype = ctypes.c_int
+        L.sro_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def validate(ops, ch) -> int:
+    ops = _c(ops, np.int64)
+    ch = _c(ch, np.int64)
+    B, M = ops.shape
+    return lib().sro_validate(_p(ops), _p(ch), B, M, M, 1, 2 * M, 2)
+
+
+def eval_fwd(X, ops, ch, C, dtype=np.float32):
+    """Node values (B,M,N) of every tape at every point."""
+    X = _c(X, dtype)
+    ops = _c(ops, np.int64)
+    ch = _c(ch, np.int64)
+    C = _c(C, dtype)
+    N, nx = X.shape
+    B, M = ops.shape
+    out = np.empty((B, M, N), dtype=dtype)
+    fn = lib().sro_eval_fwd_f32 if dtype == np.float32 else lib().sro_eval_fwd_f64
+    fn(_p(X), N, nx, _p(ops), _p(ch), _p(C), B, M, _p(out))
+    return out
+
+
+def eval_bwd(X, ops, ch, C, gout, dtype=np.float32, want_gx=True):
+    """Adjoint sweep for a dense (B,M,N) output gradient -> (gC (B,M), gX (N,nx), err)."""
+    X = _c(X, dtype)
+    ops = _c(ops, np.int64)
+    ch = _c(ch, np.int64)
+    C = _c(C, dtype)
+    gout = _c(gout, dtype)
+    N, nx = X.shape
+    B, M = ops.shape
+    gC = np.zeros((B, M), dtype=dtype)
+    gX = np.zeros((N, nx), dtype=dtype) if want_gx else None
+    fn = lib().sro_eval_bwd_f32 if dtype == np.float32 else lib().sro_eval_bwd_f64
+    err = fn(_p(X), N, nx, _p(ops), _p(ch), _p(C), B, M, _p(gout), _p(gC), _p(gX))
+    return gC, gX, err
+
+
+def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_grad=1e-7,
+             line_search_fn="strong_wolfe", line_search_max_iter=10, dot_mode=1):
+    """Per-problem restatement of ``symbolic_torch.optimize``.
+
+    dot_mode=0 follows the reference's float32 arithmetic; dot_mode=1 follows the
+    fused kernel's (double dots and two-loop scalars).
+    Returns dict(C, Y, iters, evals, loss, err).  Y=None selects the raw
+    objective (mean of the root value) used by the Rosenbrock test.
+    """
+    X = _c(X, np.float32)
+    ops = _c(ops, np.int64)
+    ch = _c(ch, np.int64)
+    C_init = _c(C_init, np.float32)
+    Yc = None if Y is None else _c(Y, np.float32)
+    N, nx = X.shape
+    B, M = ops.shape
+    C = np.empty((B, M), np.float32)
+    Yo = np.empty((B, N), np.float32)
+    iters = np.empty(B, np.int32)
+    evals = np.empty(B, np.int64)
+    loss = np.empty(B, np.float32)
+    ls = {"strong_wolfe": 0, "backtracking": 1}[line_search_fn]
+    err = lib().sro_optimize_f32(_p(X), N, nx, _p(Yc), _p(ops), _p(ch), _p(C_init), B, M,
+                                 int(max_iter), int(history_size), float(tolerance_grad), ls,
+                                 int(line_search_max_iter), int(dot_mode),
+                                 _p(C), _p(Yo), _p(iters), _p(evals), _p(loss))
+    return dict(C=C, Y=Yo, iters=iters, evals=evals, loss=loss, err=err)
+
+
+def num_threads() -> int:
+    return lib().sro_num_threads()

@@ -1,0 +1,284 @@
+"""Writes the golden fixtures in tests/golden/ by running the reference itself.
+
+Run in the development container, where the reference checkout exists:
+
+    python tests/golden/make_golden.py
+
+The reference extension is compiled from its own sources by
+``oracle/build_ref.py`` into ``oracle/_ref`` and imported as ``symbolic_torch``.
+Every fixture stores its inputs next to the reference's outputs, so the tests
+can replay them on a machine without the reference.  Inputs are seeded.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, ROOT)
+
+import build_ref  # noqa: E402
+
+from cudasymbolicregression_gb300 import tapes  # noqa: E402
+from cudasymbolicregression_gb300.operators import BINARY_OPS, UNARY_OPS, Operator  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+ALL_UNARY = UNARY_OPS
+ALL_BINARY = BINARY_OPS
+
+
+def ref_eval(st, X, ops, ch, C, gout=None):
+    """Reference forward (B,M,N) and, with gout, gradients w.r.t. C and X."""
+    Xt = torch.tensor(X, requires_grad=True)
+    Ct = torch.tensor(C, requires_grad=True)
+    out = st.evaluation.evaluate(Xt, torch.tensor(ops), torch.tensor(ch), Ct)
+    cache = out.detach().numpy().copy()
+    if gout is None:
+        return cache, None, None
+    out.backward(torch.tensor(gout))
+    return cache, Ct.grad.numpy().copy(), Xt.grad.numpy().copy()
+
+
+def edge_inputs():
+    """X rows that hit every domain policy (zero, +-1, negatives, large, tiny)."""
+    vals = np.array([-3.0, -2.0, -1.0, -0.5, -1e-30, 0.0, 1e-30, 0.5, 1.0, 2.0, 3.0, 40.0, 100.0,
+                     -100.0, 0.25, 7.5], np.float32)
+    a = np.repeat(vals, len(vals))
+    b = np.tile(vals, len(vals))
+    return np.stack([a, b], 1).astype(np.float32)
+
+
+def case_single_ops(st, rng):
+    """Every unary/binary operator applied to X0 (and X1) at the edge inputs."""
+    X = edge_inputs()
+    ops_list = list(ALL_UNARY) + list(ALL_BINARY)
+    B, M = len(ops_list), 3
+    ops = np.zeros((B, M), np.int64)
+    ch = np.full((B, M, 2), -1, np.int64)
+    for b, op in enumerate(ops_list):
+        ops[b, 0] = int(Operator.VAR_START_ID)
+        ops[b, 1] = int(Operator.VAR_START_ID) + 1
+        ops[b, 2] = op
+        ch[b, 2, 0] = 0
+        if op in ALL_BINARY:
+            ch[b, 2, 1] = 1
+    C = np.zeros((B, M), np.float32)
+    cache, _, _ = ref_eval(st, X, ops, ch, C)
+    # gradient through the root only; the reference raises 204 for a/0 with g != 0,
+    # so the DIV row gets zero gradient where its denominator is 0.
+    gout = np.zeros_like(cache)
+    gout[:, 2, :] = rng.standard_normal((B, X.shape[0])).astype(np.float32)
+    div_row = ops_list.index(int(Operator.DIV))
+    gout[div_row, 2, X[:, 1] == 0] = 0.0
+    _, gC, gX = ref_eval(st, X, ops, ch, C, gout)
+    # per-row X gradients: run each row alone so gX is not summed over the batch
+    gX_rows = np.zeros((B,) + X.shape, np.float32)
+    for b in range(B):
+        _, _, gx = ref_eval(st, X, ops[b:b + 1], ch[b:b + 1], C[b:b + 1], gout[b:b + 1])
+        gX_rows[b] = gx
+    np.savez_compressed(os.path.join(OUT, "single_ops.npz"), X=X, ops=ops, ch=ch, C=C, cache=cache,
+                        gout=gout, gC=gC, gX=gX, gX_rows=gX_rows)
+
+
+def case_random_dags(st, rng, name, B, M, N, n_vars, seed, unary, binary, mean_length, dense=True):
+    X = rng.uniform(-3, 3, (N, n_vars)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    tb = tapes.generate(B, M, seed=seed, mean_length=mean_length, n_vars=n_vars, unary=unary,
+                        binary=binary, p_const_leaf=0.3)
+    ops, ch = tb.ops, tb.ch
+    # sprinkle a few hard constants so CONST_1..E are covered
+    consts = np.array([2, 3, 4, 5, 6, 7, 8], np.int64)
+    hard = (ops == int(Operator.LEARNABLE_CONSTANT)) & (rng.random(ops.shape) < 0.25)
+    ops[hard] = consts[rng.integers(0, len(consts), size=int(hard.sum()))]
+    cache, _, _ = ref_eval(st, X, ops, ch, C)
+    if dense:
+        gout = rng.standard_normal(cache.shape).astype(np.float32)
+    else:
+        gout = np.zeros_like(cache)
+        root = np.maximum((ops != 0).sum(1) - 1, 0)
+        gout[np.arange(B), root, :] = rng.standard_normal((B, N)).astype(np.float32)
+    gout[np.isnan(cache)] = 0.0
+    # drop gradients that would reach a zero denominator (the reference raises 204)
+    for _ in range(4):
+        try:
+            _, gC, gX = ref_eval(st, X, ops, ch, C, gout)
+            break
+        except RuntimeError:
+            # zero the gradient of tapes that contain a DIV with a zero denominator
+            zero_den = np.zeros(B, bool)
+            for b in range(B):
+                for k in range(M):
+                    if ops[b, k] == int(Operator.DIV) and (cache[b, ch[b, k, 1]] == 0).any():
+                        zero_den[b] = True
+            gout[zero_den] = 0.0
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), X=X, ops=ops, ch=ch, C=C, cache=cache,
+                        gout=gout, gC=gC, gX=gX)
+
+
+def case_errors(st):
+    """Validation / backward error messages, as the reference raises them."""
+    rows = []
+    VAR = int(Operator.VAR_START_ID)
+    X = np.ones((3, 2), np.float32)
+    # child index >= parent
+    rows.append(("child_geq", [[VAR, int(Operator.ADD)]], [[[-1, -1], [0, 2]]], "fwd"))
+    # unary with no child / binary with one child / leaf with a child
+    rows.append(("unary_nochild", [[int(Operator.SIN)]], [[[-1, -1]]], "fwd"))
+    rows.append(("binary_onechild", [[VAR, int(Operator.MUL)]], [[[-1, -1], [0, -1]]], "fwd"))
+    rows.append(("leaf_child", [[VAR, VAR]], [[[-1, -1], [0, -1]]], "fwd"))
+    # backward: grad on NO_OP, and 1/0
+    rows.append(("noop_grad", [[0]], [[[-1, -1]]], "bwd"))
+    rows.append(("div_zero", [[int(Operator.CONST_1), VAR, int(Operator.DIV)]],
+                 [[[-1, -1], [-1, -1], [0, 1]]], "bwd_x0zero"))
+    out = {}
+    for name, ops, ch, kind in rows:
+        ops = np.array(ops, np.int64)
+        ch = np.array(ch, np.int64)
+        C = np.zeros(ops.shape, np.float32)
+        Xc = X.copy()
+        if kind == "bwd_x0zero":
+            Xc[:, 0] = 0.0
+        msg = ""
+        try:
+            cache, _, _ = ref_eval(st, Xc, ops, ch, C)
+            if kind.startswith("bwd"):
+                gout = np.zeros_like(cache)
+                gout[:, -1, :] = 1.0
+                ref_eval(st, Xc, ops, ch, C, gout)
+        except RuntimeError as e:
+            msg = str(e).splitlines()[0]
+        out[name + "__ops"] = ops
+        out[name + "__ch"] = ch
+        out[name + "__X"] = Xc
+        out[name + "__msg"] = np.array(msg)
+    np.savez_compressed(os.path.join(OUT, "errors.npz"), **out)
+
+
+def case_optimize_linear(st):
+    """tests/test_optimization.py:10-80 known answer: y = c1*X0 + c2."""
+    torch.manual_seed(1234)
+    B, N, M = 2, 100, 5
+    X = torch.randn(N, 1)
+    c1 = torch.tensor([2.5, -1.5]).view(B, 1)
+    c2 = torch.tensor([0.5, 3.0]).view(B, 1)
+    Y = c1 * X[:, 0].T + c2
+    Ops = torch.full((B, M), 0, dtype=torch.int64)
+    Ops[:, 0] = int(Operator.VAR_START_ID)
+    Ops[:, 1] = 1
+    Ops[:, 2] = int(Operator.MUL)
+    Ops[:, 3] = 1
+    Ops[:, 4] = int(Operator.ADD)
+    Ch = torch.full((B, M, 2), -1, dtype=torch.int64)
+    Ch[:, 2, 0] = 0
+    Ch[:, 2, 1] = 1
+    Ch[:, 4, 0] = 2
+    Ch[:, 4, 1] = 3
+    C = st.create_constants(Ops, method="randn", mean=0.0, std=1.0)
+    Cf, Yf = st.optimize(X, Y, Ops, Ch, C)
+    np.savez_compressed(os.path.join(OUT, "optimize_linear.npz"), X=X.numpy(), Y=Y.numpy(), ops=Ops.numpy(),
+                        ch=Ch.numpy(), C=C.numpy(), C_final=Cf.numpy(), Y_final=Yf.numpy())
+
+
+README_GRAMMAR = """E -> E + T [0.4]
+E -> T [0.6]
+T -> F * T [0.4]
+T -> F [0.6]
+F -> R ( V ) [0.3]
+F -> V [0.7]
+R -> sin [0.5]
+R -> cos [0.5]
+V -> X_0 [0.5]
+V -> C [0.5]
+"""
+
+
+def case_optimize_readme(st, B=128, max_iter=100):
+    """The README grammar workload (plain method, small): PCFG-sampled postfix
+    tapes, X = 2 randn, Y = 2.5 cos(X0) - 1.5, randn constants."""
+    torch.manual_seed(0)
+    pcfg = st.ProbabilisticContextFreeGrammar(README_GRAMMAR, "E", 32, 1, torch.device("cpu"))
+    infix = pcfg.sample_infix(B)
+    ops = pcfg.infix_to_postfix(infix)
+    ch = pcfg.get_postfix_children(ops)
+    X = 2 * torch.randn(100, 1)
+    Y = (2.5 * torch.cos(X[:, 0]) - 1.5).unsqueeze(0).repeat(B, 1)
+    C = st.create_constants(ops)
+    Cf, Yf = st.optimize(X, Y, ops, ch, C, max_iter=max_iter, tolerance_grad=1e-7,
+                         line_search_fn="strong_wolfe")
+    infix_out = pcfg.postfix_to_infix(ops, 64)
+    np.savez_compressed(os.path.join(OUT, "optimize_readme.npz"), X=X.numpy(), Y=Y.numpy(), ops=ops.numpy(),
+                        ch=ch.numpy(), C=C.numpy(), C_final=Cf.numpy(), Y_final=Yf.numpy(),
+                        infix=infix.numpy(), infix_from_postfix=infix_out.numpy(),
+                        max_iter=np.array(max_iter))
+
+
+def case_optimize_ragged(st, B=96, N=64, M=32, max_iter=40, line_search="strong_wolfe", name="optimize_ragged"):
+    """Ragged tapes (lengths 3..M, 0..8 constants, 2 variables), noisy hidden targets."""
+    rng = np.random.default_rng(77)
+    X = rng.uniform(-3, 3, (N, 2)).astype(np.float32)
+    lengths = rng.integers(3, M + 1, size=B)
+    kc = rng.integers(0, 9, size=B)
+    Cs = rng.standard_normal((B, M)).astype(np.float32)
+    tb = tapes.generate(B, M, seed=5, lengths=lengths, const_counts=kc, n_vars=2, X_screen=X, C_screen=Cs)
+    hid = tapes.generate(B, M, seed=6, lengths=rng.integers(3, 16, size=B), const_counts=rng.integers(0, 4, size=B),
+                         n_vars=2, X_screen=X, C_screen=Cs)
+    Ch_hidden = rng.standard_normal((B, M)).astype(np.float32)
+    yh, _, _ = ref_eval(st, X, hid.ops, hid.ch, Ch_hidden)
+    root = np.maximum((hid.ops != 0).sum(1) - 1, 0)
+    Y = yh[np.arange(B), root] + 0.01 * rng.standard_normal((B, N)).astype(np.float32)
+    Y = np.where(np.isfinite(Y), Y, 0.0).astype(np.float32)
+    C = Cs.copy()
+    Cf, Yf = st.optimize(torch.tensor(X), torch.tensor(Y), torch.tensor(tb.ops), torch.tensor(tb.ch),
+                         torch.tensor(C), max_iter=max_iter, line_search_fn=line_search)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), X=X, Y=Y, ops=tb.ops, ch=tb.ch, C=C,
+                        C_final=Cf.numpy(), Y_final=Yf.numpy(), max_iter=np.array(max_iter))
+
+
+def case_rosenbrock(st):
+    """tests/test_lbfgs_batch.py:38-75: batched Rosenbrock from fixed starts."""
+    from symbolic_torch.lbfgs_batch import LBFGS_batch
+    torch.manual_seed(7)
+    x0 = torch.randn(2, 10)
+    res = {}
+    for ls in ("strong_wolfe", "backtracking"):
+        x = x0.clone().requires_grad_(True)
+        opt = LBFGS_batch([x], max_iter=250, history_size=15, tolerance_grad=1e-7, line_search_fn=ls)
+
+        def closure():
+            opt.zero_grad(set_to_none=True)
+            f = (1.0 - x[0]) ** 2 + 100.0 * (x[1] - x[0] ** 2) ** 2
+            f.sum().backward()
+            return f
+
+        opt.step(closure)
+        res[ls] = x.detach().numpy().copy()
+    np.savez_compressed(os.path.join(OUT, "rosenbrock.npz"), x0=x0.numpy(), x_wolfe=res["strong_wolfe"],
+                        x_backtracking=res["backtracking"])
+
+
+def main():
+    st = build_ref.load_reference()
+    torch.set_num_threads(1)
+    rng = np.random.default_rng(2024)
+    case_single_ops(st, rng)
+    case_random_dags(st, rng, "random_dags", B=160, M=24, N=37, n_vars=3, seed=11,
+                     unary=ALL_UNARY, binary=ALL_BINARY, mean_length=10)
+    case_random_dags(st, rng, "random_default_ops", B=128, M=64, N=70, n_vars=4, seed=12,
+                     unary=tapes.UN_DEFAULT, binary=tapes.BIN_DEFAULT, mean_length=20, dense=False)
+    case_errors(st)
+    case_optimize_linear(st)
+    case_optimize_readme(st)
+    case_optimize_ragged(st)
+    case_optimize_ragged(st, B=48, max_iter=30, line_search="backtracking", name="optimize_ragged_bt")
+    case_rosenbrock(st)
+    for f in sorted(os.listdir(OUT)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(OUT, f)))
+
+
+if __name__ == "__main__":
+    main()
