@@ -1,0 +1,791 @@
+// sr_fit.cu -- fused batched L-BFGS fit of the learnable constants.
+//
+// One persistent kernel.  Each warp takes one problem (one tape, one target row)
+// from a work queue and runs the complete optimisation for it on chip:
+//
+//   closure(x)  forward sweep over the tape for all N points (lanes over points,
+//               node values in shared memory), residuals against Y, then the
+//               reverse (adjoint) sweep; the gradient of every constant is summed
+//               per lane in double and reduced in a fixed order, so results are
+//               bit-reproducible run to run.
+//   direction   two-loop recursion over the last `history_size` (s, y) pairs held in
+//               the warp's slice of the workspace; dots, rho, alpha, beta, gamma in
+//               double, vectors in float (one slot per lane).
+//   line search strong Wolfe (bracket + bisection zoom) or Armijo backtracking, with
+//               the reference's acceptance rules and float32 scalar arithmetic.
+//
+// Per problem the control flow is exactly the reference's LBFGS_batch column
+// (symbolic_torch/lbfgs_batch.py:61-326) as driven by optimize()
+// (symbolic_torch/optimization.py:51-112).  Every problem of the reference batch
+// evolves independently, so the batch-wide early exits of the reference only
+// change how much work is done, not the result.  Points the reference evaluates
+// twice (phi(0) at the start of each line search and zoom, phi(alpha_lo) at the
+// start of a zoom, and the closure after the update when the accepted step was
+// already evaluated) are reused here; they are bit-identical because the kernel is
+// deterministic.  A problem whose gradient norm drops below tolerance_grad is
+// retired at once (the reference keeps computing its unused search direction).
+//
+// Parameter slots.  The reference optimises all M slots of C but zeroes the
+// gradient of every slot that is not a learnable constant; such slots can only
+// ever change by picking up NaN through 0*NaN in the vector updates.  Here the
+// learnable constants up to the root are the real slots and one extra "virtual"
+// slot (gradient always 0) stands for all the others, reproducing that NaN
+// propagation through the dots; at the end they are written back as C_init, or as
+// NaN when the virtual slot was poisoned.
+#include <cstdint>
+
+#include "sr_common.cuh"
+#include "sr_ops.cuh"
+
+namespace sr {
+
+__host__ __device__ __forceinline__ size_t fit_align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+struct FitArgs {
+  const float* X;
+  int64_t N, n_x;
+  const float* Y;
+  const uint32_t* desc;
+  const int32_t* meta;
+  int64_t B, M;
+  const float* C_init;
+  float* C_out;
+  int64_t c_sb, c_sm;
+  float* Y_final;
+  int32_t* iters_out;
+  float* loss_out;
+  int32_t* evals_out;
+  const int32_t* order;
+  int max_iter, hist, ls_kind, ls_max, objective;
+  double tol, eps;
+  int Lmax, Kmax;
+  float* ws_vec;    // per warp: 2 * hist * SPL*32 floats (s and y rings)
+  double* ws_scal;  // per warp: 2 * hist doubles (alpha, rho)
+  int* counter;
+  int32_t* status;
+};
+
+// Shared memory of one warp.
+struct WarpSmem {
+  uint32_t* tape;  // [Lmax]
+  float* cnode;    // [Lmax] constant value of each node for the point being evaluated
+  int* node_slot;  // [Lmax] slot of each LEARNABLE node
+  int* slot_node;  // [Kmax]
+  float* vals;     // [Lmax][32V]
+  float* adj;      // [Lmax][32V]
+  double* gl;      // [Kmax][32] per-lane gradient partial sums
+};
+
+__host__ __device__ __forceinline__ size_t fit_warp_bytes(int Lmax, int Kmax, int V) {
+  return fit_align16((size_t)Lmax * 4) * 3 + fit_align16((size_t)(Kmax > 0 ? Kmax : 1) * 4) +
+         2 * (size_t)Lmax * 32 * V * 4 + (size_t)(Kmax > 0 ? Kmax : 1) * 32 * 8;
+}
+
+__device__ __forceinline__ WarpSmem carve(unsigned char* p, int Lmax, int Kmax, int V) {
+  WarpSmem s;
+  const size_t l4 = fit_align16((size_t)Lmax * 4);
+  const size_t k4 = fit_align16((size_t)(Kmax > 0 ? Kmax : 1) * 4);
+  s.gl = reinterpret_cast<double*>(p);
+  p += (size_t)(Kmax > 0 ? Kmax : 1) * 32 * 8;
+  s.vals = reinterpret_cast<float*>(p);
+  p += (size_t)Lmax * 32 * V * 4;
+  s.adj = reinterpret_cast<float*>(p);
+  p += (size_t)Lmax * 32 * V * 4;
+  s.tape = reinterpret_cast<uint32_t*>(p);
+  p += l4;
+  s.cnode = reinterpret_cast<float*>(p);
+  p += l4;
+  s.node_slot = reinterpret_cast<int*>(p);
+  p += l4;
+  s.slot_node = reinterpret_cast<int*>(p);
+  p += k4;
+  return s;
+}
+
+__device__ __forceinline__ double wsum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Per-problem context held in registers.
+template <int SPL>
+struct Slots {
+  float v[SPL];
+};
+
+template <int SPL>
+struct Problem {
+  int64_t b;
+  int root;       // index of the root node
+  int K;          // real slots
+  int nslots;     // K + (has virtual slot)
+  bool has_virtual;
+  int lane;
+  __device__ __forceinline__ bool active(int s) const { return s * 32 + lane < nslots; }
+  __device__ __forceinline__ bool real(int s) const { return s * 32 + lane < K; }
+};
+
+template <int SPL>
+__device__ __forceinline__ double dot(const Problem<SPL>& P, const Slots<SPL>& a, const Slots<SPL>& b) {
+  double acc = 0.0;
+#pragma unroll
+  for (int s = 0; s < SPL; ++s)
+    if (P.active(s)) acc += (double)a.v[s] * (double)b.v[s];
+  return wsum_d(acc);
+}
+
+// x + a * p, rounded as two separate float operations (never fused), so that the
+// trial point and the later update x += a*p give identical bits.
+template <int SPL>
+__device__ __forceinline__ Slots<SPL> axpy(const Slots<SPL>& x, float a, const Slots<SPL>& p) {
+  Slots<SPL> r;
+#pragma unroll
+  for (int s = 0; s < SPL; ++s) r.v[s] = __fadd_rn(x.v[s], __fmul_rn(a, p.v[s]));
+  return r;
+}
+
+// ---------------------------------------------------------------------------------
+// closure: loss and gradient at the constants xt.
+// ---------------------------------------------------------------------------------
+template <int V, int SPL>
+__device__ __noinline__ float closure(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P, const Slots<SPL>& xt,
+                         Slots<SPL>& grad, int& err) {
+  const int lane = P.lane;
+  // publish the trial constants to their nodes; clear the per-lane gradient sums
+#pragma unroll
+  for (int s = 0; s < SPL; ++s)
+    if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = xt.v[s];
+  for (int j = 0; j < P.K; ++j) S.gl[j * 32 + lane] = 0.0;
+  __syncwarp();
+  const int R = P.root;
+  const int64_t N = A.N;
+  const float invN = 1.0f / (float)N;
+  const float* Yrow = A.Y ? A.Y + P.b * N : nullptr;
+  double loss_part = 0.0;
+  for (int64_t base = 0; base < N; base += 32 * V) {
+    int64_t nn[V];
+    bool valid[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int64_t n = base + v * 32 + lane;
+      valid[v] = n < N;
+      nn[v] = valid[v] ? n : N - 1;
+    }
+    // forward
+    for (int k = 0; k <= R; ++k) {
+      const uint32_t d = S.tape[k];
+      const int code = code_of(d);
+      float* out = S.vals + k * (32 * V);
+      if (code == VAR) {
+        const int var = child0(d);
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v * 32 + lane] = __ldg(A.X + nn[v] * A.n_x + var);
+      } else if (code == LEARNABLE) {
+        const float c = S.cnode[k];
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v * 32 + lane] = c;
+      } else {
+        const float* a = S.vals + child0(d) * (32 * V);
+        const float* bb = S.vals + child1(d) * (32 * V);
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v * 32 + lane] = node_value<float>(code, a[v * 32 + lane], bb[v * 32 + lane], 0.f, 0.f);
+      }
+      S.adj[k * (32 * V) + 0 * 32 + lane] = 0.f;
+#pragma unroll
+      for (int v = 1; v < V; ++v) S.adj[k * (32 * V) + v * 32 + lane] = 0.f;
+    }
+    // residuals and the root adjoint: (2 (f - y)) * (1/N), as autograd forms it
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const float f = S.vals[R * (32 * V) + v * 32 + lane];
+      float groot = 0.f;
+      if (valid[v]) {
+        if (A.objective == 0) {
+          const float r = f - __ldg(Yrow + nn[v]);
+          loss_part += (double)(r * r);
+          groot = __fmul_rn(r * 2.0f, invN);
+        } else {
+          loss_part += (double)f;
+          groot = invN;
+        }
+      }
+      S.adj[R * (32 * V) + v * 32 + lane] = groot;
+    }
+    // reverse sweep
+    for (int k = R; k >= 0; --k) {
+      const uint32_t d = S.tape[k];
+      const int code = code_of(d);
+      const float* gk = S.adj + k * (32 * V);
+      if (code == LEARNABLE) {
+        const int slot = S.node_slot[k];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const float g = gk[v * 32 + lane];
+          if (valid[v] && g != 0.f) S.gl[slot * 32 + lane] += (double)g;
+        }
+        continue;
+      }
+      if (code == VAR || code == ZERO || (code >= C1 && code <= E_) || code == FLOOR || code == CEIL) continue;
+      const int c0 = child0(d), c1 = child1(d);
+      float* A0 = S.adj + c0 * (32 * V);
+      float* A1 = S.adj + c1 * (32 * V);
+      const float* av = S.vals + c0 * (32 * V);
+      const float* bv = S.vals + c1 * (32 * V);
+      const float* kv = S.vals + k * (32 * V);
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const int i = v * 32 + lane;
+        bool a0, a1;
+        float o0, o1;
+        const int e = node_adjoint<float>(code, gk[i], av[i], bv[i], kv[i], a0, o0, a1, o1);
+        if (valid[v]) {
+          if (e && !err) err = e;
+          if (a0) A0[i] = __fadd_rn(A0[i], o0);
+          if (a1) A1[i] = __fadd_rn(A1[i], o1);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  // gradient of each real slot: the lane owning the slot sums the 32 lane partials
+#pragma unroll
+  for (int s = 0; s < SPL; ++s) {
+    float gv = 0.f;
+    if (P.real(s)) {
+      const int j = s * 32 + lane;
+      double acc = 0.0;
+      for (int l = 0; l < 32; ++l) acc += S.gl[j * 32 + l];
+      gv = (float)acc;
+    }
+    grad.v[s] = gv;
+  }
+  __syncwarp();
+  return (float)(wsum_d(loss_part) / (double)N);
+}
+
+// Forward only: root values of the final constants into Y_final.
+template <int V, int SPL>
+__device__ void final_forward(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P, const Slots<SPL>& x) {
+  const int lane = P.lane;
+#pragma unroll
+  for (int s = 0; s < SPL; ++s)
+    if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = x.v[s];
+  __syncwarp();
+  const int R = P.root;
+  const int64_t N = A.N;
+  for (int64_t base = 0; base < N; base += 32 * V) {
+    int64_t nn[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int64_t n = base + v * 32 + lane;
+      nn[v] = n < N ? n : N - 1;
+    }
+    for (int k = 0; k <= R; ++k) {
+      const uint32_t d = S.tape[k];
+      const int code = code_of(d);
+      float* out = S.vals + k * (32 * V);
+      if (code == VAR) {
+        const int var = child0(d);
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v * 32 + lane] = __ldg(A.X + nn[v] * A.n_x + var);
+      } else if (code == LEARNABLE) {
+        const float c = S.cnode[k];
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v * 32 + lane] = c;
+      } else {
+        const float* a = S.vals + child0(d) * (32 * V);
+        const float* bb = S.vals + child1(d) * (32 * V);
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v * 32 + lane] = node_value<float>(code, a[v * 32 + lane], bb[v * 32 + lane], 0.f, 0.f);
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int64_t n = base + v * 32 + lane;
+      if (n < N) A.Y_final[P.b * N + n] = S.vals[R * (32 * V) + v * 32 + lane];
+    }
+  }
+  __syncwarp();
+}
+
+// phi0 + (c * a) * dphi0 in float32, each operation rounded on its own as the
+// reference's tensor arithmetic does.
+__device__ __forceinline__ float armijo(float phi0, float c, float a, float dphi0) {
+  return __fadd_rn(phi0, __fmul_rn(__fmul_rn(c, a), dphi0));
+}
+
+// Evaluated point: value and gradient.
+template <int SPL>
+struct Point {
+  float phi;
+  Slots<SPL> g;
+};
+
+template <int V, int SPL>
+__global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const size_t wbytes = fit_warp_bytes(A.Lmax, A.Kmax, V);
+  const WarpSmem S = carve(smem + warp * wbytes, A.Lmax, A.Kmax, V);
+  const int64_t gwarp = (int64_t)blockIdx.x * nwarp + warp;
+  float* ringS = A.ws_vec + gwarp * (int64_t)2 * A.hist * SPL * 32;
+  float* ringY = ringS + (int64_t)A.hist * SPL * 32;
+  double* alph = A.ws_scal + gwarp * (int64_t)2 * A.hist;
+  double* rhos = alph + A.hist;
+
+  while (true) {
+    int64_t idx = 0;
+    if (lane == 0) idx = atomicAdd(A.counter, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= A.B) break;
+    Problem<SPL> P;
+    P.b = A.order ? (int64_t)A.order[idx] : idx;
+    P.lane = lane;
+    P.root = A.meta[P.b * 4 + 1];
+    P.K = A.meta[P.b * 4 + 2];
+    P.has_virtual = A.M > P.K;
+    P.nslots = P.K + (P.has_virtual ? 1 : 0);
+    const int L = P.root + 1;
+
+    // stage the tape, map learnable nodes to slots
+    for (int k = lane; k < L; k += 32) S.tape[k] = A.desc[P.b * A.M + k];
+    __syncwarp();
+    {
+      int base = 0;
+      for (int k0 = 0; k0 < L; k0 += 32) {
+        const int k = k0 + lane;
+        const bool lc = k < L && code_of(S.tape[k]) == LEARNABLE;
+        const unsigned m = __ballot_sync(0xffffffffu, lc);
+        if (lc) {
+          const int slot = base + __popc(m & ((1u << lane) - 1u));
+          S.node_slot[k] = slot;
+          S.slot_node[slot] = k;
+        }
+        base += __popc(m);
+      }
+    }
+    __syncwarp();
+
+    const float* Cin = A.C_init + P.b * A.c_sb;
+    Slots<SPL> x, g;
+#pragma unroll
+    for (int s = 0; s < SPL; ++s) {
+      const int j = s * 32 + lane;
+      x.v[s] = P.real(s) ? Cin[(int64_t)S.slot_node[j] * A.c_sm] : 0.f;
+    }
+    int err = 0;
+    int evals = 1;
+    float f = closure<V, SPL>(A, S, P, x, g, err);
+    bool poison = false;
+    int h = 0, head = 0;  // history length and index of the oldest pair
+    int it = 0;
+    for (it = 0; it < A.max_iter; ++it) {
+      const double gn = sqrt(dot(P, g, g));
+      if (gn < A.tol) break;
+
+      // ---- two-loop recursion (lbfgs_batch.py:65-103) ----
+      Slots<SPL> q = g, p;
+      if (h > 0) {
+        for (int i = h - 1; i >= 0; --i) {
+          const int slot = (head + i) % A.hist;
+          Slots<SPL> si, yi;
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) {
+            si.v[s] = ringS[slot * SPL * 32 + s * 32 + lane];
+            yi.v[s] = ringY[slot * SPL * 32 + s * 32 + lane];
+          }
+          const double rho = 1.0 / __dadd_rn(dot(P, yi, si), A.eps);
+          const double al = __dmul_rn(rho, dot(P, si, q));
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dsub_rn((double)q.v[s], __dmul_rn(al, (double)yi.v[s]));
+          if (lane == 0) { alph[i] = al; rhos[i] = rho; }
+        }
+        __syncwarp();
+        {
+          const int slot = (head + h - 1) % A.hist;
+          Slots<SPL> sl, yl;
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) {
+            sl.v[s] = ringS[slot * SPL * 32 + s * 32 + lane];
+            yl.v[s] = ringY[slot * SPL * 32 + s * 32 + lane];
+          }
+          const double gam = dot(P, sl, yl) / __dadd_rn(dot(P, yl, yl), A.eps);
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) q.v[s] = (float)(gam * (double)q.v[s]);
+        }
+        for (int i = 0; i < h; ++i) {
+          const int slot = (head + i) % A.hist;
+          Slots<SPL> si, yi;
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) {
+            si.v[s] = ringS[slot * SPL * 32 + s * 32 + lane];
+            yi.v[s] = ringY[slot * SPL * 32 + s * 32 + lane];
+          }
+          const double be = __dmul_rn(rhos[i], dot(P, yi, q));
+          const double coef = __dsub_rn(alph[i], be);
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dadd_rn((double)q.v[s], __dmul_rn((double)si.v[s], coef));
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < SPL; ++s) p.v[s] = P.active(s) ? -q.v[s] : 0.f;
+
+      // ---- line search ----
+      float alpha;
+      bool known = false;
+      Point<SPL> acc;
+      acc.phi = 0.f;
+      if (A.ls_kind == 0) {
+        // strong Wolfe (lbfgs_batch.py:138-202) with zoom (lbfgs_batch.py:204-264)
+        const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
+        const float phi0 = f;
+        const float dphi0 = (float)dot(P, g, p);
+        float a_prev = 0.f, phi_prev = phi0, a_i = 1.f;
+        Slots<SPL> g_prev = g;
+        bool done = false;
+        alpha = 0.f;
+        for (int i = 0; i < A.ls_max && !done; ++i) {
+          Point<SPL> cur;
+          cur.phi = closure<V, SPL>(A, S, P, axpy(x, a_i, p), cur.g, err);
+          ++evals;
+          const float dphi = (float)dot(P, cur.g, p);
+          const bool bad = (cur.phi > armijo(phi0, c1, a_i, dphi0)) || (i > 0 && cur.phi >= phi_prev);
+          const bool good = fabsf(dphi) <= __fmul_rn(c2, fabsf(dphi0));
+          const bool passed = dphi >= 0.f;
+          if (good) {
+            alpha = a_i;
+            acc = cur;
+            known = true;
+            done = true;
+          } else if (bad || passed) {
+            float lo = bad ? a_prev : a_i, hi = bad ? a_i : a_prev;
+            Point<SPL> plo;
+            if (!bad) {
+              plo = cur;
+            } else if (i > 0) {
+              plo.phi = phi_prev;
+              plo.g = g_prev;
+            } else {
+              // alpha_lo = 0: the point x + 0*p is x unless p holds inf/NaN
+              const Slots<SPL> x0 = axpy(x, 0.f, p);
+              bool same = true;
+#pragma unroll
+              for (int s = 0; s < SPL; ++s)
+                if (P.real(s) && __float_as_uint(x0.v[s]) != __float_as_uint(x.v[s])) same = false;
+              same = __all_sync(0xffffffffu, same);
+              if (same) {
+                plo.phi = f;
+                plo.g = g;
+              } else {
+                plo.phi = closure<V, SPL>(A, S, P, x0, plo.g, err);
+                ++evals;
+              }
+            }
+            // zoom
+            float za = 0.f;
+            bool zdone = false;
+            Point<SPL> zacc;
+            for (int j = 0; j < 10 && !zdone; ++j) {
+              const float aj = __fdiv_rn(__fadd_rn(lo, hi), 2.0f);
+              Point<SPL> pj;
+              pj.phi = closure<V, SPL>(A, S, P, axpy(x, aj, p), pj.g, err);
+              ++evals;
+              const float dphij = (float)dot(P, pj.g, p);
+              const bool zbad = (pj.phi > armijo(phi0, c1, aj, dphi0)) || (pj.phi >= plo.phi);
+              const bool zgood = fabsf(dphij) <= __fmul_rn(c2, fabsf(dphi0));
+              if (zgood) {
+                za = aj;
+                zacc = pj;
+                zdone = true;
+              }
+              if (!zdone) {
+                const float thi = zbad ? aj : hi;
+                const bool cond3 = __fmul_rn(dphij, __fsub_rn(thi, lo)) >= 0.f;
+                hi = (!zbad && cond3) ? lo : thi;
+                if (!zbad) {
+                  lo = aj;
+                  plo = pj;
+                }
+              }
+              if (!zdone && fabsf(__fsub_rn(hi, lo)) < 1e-9f) {
+                za = aj;
+                zacc = pj;
+                zdone = true;
+              }
+            }
+            if (!zdone) {
+              za = lo;
+              zacc = plo;
+            }
+            alpha = za;
+            acc = zacc;
+            known = true;
+            done = true;
+          }
+          if (!done) {
+            a_prev = a_i;
+            phi_prev = cur.phi;
+            g_prev = cur.g;
+            a_i = __fadd_rn(a_i, __fmul_rn(__fsub_rn(amax, a_i), 0.8f));
+          }
+        }
+        if (!done) alpha = a_i;  // unfinished bracket: the next extrapolated step
+      } else {
+        // Armijo backtracking (lbfgs_batch.py:105-136)
+        const float gfp = (float)dot(P, g, p);
+        float al = 1.f;
+        for (int t = 0; t < A.ls_max; ++t) {
+          Point<SPL> cur;
+          cur.phi = closure<V, SPL>(A, S, P, axpy(x, al, p), cur.g, err);
+          ++evals;
+          if (cur.phi <= armijo(f, 1e-4f, al, gfp)) {
+            acc = cur;
+            known = true;
+            break;
+          }
+          al = al * 0.5f;
+        }
+        alpha = al;
+      }
+
+      // ---- update (lbfgs_batch.py:305-322) ----
+      Slots<SPL> sv, xn;
+#pragma unroll
+      for (int s = 0; s < SPL; ++s) {
+        sv.v[s] = P.active(s) ? __fmul_rn(alpha, p.v[s]) : 0.f;
+        xn.v[s] = __fadd_rn(x.v[s], sv.v[s]);
+      }
+      Point<SPL> nxt;
+      if (known) {
+        nxt = acc;
+      } else {
+        nxt.phi = closure<V, SPL>(A, S, P, xn, nxt.g, err);
+        ++evals;
+      }
+      if (P.has_virtual) {
+        const int vs = P.K;  // virtual slot index
+        bool vnan = false;
+#pragma unroll
+        for (int s = 0; s < SPL; ++s)
+          if (s * 32 + lane == vs && isnan(sv.v[s])) vnan = true;
+        poison = poison || __any_sync(0xffffffffu, vnan);
+      }
+      // push (s, y): drop the oldest pair when the history is full
+      int slot;
+      if (h < A.hist) {
+        slot = (head + h) % A.hist;
+        ++h;
+      } else {
+        slot = head;
+        head = (head + 1) % A.hist;
+      }
+#pragma unroll
+      for (int s = 0; s < SPL; ++s) {
+        ringS[slot * SPL * 32 + s * 32 + lane] = sv.v[s];
+        ringY[slot * SPL * 32 + s * 32 + lane] = P.active(s) ? __fsub_rn(nxt.g.v[s], g.v[s]) : 0.f;
+      }
+      __syncwarp();
+      x = xn;
+      g = nxt.g;
+      f = nxt.phi;
+
+      // all real slots NaN and the others poisoned: nothing can change any more
+      bool allnan = true;
+#pragma unroll
+      for (int s = 0; s < SPL; ++s)
+        if (P.real(s) && !isnan(x.v[s])) allnan = false;
+      allnan = __all_sync(0xffffffffu, allnan);
+      if (P.K > 0 && allnan && (poison || !P.has_virtual)) {
+        it = A.max_iter;
+        break;
+      }
+    }
+
+    if (err) report(A.status, err);
+    // ---- outputs ----
+    const float qnan = __int_as_float(0x7fffffff);
+    float* Cout = A.C_out + P.b * A.c_sb;
+    for (int64_t k = lane; k < A.M; k += 32) Cout[k * A.c_sm] = poison ? qnan : Cin[k * A.c_sm];
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < SPL; ++s)
+      if (P.real(s)) Cout[(int64_t)S.slot_node[s * 32 + lane] * A.c_sm] = x.v[s];
+    if (lane == 0) {
+      if (A.iters_out) A.iters_out[P.b] = it;
+      if (A.loss_out) A.loss_out[P.b] = f;
+      if (A.evals_out) A.evals_out[P.b] = evals;
+    }
+    if (A.Y_final) final_forward<V, SPL>(A, S, P, x);
+    __syncwarp();
+  }
+}
+
+static int fit_defaults(const sr_fit_options* o, sr_fit_options& r) {
+  r.max_iter = 100;
+  r.history_size = 10;
+  r.tolerance_grad = 1e-7;
+  r.line_search = 0;
+  r.line_search_max_iter = 10;
+  r.eps = 1e-10;
+  r.objective = 0;
+  r.warps_per_block = 0;
+  r.points_per_lane = 0;
+  r.grid_blocks = 0;
+  if (o) r = *o;
+  if (r.max_iter < 0 || r.history_size < 1 || r.line_search < 0 || r.line_search > 1 || r.line_search_max_iter < 0 ||
+      r.objective < 0 || r.objective > 1) {
+    set_error("invalid fit options");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
+  if (r.points_per_lane == 0) r.points_per_lane = 1;
+  if (r.points_per_lane != 1 && r.points_per_lane != 2 && r.points_per_lane != 4) {
+    set_error("points_per_lane must be 1, 2 or 4");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
+  return SR_OK;
+}
+
+static int spl_for(int Kmax) {
+  if (Kmax + 1 <= 32) return 1;
+  if (Kmax + 1 <= 64) return 2;
+  if (Kmax + 1 <= 128) return 4;
+  return 0;
+}
+
+struct FitShape {
+  int V, SPL, warps, blocks;
+  size_t smem;
+  int64_t total_warps;
+};
+
+template <int V, int SPL>
+static void* fit_kernel_ptr() {
+  return reinterpret_cast<void*>(fit_lbfgs_kernel<V, SPL>);
+}
+
+static void* pick_kernel(int V, int SPL) {
+  switch (V * 10 + SPL) {
+    case 11: return fit_kernel_ptr<1, 1>();
+    case 12: return fit_kernel_ptr<1, 2>();
+    case 14: return fit_kernel_ptr<1, 4>();
+    case 21: return fit_kernel_ptr<2, 1>();
+    case 22: return fit_kernel_ptr<2, 2>();
+    case 24: return fit_kernel_ptr<2, 4>();
+    case 41: return fit_kernel_ptr<4, 1>();
+    case 42: return fit_kernel_ptr<4, 2>();
+    case 44: return fit_kernel_ptr<4, 4>();
+    default: return nullptr;
+  }
+}
+
+static int fit_shape(int64_t B, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
+  sh.V = o.points_per_lane;
+  sh.SPL = spl_for(Kmax);
+  if (!sh.SPL) {
+    set_error("at most 127 learnable constants per tape are supported (got %d)", Kmax);
+    return SR_ERR_UNSUPPORTED;
+  }
+  int dev = 0, sms = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t wb = fit_warp_bytes(Lmax, Kmax, sh.V);
+  int warps = o.warps_per_block > 0 ? o.warps_per_block : 4;
+  if (warps > 8) warps = 8;  // __launch_bounds__(256)
+  while (warps > 1 && wb * warps > (size_t)optin) warps >>= 1;
+  if (wb * warps > (size_t)optin) {
+    set_error("tape of %d nodes does not fit in shared memory for the fit kernel", Lmax);
+    return SR_ERR_UNSUPPORTED;
+  }
+  sh.warps = warps;
+  sh.smem = wb * warps;
+  void* k = pick_kernel(sh.V, sh.SPL);
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem) != cudaSuccess) {
+    set_error("fit kernel shared memory attribute failed");
+    return SR_ERR_CUDA;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, warps * 32, sh.smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  int64_t blocks = o.grid_blocks > 0 ? o.grid_blocks : (int64_t)sms * per_sm;
+  const int64_t need = (B + warps - 1) / warps;
+  if (blocks > need) blocks = need;
+  if (blocks < 1) blocks = 1;
+  sh.blocks = (int)blocks;
+  sh.total_warps = blocks * warps;
+  return SR_OK;
+}
+
+static int64_t ws_bytes_for(const FitShape& sh, int hist) {
+  const int64_t vec = sh.total_warps * 2LL * hist * sh.SPL * 32 * (int64_t)sizeof(float);
+  const int64_t scal = sh.total_warps * 2LL * hist * (int64_t)sizeof(double);
+  return 256 + fit_align16((size_t)vec) + fit_align16((size_t)scal);
+}
+
+}  // namespace sr
+
+extern "C" {
+
+int64_t sr_fit_workspace_bytes(int64_t B, int32_t max_len, int32_t max_consts, const sr_fit_options* opt) {
+  sr_fit_options o;
+  if (sr::fit_defaults(opt, o)) return -1;
+  sr::FitShape sh;
+  const int Lmax = max_len < 1 ? 1 : max_len;
+  if (sr::fit_shape(B, Lmax, max_consts, o, sh)) return -1;
+  return sr::ws_bytes_for(sh, o.history_size);
+}
+
+int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const uint32_t* desc, const int32_t* meta,
+                 int64_t B, int64_t M, const float* C_init, float* C_out, int64_t c_sb, int64_t c_sm, float* Y_final,
+                 int32_t* iters_out, float* loss_out, int32_t* evals_out, const int32_t* order, int32_t max_len,
+                 int32_t max_consts, const sr_fit_options* opt, void* workspace, int64_t workspace_bytes, int32_t* status,
+                 void* stream) {
+  using namespace sr;
+  sr_fit_options o;
+  int rc = fit_defaults(opt, o);
+  if (rc) return rc;
+  if (B < 0 || M < 0 || N < 0 || n_x < 0 || max_consts < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (M > kMaxNodes) { set_error("tapes longer than %d nodes are not supported", kMaxNodes); return SR_ERR_UNSUPPORTED; }
+  if (!status) { set_error("null status"); return SR_ERR_INVALID_ARGUMENT; }
+  cudaStream_t st = as_stream(stream);
+  rc = cuda_check(cudaMemsetAsync(status, 0, sizeof(int32_t), st), "status reset");
+  if (rc || B == 0 || M == 0) return rc;
+  if (N == 0) { set_error("optimize needs at least one data point"); return SR_ERR_INVALID_ARGUMENT; }
+  if (!desc || !meta || !C_init || !C_out || (o.objective == 0 && !Y) || (n_x > 0 && !X) || !workspace) {
+    set_error("null pointer argument");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
+  FitShape sh;
+  const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
+  rc = fit_shape(B, Lmax, max_consts, o, sh);
+  if (rc) return rc;
+  const int64_t need = ws_bytes_for(sh, o.history_size);
+  if (workspace_bytes < need) {
+    set_error("workspace too small: %lld < %lld bytes", (long long)workspace_bytes, (long long)need);
+    return SR_ERR_WORKSPACE;
+  }
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  FitArgs A;
+  A.X = X; A.N = N; A.n_x = n_x; A.Y = o.objective == 0 ? Y : nullptr;
+  A.desc = desc; A.meta = meta; A.B = B; A.M = M;
+  A.C_init = C_init; A.C_out = C_out; A.c_sb = c_sb; A.c_sm = c_sm;
+  A.Y_final = Y_final; A.iters_out = iters_out; A.loss_out = loss_out; A.evals_out = evals_out;
+  A.order = order;
+  A.max_iter = o.max_iter; A.hist = o.history_size; A.ls_kind = o.line_search; A.ls_max = o.line_search_max_iter;
+  A.objective = o.objective; A.tol = o.tolerance_grad; A.eps = o.eps;
+  A.Lmax = Lmax; A.Kmax = max_consts;
+  A.counter = reinterpret_cast<int*>(ws);
+  const int64_t vec = sh.total_warps * 2LL * o.history_size * sh.SPL * 32 * (int64_t)sizeof(float);
+  A.ws_vec = reinterpret_cast<float*>(ws + 256);
+  A.ws_scal = reinterpret_cast<double*>(ws + 256 + fit_align16((size_t)vec));
+  A.status = status;
+  rc = cuda_check(cudaMemsetAsync(ws, 0, 256, st), "work counter reset");
+  if (rc) return rc;
+  void* k = pick_kernel(sh.V, sh.SPL);
+  void* args[] = {&A};
+  rc = cuda_check(cudaLaunchKernel(k, dim3(sh.blocks), dim3(sh.warps * 32), args, sh.smem, st), "fit_lbfgs_kernel");
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,133 @@
+"""Batched postfix-tape evaluation with its adjoint, behind torch autograd.
+
+Drop-in for ``symbolic_torch.evaluation`` (reference symbolic_torch/evaluation.py:4-34
+and the C++ entry src/symbolic_evaluation.cpp:306-355):
+
+* ``evaluate(X, Ops, Ch, C)`` with batch-first inputs returns the (B, M, N) value
+  cache; it is differentiable w.r.t. X and C and accepts any dense gradient on
+  every node.
+* ``evaluate_backend(X, Ops, Ch, C)`` takes the M-first layout and returns a
+  (M, N, B) view, as the reference's backend does.
+
+The cache is written directly in (B, M, N) order by one kernel launch (the
+reference launches one kernel per tape position); the adjoint recomputes node
+values and never reads the cache.  Shape, dtype and validation errors carry the
+reference's messages.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .operators import error_message
+from .tape import CompiledTapes, compile_tapes
+
+
+def _check_backend_inputs(X, Ops, Ch, C):
+    """The reference's argument checks, in its order and with its messages
+    (src/symbolic_evaluation.cpp:312-334).  Ops/Ch/C are M-first here."""
+    dev = X.device
+    if Ops.device != dev or Ch.device != dev or C.device != dev:
+        raise RuntimeError("All input tensors must be on the same device.")
+    if Ops.dim() != 2:
+        raise RuntimeError("Ops must be a 2D tensor")
+    if Ch.dim() != 3:
+        raise RuntimeError("Ch must be a 3D tensor")
+    if C.dim() != 2:
+        raise RuntimeError("C must be a 2D tensor")
+    if Ops.size(0) != Ch.size(0):
+        raise RuntimeError("Ops and Ch must have the same max length (dim 0)")
+    if Ops.size(1) != Ch.size(1):
+        raise RuntimeError("Ops and Ch must have the same batch size (dim 1)")
+    if Ops.shape != C.shape:
+        raise RuntimeError("Ops and C must have the same shape")
+    if Ch.size(2) != 2:
+        raise RuntimeError("Ch must have MaxArity as its last dimension")
+    if X.dtype not in (torch.float32, torch.float64):
+        raise RuntimeError("X must be a floating-point tensor (float or double)")
+    if C.dtype not in (torch.float32, torch.float64):
+        raise RuntimeError("C must be a floating-point tensor (float or double)")
+    if Ops.dtype != torch.int64:
+        raise RuntimeError("Ops must be a Long tensor")
+    if Ch.dtype != torch.int64:
+        raise RuntimeError("Ch must be a Long tensor")
+    if X.dim() != 2:
+        raise RuntimeError("X must be a 2D tensor (N, n_x)")
+    if C.dtype != X.dtype:
+        raise RuntimeError(f"C must have the same dtype as X (got {C.dtype} and {X.dtype})")
+    _lib.require_cuda(X, Ops, Ch, C)
+
+
+class _Evaluate(torch.autograd.Function):
+    """Forward: sr_eval_forward_*; backward: sr_eval_backward_* (dense grad)."""
+
+    @staticmethod
+    def forward(ctx, X: torch.Tensor, C_bm: torch.Tensor, tapes: CompiledTapes):
+        Xc = X.contiguous()
+        B, M = tapes.B, tapes.M
+        N, nx = Xc.shape
+        cache = torch.empty((B, M, N), dtype=Xc.dtype, device=Xc.device)
+        L = _lib.lib()
+        fn = L.sr_eval_forward_f32 if Xc.dtype == torch.float32 else L.sr_eval_forward_f64
+        cb, cm = C_bm.stride()
+        rc = fn(_lib.ptr(Xc), N, nx, _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), B, M, tapes.max_len,
+                _lib.ptr(C_bm), cb, cm, _lib.ptr(cache), _lib.stream_ptr(Xc.device))
+        _lib.check(rc, "sr_eval_forward")
+        ctx.tapes = tapes
+        ctx.save_for_backward(Xc, C_bm)
+        return cache
+
+    @staticmethod
+    def backward(ctx, grad):
+        Xc, C_bm = ctx.saved_tensors
+        tapes: CompiledTapes = ctx.tapes
+        B, M = tapes.B, tapes.M
+        N, nx = Xc.shape
+        grad = grad.contiguous()
+        gC = torch.empty((B, M), dtype=Xc.dtype, device=Xc.device)
+        gX = torch.zeros_like(Xc) if ctx.needs_input_grad[0] else None
+        status = torch.empty(1, dtype=torch.int32, device=Xc.device)
+        L = _lib.lib()
+        fn = L.sr_eval_backward_f32 if Xc.dtype == torch.float32 else L.sr_eval_backward_f64
+        cb, cm = C_bm.stride()
+        rc = fn(_lib.ptr(Xc), N, nx, _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), B, M, tapes.max_len,
+                _lib.ptr(C_bm), cb, cm, _lib.ptr(grad), _lib.ptr(gC), _lib.ptr(gX), _lib.ptr(status),
+                _lib.stream_ptr(Xc.device))
+        _lib.check(rc, "sr_eval_backward")
+        code = int(status.item())
+        if code:
+            raise RuntimeError(error_message(code, "symbolic evaluation backward pass"))
+        return gX, gC, None
+
+
+def _evaluate_bmn(X, ops_bm, ch_bm, C_bm):
+    tapes = compile_tapes(ops_bm, ch_bm, X.shape[1])
+    return _Evaluate.apply(X, C_bm, tapes)
+
+
+def evaluate_backend(X: torch.Tensor, Ops: torch.Tensor, Ch: torch.Tensor, C: torch.Tensor) -> torch.Tensor:
+    """M-first entry point: X (N, n_x), Ops (M, B), Ch (M, B, 2), C (M, B) -> (M, N, B).
+
+    The result is a view of the (B, M, N) cache."""
+    _check_backend_inputs(X, Ops, Ch, C)
+    out = _evaluate_bmn(X, Ops.permute(1, 0), Ch.permute(1, 0, 2), C.permute(1, 0))
+    return out.permute(1, 2, 0)
+
+
+def evaluate(X: torch.Tensor, Ops: torch.Tensor, Ch: torch.Tensor, C: torch.Tensor) -> torch.Tensor:
+    """Evaluate B postfix tapes at N points.
+
+    Args:
+        X: (N, n_x) float32/float64 inputs.
+        Ops: (B, M) int64 operator codes (postfix, child indices below parents).
+        Ch: (B, M, 2) int64 child indices, -1 where absent.
+        C: (B, M) learnable constants (read where Ops is LEARNABLE_CONSTANT).
+
+    Returns:
+        (B, M, N) values of every node at every point; NO_OP nodes are NaN.
+    """
+    # same checks as the reference, which permutes to M-first before checking
+    _check_backend_inputs(X, Ops.permute(1, 0) if Ops.dim() == 2 else Ops,
+                          Ch.permute(1, 0, 2) if Ch.dim() == 3 else Ch,
+                          C.permute(1, 0) if C.dim() == 2 else C)
+    return _evaluate_bmn(X, Ops, Ch, C)

@@ -1,0 +1,130 @@
+"""Batched constant fitting: drop-in for ``symbolic_torch.optimize``
+(reference symbolic_torch/optimization.py:9-112 with symbolic_torch/lbfgs_batch.py).
+
+The whole L-BFGS run of every expression happens inside one persistent CUDA kernel
+(``sr_fit_lbfgs``): no per-iteration host round trips, no (M, N, B) cache.
+``optimize`` returns what the reference returns; ``optimize_ex`` also returns the
+per-expression iteration counts, final losses and closure counts.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Literal, Optional, Tuple
+
+import torch
+
+from . import _lib
+from .evaluation import _check_backend_inputs
+from .operators import error_message
+from .tape import compile_tapes
+
+
+@dataclass
+class FitResult:
+    C: torch.Tensor        # (B, M) fitted constants
+    Y: torch.Tensor        # (B, N) root values at the fitted constants
+    iters: torch.Tensor    # (B,) int32 L-BFGS iterations run
+    loss: torch.Tensor     # (B,) float32 final mean squared error
+    evals: torch.Tensor    # (B,) int32 closures (forward + adjoint passes) evaluated
+
+
+def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, *,
+         objective: int = 0, line_search_max_iter: int = 10, eps: float = 1e-10,
+         warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
+         order: Optional[torch.Tensor] = None, want_y: bool = True) -> FitResult:
+    if line_search_fn not in ("strong_wolfe", "backtracking"):
+        raise ValueError(f"Invalid line_search_fn: {line_search_fn}. Choose 'strong_wolfe' or 'backtracking'.")
+    if Ops.dim() != 2:
+        raise RuntimeError("Ops must be a 2D tensor")
+    _check_backend_inputs(X, Ops.permute(1, 0), Ch.permute(1, 0, 2) if Ch.dim() == 3 else Ch,
+                          C_init.permute(1, 0) if C_init.dim() == 2 else C_init)
+    if X.dtype != torch.float32:
+        raise RuntimeError("optimize runs in float32: X and C_init must be float32")
+    dev = X.device
+    B, M = Ops.shape
+    N, nx = X.shape
+    if Y is not None:
+        if Y.shape != (B, N):
+            raise RuntimeError(f"Y must have shape (B, N) = ({B}, {N}), got {tuple(Y.shape)}")
+        if Y.device != dev:
+            raise RuntimeError("All input tensors must be on the same device.")
+        Y = Y.to(torch.float32).contiguous()
+    tapes = compile_tapes(Ops, Ch, nx)
+    Xc = X.contiguous()
+    opts = _lib.FitOptions(max_iter=int(max_iter), history_size=int(history_size),
+                           tolerance_grad=float(tolerance_grad),
+                           line_search=0 if line_search_fn == "strong_wolfe" else 1,
+                           line_search_max_iter=int(line_search_max_iter), eps=float(eps),
+                           objective=int(objective), warps_per_block=int(warps_per_block),
+                           points_per_lane=int(points_per_lane), grid_blocks=int(grid_blocks))
+    L = _lib.lib()
+    max_len = max(tapes.max_root, 1)
+    wsb = L.sr_fit_workspace_bytes(B, max_len, tapes.max_consts, opts)
+    if wsb < 0:
+        _lib.check(-1, "sr_fit_workspace_bytes")
+    ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)
+    C_out = torch.empty((B, M), dtype=torch.float32, device=dev)
+    Y_out = torch.empty((B, N), dtype=torch.float32, device=dev) if want_y else None
+    iters = torch.empty(B, dtype=torch.int32, device=dev)
+    loss = torch.empty(B, dtype=torch.float32, device=dev)
+    evals = torch.empty(B, dtype=torch.int32, device=dev)
+    status = torch.empty(1, dtype=torch.int32, device=dev)
+    if order is None and B > 1:
+        # longest tapes first: the persistent warps then finish at about the same time
+        order = torch.argsort(tapes.meta[:, 1], descending=True, stable=True).to(torch.int32)
+    rc = _fit_call(L, Xc, N, nx, Y, tapes, B, M, C_init, C_out, Y_out, iters, loss, evals, order, max_len, opts, ws,
+                   status, dev)
+    _lib.check(rc, "sr_fit_lbfgs")
+    code = int(status.item())
+    if code:
+        ctx = "input validation" if code in (101, 102) else "symbolic evaluation backward pass"
+        raise RuntimeError(error_message(code, ctx))
+    return FitResult(C=C_out, Y=Y_out, iters=iters, loss=loss, evals=evals)
+
+
+def _fit_call(L, Xc, N, nx, Y, tapes, B, M, C_init, C_out, Y_out, iters, loss, evals, order, max_len, opts, ws,
+              status, dev):
+    # The kernel reads C_init and writes C_out through the same (b, m) strides, so
+    # C_init is made contiguous like C_out.
+    Cin = C_init.to(torch.float32).contiguous()
+    return L.sr_fit_lbfgs(_lib.ptr(Xc), N, nx, _lib.ptr(Y), _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), B, M,
+                          _lib.ptr(Cin), _lib.ptr(C_out), M, 1, _lib.ptr(Y_out), _lib.ptr(iters), _lib.ptr(loss),
+                          _lib.ptr(evals), _lib.ptr(order), max_len, tapes.max_consts, opts, _lib.ptr(ws),
+                          ws.numel(), _lib.ptr(status), _lib.stream_ptr(dev))
+
+
+def optimize(
+    X: torch.Tensor,
+    Y: torch.Tensor,
+    Ops: torch.Tensor,
+    Ch: torch.Tensor,
+    C_init: torch.Tensor,
+    max_iter: int = 100,
+    history_size: int = 10,
+    tolerance_grad: float = 1e-7,
+    line_search_fn: Literal["strong_wolfe", "backtracking"] = "strong_wolfe",
+) -> Tuple[torch.Tensor, torch.Tensor]:
+    """Fit the learnable constants of every expression to its target row.
+
+    Args:
+        X: (N, n_x) float32 inputs.  Y: (B, N) float32 targets.
+        Ops: (B, M) int64 postfix tapes, left-packed (root = number of non-NO_OP
+            entries - 1).  Ch: (B, M, 2) int64 children.  C_init: (B, M) float32.
+        max_iter, history_size, tolerance_grad, line_search_fn: as LBFGS_batch.
+
+    Returns:
+        (C_final (B, M), Y_final (B, N)).
+    """
+    r = _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn)
+    return r.C, r.Y
+
+
+def optimize_ex(X, Y, Ops, Ch, C_init, max_iter=100, history_size=10, tolerance_grad=1e-7,
+                line_search_fn="strong_wolfe", **kw) -> FitResult:
+    """``optimize`` plus per-expression iterations, final loss and closure counts.
+
+    Extra keywords: line_search_max_iter, eps, objective (0 = MSE against Y,
+    1 = mean of the root value; Y may be None), warps_per_block, points_per_lane,
+    grid_blocks (kernel shape), order (processing order), want_y.
+    """
+    return _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, **kw)

@@ -1,0 +1,117 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+* ``ragged_fit``: ragged batched L-BFGS -- B tapes of uniform length 3..64 with
+  0..8 learnable constants, 2 variables, N points with X ~ U[-3, 3]; each target
+  row is a hidden random expression from the same generator with N(0, 1)
+  constants plus N(0, 0.01^2) noise.  Defaults: B=16384, N=512.
+* ``eval_batch``: forward+adjoint evaluation -- B=65536 tapes of padded length
+  64 over {+,-,*,/,sin,cos,exp,log,X0..X3,C} with mean length about 20,
+  X ~ U[-3, 3] (1024, 4), C ~ N(0, 1).
+
+Hidden targets are evaluated with the library's own forward kernel; rows that
+are not finite everywhere are redrawn.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import tapes
+from .operators import Operator
+
+# Floating-point operations per node and point, forward and adjoint, counted as
+# FP32 add/mul = 1, FMA = 2, reciprocal/sqrt/transcendental unit op = 1, with the
+# polynomial/range-reduction work of the accurate CUDA math routines counted in
+# FMAs.  Used for the fit kernel's FLOP roofline.
+FWD_FLOPS = {int(Operator.ADD): 1, int(Operator.SUB): 1, int(Operator.MUL): 1, int(Operator.DIV): 5,
+             int(Operator.SIN): 20, int(Operator.COS): 20, int(Operator.EXP): 10, int(Operator.LOG): 16}
+ADJ_FLOPS = {int(Operator.ADD): 2, int(Operator.SUB): 2, int(Operator.MUL): 4, int(Operator.DIV): 13,
+             int(Operator.SIN): 22, int(Operator.COS): 22, int(Operator.EXP): 2, int(Operator.LOG): 6,
+             int(Operator.LEARNABLE_CONSTANT): 1}
+
+
+@dataclass
+class FitWorkload:
+    X: np.ndarray
+    Y: np.ndarray
+    ops: np.ndarray
+    ch: np.ndarray
+    C: np.ndarray
+    name: str
+
+    @property
+    def B(self):
+        return self.ops.shape[0]
+
+    def flops_per_closure(self) -> np.ndarray:
+        """(B,) algorithmic FLOPs of one closure (forward + adjoint over all N points)."""
+        f = np.zeros(self.ops.shape, np.float64)
+        for op, w in FWD_FLOPS.items():
+            f += (self.ops == op) * w
+        for op, w in ADJ_FLOPS.items():
+            f += (self.ops == op) * w
+        return f.sum(1) * self.X.shape[0]
+
+
+def _gpu_roots(X, ops, ch, C, device="cuda"):
+    """Root values (B, N) of each tape with the library's forward kernel."""
+    from .evaluation import evaluate
+    with torch.no_grad():
+        cache = evaluate(torch.tensor(X, device=device), torch.tensor(ops, device=device),
+                         torch.tensor(ch, device=device), torch.tensor(C, device=device))
+        root = torch.tensor(np.maximum((ops != 0).sum(1) - 1, 0), device=device)
+        return cache[torch.arange(ops.shape[0], device=device), root].cpu().numpy()
+
+
+def ragged_fit(B: int = 16384, N: int = 512, M: int = 64, n_vars: int = 2, seed: int = 0,
+               device: str = "cuda", root_eval=None) -> FitWorkload:
+    """root_eval(X, ops, ch, C) -> (B, N) root values of the hidden targets
+    (default: the library's forward kernel on ``device``)."""
+    root_eval = root_eval or (lambda X_, o, c, C_: _gpu_roots(X_, o, c, C_, device))
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-3, 3, (N, n_vars)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    lengths = rng.integers(3, M + 1, size=B)
+    kc = rng.integers(0, 9, size=B)
+    Xs = X[rng.choice(N, size=min(N, 32), replace=False)]
+    tb = tapes.generate(B, M, seed=seed + 1, lengths=lengths, const_counts=kc, n_vars=n_vars,
+                        X_screen=Xs, C_screen=C)
+    # hidden target expressions
+    Y = np.zeros((B, N), np.float32)
+    todo = np.arange(B)
+    for attempt in range(20):
+        nb = todo.size
+        hl = rng.integers(3, M + 1, size=nb)
+        hk = rng.integers(0, 9, size=nb)
+        Ch_ = rng.standard_normal((nb, M)).astype(np.float32)
+        hid = tapes.generate(nb, M, seed=seed + 100 + attempt, lengths=hl, const_counts=hk, n_vars=n_vars,
+                             X_screen=Xs, C_screen=Ch_)
+        yh = np.asarray(root_eval(X, hid.ops, hid.ch, Ch_), np.float32)
+        ok = np.isfinite(yh).all(1) & (np.abs(yh).max(1) < 1e4)
+        Y[todo[ok]] = yh[ok]
+        todo = todo[~ok]
+        if todo.size == 0:
+            break
+    Y[todo] = 0.0
+    Y = (Y + 0.01 * rng.standard_normal((B, N))).astype(np.float32)
+    return FitWorkload(X=X, Y=Y, ops=tb.ops, ch=tb.ch, C=C, name=f"ragged_fit_B{B}_N{N}_M{M}")
+
+
+@dataclass
+class EvalWorkload:
+    X: np.ndarray
+    ops: np.ndarray
+    ch: np.ndarray
+    C: np.ndarray
+
+
+def eval_batch(B: int = 65536, N: int = 1024, M: int = 64, n_vars: int = 4, seed: int = 0) -> EvalWorkload:
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-3, 3, (N, n_vars)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    Xs = X[rng.choice(N, size=min(N, 32), replace=False)]
+    tb = tapes.generate(B, M, seed=seed + 1, mean_length=20.0, n_vars=n_vars, p_const_leaf=0.2, X_screen=Xs,
+                        C_screen=C)
+    return EvalWorkload(X=X, ops=tb.ops, ch=tb.ch, C=C)

@@ -1,0 +1,167 @@
+/*
+ * sr_gb300.h -- C ABI of the GB300 expression-fitting library (libsr_gb300.so).
+ *
+ * Plain pointers, sizes and strides only.  Every pointer argument named *_dev is
+ * device memory owned by the caller; nothing here allocates device memory except
+ * where a function says so.  `stream` is a cudaStream_t passed as void* (NULL =
+ * legacy default stream).  Work is enqueued on that stream; functions return after
+ * enqueueing, without synchronising.
+ *
+ * Return values: SR_OK (0) when the work was enqueued, a negative SR_ERR_* for an
+ * API-level problem (sr_last_error() gives the text).  Data-dependent errors found
+ * by the kernels (the reference's ErrorCode values 101, 102, 201, 204) are written
+ * to the caller's device status word, which the caller reads once per call, as
+ * the reference reads its error flag with .item().
+ *
+ * Layouts use the reference's user-facing (batch-first) view:
+ *   X (N, n_x) row-major; Ops/C (B, M) addressed through (b, m) strides;
+ *   Ch (B, M, 2) through (b, m, child) strides; cache and grad_out (B, M, N)
+ *   contiguous; grad_C (B, M) contiguous; Y, Y_final (B, N) contiguous.
+ * Staged tapes: desc (B, M) uint32 and meta (B, 4) int32 written by
+ * sr_tape_compile (meta = {L_eff, root, n_const_to_root, n_const}).
+ */
+#ifndef SR_GB300_H
+#define SR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SR_OK 0
+#define SR_ERR_INVALID_ARGUMENT (-1)
+#define SR_ERR_CUDA (-2)
+#define SR_ERR_UNSUPPORTED (-3)
+#define SR_ERR_WORKSPACE (-4)
+
+/* Largest tape (M) and variable count the node encoding holds. */
+#define SR_MAX_NODES 4095
+#define SR_MAX_VARS 4095
+
+/* Text of the last API-level error on this host thread ("" if none). */
+const char *sr_last_error(void);
+
+/* Library version string. */
+const char *sr_version(void);
+
+/*
+ * Input validation: child index below the parent's (101) and child count equal to
+ * the arity (102).  Replaces validate_inputs_cuda_impl
+ * (reference src/evaluation_kernels_cuda.cu:13-49, 675-689) and the validation
+ * half of validate_inputs (reference src/symbolic_evaluation.cpp:7-37).
+ * status_dev is zeroed and then receives the first error found.
+ */
+int sr_validate(const int64_t *ops_dev, const int64_t *ch_dev, int64_t B, int64_t M,
+                int64_t ops_sb, int64_t ops_sm, int64_t ch_sb, int64_t ch_sm, int64_t ch_si,
+                int32_t *status_dev, void *stream);
+
+/*
+ * Validation plus staging of the tapes into the compact node encoding used by
+ * every kernel here (one pass over Ops/Ch).  desc_dev (B, M) uint32 and
+ * meta_dev (B, 4) int32 are outputs.  stats_dev is int32[4], zeroed by the call:
+ * stats[0] = status as in sr_validate, stats[1] = largest L_eff, stats[2] = largest
+ * root + 1, stats[3] = largest number of constants up to the root.
+ * Covers the validation of validate_inputs (reference src/symbolic_evaluation.cpp:7-37)
+ * and the root/constant-mask bookkeeping of optimize
+ * (reference symbolic_torch/optimization.py:51-61).
+ */
+int sr_tape_compile(const int64_t *ops_dev, const int64_t *ch_dev, int64_t B, int64_t M,
+                    int64_t ops_sb, int64_t ops_sm, int64_t ch_sb, int64_t ch_sm, int64_t ch_si,
+                    int32_t n_vars, uint32_t *desc_dev, int32_t *meta_dev, int32_t *stats_dev,
+                    void *stream);
+
+/*
+ * Forward evaluation: cache (B, M, N) of every node at every point; NO_OP nodes
+ * and the padding after the last real node are NaN.  Replaces the reference's
+ * host loop of M launches of evaluation_forward_step_k
+ * (reference src/symbolic_evaluation.cpp:39-92, src/evaluation_kernels_cuda.cu:51-216,
+ * 634-652).  One warp interprets one tape, lanes over data points.
+ * max_len: largest meta[0] of the batch (stats[1] of sr_tape_compile), or 0 for M;
+ * it sizes the per-warp shared-memory node table.
+ */
+int sr_eval_forward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
+                        const int32_t *meta_dev, int64_t B, int64_t M, int32_t max_len,
+                        const float *C_dev, int64_t c_sb, int64_t c_sm, float *cache_dev, void *stream);
+int sr_eval_forward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
+                        const int32_t *meta_dev, int64_t B, int64_t M, int32_t max_len,
+                        const double *C_dev, int64_t c_sb, int64_t c_sm, double *cache_dev, void *stream);
+
+/*
+ * Adjoint of the forward evaluation for a dense output gradient grad_out (B, M, N).
+ * Node values are recomputed from X and C (the cache is not read).  Writes
+ * grad_C (B, M) (zero at non-constant nodes) and, when grad_X_dev is not NULL,
+ * accumulates into grad_X (N, n_x), which the caller zeroes first.  status_dev
+ * is zeroed and then receives 201 (nonzero gradient on a NO_OP node) or 204
+ * (a/b with b = 0 and a nonzero gradient).  Replaces SymbolicEvaluation::backward
+ * and evaluation_backward_step_k (reference src/symbolic_evaluation.cpp:94-168,
+ * src/evaluation_kernels_cuda.cu:218-632, 654-673).
+ */
+int sr_eval_backward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
+                         const int32_t *meta_dev, int64_t B, int64_t M, int32_t max_len,
+                         const float *C_dev, int64_t c_sb, int64_t c_sm, const float *grad_out_dev,
+                         float *grad_C_dev, float *grad_X_dev, int32_t *status_dev, void *stream);
+int sr_eval_backward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
+                         const int32_t *meta_dev, int64_t B, int64_t M, int32_t max_len,
+                         const double *C_dev, int64_t c_sb, int64_t c_sm, const double *grad_out_dev,
+                         double *grad_C_dev, double *grad_X_dev, int32_t *status_dev, void *stream);
+
+/* Options of sr_fit_lbfgs; mirrors optimize()/LBFGS_batch's arguments
+ * (reference symbolic_torch/optimization.py:9-19, symbolic_torch/lbfgs_batch.py:15-23). */
+typedef struct sr_fit_options {
+  int32_t max_iter;             /* 100 */
+  int32_t history_size;         /* 10 */
+  double tolerance_grad;        /* 1e-7 */
+  int32_t line_search;          /* 0 = strong Wolfe, 1 = Armijo backtracking */
+  int32_t line_search_max_iter; /* 10 */
+  double eps;                   /* 1e-10 */
+  int32_t objective;            /* 0 = mean squared error vs Y, 1 = mean of the root value */
+  int32_t warps_per_block;      /* problems per CTA (0 = library default) */
+  int32_t points_per_lane;      /* data points per lane per pass: 1, 2 or 4 (0 = default) */
+  int32_t grid_blocks;          /* persistent CTAs (0 = one wave over all SMs) */
+} sr_fit_options;
+
+/* Bytes of device workspace sr_fit_lbfgs needs for this problem set
+ * (max_len / max_consts as passed to sr_fit_lbfgs). */
+int64_t sr_fit_workspace_bytes(int64_t B, int32_t max_len, int32_t max_consts, const sr_fit_options *opt);
+
+/*
+ * Fused batched L-BFGS fit of the learnable constants of every tape: one
+ * persistent kernel in which each warp owns one problem at a time and runs the
+ * whole optimisation (closure = forward + adjoint over all N points, two-loop
+ * recursion, strong-Wolfe or backtracking line search, history update) on chip.
+ * Follows optimize() and LBFGS_batch per problem (reference
+ * symbolic_torch/optimization.py:9-112, symbolic_torch/lbfgs_batch.py:61-326).
+ * C_init/C_out (B, M) use (c_sb, c_sm) strides; Y and Y_final (B, N) are
+ * contiguous (Y_final may be NULL); iters_out/loss_out/evals_out (B) may be NULL.
+ * order_dev (B) int32 gives the processing order (NULL = 0..B-1).
+ * max_len: largest root + 1 (stats[2] of sr_tape_compile; 0 = M); max_consts:
+ * largest meta[2] (stats[3]).  workspace_dev must hold sr_fit_workspace_bytes(...)
+ * bytes; it is initialised by the call.
+ */
+int sr_fit_lbfgs(const float *X_dev, int64_t N, int64_t n_x, const float *Y_dev,
+                 const uint32_t *desc_dev, const int32_t *meta_dev, int64_t B, int64_t M,
+                 const float *C_init_dev, float *C_out_dev, int64_t c_sb, int64_t c_sm,
+                 float *Y_final_dev, int32_t *iters_out_dev, float *loss_out_dev,
+                 int32_t *evals_out_dev, const int32_t *order_dev, int32_t max_len,
+                 int32_t max_consts, const sr_fit_options *opt, void *workspace_dev,
+                 int64_t workspace_bytes, int32_t *status_dev, void *stream);
+
+/*
+ * create_constants support (reference symbolic_torch/utils.py:7-41).
+ * sr_const_offsets: for a 2-D Ops view (R, Cc) with strides (s0, s1), writes
+ * offsets_dev (R + 1) int64: the exclusive prefix count of LEARNABLE_CONSTANT
+ * entries in row-major order; offsets[R] is the total.
+ * sr_const_scatter: out (R, Cc) contiguous float32 gets values[rank] at the k-th
+ * LEARNABLE_CONSTANT entry in row-major order and 0 elsewhere.
+ */
+int sr_const_offsets(const int64_t *ops_dev, int64_t R, int64_t Cc, int64_t s0, int64_t s1,
+                     int64_t *offsets_dev, void *stream);
+int sr_const_scatter(const int64_t *ops_dev, int64_t R, int64_t Cc, int64_t s0, int64_t s1,
+                     const int64_t *offsets_dev, const float *values_dev, float *out_dev,
+                     void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SR_GB300_H */

@@ -268,7 +268,8 @@ DEFINE_BATCH(double, f64)
  * summed in slot order, float32 scalars.
  * dot_mode 1 is the fused kernel's arithmetic: dots and two-loop scalars in
  * double (s.y, y.y, the alphas, beta, gamma, rho), vector updates rounded once
- * to float, line-search scalars in float.
+ * to float, line-search scalars in float, and the per-constant gradient summed
+ * over the points in double.
  */
 typedef struct {
     const float *X; int64_t N, nx;
@@ -276,6 +277,8 @@ typedef struct {
     const int64_t *ops, *ch;        /* (M), (M,2) rows of this problem */
     int64_t M, root;
     float *val, *adj;
+    double *gacc;                   /* per-slot gradient sums (dot_mode 1 sums in double) */
+    int dmode;
     long n_evals;
     int err;
 } problem_t;
@@ -289,7 +292,7 @@ static float closure_f32(problem_t *P, const float *x, float *g)
     const int64_t M = P->M, N = P->N;
     const float invN = 1.0f / (float)N;
     double acc = 0.0;
-    for (int64_t j = 0; j < M; ++j) g[j] = 0.0f;
+    for (int64_t j = 0; j < M; ++j) { g[j] = 0.0f; P->gacc[j] = 0.0; }
     for (int64_t n = 0; n < N; ++n) {
         for (int64_t k = 0; k < M; ++k) {
             int64_t op = P->ops[k];
@@ -318,12 +321,17 @@ static float closure_f32(problem_t *P, const float *x, float *g)
             float gcl = 0.0f;
             int e = bwd_f32(op, P->ch[k * 2], P->ch[k * 2 + 1], P->adj[k], P->val, P->adj, k, &gcl,
                             NULL, P->nx);
-            if (op == OP_LEARNABLE) g[k] += gcl;
+            if (op == OP_LEARNABLE) {
+                if (P->dmode) P->gacc[k] += (double)gcl;
+                else g[k] += gcl;
+            }
             if (e && !P->err) P->err = e;
         }
     }
-    for (int64_t k = 0; k < M; ++k)
+    for (int64_t k = 0; k < M; ++k) {
+        if (P->dmode) g[k] = (float)P->gacc[k];
         if (P->ops[k] != OP_LEARNABLE) g[k] = 0.0f;
+    }
     P->n_evals++;
     return (float)(acc / (double)N);
 }
@@ -492,6 +500,8 @@ int sro_optimize_f32(const float *X, int64_t N, int64_t nx, const float *Y, cons
         P.root = cnt > 0 ? cnt - 1 : 0;
         P.val = (float *)malloc(sizeof(float) * (size_t)M);
         P.adj = (float *)malloc(sizeof(float) * (size_t)M);
+        P.gacc = (double *)malloc(sizeof(double) * (size_t)M);
+        P.dmode = dot_mode;
         size_t vb = sizeof(float) * (size_t)D;
         float *x = malloc(vb), *g = malloc(vb), *p = malloc(vb), *q = malloc(vb), *xt = malloc(vb),
               *gt = malloc(vb), *gn = malloc(vb);
@@ -555,7 +565,7 @@ int sro_optimize_f32(const float *X, int64_t N, int64_t nx, const float *Y, cons
         for (int i = 0; i <= history; ++i) { free(S[i]); free(Yh[i]); }
         free(S); free(Yh); free(alph);
         free(x); free(g); free(p); free(q); free(xt); free(gt); free(gn);
-        free(P.val); free(P.adj);
+        free(P.val); free(P.adj); free(P.gacc);
     }
     return err_all;
 }

@@ -1,0 +1,253 @@
+"""GPU parity of evaluate / evaluate_backend and their adjoint.
+
+Checked against (a) the reference's own outputs (tests/golden, written from the
+reference's CPU path) and (b) the CPU oracle on seeded tapes.  Tolerance: node
+values and gradients within 1e-5 relative on finite entries with identical NaN
+placement (CUDA's and glibc's transcendentals differ by a few ulps).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+
+
+def _sr():
+    import cudasymbolicregression_gb300 as sr
+    return sr
+
+
+def assert_close_nan(mine, ref, rtol=RTOL, atol_scale=1e-5):
+    mine = np.asarray(mine)
+    ref = np.asarray(ref)
+    assert mine.shape == ref.shape
+    nan_m, nan_r = np.isnan(mine), np.isnan(ref)
+    assert np.array_equal(nan_m, nan_r), f"NaN placement differs at {np.argwhere(nan_m != nan_r)[:5]}"
+    fin = np.isfinite(ref) & np.isfinite(mine)
+    inf_ok = np.array_equal(np.isinf(mine), np.isinf(ref))
+    assert inf_ok, "inf placement differs"
+    if fin.any():
+        d = np.abs(mine[fin].astype(np.float64) - ref[fin].astype(np.float64))
+        tol = rtol * np.abs(ref[fin].astype(np.float64)) + atol_scale
+        bad = d > tol
+        assert not bad.any(), f"max rel err {np.max(d / np.maximum(np.abs(ref[fin]), 1e-30))}, {bad.sum()} entries"
+
+
+def cuda(a, dtype=None):
+    t = torch.as_tensor(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+@pytest.mark.parametrize("name", ["single_ops", "random_dags", "random_default_ops"])
+def test_forward_vs_reference_golden(golden, name):
+    sr = _sr()
+    g = golden(name)
+    out = sr.evaluation.evaluate(cuda(g["X"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]))
+    assert out.shape == g["cache"].shape
+    assert_close_nan(out.cpu().numpy(), g["cache"])
+
+
+@pytest.mark.parametrize("name", ["single_ops", "random_dags", "random_default_ops"])
+def test_backward_vs_reference_golden(golden, name):
+    sr = _sr()
+    g = golden(name)
+    X = cuda(g["X"]).requires_grad_(True)
+    C = cuda(g["C"]).requires_grad_(True)
+    out = sr.evaluation.evaluate(X, cuda(g["ops"]), cuda(g["ch"]), C)
+    out.backward(cuda(g["gout"]))
+    assert_close_nan(C.grad.cpu().numpy(), g["gC"], rtol=1e-4, atol_scale=1e-4)
+    assert_close_nan(X.grad.cpu().numpy(), g["gX"], rtol=1e-4, atol_scale=1e-3)
+
+
+def test_evaluate_backend_layout(golden):
+    """M-first entry point: (M, B) inputs, (M, N, B) output (reference src/symbolic_evaluation.cpp:306)."""
+    sr = _sr()
+    g = golden("random_dags")
+    ops = cuda(g["ops"]).permute(1, 0)
+    ch = cuda(g["ch"]).permute(1, 0, 2)
+    C = cuda(g["C"]).permute(1, 0)
+    out = sr.evaluation.evaluate_backend(cuda(g["X"]), ops, ch, C)
+    assert out.shape == (g["ops"].shape[1], g["X"].shape[0], g["ops"].shape[0])
+    assert_close_nan(out.permute(2, 0, 1).cpu().numpy(), g["cache"])
+
+
+@pytest.mark.parametrize("seed,B,M,N,nx", [(1, 300, 40, 45, 3), (2, 64, 64, 1000, 4), (3, 7, 5, 1, 1),
+                                             (4, 33, 17, 129, 2)])
+def test_forward_backward_vs_oracle(seed, B, M, N, nx):
+    from cudasymbolicregression_gb300 import tapes
+    from cudasymbolicregression_gb300.operators import BINARY_OPS, UNARY_OPS
+    sr = _sr()
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-3, 3, (N, nx)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    tb = tapes.generate(B, M, seed=seed, mean_length=M / 3, n_vars=nx, unary=UNARY_OPS, binary=BINARY_OPS,
+                        X_screen=X, C_screen=C)
+    ref = oracle.eval_fwd(X, tb.ops, tb.ch, C)
+    Xt = cuda(X).requires_grad_(True)
+    Ct = cuda(C).requires_grad_(True)
+    out = sr.evaluation.evaluate(Xt, cuda(tb.ops), cuda(tb.ch), Ct)
+    assert_close_nan(out.detach().cpu().numpy(), ref)
+    gout = rng.standard_normal(ref.shape).astype(np.float32)
+    gout[np.isnan(ref)] = 0.0
+    gC, gX, err = oracle.eval_bwd(X, tb.ops, tb.ch, C, gout)
+    if err:
+        pytest.skip("seeded tapes hit a zero denominator")
+    out.backward(cuda(gout))
+    assert_close_nan(Ct.grad.cpu().numpy(), gC, rtol=1e-4, atol_scale=1e-4)
+    assert_close_nan(Xt.grad.cpu().numpy(), gX, rtol=1e-4, atol_scale=1e-3)
+
+
+def test_float64_matches_oracle():
+    from cudasymbolicregression_gb300 import tapes
+    from cudasymbolicregression_gb300.operators import BINARY_OPS, UNARY_OPS
+    sr = _sr()
+    rng = np.random.default_rng(9)
+    B, M, N, nx = 100, 30, 77, 2
+    X = rng.uniform(-3, 3, (N, nx))
+    C = rng.standard_normal((B, M))
+    tb = tapes.generate(B, M, seed=9, mean_length=10, n_vars=nx, unary=UNARY_OPS, binary=BINARY_OPS)
+    ref = oracle.eval_fwd(X, tb.ops, tb.ch, C, dtype=np.float64)
+    Ct = cuda(C, torch.float64).requires_grad_(True)
+    out = sr.evaluation.evaluate(cuda(X, torch.float64), cuda(tb.ops), cuda(tb.ch), Ct)
+    assert out.dtype == torch.float64
+    assert_close_nan(out.detach().cpu().numpy(), ref, rtol=1e-12, atol_scale=1e-12)
+    gout = rng.standard_normal(ref.shape)
+    gout[np.isnan(ref)] = 0.0
+    gC, _, err = oracle.eval_bwd(X, tb.ops, tb.ch, C, gout, dtype=np.float64)
+    if err:
+        pytest.skip("seeded tapes hit a zero denominator")
+    out.backward(cuda(gout, torch.float64))
+    assert_close_nan(Ct.grad.cpu().numpy(), gC, rtol=1e-10, atol_scale=1e-10)
+
+
+def test_constants_known_answers():
+    """reference tests/test_symbolic_evaluation.py:435-478: C=3.14 -> 4.14, sin(3.14)."""
+    sr = _sr()
+    X = torch.randn(4, 1).cuda()
+    ops = torch.tensor([[1], [2], [40]], dtype=torch.int64).cuda()
+    ch = -torch.ones(3, 1, 2, dtype=torch.int64).cuda()
+    ch[2, 0, 0] = 0
+    ch[2, 0, 1] = 1
+    C = torch.zeros(3, 1).cuda()
+    C[0, 0] = 3.14
+    y = sr.evaluation.evaluate_backend(X, ops, ch, C)
+    assert torch.allclose(y[2, :, 0], torch.full((4,), 4.14, device="cuda"), atol=1e-6)
+    ops = torch.tensor([[1], [10]], dtype=torch.int64).cuda()
+    ch = -torch.ones(2, 1, 2, dtype=torch.int64).cuda()
+    ch[1, 0, 0] = 0
+    C = torch.zeros(2, 1).cuda()
+    C[0, 0] = 3.14
+    y = sr.evaluation.evaluate_backend(X, ops, ch, C)
+    assert torch.allclose(y[1, :, 0], torch.sin(torch.tensor(3.14)).cuda().expand(4), atol=1e-6)
+
+
+def test_noop_nan_and_zero_grads():
+    """reference tests/test_symbolic_evaluation.py:192-217."""
+    sr = _sr()
+    X = torch.randn(10, 2).cuda().requires_grad_(True)
+    ops = torch.tensor([[0]], dtype=torch.int64).cuda()
+    ch = -torch.ones(1, 1, 2, dtype=torch.int64).cuda()
+    C = torch.zeros(1, 1).cuda().requires_grad_(True)
+    y = sr.evaluation.evaluate_backend(X, ops, ch, C)
+    assert torch.isnan(y).all()
+    y[-1].backward(torch.zeros(10, 1).cuda())
+    assert torch.all(X.grad == 0) and torch.all(C.grad == 0)
+
+
+def test_validation_errors(golden):
+    sr = _sr()
+    g = golden("errors")
+    for name in ("child_geq", "unary_nochild", "binary_onechild", "leaf_child"):
+        ops, ch = cuda(g[name + "__ops"]), cuda(g[name + "__ch"])
+        X = cuda(g[name + "__X"])
+        C = torch.zeros(ops.shape, device="cuda")
+        with pytest.raises(RuntimeError) as e:
+            sr.evaluation.evaluate(X, ops, ch, C)
+        assert str(e.value) == str(g[name + "__msg"])
+
+
+def test_backward_errors(golden):
+    sr = _sr()
+    g = golden("errors")
+    for name in ("noop_grad", "div_zero"):
+        ops, ch = cuda(g[name + "__ops"]), cuda(g[name + "__ch"])
+        X = cuda(g[name + "__X"]).requires_grad_(True)
+        C = torch.zeros(ops.shape, device="cuda").requires_grad_(True)
+        y = sr.evaluation.evaluate(X, ops, ch, C)
+        gout = torch.zeros_like(y)
+        gout[:, -1, :] = 1.0
+        with pytest.raises(RuntimeError) as e:
+            y.backward(gout)
+        assert str(g[name + "__msg"]) in str(e.value)
+
+
+def test_ragged_batch_and_padding_rows():
+    """Ragged tapes: rows after the last real node are NaN, NO_OP inside a tape is NaN."""
+    sr = _sr()
+    V = 50
+    ops = torch.tensor([[V, V + 1, 40, 0, 0], [V, 10, 0, 0, 0], [V, 0, 0, 0, 0]], dtype=torch.int64).cuda()
+    ch = -torch.ones(3, 5, 2, dtype=torch.int64).cuda()
+    ch[0, 2, 0], ch[0, 2, 1], ch[1, 1, 0] = 0, 1, 0
+    X = torch.randn(70, 2).cuda()
+    y = sr.evaluation.evaluate(X, ops, ch, torch.zeros(3, 5).cuda())
+    assert torch.equal(y[0, 2], X[:, 0] + X[:, 1])
+    assert torch.equal(y[1, 1], torch.sin(X[:, 0])) or torch.allclose(y[1, 1], torch.sin(X[:, 0]), atol=1e-6)
+    assert torch.isnan(y[0, 3:]).all() and torch.isnan(y[1, 2:]).all() and torch.isnan(y[2, 1:]).all()
+
+
+def test_empty_inputs():
+    sr = _sr()
+    X = torch.randn(5, 1).cuda()
+    y = sr.evaluation.evaluate(X, torch.zeros(0, 3, dtype=torch.int64).cuda(),
+                               -torch.ones(0, 3, 2, dtype=torch.int64).cuda(), torch.zeros(0, 3).cuda())
+    assert y.shape == (0, 3, 5)
+    y = sr.evaluation.evaluate(torch.randn(0, 1).cuda(), torch.full((2, 1), 50, dtype=torch.int64).cuda(),
+                               -torch.ones(2, 1, 2, dtype=torch.int64).cuda(), torch.zeros(2, 1).cuda())
+    assert y.shape == (2, 1, 0)
+
+
+def test_create_constants_rng_stream():
+    """Same RNG draws as the reference (symbolic_torch/utils.py:7-41) on the same device."""
+    sr = _sr()
+    ops = torch.tensor([[50, 1, 42, 1, 40], [1, 1, 40, 0, 0], [50, 0, 0, 0, 0]], dtype=torch.int64).cuda()
+    for method, kw in (("randn", {"mean": 0.5, "std": 2.0}), ("range", {"lower": -1.0, "upper": 3.0})):
+        torch.manual_seed(123)
+        mine = sr.create_constants(ops, method=method, **kw)
+        torch.manual_seed(123)
+        mask = ops == 1
+        n = int(mask.sum())
+        if method == "randn":
+            flat = torch.randn(n, dtype=torch.float32, device="cuda") * kw["std"] + kw["mean"]
+        else:
+            flat = torch.rand(n, dtype=torch.float32, device="cuda") * (kw["upper"] - kw["lower"]) + kw["lower"]
+        ref = torch.zeros(ops.shape, dtype=torch.float32, device="cuda")
+        ref[mask] = flat
+        assert torch.equal(mine, ref)
+    # non-contiguous view: row-major order of the view
+    torch.manual_seed(5)
+    mine = sr.create_constants(ops.t())
+    torch.manual_seed(5)
+    m = ops.t() == 1
+    ref = torch.zeros(m.shape, device="cuda")
+    ref[m] = torch.randn(int(m.sum()), device="cuda")
+    assert torch.equal(mine, ref)
+
+
+@pytest.mark.parametrize("B", [1, 1000, 70001])
+def test_create_constants_large(B):
+    sr = _sr()
+    torch.manual_seed(0)
+    ops = torch.randint(0, 3, (B, 33), device="cuda")
+    torch.manual_seed(1)
+    mine = sr.create_constants(ops)
+    torch.manual_seed(1)
+    m = ops == 1
+    ref = torch.zeros(m.shape, device="cuda")
+    ref[m] = torch.randn(int(m.sum()), device="cuda")
+    assert torch.equal(mine, ref)

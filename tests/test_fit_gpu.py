@@ -1,0 +1,225 @@
+"""GPU parity of optimize() (the fused batched L-BFGS kernel).
+
+References: the reference's own optimize() outputs (tests/golden) and the CPU
+oracle's per-problem restatement.  Tolerances, as stated for the fitted MSE:
+within 1e-4 relative at equal iteration counts.  Trajectories of ill-conditioned
+problems diverge from ulp-level differences (different libm, different summation
+order), so agreement is asserted on the fraction of problems and on the median.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _sr():
+    import cudasymbolicregression_gb300 as sr
+    return sr
+
+
+def cuda(a, dtype=None):
+    t = torch.as_tensor(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+def mse(Yf, Y):
+    return ((np.asarray(Yf, np.float64) - np.asarray(Y, np.float64)) ** 2).mean(1)
+
+
+def rel_close(a, b, rtol):
+    with np.errstate(invalid="ignore", divide="ignore"):
+        r = np.abs(a - b) / np.maximum(np.abs(b), 1e-30)
+    return (r <= rtol) | (np.isnan(a) & np.isnan(b)) | (a == b)
+
+
+def test_linear_known_answer(golden):
+    """reference tests/test_optimization.py:10-80."""
+    sr = _sr()
+    g = golden("optimize_linear")
+    C_init = cuda(g["C"])
+    Cf, Yf = sr.optimize(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), C_init)
+    Cf = Cf.cpu().numpy()
+    np.testing.assert_allclose(Cf[:, 1], [2.5, -1.5], atol=1e-3)
+    np.testing.assert_allclose(Cf[:, 3], [0.5, 3.0], atol=1e-3)
+    mask = g["ops"] == 1
+    np.testing.assert_array_equal(Cf[~mask], g["C"][~mask])
+    np.testing.assert_allclose(Yf.cpu().numpy(), g["Y"], atol=1e-3)
+    np.testing.assert_allclose(Cf, g["C_final"], rtol=1e-4, atol=1e-5)
+
+
+@pytest.mark.parametrize("name,ls,min_frac", [("optimize_readme", "strong_wolfe", 0.9),
+                                              ("optimize_ragged", "strong_wolfe", 0.7),
+                                              ("optimize_ragged_bt", "backtracking", 0.8)])
+def test_matches_reference_golden(golden, name, ls, min_frac):
+    sr = _sr()
+    g = golden(name)
+    r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]),
+                       max_iter=int(g["max_iter"]), line_search_fn=ls)
+    m_gpu = mse(r.Y.cpu().numpy(), g["Y"])
+    m_ref = mse(g["Y_final"], g["Y"])
+    assert rel_close(m_gpu, m_ref, 1e-4).mean() >= min_frac
+    assert np.nanmedian(m_gpu) <= np.nanmedian(m_ref) * 1.05 + 1e-6
+    # NaN placement of the constants: NaN expressions end with every slot NaN
+    nan_ref = np.isnan(g["C_final"]).all(1)
+    nan_gpu = np.isnan(r.C.cpu().numpy()).all(1)
+    assert (nan_ref == nan_gpu).mean() >= min_frac
+
+
+@pytest.mark.parametrize("ls", ["strong_wolfe", "backtracking"])
+def test_matches_oracle_kernel_arithmetic(golden, ls):
+    """The oracle in the kernel's arithmetic (double dots): equal iteration counts
+    and final MSE within 1e-4 for the large majority of problems."""
+    sr = _sr()
+    g = golden("optimize_ragged")
+    mi = 25
+    r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=mi,
+                       line_search_fn=ls)
+    o = oracle.optimize(g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=mi, dot_mode=1, line_search_fn=ls)
+    it_gpu = r.iters.cpu().numpy()
+    same_it = it_gpu == o["iters"]
+    assert same_it.mean() >= 0.75
+    close = rel_close(mse(r.Y.cpu().numpy(), g["Y"]), mse(o["Y"], g["Y"]), 1e-4)
+    assert close[same_it].mean() >= 0.8
+    # the kernel's reported loss is the MSE of its own Y_final
+    m = mse(r.Y.cpu().numpy(), g["Y"])
+    fin = np.isfinite(m)
+    np.testing.assert_allclose(r.loss.cpu().numpy()[fin], m[fin], rtol=1e-5, atol=1e-6)
+
+
+def test_initial_closure_matches_oracle(golden):
+    """max_iter=0: only the first closure runs; C is returned unchanged."""
+    sr = _sr()
+    g = golden("optimize_ragged")
+    r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=0)
+    o = oracle.optimize(g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=0, dot_mode=1)
+    np.testing.assert_array_equal(r.C.cpu().numpy(), g["C"])
+    a, b = r.loss.cpu().numpy(), o["loss"]
+    assert rel_close(a, b, 1e-5).all()
+    assert (r.iters.cpu().numpy() == 0).all()
+
+
+def _rosenbrock_tape():
+    """f = (1 - c0)^2 + 100 (c1 - c0^2)^2 as a postfix tape over two constants."""
+    ops = [2, 1, 41, 14, 1, 14, 41, 14, 6, 6, 42, 5, 42, 42, 40]
+    ch = [(-1, -1), (-1, -1), (0, 1), (2, -1), (-1, -1), (1, -1), (4, 5), (6, -1), (-1, -1), (-1, -1), (8, 9),
+          (-1, -1), (10, 11), (12, 7), (3, 13)]
+    return np.array(ops, np.int64), np.array(ch, np.int64)
+
+
+@pytest.mark.parametrize("ls,key", [("strong_wolfe", "x_wolfe"), ("backtracking", "x_backtracking")])
+def test_rosenbrock_known_answer(golden, ls, key):
+    """reference tests/test_lbfgs_batch.py:38-75 through the raw-objective mode."""
+    sr = _sr()
+    g = golden("rosenbrock")
+    x0 = g["x0"]  # (2, B)
+    B = x0.shape[1]
+    ops1, ch1 = _rosenbrock_tape()
+    M = ops1.shape[0]
+    ops = np.tile(ops1, (B, 1))
+    ch = np.tile(ch1, (B, 1, 1))
+    C = np.zeros((B, M), np.float32)
+    C[:, 1] = x0[0]
+    C[:, 4] = x0[1]
+    X = np.zeros((1, 1), np.float32)
+    r = sr.optimize_ex(cuda(X), None, cuda(ops), cuda(ch), cuda(C), max_iter=250, history_size=15,
+                       line_search_fn=ls, objective=1)
+    Cf = r.C.cpu().numpy()
+    np.testing.assert_allclose(Cf[:, 1], 1.0, atol=1e-3)
+    np.testing.assert_allclose(Cf[:, 4], 1.0, atol=1e-3)
+    np.testing.assert_allclose(Cf[:, 1], g[key][0], atol=1e-3)
+    np.testing.assert_allclose(Cf[:, 4], g[key][1], atol=1e-3)
+    o = oracle.optimize(X, None, ops, ch, C, max_iter=250, history_size=15, line_search_fn=ls, dot_mode=1)
+    np.testing.assert_allclose(Cf[:, [1, 4]], o["C"][:, [1, 4]], atol=1e-4)
+
+
+def test_error_all_noop_row():
+    """An all-NO_OP row sends a NaN gradient into a NO_OP node: error 201, as the reference."""
+    sr = _sr()
+    ops = torch.tensor([[50, 1, 40], [0, 0, 0]], dtype=torch.int64).cuda()
+    ch = -torch.ones(2, 3, 2, dtype=torch.int64).cuda()
+    ch[0, 2, 0], ch[0, 2, 1] = 0, 1
+    X = torch.randn(10, 1).cuda()
+    Y = torch.randn(2, 10).cuda()
+    with pytest.raises(RuntimeError, match="A non-zero gradient was passed to a NO_OP node"):
+        sr.optimize(X, Y, ops, ch, torch.zeros(2, 3).cuda())
+
+
+def test_error_division_by_zero():
+    sr = _sr()
+    # C / X0 with X0 = 0 at one point
+    ops = torch.tensor([[1, 50, 43]], dtype=torch.int64).cuda()
+    ch = -torch.ones(1, 3, 2, dtype=torch.int64).cuda()
+    ch[0, 2, 0], ch[0, 2, 1] = 0, 1
+    X = torch.linspace(-1, 1, 5).reshape(5, 1).cuda()
+    Y = torch.ones(1, 5).cuda()
+    with pytest.raises(RuntimeError, match=r"Gradient for a/b where b = 0"):
+        sr.optimize(X, Y, ops, ch, torch.ones(1, 3).cuda())
+
+
+def test_validation_error_message():
+    sr = _sr()
+    ops = torch.tensor([[50, 40]], dtype=torch.int64).cuda()
+    ch = -torch.ones(1, 2, 2, dtype=torch.int64).cuda()
+    ch[0, 1, 0], ch[0, 1, 1] = 0, 1
+    with pytest.raises(RuntimeError, match="Error during input validation: Validation failed: A child's index"):
+        sr.optimize(torch.randn(4, 1).cuda(), torch.randn(1, 4).cuda(), ops, ch, torch.zeros(1, 2).cuda())
+
+
+def test_nan_expression_poisons_every_slot():
+    """A NaN gradient ends with all M slots NaN (0*NaN in the vector update), as in the reference."""
+    sr = _sr()
+    # log(C * X0) with X0 of both signs: NaN loss and NaN gradient
+    ops = np.array([[1, 50, 42, 13, 0]], np.int64)
+    ch = -np.ones((1, 5, 2), np.int64)
+    ch[0, 2] = (0, 1)
+    ch[0, 3, 0] = 2
+    X = np.linspace(-2, 2, 9, dtype=np.float32).reshape(9, 1)
+    Y = np.zeros((1, 9), np.float32)
+    C = np.array([[0.7, 0, 0, 0, 0]], np.float32)
+    r = sr.optimize_ex(cuda(X), cuda(Y), cuda(ops), cuda(ch), cuda(C), max_iter=5)
+    o = oracle.optimize(X, Y, ops, ch, C, max_iter=5, dot_mode=0)
+    assert np.isnan(o["C"]).all()
+    assert np.isnan(r.C.cpu().numpy()).all()
+
+
+def test_no_constants_and_determinism():
+    from cudasymbolicregression_gb300 import tapes
+    sr = _sr()
+    rng = np.random.default_rng(3)
+    B, M, N = 200, 24, 50
+    X = rng.uniform(-3, 3, (N, 2)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    kc = rng.integers(0, 4, size=B)
+    tb = tapes.generate(B, M, seed=4, lengths=rng.integers(1, M + 1, size=B), const_counts=kc, n_vars=2,
+                        X_screen=X, C_screen=C)
+    Y = rng.standard_normal((B, N)).astype(np.float32)
+    args = (cuda(X), cuda(Y), cuda(tb.ops), cuda(tb.ch), cuda(C))
+    r1 = sr.optimize_ex(*args, max_iter=30)
+    r2 = sr.optimize_ex(*args, max_iter=30)
+    for a, b in ((r1.C, r2.C), (r1.Y, r2.Y), (r1.iters, r2.iters)):
+        assert torch.equal(torch.nan_to_num(a, nan=7.0), torch.nan_to_num(b, nan=7.0))
+    nc = tb.n_consts == 0
+    Cf = r1.C.cpu().numpy()
+    np.testing.assert_array_equal(Cf[nc], C[nc])
+    assert (r1.iters.cpu().numpy()[nc] == 0).all()
+    # a problem's result does not depend on the rest of the batch
+    sub = np.where(~nc)[0][:5]
+    rs = sr.optimize_ex(cuda(X), cuda(Y[sub]), cuda(tb.ops[sub]), cuda(tb.ch[sub]), cuda(C[sub]), max_iter=30)
+    assert torch.equal(torch.nan_to_num(rs.C, nan=7.0), torch.nan_to_num(r1.C[torch.as_tensor(sub).cuda()], nan=7.0))
+
+
+@pytest.mark.parametrize("ppl,wpb", [(1, 1), (2, 4), (4, 2), (1, 8)])
+def test_kernel_shapes_agree(golden, ppl, wpb):
+    """Every launch shape the autotuner may pick gives the same answers."""
+    sr = _sr()
+    g = golden("optimize_readme")
+    base = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=20)
+    r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=20,
+                       points_per_lane=ppl, warps_per_block=wpb)
+    close = rel_close(mse(r.Y.cpu().numpy(), g["Y"]), mse(base.Y.cpu().numpy(), g["Y"]), 1e-4)
+    assert close.mean() >= 0.9
