@@ -612,7 +612,8 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
     for (int s = 0; s < SPL; ++s)
       if (P.real(s)) Cout[(int64_t)S.slot_node[s * 32 + lane] * A.c_sm] = x.v[s];
     if (lane == 0) {
-      if (A.iters_out) A.iters_out[P.b] = it;
+      // a problem whose closures raised an error reports -code instead of its iterations
+      if (A.iters_out) A.iters_out[P.b] = err ? -err : it;
       if (A.loss_out) A.loss_out[P.b] = f;
       if (A.evals_out) A.evals_out[P.b] = evals;
     }

@@ -23,7 +23,7 @@ from .tape import compile_tapes
 class FitResult:
     C: torch.Tensor        # (B, M) fitted constants
     Y: torch.Tensor        # (B, N) root values at the fitted constants
-    iters: torch.Tensor    # (B,) int32 L-BFGS iterations run
+    iters: torch.Tensor    # (B,) int32 L-BFGS iterations run (-code for a problem that hit an error)
     loss: torch.Tensor     # (B,) float32 final mean squared error
     evals: torch.Tensor    # (B,) int32 closures (forward + adjoint passes) evaluated
 
@@ -31,7 +31,7 @@ class FitResult:
 def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, *,
          objective: int = 0, line_search_max_iter: int = 10, eps: float = 1e-10,
          warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
-         order: Optional[torch.Tensor] = None, want_y: bool = True) -> FitResult:
+         order: Optional[torch.Tensor] = None, want_y: bool = True, raise_errors: bool = True) -> FitResult:
     if line_search_fn not in ("strong_wolfe", "backtracking"):
         raise ValueError(f"Invalid line_search_fn: {line_search_fn}. Choose 'strong_wolfe' or 'backtracking'.")
     if Ops.dim() != 2:
@@ -76,7 +76,7 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
                    status, dev)
     _lib.check(rc, "sr_fit_lbfgs")
     code = int(status.item())
-    if code:
+    if code and raise_errors:
         ctx = "input validation" if code in (101, 102) else "symbolic evaluation backward pass"
         raise RuntimeError(error_message(code, ctx))
     return FitResult(C=C_out, Y=Y_out, iters=iters, loss=loss, evals=evals)
@@ -125,6 +125,8 @@ def optimize_ex(X, Y, Ops, Ch, C_init, max_iter=100, history_size=10, tolerance_
 
     Extra keywords: line_search_max_iter, eps, objective (0 = MSE against Y,
     1 = mean of the root value; Y may be None), warps_per_block, points_per_lane,
-    grid_blocks (kernel shape), order (processing order), want_y.
+    grid_blocks (kernel shape), order (processing order), want_y, raise_errors
+    (False: problems whose closures hit error 201/204 are reported through
+    ``iters < 0`` instead of aborting the whole batch as the reference does).
     """
     return _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, **kw)

@@ -119,10 +119,29 @@ def _screen_eval(ops: np.ndarray, ch: np.ndarray, X: np.ndarray, C: np.ndarray) 
     return bad
 
 
+def _exp_under_div(ops: np.ndarray, ch: np.ndarray) -> np.ndarray:
+    """Mask of tapes with an EXP node inside the denominator of a DIV.  exp of a
+    fitted argument can underflow to exactly 0 (or overflow to inf, which turns an
+    enclosing quotient into 0) while L-BFGS extrapolates, and the reference then
+    raises error 204 for the whole batch."""
+    B, M = ops.shape
+    has = np.zeros((B, M), bool)
+    bad = np.zeros(B, bool)
+    rows = np.arange(B)
+    for k in range(M):
+        c0 = np.maximum(ch[:, k, 0], 0)
+        c1 = np.maximum(ch[:, k, 1], 0)
+        h0 = has[rows, c0] & (ch[:, k, 0] >= 0)
+        h1 = has[rows, c1] & (ch[:, k, 1] >= 0)
+        has[:, k] = (ops[:, k] == int(Operator.EXP)) | h0 | h1
+        bad |= (ops[:, k] == int(Operator.DIV)) & h1
+    return bad
+
+
 def generate(B: int, M: int = 64, *, seed: int = 0, lengths=None, mean_length: float | None = None,
              n_vars: int = 4, binary=BIN_DEFAULT, unary=UN_DEFAULT, const_counts=None,
              p_const_leaf: float = 0.2, X_screen: np.ndarray | None = None,
-             C_screen: np.ndarray | None = None) -> TapeBatch:
+             C_screen: np.ndarray | None = None, no_exp_in_denominator: bool = False) -> TapeBatch:
     """Draw B postfix tapes of padded length M.
 
     lengths: (B,) int array of exact tape lengths, or None to draw them from a
@@ -131,6 +150,7 @@ def generate(B: int, M: int = 64, *, seed: int = 0, lengths=None, mean_length: f
       by the number of leaves); None makes every leaf a constant with
       probability ``p_const_leaf`` and otherwise a uniform variable.
     X_screen/C_screen: rows used to reject exact-zero denominators (None skips).
+    no_exp_in_denominator: also redraw tapes with EXP under a DIV denominator.
     """
     rng = np.random.default_rng(seed)
     if lengths is None:
@@ -163,10 +183,12 @@ def generate(B: int, M: int = 64, *, seed: int = 0, lengths=None, mean_length: f
         c = _children(ar)
         ops[todo] = o
         ch[todo] = c
-        if X_screen is None:
+        bad = _exp_under_div(o, c) if no_exp_in_denominator else np.zeros(nb, bool)
+        if X_screen is None and not bad.any():
             break
-        Cs = np.zeros((nb, M), np.float32) if C_screen is None else np.asarray(C_screen, np.float32)[todo]
-        bad = _screen_eval(o, c, np.asarray(X_screen, np.float32), Cs)
+        if X_screen is not None:
+            Cs = np.zeros((nb, M), np.float32) if C_screen is None else np.asarray(C_screen, np.float32)[todo]
+            bad |= _screen_eval(o, c, np.asarray(X_screen, np.float32), Cs)
         todo = todo[bad]
         if todo.size == 0:
             break

@@ -134,6 +134,8 @@ int64_t sr_fit_workspace_bytes(int64_t B, int32_t max_len, int32_t max_consts, c
  * symbolic_torch/optimization.py:9-112, symbolic_torch/lbfgs_batch.py:61-326).
  * C_init/C_out (B, M) use (c_sb, c_sm) strides; Y and Y_final (B, N) are
  * contiguous (Y_final may be NULL); iters_out/loss_out/evals_out (B) may be NULL.
+ * iters_out[b] is the number of L-BFGS iterations run, or -code when a closure
+ * of problem b hit error 201/204 (status_dev then holds the first such code).
  * order_dev (B) int32 gives the processing order (NULL = 0..B-1).
  * max_len: largest root + 1 (stats[2] of sr_tape_compile; 0 = M); max_consts:
  * largest meta[2] (stats[3]).  workspace_dev must hold sr_fit_workspace_bytes(...)

