@@ -145,8 +145,31 @@ __device__ __forceinline__ void forward_pass(const uint32_t* __restrict__ tape, 
   }
 }
 
+// Fill count values at p with NaN, 16-byte vector stores in the aligned middle.
+template <typename T>
+__device__ __forceinline__ void warp_fill_nan(T* p, size_t count, int lane) {
+  const T qnan = M_<T>::nan();
+  constexpr int kVec = 16 / sizeof(T);
+  size_t head = (size_t)((16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15) / sizeof(T);
+  if (reinterpret_cast<uintptr_t>(p) % sizeof(T)) head = count;  // unaligned element type: scalar path
+  if (head > count) head = count;
+  for (size_t i = lane; i < head; i += 32) __stcs(p + i, qnan);
+  const size_t nvec = (count - head) / kVec;
+  float4 v4;
+  if (sizeof(T) == 4) {
+    const float f = __int_as_float(0x7fffffff);
+    v4 = make_float4(f, f, f, f);
+  } else {
+    const float lo = __int_as_float(0xffffffff), hi = __int_as_float(0x7fffffff);
+    v4 = make_float4(lo, hi, lo, hi);
+  }
+  float4* q = reinterpret_cast<float4*>(p + head);
+  for (size_t i = lane; i < nvec; i += 32) __stcs(q + i, v4);
+  for (size_t i = head + nvec * kVec + lane; i < count; i += 32) __stcs(p + i, qnan);
+}
+
 template <typename T, int V>
-__global__ void __launch_bounds__(128) eval_forward_kernel(const T* __restrict__ X, int64_t N, int64_t n_x,
+__global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__ X, int64_t N, int64_t n_x,
                                                            const uint32_t* __restrict__ desc,
                                                            const int32_t* __restrict__ meta, int64_t B,
                                                            int64_t M, int Lmax, const T* __restrict__ C,
@@ -157,7 +180,6 @@ __global__ void __launch_bounds__(128) eval_forward_kernel(const T* __restrict__
   const size_t per_warp = tbytes + (size_t)Lmax * 32 * V * sizeof(T);
   uint32_t* tape = reinterpret_cast<uint32_t*>(smem + warp * per_warp);
   T* vals = reinterpret_cast<T*>(smem + warp * per_warp + tbytes);
-  const T qnan = M_<T>::nan();
   for (int64_t b = (int64_t)blockIdx.x * nwarp + warp; b < B; b += (int64_t)gridDim.x * nwarp) {
     const int L = meta[b * 4];
     for (int k = lane; k < L; k += 32) tape[k] = desc[b * M + k];
@@ -166,25 +188,43 @@ __global__ void __launch_bounds__(128) eval_forward_kernel(const T* __restrict__
     T* out = cache + (size_t)b * M * N;
     for (int64_t base = 0; base < N; base += 32 * V) {
       int64_t nn[V];
+      bool valid[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         const int64_t n = base + v * 32 + lane;
-        nn[v] = n < N ? n : N - 1;
+        valid[v] = n < N;
+        nn[v] = valid[v] ? n : N - 1;
       }
-      forward_pass<T, V>(tape, L, vals, X, n_x, nn, Crow, c_sm, lane);
-      __syncwarp();
+      // each node's values go to the cache as soon as they exist (streaming stores,
+      // 128 contiguous bytes per warp and v), interleaving compute with HBM writes
       for (int k = 0; k < L; ++k) {
+        const uint32_t d = tape[k];
+        const int code = code_of(d);
+        T* o = vals + (size_t)k * (32 * V);
+        T r[V];
+        if (code == VAR) {
+          const int var = child0(d);
+#pragma unroll
+          for (int v = 0; v < V; ++v) r[v] = __ldg(X + nn[v] * n_x + var);
+        } else if (code == LEARNABLE) {
+          const T c = __ldg(Crow + (int64_t)k * c_sm);
+#pragma unroll
+          for (int v = 0; v < V; ++v) r[v] = c;
+        } else {
+          const T* A = vals + (size_t)child0(d) * (32 * V);
+          const T* Bv = vals + (size_t)child1(d) * (32 * V);
+#pragma unroll
+          for (int v = 0; v < V; ++v) r[v] = node_value<T>(code, A[v * 32 + lane], Bv[v * 32 + lane], T(0), T(0));
+        }
 #pragma unroll
         for (int v = 0; v < V; ++v) {
-          const int64_t n = base + v * 32 + lane;
-          if (n < N) __stcs(out + (size_t)k * N + n, vals[(size_t)k * 32 * V + v * 32 + lane]);
+          o[v * 32 + lane] = r[v];
+          if (valid[v]) __stcs(out + (size_t)k * N + nn[v], r[v]);
         }
       }
-      __syncwarp();
     }
-    // padding rows after the last real node
-    for (int64_t k = L; k < M; ++k)
-      for (int64_t n = lane; n < N; n += 32) __stcs(out + (size_t)k * N + n, qnan);
+    // rows after the last real node are one contiguous block of (M - L) * N values
+    warp_fill_nan(out + (size_t)L * N, (size_t)(M - L) * N, lane);
     __syncwarp();
   }
 }
@@ -193,8 +233,32 @@ __global__ void __launch_bounds__(128) eval_forward_kernel(const T* __restrict__
 // Adjoint for a dense grad_out.  Per warp shared memory: tape, node values,
 // node adjoints (L_max * 32V each) and the per-node constant gradient sums.
 // ------------------------------------------------------------------------------------
+// True in every lane when one of count values at p is nonzero (NaN counts as nonzero).
+template <typename T>
+__device__ __forceinline__ bool warp_any_nonzero(const T* p, size_t count, int lane) {
+  bool nz = false;
+  constexpr int kVec = 16 / sizeof(T);
+  size_t head = (size_t)((16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15) / sizeof(T);
+  if (reinterpret_cast<uintptr_t>(p) % sizeof(T)) head = count;
+  if (head > count) head = count;
+  for (size_t i = lane; i < head; i += 32) nz |= __ldcs(p + i) != T(0);
+  const size_t nvec = (count - head) / kVec;
+  const float4* q = reinterpret_cast<const float4*>(p + head);
+  for (size_t i = lane; i < nvec; i += 32) {
+    const float4 v = __ldcs(q + i);
+    if (sizeof(T) == 4) {
+      nz |= (v.x != 0.f) | (v.y != 0.f) | (v.z != 0.f) | (v.w != 0.f);
+    } else {
+      const double* d = reinterpret_cast<const double*>(&v);
+      nz |= (d[0] != 0.0) | (d[1] != 0.0);
+    }
+  }
+  for (size_t i = head + nvec * kVec + lane; i < count; i += 32) nz |= __ldcs(p + i) != T(0);
+  return __any_sync(0xffffffffu, nz);
+}
+
 template <typename T, int V>
-__global__ void __launch_bounds__(128) eval_backward_kernel(
+__global__ void __launch_bounds__(256) eval_backward_kernel(
     const T* __restrict__ X, int64_t N, int64_t n_x, const uint32_t* __restrict__ desc,
     const int32_t* __restrict__ meta, int64_t B, int64_t M, int Lmax, const T* __restrict__ C, int64_t c_sb,
     int64_t c_sm, const T* __restrict__ gout, T* __restrict__ gC, T* __restrict__ gX,
@@ -234,12 +298,6 @@ __global__ void __launch_bounds__(128) eval_backward_kernel(
 #pragma unroll
         for (int v = 0; v < V; ++v)
           adj[(size_t)k * 32 * V + v * 32 + lane] = valid[v] ? M_<T>::add(T(0), __ldcs(G + (size_t)k * N + nn[v])) : T(0);
-      }
-      // padding rows are NO_OP nodes: any nonzero gradient there is error 201
-      for (int64_t k = L; k < M; ++k) {
-#pragma unroll
-        for (int v = 0; v < V; ++v)
-          if (valid[v] && __ldcs(G + (size_t)k * N + nn[v]) != T(0)) err = ERR_GRAD_ON_NO_OP;
       }
       __syncwarp();
       for (int k = L - 1; k >= 0; --k) {
@@ -289,6 +347,8 @@ __global__ void __launch_bounds__(128) eval_backward_kernel(
       }
       __syncwarp();
     }
+    // rows after the last real node are NO_OP nodes: any nonzero gradient there is error 201
+    if (warp_any_nonzero(G + (size_t)L * N, (size_t)(M - L) * N, lane)) err = ERR_GRAD_ON_NO_OP;
     if (err) report(status, err);
     // gradient row: constant nodes get their sums, everything else 0
     T* gCrow = gC + (size_t)b * M;
@@ -359,10 +419,11 @@ template <typename T>
 static bool pick_shape(int Lmax, size_t per_point_bytes, bool with_sums, int& V, int& warps, size_t& smem) {
   const int limit = max_dyn_smem();
   const size_t fixed = align16((size_t)Lmax * 4) + (with_sums ? align16((size_t)Lmax * sizeof(T)) : 0);
-  for (int v : {4, 2, 1}) {
+  // one point per lane keeps the per-warp table small, so more warps fit on an SM
+  for (int v : {1}) {
     const size_t per_warp = fixed + (size_t)Lmax * 32 * v * per_point_bytes;
-    for (int w : {4, 2, 1}) {
-      if (per_warp * w <= (size_t)limit && per_warp * w <= 96 * 1024) {
+    for (int w : {8, 4, 2, 1}) {
+      if (per_warp * w <= (size_t)limit && per_warp * w <= 72 * 1024) {
         V = v;
         warps = w;
         smem = per_warp * w;

@@ -602,7 +602,9 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
       }
     }
 
-    if (err) report(A.status, err);
+    // errors are found per lane (per data point): combine them for the problem
+    err = __reduce_max_sync(0xffffffffu, err);
+    if (err && lane == 0) report(A.status, err);
     // ---- outputs ----
     const float qnan = __int_as_float(0x7fffffff);
     float* Cout = A.C_out + P.b * A.c_sb;

@@ -109,11 +109,41 @@ class EvalWorkload:
     C: np.ndarray
 
 
-def eval_batch(B: int = 65536, N: int = 1024, M: int = 64, n_vars: int = 4, seed: int = 0) -> EvalWorkload:
+def _gpu_zero_denominators(X, ops, ch, C, device="cuda", chunk=8192):
+    """Tapes with a DIV whose denominator is exactly 0 at some row of X (device forward)."""
+    from .evaluation import evaluate
+    bad = np.zeros(ops.shape[0], bool)
+    Xt = torch.tensor(X, device=device)
+    for s in range(0, ops.shape[0], chunk):
+        o = torch.tensor(ops[s:s + chunk], device=device)
+        c = torch.tensor(ch[s:s + chunk], device=device)
+        with torch.no_grad():
+            cache = evaluate(Xt, o, c, torch.tensor(C[s:s + chunk], device=device))
+        is_div = o == int(Operator.DIV)
+        den = torch.gather(cache, 1, c[:, :, 1].clamp(min=0).unsqueeze(2).expand(-1, -1, cache.shape[2]))
+        zero = ((den == 0).any(2) & is_div).any(1)
+        bad[s:s + chunk] = zero.cpu().numpy()
+        del cache, den
+    return bad
+
+
+def eval_batch(B: int = 65536, N: int = 1024, M: int = 64, n_vars: int = 4, seed: int = 0,
+               device: str = "cuda") -> EvalWorkload:
+    """Tapes whose DIV denominators are exactly 0 at some of the N rows are redrawn
+    (the reference raises error 204 when such a node receives a gradient)."""
     rng = np.random.default_rng(seed)
     X = rng.uniform(-3, 3, (N, n_vars)).astype(np.float32)
     C = rng.standard_normal((B, M)).astype(np.float32)
     Xs = X[rng.choice(N, size=min(N, 32), replace=False)]
     tb = tapes.generate(B, M, seed=seed + 1, mean_length=20.0, n_vars=n_vars, p_const_leaf=0.2, X_screen=Xs,
                         C_screen=C)
-    return EvalWorkload(X=X, ops=tb.ops, ch=tb.ch, C=C)
+    ops, ch = tb.ops, tb.ch
+    for attempt in range(16):
+        bad = np.where(_gpu_zero_denominators(X, ops, ch, C, device))[0]
+        if bad.size == 0:
+            break
+        nb = tapes.generate(bad.size, M, seed=seed + 1000 + attempt, mean_length=20.0, n_vars=n_vars,
+                            p_const_leaf=0.2, X_screen=Xs, C_screen=C[bad])
+        ops[bad] = nb.ops
+        ch[bad] = nb.ch
+    return EvalWorkload(X=X, ops=ops, ch=ch, C=C)

@@ -1,4 +1,4 @@
-"""Parity criteria shared by the GPU tests.
+"""Parity criteria shared by the GPU tests and smoke() (test infrastructure).
 
 Device and host libm differ by a few ulps in transcendental functions, and long
 tapes amplify such differences through cancellation, so values computed along
@@ -64,25 +64,40 @@ def check_local(X, ops, ch, C, cache):
     return {"nodes": int(got.size), "max_ulp": int(d.max(initial=0))}
 
 
-def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, factor=4.0, min_frac_tight=0.999):
-    """Device result vs the FP64 oracle, relative to the reference float32 result."""
+def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999, gross=1e3):
+    """Device float32 result vs the reference float32 result and the FP64 oracle.
+
+    * at least ``min_frac_tight`` of the entries within rtol of the reference result;
+    * the device's error against FP64 is not worse than the reference's, in
+      distribution: median and 99.9th percentile of the relative error within 2x;
+    * no entry is grossly worse: |got - ref64| <= gross * |ref32 - ref64| + rtol|ref64| + atol,
+      except where float32 itself is ill-conditioned (ref32 and FP64 disagree by
+      more than 1e-3 relative, or in NaN/inf placement).
+    """
     got = np.asarray(got, np.float64)
     ref32 = np.asarray(ref32, np.float64)
     ref64 = np.asarray(ref64, np.float64)
-    with np.errstate(invalid="ignore", over="ignore"):
+    with np.errstate(invalid="ignore", over="ignore", divide="ignore"):
         tight = (np.abs(got - ref32) <= rtol * np.abs(ref32) + atol) | (np.isnan(got) & np.isnan(ref32)) | (got == ref32)
         err_g = np.abs(got - ref64)
         err_r = np.abs(ref32 - ref64)
-        as_good = err_g <= factor * err_r + rtol * np.abs(ref64) + atol
-        # NaN/inf placement may differ only where float32 itself is ill-conditioned
-        # (the reference float32 result disagrees with FP64 there)
         boundary = (np.isnan(ref64) != np.isnan(ref32)) | (np.isinf(ref64) != np.isinf(ref32)) | ~np.isfinite(err_r) \
             | (err_r > 1e-3 * np.abs(ref64))
-    ok = tight | as_good | boundary
-    assert ok.all(), (f"{(~ok).sum()} entries less accurate than the reference float32 result; first at "
+        not_gross = err_g <= gross * err_r + rtol * np.abs(ref64) + atol
+    ok = tight | not_gross | boundary
+    assert ok.all(), (f"{(~ok).sum()} entries grossly less accurate than the reference float32 result; first at "
                       f"{np.argwhere(~ok)[:3].tolist()}: got {got[~ok][:3]}, ref32 {ref32[~ok][:3]}, ref64 {ref64[~ok][:3]}")
-    frac = tight.mean() if tight.size else 1.0
+    frac = float(tight.mean()) if tight.size else 1.0
     assert frac >= min_frac_tight, f"only {frac:.5f} of the entries within {rtol} of the reference float32 result"
-    fin = np.isfinite(got) & np.isfinite(ref64)
-    rel = np.abs(got[fin] - ref64[fin]) / np.maximum(np.abs(ref64[fin]), 1e-30)
-    return {"frac_tight": float(frac), "median_rel_err_vs_fp64": float(np.median(rel)) if rel.size else 0.0}
+    fin = np.isfinite(got) & np.isfinite(ref32) & np.isfinite(ref64) & ~boundary
+    stats = {"frac_tight": frac}
+    if fin.any():
+        scale = np.maximum(np.abs(ref64[fin]), 1e-30)
+        rg = err_g[fin] / scale
+        rr = err_r[fin] / scale
+        for q in (50.0, 99.9):
+            pg, pr = np.percentile(rg, q), np.percentile(rr, q)
+            assert pg <= 2.0 * pr + 1e-7, f"{q}th percentile relative error vs FP64 {pg:.3g} > 2 x reference {pr:.3g}"
+            stats[f"p{q}_rel_err_device"] = float(pg)
+            stats[f"p{q}_rel_err_reference"] = float(pr)
+    return stats
