@@ -42,10 +42,12 @@ _SIGS = {
     "sr_version": ([], ctypes.c_char_p),
     "sr_validate": ([vp, vp, i64, i64, i64, i64, i64, i64, i64, vp, vp], ctypes.c_int),
     "sr_tape_compile": ([vp, vp, i64, i64, i64, i64, i64, i64, i64, i32, vp, vp, vp, vp], ctypes.c_int),
-    "sr_eval_forward_f32": ([vp, i64, i64, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp], ctypes.c_int),
-    "sr_eval_forward_f64": ([vp, i64, i64, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp], ctypes.c_int),
-    "sr_eval_backward_f32": ([vp, i64, i64, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp], ctypes.c_int),
-    "sr_eval_backward_f64": ([vp, i64, i64, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp], ctypes.c_int),
+    "sr_eval_forward_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp], ctypes.c_int),
+    "sr_eval_forward_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp], ctypes.c_int),
+    "sr_eval_backward_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp],
+                             ctypes.c_int),
+    "sr_eval_backward_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp],
+                             ctypes.c_int),
     "sr_fit_workspace_bytes": ([i64, i32, i32, ctypes.POINTER(FitOptions)], i64),
     "sr_fit_lbfgs": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, vp, vp, i32, i32,
                       ctypes.POINTER(FitOptions), vp, i64, vp, vp], ctypes.c_int),

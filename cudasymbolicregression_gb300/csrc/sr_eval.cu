@@ -113,37 +113,12 @@ __global__ void __launch_bounds__(256) tape_compile_kernel(const int64_t* __rest
 }
 
 // ------------------------------------------------------------------------------------
-// Forward.  V points per lane per pass (point = base + v*32 + lane).
-// Shared memory per warp: M tape words + L_max * 32V node values.
+// Forward.  Work unit = (tape, slice of at most kSlice points); units are taken in
+// grid-stride order over the tapes sorted longest first, so every warp of the
+// persistent grid gets a similar mix of long and short tapes.  One point per lane:
+// the per-warp node table is L_max * 128 bytes, which keeps ~24 warps per SM.
 // ------------------------------------------------------------------------------------
-template <typename T, int V>
-__device__ __forceinline__ void forward_pass(const uint32_t* __restrict__ tape, int L, T* __restrict__ vals,
-                                             const T* __restrict__ X, int64_t n_x, const int64_t* nn,
-                                             const T* __restrict__ Crow, int64_t c_sm, int lane) {
-  for (int k = 0; k < L; ++k) {
-    const uint32_t d = tape[k];
-    const int code = code_of(d);
-    T* out = vals + (size_t)k * (32 * V);
-    if (code == VAR) {
-      const int var = child0(d);
-#pragma unroll
-      for (int v = 0; v < V; ++v) out[v * 32 + lane] = __ldg(X + nn[v] * n_x + var);
-    } else if (code == LEARNABLE) {
-      const T c = __ldg(Crow + (int64_t)k * c_sm);
-#pragma unroll
-      for (int v = 0; v < V; ++v) out[v * 32 + lane] = c;
-    } else {
-      const T* A = vals + (size_t)child0(d) * (32 * V);
-      const T* Bv = vals + (size_t)child1(d) * (32 * V);
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        const T a = A[v * 32 + lane];
-        const T b = Bv[v * 32 + lane];
-        out[v * 32 + lane] = node_value<T>(code, a, b, T(0), T(0));
-      }
-    }
-  }
-}
+constexpr int kSlice = 256;
 
 // Fill count values at p with NaN, 16-byte vector stores in the aligned middle.
 template <typename T>
@@ -168,71 +143,76 @@ __device__ __forceinline__ void warp_fill_nan(T* p, size_t count, int lane) {
   for (size_t i = head + nvec * kVec + lane; i < count; i += 32) __stcs(p + i, qnan);
 }
 
-template <typename T, int V>
+// Node values of one tape at the 32 points nn (one per lane) into vals[k][lane];
+// with `out` also streamed to the cache rows as they are produced.
+template <typename T>
+__device__ __forceinline__ void forward_points(const uint32_t* __restrict__ tape, int L, T* __restrict__ vals,
+                                               const T* __restrict__ X, int64_t n_x, int64_t nn, bool valid,
+                                               const T* __restrict__ Crow, int64_t c_sm, int lane,
+                                               T* __restrict__ out, int64_t N) {
+  for (int k = 0; k < L; ++k) {
+    const uint32_t d = tape[k];
+    const int code = code_of(d);
+    T r;
+    if (code == VAR) {
+      r = __ldg(X + nn * n_x + child0(d));
+    } else if (code == LEARNABLE) {
+      r = __ldg(Crow + (int64_t)k * c_sm);
+    } else {
+      r = node_value<T>(code, vals[child0(d) * 32 + lane], vals[child1(d) * 32 + lane], T(0), T(0));
+    }
+    vals[k * 32 + lane] = r;
+    if (out && valid) __stcs(out + (size_t)k * N + nn, r);
+  }
+}
+
+template <typename T>
 __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__ X, int64_t N, int64_t n_x,
                                                            const uint32_t* __restrict__ desc,
-                                                           const int32_t* __restrict__ meta, int64_t B,
+                                                           const int32_t* __restrict__ meta,
+                                                           const int32_t* __restrict__ order, int64_t B,
                                                            int64_t M, int Lmax, const T* __restrict__ C,
                                                            int64_t c_sb, int64_t c_sm, T* __restrict__ cache) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const size_t tbytes = align16((size_t)Lmax * 4);
-  const size_t per_warp = tbytes + (size_t)Lmax * 32 * V * sizeof(T);
+  const size_t per_warp = tbytes + (size_t)Lmax * 32 * sizeof(T);
   uint32_t* tape = reinterpret_cast<uint32_t*>(smem + warp * per_warp);
   T* vals = reinterpret_cast<T*>(smem + warp * per_warp + tbytes);
-  for (int64_t b = (int64_t)blockIdx.x * nwarp + warp; b < B; b += (int64_t)gridDim.x * nwarp) {
+  const int64_t nslices = (N + kSlice - 1) / kSlice;
+  const int64_t units = B * nslices;
+  for (int64_t u = (int64_t)blockIdx.x * nwarp + warp; u < units; u += (int64_t)gridDim.x * nwarp) {
+    const int64_t ti = u / nslices, sl = u - ti * nslices;
+    const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
     for (int k = lane; k < L; k += 32) tape[k] = desc[b * M + k];
     __syncwarp();
     const T* Crow = C + b * c_sb;
     T* out = cache + (size_t)b * M * N;
-    for (int64_t base = 0; base < N; base += 32 * V) {
-      int64_t nn[V];
-      bool valid[V];
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        const int64_t n = base + v * 32 + lane;
-        valid[v] = n < N;
-        nn[v] = valid[v] ? n : N - 1;
-      }
-      // each node's values go to the cache as soon as they exist (streaming stores,
-      // 128 contiguous bytes per warp and v), interleaving compute with HBM writes
-      for (int k = 0; k < L; ++k) {
-        const uint32_t d = tape[k];
-        const int code = code_of(d);
-        T* o = vals + (size_t)k * (32 * V);
-        T r[V];
-        if (code == VAR) {
-          const int var = child0(d);
-#pragma unroll
-          for (int v = 0; v < V; ++v) r[v] = __ldg(X + nn[v] * n_x + var);
-        } else if (code == LEARNABLE) {
-          const T c = __ldg(Crow + (int64_t)k * c_sm);
-#pragma unroll
-          for (int v = 0; v < V; ++v) r[v] = c;
-        } else {
-          const T* A = vals + (size_t)child0(d) * (32 * V);
-          const T* Bv = vals + (size_t)child1(d) * (32 * V);
-#pragma unroll
-          for (int v = 0; v < V; ++v) r[v] = node_value<T>(code, A[v * 32 + lane], Bv[v * 32 + lane], T(0), T(0));
-        }
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-          o[v * 32 + lane] = r[v];
-          if (valid[v]) __stcs(out + (size_t)k * N + nn[v], r[v]);
-        }
-      }
+    const int64_t n0 = sl * kSlice, n1 = min(N, n0 + kSlice);
+    for (int64_t base = n0; base < n1; base += 32) {
+      const int64_t n = base + lane;
+      const bool valid = n < n1;
+      forward_points<T>(tape, L, vals, X, n_x, valid ? n : n1 - 1, valid, Crow, c_sm, lane, out, N);
     }
-    // rows after the last real node are one contiguous block of (M - L) * N values
-    warp_fill_nan(out + (size_t)L * N, (size_t)(M - L) * N, lane);
+    // rows after the last real node: NaN (one contiguous block when the unit spans all points)
+    if (nslices == 1) {
+      warp_fill_nan(out + (size_t)L * N, (size_t)(M - L) * N, lane);
+    } else {
+      for (int64_t k = L; k < M; ++k) warp_fill_nan(out + (size_t)k * N + n0, (size_t)(n1 - n0), lane);
+    }
     __syncwarp();
   }
 }
 
 // ------------------------------------------------------------------------------------
-// Adjoint for a dense grad_out.  Per warp shared memory: tape, node values,
-// node adjoints (L_max * 32V each) and the per-node constant gradient sums.
+// Adjoint for a dense grad_out.  One warp per tape (tapes in the same longest-first
+// grid-stride order); per-warp shared memory: tape, node values, node adjoints and
+// per-node constant-gradient sums, all for one point per lane.  The gradient of a
+// constant is summed over points in a fixed order (per lane, then a butterfly), so
+// grad_C is deterministic.
 // ------------------------------------------------------------------------------------
+
 // True in every lane when one of count values at p is nonzero (NaN counts as nonzero).
 template <typename T>
 __device__ __forceinline__ bool warp_any_nonzero(const T* p, size_t count, int lane) {
@@ -257,23 +237,24 @@ __device__ __forceinline__ bool warp_any_nonzero(const T* p, size_t count, int l
   return __any_sync(0xffffffffu, nz);
 }
 
-template <typename T, int V>
+template <typename T>
 __global__ void __launch_bounds__(256) eval_backward_kernel(
     const T* __restrict__ X, int64_t N, int64_t n_x, const uint32_t* __restrict__ desc,
-    const int32_t* __restrict__ meta, int64_t B, int64_t M, int Lmax, const T* __restrict__ C, int64_t c_sb,
-    int64_t c_sm, const T* __restrict__ gout, T* __restrict__ gC, T* __restrict__ gX,
-    int32_t* __restrict__ status) {
+    const int32_t* __restrict__ meta, const int32_t* __restrict__ order, int64_t B, int64_t M, int Lmax,
+    const T* __restrict__ C, int64_t c_sb, int64_t c_sm, const T* __restrict__ gout, T* __restrict__ gC,
+    T* __restrict__ gX, int32_t* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const size_t tbytes = align16((size_t)Lmax * 4);
-  const size_t vbytes = (size_t)Lmax * 32 * V * sizeof(T);
+  const size_t vbytes = (size_t)Lmax * 32 * sizeof(T);
   const size_t per_warp = tbytes + 2 * vbytes + align16((size_t)Lmax * sizeof(T));
   unsigned char* base_ptr = smem + warp * per_warp;
   uint32_t* tape = reinterpret_cast<uint32_t*>(base_ptr);
   T* vals = reinterpret_cast<T*>(base_ptr + tbytes);
   T* adj = reinterpret_cast<T*>(base_ptr + tbytes + vbytes);
   T* gsum = reinterpret_cast<T*>(base_ptr + tbytes + 2 * vbytes);
-  for (int64_t b = (int64_t)blockIdx.x * nwarp + warp; b < B; b += (int64_t)gridDim.x * nwarp) {
+  for (int64_t ti = (int64_t)blockIdx.x * nwarp + warp; ti < B; ti += (int64_t)gridDim.x * nwarp) {
+    const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
     for (int k = lane; k < L; k += 32) {
       tape[k] = desc[b * M + k];
@@ -283,73 +264,52 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
     const T* Crow = C + b * c_sb;
     const T* G = gout + (size_t)b * M * N;
     int err = 0;
-    for (int64_t base = 0; base < N; base += 32 * V) {
-      int64_t nn[V];
-      bool valid[V];
+    for (int64_t base = 0; base < N; base += 32) {
+      const int64_t n = base + lane;
+      const bool valid = n < N;
+      const int64_t nn = valid ? n : N - 1;
+      // adjoint seeds 0 + grad_out (the reference's zeros_like(cache).add_(grad_output)),
+      // loaded four rows at a time so the loads are in flight together
+      int k = 0;
+      for (; k + 4 <= L; k += 4) {
+        T g4[4];
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        const int64_t n = base + v * 32 + lane;
-        valid[v] = n < N;
-        nn[v] = valid[v] ? n : N - 1;
-      }
-      forward_pass<T, V>(tape, L, vals, X, n_x, nn, Crow, c_sm, lane);
-      // adjoint seeds: 0 + grad_out, as the reference's zeros_like(cache).add_(grad_output)
-      for (int k = 0; k < L; ++k) {
+        for (int j = 0; j < 4; ++j) g4[j] = valid ? __ldcs(G + (size_t)(k + j) * N + nn) : T(0);
 #pragma unroll
-        for (int v = 0; v < V; ++v)
-          adj[(size_t)k * 32 * V + v * 32 + lane] = valid[v] ? M_<T>::add(T(0), __ldcs(G + (size_t)k * N + nn[v])) : T(0);
+        for (int j = 0; j < 4; ++j) adj[(k + j) * 32 + lane] = M_<T>::add(T(0), g4[j]);
       }
-      __syncwarp();
-      for (int k = L - 1; k >= 0; --k) {
-        const uint32_t d = tape[k];
+      for (; k < L; ++k) adj[k * 32 + lane] = valid ? M_<T>::add(T(0), __ldcs(G + (size_t)k * N + nn)) : T(0);
+      forward_points<T>(tape, L, vals, X, n_x, nn, valid, Crow, c_sm, lane, nullptr, N);
+      for (int kk = L - 1; kk >= 0; --kk) {
+        const uint32_t d = tape[kk];
         const int code = code_of(d);
-        const T* gk = adj + (size_t)k * 32 * V;
+        const T g = adj[kk * 32 + lane];
         if (code == LEARNABLE) {
-          T part = T(0);
-#pragma unroll
-          for (int v = 0; v < V; ++v) {
-            const T g = gk[v * 32 + lane];
-            if (valid[v] && g != T(0)) part = M_<T>::add(part, g);
-          }
-          part = warp_sum(part);
-          if (lane == 0) gsum[k] = M_<T>::add(gsum[k], part);
+          const T part = warp_sum((valid && g != T(0)) ? g : T(0));
+          if (lane == 0) gsum[kk] = M_<T>::add(gsum[kk], part);
           continue;
         }
         if (code == VAR) {
-          if (gX) {
-            const int var = child0(d);
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-              const T g = gk[v * 32 + lane];
-              if (valid[v] && g != T(0)) atomicAdd(gX + nn[v] * n_x + var, g);
-            }
-          }
+          if (gX && valid && g != T(0)) atomicAdd(gX + nn * n_x + child0(d), g);
           continue;
         }
         const int c0 = child0(d), c1 = child1(d);
-        T* A = adj + (size_t)c0 * 32 * V;
-        T* Bb = adj + (size_t)c1 * 32 * V;
-        const T* av = vals + (size_t)c0 * 32 * V;
-        const T* bv = vals + (size_t)c1 * 32 * V;
-        const T* kv = vals + (size_t)k * 32 * V;
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const int i = v * 32 + lane;
-          bool a0, a1;
-          T o0, o1;
-          const int e = node_adjoint<T>(code, gk[i], av[i], bv[i], kv[i], a0, o0, a1, o1);
-          if (valid[v]) {
-            if (e && !err) err = e;
-            if (a0) A[i] = M_<T>::add(A[i], o0);
-            if (a1) Bb[i] = M_<T>::add(Bb[i], o1);
-          }
+        bool a0, a1;
+        T o0, o1;
+        const int e = node_adjoint<T>(code, g, vals[c0 * 32 + lane], vals[c1 * 32 + lane], vals[kk * 32 + lane], a0,
+                                      o0, a1, o1);
+        if (valid) {
+          if (e && !err) err = e;
+          if (a0) adj[c0 * 32 + lane] = M_<T>::add(adj[c0 * 32 + lane], o0);
+          if (a1) adj[c1 * 32 + lane] = M_<T>::add(adj[c1 * 32 + lane], o1);
         }
       }
-      __syncwarp();
     }
+    __syncwarp();
     // rows after the last real node are NO_OP nodes: any nonzero gradient there is error 201
     if (warp_any_nonzero(G + (size_t)L * N, (size_t)(M - L) * N, lane)) err = ERR_GRAD_ON_NO_OP;
-    if (err) report(status, err);
+    err = __reduce_max_sync(0xffffffffu, err);
+    if (err && lane == 0) report(status, err);
     // gradient row: constant nodes get their sums, everything else 0
     T* gCrow = gC + (size_t)b * M;
     for (int64_t k = lane; k < M; k += 32) {
@@ -413,53 +373,36 @@ static int launch_compile(const int64_t* ops, const int64_t* ch, int64_t B, int6
   return launch_check("tape_compile_kernel");
 }
 
-// Warps per CTA and points per lane for the interpreter kernels, given the
-// per-warp shared memory they need.
-template <typename T>
-static bool pick_shape(int Lmax, size_t per_point_bytes, bool with_sums, int& V, int& warps, size_t& smem) {
-  const int limit = max_dyn_smem();
-  const size_t fixed = align16((size_t)Lmax * 4) + (with_sums ? align16((size_t)Lmax * sizeof(T)) : 0);
-  // one point per lane keeps the per-warp table small, so more warps fit on an SM
-  for (int v : {1}) {
-    const size_t per_warp = fixed + (size_t)Lmax * 32 * v * per_point_bytes;
-    for (int w : {8, 4, 2, 1}) {
-      if (per_warp * w <= (size_t)limit && per_warp * w <= 72 * 1024) {
-        V = v;
-        warps = w;
-        smem = per_warp * w;
-        return true;
-      }
-    }
-  }
-  const size_t per_warp = fixed + (size_t)Lmax * 32 * per_point_bytes;
-  if (per_warp <= (size_t)limit) {
-    V = 1;
-    warps = 1;
-    smem = per_warp;
-    return true;
-  }
-  return false;
-}
+// Persistent grid for an interpreter kernel: warps per CTA and CTAs from the
+// per-warp shared memory and the occupancy the kernel reaches.
+struct Shape {
+  int warps;
+  size_t smem;
+  int64_t blocks;
+};
 
-template <typename T, int V>
-static int launch_forward_v(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
-                            int64_t B, int64_t M, int Lmax, const T* C, int64_t c_sb, int64_t c_sm, T* cache,
-                            int warps, size_t smem, cudaStream_t st) {
-  auto kern = eval_forward_kernel<T, V>;
-  int rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "forward smem attribute");
-  if (rc) return rc;
-  int64_t blocks = (B + warps - 1) / warps;
-  const int64_t cap = (int64_t)device_sm_count() * 64;
-  if (blocks > cap) blocks = cap;
-  kern<<<(unsigned)blocks, warps * 32, smem, st>>>(X, N, n_x, desc, meta, B, M, Lmax, C, c_sb, c_sm, cache);
-  return launch_check("eval_forward_kernel");
+static bool pick_shape(const void* kern, size_t per_warp, int64_t work_items, Shape& sh) {
+  const int limit = max_dyn_smem();
+  int w = 8;
+  while (w > 1 && per_warp * w > (size_t)limit) w >>= 1;
+  if (per_warp * w > (size_t)limit) return false;
+  sh.warps = w;
+  sh.smem = per_warp * w;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem) != cudaSuccess) return false;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, w * 32, sh.smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  int64_t blocks = (int64_t)device_sm_count() * per_sm;
+  const int64_t need = (work_items + w - 1) / w;
+  sh.blocks = blocks < need ? blocks : need;
+  if (sh.blocks < 1) sh.blocks = 1;
+  return true;
 }
 
 template <typename T>
 static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
-                          int64_t B, int64_t M, int32_t max_len, const T* C, int64_t c_sb, int64_t c_sm, T* cache,
-                          void* stream) {
+                          const int32_t* order, int64_t B, int64_t M, int32_t max_len, const T* C, int64_t c_sb,
+                          int64_t c_sm, T* cache, void* stream) {
   int rc = check_tape_args(B, M);
   if (rc) return rc;
   if (N < 0 || n_x < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
@@ -467,41 +410,23 @@ static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* de
   if (!X && n_x > 0) { set_error("null X"); return SR_ERR_INVALID_ARGUMENT; }
   if (!desc || !meta || !C || !cache) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  int V = 1, warps = 1;
-  size_t smem = 0;
-  if (!pick_shape<T>(Lmax, sizeof(T), false, V, warps, smem)) {
-    set_error("tape of %lld nodes does not fit in shared memory", (long long)M);
+  const size_t per_warp = align16((size_t)Lmax * 4) + (size_t)Lmax * 32 * sizeof(T);
+  Shape sh;
+  auto kern = eval_forward_kernel<T>;
+  const int64_t units = B * ((N + kSlice - 1) / kSlice);
+  if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, units, sh)) {
+    set_error("tape of %d nodes does not fit in shared memory", Lmax);
     return SR_ERR_UNSUPPORTED;
   }
-  cudaStream_t st = as_stream(stream);
-  switch (V) {
-    case 4: return launch_forward_v<T, 4>(X, N, n_x, desc, meta, B, M, Lmax, C, c_sb, c_sm, cache, warps, smem, st);
-    case 2: return launch_forward_v<T, 2>(X, N, n_x, desc, meta, B, M, Lmax, C, c_sb, c_sm, cache, warps, smem, st);
-    default: return launch_forward_v<T, 1>(X, N, n_x, desc, meta, B, M, Lmax, C, c_sb, c_sm, cache, warps, smem, st);
-  }
-}
-
-template <typename T, int V>
-static int launch_backward_v(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
-                             int64_t B, int64_t M, int Lmax, const T* C, int64_t c_sb, int64_t c_sm,
-                             const T* gout, T* gC, T* gX, int32_t* status, int warps, size_t smem,
-                             cudaStream_t st) {
-  auto kern = eval_backward_kernel<T, V>;
-  int rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "backward smem attribute");
-  if (rc) return rc;
-  int64_t blocks = (B + warps - 1) / warps;
-  const int64_t cap = (int64_t)device_sm_count() * 64;
-  if (blocks > cap) blocks = cap;
-  kern<<<(unsigned)blocks, warps * 32, smem, st>>>(X, N, n_x, desc, meta, B, M, Lmax, C, c_sb, c_sm, gout, gC, gX,
-                                                     status);
-  return launch_check("eval_backward_kernel");
+  kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, as_stream(stream)>>>(X, N, n_x, desc, meta, order, B, M, Lmax,
+                                                                          C, c_sb, c_sm, cache);
+  return launch_check("eval_forward_kernel");
 }
 
 template <typename T>
 static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
-                           int64_t B, int64_t M, int32_t max_len, const T* C, int64_t c_sb, int64_t c_sm,
-                           const T* gout, T* gC, T* gX, int32_t* status, void* stream) {
+                           const int32_t* order, int64_t B, int64_t M, int32_t max_len, const T* C, int64_t c_sb,
+                           int64_t c_sm, const T* gout, T* gC, T* gX, int32_t* status, void* stream) {
   int rc = check_tape_args(B, M);
   if (rc) return rc;
   if (N < 0 || n_x < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
@@ -513,17 +438,16 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
   if (!desc || !meta || !C || !gC || (N > 0 && !gout)) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
   if (N == 0) return cuda_check(cudaMemsetAsync(gC, 0, sizeof(T) * B * M, st), "grad_C reset");
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  int V = 1, warps = 1;
-  size_t smem = 0;
-  if (!pick_shape<T>(Lmax, 2 * sizeof(T), true, V, warps, smem)) {
-    set_error("tape of %lld nodes does not fit in shared memory", (long long)M);
+  const size_t per_warp = align16((size_t)Lmax * 4) + 2 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
+  Shape sh;
+  auto kern = eval_backward_kernel<T>;
+  if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, B, sh)) {
+    set_error("tape of %d nodes does not fit in shared memory", Lmax);
     return SR_ERR_UNSUPPORTED;
   }
-  switch (V) {
-    case 4: return launch_backward_v<T, 4>(X, N, n_x, desc, meta, B, M, Lmax, C, c_sb, c_sm, gout, gC, gX, status, warps, smem, st);
-    case 2: return launch_backward_v<T, 2>(X, N, n_x, desc, meta, B, M, Lmax, C, c_sb, c_sm, gout, gC, gX, status, warps, smem, st);
-    default: return launch_backward_v<T, 1>(X, N, n_x, desc, meta, B, M, Lmax, C, c_sb, c_sm, gout, gC, gX, status, warps, smem, st);
-  }
+  kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, Lmax, C, c_sb, c_sm,
+                                                           gout, gC, gX, status);
+  return launch_check("eval_backward_kernel");
 }
 
 }  // namespace sr
@@ -550,30 +474,30 @@ int sr_tape_compile(const int64_t* ops, const int64_t* ch, int64_t B, int64_t M,
                                   stream);
 }
 
-int sr_eval_forward_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta, int64_t B,
-                        int64_t M, int32_t max_len, const float* C, int64_t c_sb, int64_t c_sm, float* cache,
-                        void* stream) {
-  return sr::launch_forward<float>(X, N, n_x, desc, meta, B, M, max_len, C, c_sb, c_sm, cache, stream);
+int sr_eval_forward_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
+                        const int32_t* order, int64_t B, int64_t M, int32_t max_len, const float* C, int64_t c_sb,
+                        int64_t c_sm, float* cache, void* stream) {
+  return sr::launch_forward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, cache, stream);
 }
 
 int sr_eval_forward_f64(const double* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
-                        int64_t B, int64_t M, int32_t max_len, const double* C, int64_t c_sb, int64_t c_sm,
-                        double* cache, void* stream) {
-  return sr::launch_forward<double>(X, N, n_x, desc, meta, B, M, max_len, C, c_sb, c_sm, cache, stream);
+                        const int32_t* order, int64_t B, int64_t M, int32_t max_len, const double* C, int64_t c_sb,
+                        int64_t c_sm, double* cache, void* stream) {
+  return sr::launch_forward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, cache, stream);
 }
 
 int sr_eval_backward_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
-                         int64_t B, int64_t M, int32_t max_len, const float* C, int64_t c_sb, int64_t c_sm,
-                         const float* gout, float* gC, float* gX, int32_t* status, void* stream) {
-  return sr::launch_backward<float>(X, N, n_x, desc, meta, B, M, max_len, C, c_sb, c_sm, gout, gC, gX, status,
+                         const int32_t* order, int64_t B, int64_t M, int32_t max_len, const float* C, int64_t c_sb,
+                         int64_t c_sm, const float* gout, float* gC, float* gX, int32_t* status, void* stream) {
+  return sr::launch_backward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, gout, gC, gX, status,
                                     stream);
 }
 
 int sr_eval_backward_f64(const double* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
-                         int64_t B, int64_t M, int32_t max_len, const double* C, int64_t c_sb, int64_t c_sm,
-                         const double* gout, double* gC, double* gX, int32_t* status, void* stream) {
-  return sr::launch_backward<double>(X, N, n_x, desc, meta, B, M, max_len, C, c_sb, c_sm, gout, gC, gX, status,
-                                     stream);
+                         const int32_t* order, int64_t B, int64_t M, int32_t max_len, const double* C, int64_t c_sb,
+                         int64_t c_sm, const double* gout, double* gC, double* gX, int32_t* status, void* stream) {
+  return sr::launch_backward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, gout, gC, gX,
+                                     status, stream);
 }
 
 }  // extern "C"

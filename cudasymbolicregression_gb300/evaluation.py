@@ -70,8 +70,8 @@ class _Evaluate(torch.autograd.Function):
         L = _lib.lib()
         fn = L.sr_eval_forward_f32 if Xc.dtype == torch.float32 else L.sr_eval_forward_f64
         cb, cm = C_bm.stride()
-        rc = fn(_lib.ptr(Xc), N, nx, _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), B, M, tapes.max_len,
-                _lib.ptr(C_bm), cb, cm, _lib.ptr(cache), _lib.stream_ptr(Xc.device))
+        rc = fn(_lib.ptr(Xc), N, nx, _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), _lib.ptr(tapes.order), B, M,
+                tapes.max_len, _lib.ptr(C_bm), cb, cm, _lib.ptr(cache), _lib.stream_ptr(Xc.device))
         _lib.check(rc, "sr_eval_forward")
         ctx.tapes = tapes
         ctx.save_for_backward(Xc, C_bm)
@@ -90,9 +90,9 @@ class _Evaluate(torch.autograd.Function):
         L = _lib.lib()
         fn = L.sr_eval_backward_f32 if Xc.dtype == torch.float32 else L.sr_eval_backward_f64
         cb, cm = C_bm.stride()
-        rc = fn(_lib.ptr(Xc), N, nx, _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), B, M, tapes.max_len,
-                _lib.ptr(C_bm), cb, cm, _lib.ptr(grad), _lib.ptr(gC), _lib.ptr(gX), _lib.ptr(status),
-                _lib.stream_ptr(Xc.device))
+        rc = fn(_lib.ptr(Xc), N, nx, _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), _lib.ptr(tapes.order), B, M,
+                tapes.max_len, _lib.ptr(C_bm), cb, cm, _lib.ptr(grad), _lib.ptr(gC), _lib.ptr(gX),
+                _lib.ptr(status), _lib.stream_ptr(Xc.device))
         _lib.check(rc, "sr_eval_backward")
         code = int(status.item())
         if code:

@@ -25,6 +25,14 @@ class CompiledTapes:
     max_len: int        # largest L_eff
     max_root: int       # largest root + 1
     max_consts: int     # largest number of constants up to the root
+    _order: torch.Tensor | None = None
+
+    @property
+    def order(self) -> torch.Tensor:
+        """Tape indices, longest first (work order for the persistent kernels)."""
+        if self._order is None:
+            self._order = torch.argsort(self.meta[:, 0], descending=True, stable=True).to(torch.int32)
+        return self._order
 
 
 def compile_tapes(ops_bm: torch.Tensor, ch_bm: torch.Tensor, n_vars: int, validate_only: bool = False):

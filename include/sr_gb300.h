@@ -78,14 +78,18 @@ int sr_tape_compile(const int64_t *ops_dev, const int64_t *ch_dev, int64_t B, in
  * (reference src/symbolic_evaluation.cpp:39-92, src/evaluation_kernels_cuda.cu:51-216,
  * 634-652).  One warp interprets one tape, lanes over data points.
  * max_len: largest meta[0] of the batch (stats[1] of sr_tape_compile), or 0 for M;
- * it sizes the per-warp shared-memory node table.
+ * it sizes the per-warp shared-memory node table.  order_dev (B) int32, or NULL:
+ * the order in which the persistent warps take the tapes (longest first balances
+ * the work).
  */
 int sr_eval_forward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
-                        const int32_t *meta_dev, int64_t B, int64_t M, int32_t max_len,
-                        const float *C_dev, int64_t c_sb, int64_t c_sm, float *cache_dev, void *stream);
+                        const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
+                        int32_t max_len, const float *C_dev, int64_t c_sb, int64_t c_sm,
+                        float *cache_dev, void *stream);
 int sr_eval_forward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
-                        const int32_t *meta_dev, int64_t B, int64_t M, int32_t max_len,
-                        const double *C_dev, int64_t c_sb, int64_t c_sm, double *cache_dev, void *stream);
+                        const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
+                        int32_t max_len, const double *C_dev, int64_t c_sb, int64_t c_sm,
+                        double *cache_dev, void *stream);
 
 /*
  * Adjoint of the forward evaluation for a dense output gradient grad_out (B, M, N).
@@ -98,13 +102,15 @@ int sr_eval_forward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint3
  * src/evaluation_kernels_cuda.cu:218-632, 654-673).
  */
 int sr_eval_backward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
-                         const int32_t *meta_dev, int64_t B, int64_t M, int32_t max_len,
-                         const float *C_dev, int64_t c_sb, int64_t c_sm, const float *grad_out_dev,
-                         float *grad_C_dev, float *grad_X_dev, int32_t *status_dev, void *stream);
+                         const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
+                         int32_t max_len, const float *C_dev, int64_t c_sb, int64_t c_sm,
+                         const float *grad_out_dev, float *grad_C_dev, float *grad_X_dev,
+                         int32_t *status_dev, void *stream);
 int sr_eval_backward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
-                         const int32_t *meta_dev, int64_t B, int64_t M, int32_t max_len,
-                         const double *C_dev, int64_t c_sb, int64_t c_sm, const double *grad_out_dev,
-                         double *grad_C_dev, double *grad_X_dev, int32_t *status_dev, void *stream);
+                         const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
+                         int32_t max_len, const double *C_dev, int64_t c_sb, int64_t c_sm,
+                         const double *grad_out_dev, double *grad_C_dev, double *grad_X_dev,
+                         int32_t *status_dev, void *stream);
 
 /* Options of sr_fit_lbfgs; mirrors optimize()/LBFGS_batch's arguments
  * (reference symbolic_torch/optimization.py:9-19, symbolic_torch/lbfgs_batch.py:15-23). */

