@@ -792,3 +792,92 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Fit without any device allocation by the caller.
+//
+// Some callers cannot hand this library a workspace: a host process whose device
+// memory is owned entirely by its own pool allocator and which forbids any other
+// cudaMalloc (cudaMalloc synchronises the device and may fail under the pool's
+// budget), or a latency-bound service that must not allocate on its request path.
+// For them the fit's scratch (work counter, per-warp L-BFGS history rings) lives in
+// a file-scope device array of fixed size instead of a caller buffer.
+// ---------------------------------------------------------------------------------
+#include <mutex>
+
+namespace sr {
+
+constexpr int64_t kStaticFitScratchBytes = 16LL << 20;  // 16 MiB, held on every device that loads the library
+static __device__ __align__(256) unsigned char g_fit_static_scratch[kStaticFitScratchBytes];
+
+// Device address of g_fit_static_scratch on the current device, looked up once per
+// device (the name is only a host-side stand-in in host code).
+static int static_scratch_address(void** out) {
+  static std::mutex mu;
+  static void* addr[128] = {nullptr};
+  int dev = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  if (dev < 0 || dev >= 128) {
+    set_error("device ordinal %d out of range", dev);
+    return SR_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    rc = cuda_check(cudaGetSymbolAddress(&p, g_fit_static_scratch), "cudaGetSymbolAddress(static fit scratch)");
+    if (rc) return rc;
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return SR_OK;
+}
+
+}  // namespace sr
+
+extern "C" int sr_fit_lbfgs_static_scratch(const float* X, int64_t N, int64_t n_x, const float* Y,
+                                           const uint32_t* desc, const int32_t* meta, int64_t B, int64_t M,
+                                           const float* C_init, float* C_out, int64_t c_sb, int64_t c_sm,
+                                           float* Y_final, int32_t* iters_out, float* loss_out, int32_t* evals_out,
+                                           const int32_t* order, int32_t max_len, int32_t max_consts,
+                                           const sr_fit_options* opt, int32_t* status, void* stream) {
+  using namespace sr;
+  sr_fit_options o;
+  int rc = fit_defaults(opt, o);
+  if (rc) return rc;
+  if (B < 0 || M < 0 || max_consts < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (B == 0 || M == 0) return sr_fit_lbfgs(X, N, n_x, Y, desc, meta, B, M, C_init, C_out, c_sb, c_sm, Y_final,
+                                            iters_out, loss_out, evals_out, order, max_len, max_consts, &o, nullptr,
+                                            0, status, stream);
+  // Persistent grid: fewer CTAs only lengthen the work queue per warp, so shrink the
+  // grid until its history rings fit in the static array.
+  FitShape sh;
+  const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
+  rc = fit_shape(B, Lmax, max_consts, o, sh);
+  if (rc) return rc;
+  int64_t blocks = sh.blocks;
+  while (blocks >= 1) {
+    FitShape t = sh;
+    t.blocks = (int)blocks;
+    t.total_warps = blocks * sh.warps;
+    if (ws_bytes_for(t, o.history_size) <= kStaticFitScratchBytes) break;
+    blocks = blocks > 8 ? blocks * 3 / 4 : blocks - 1;
+  }
+  if (blocks < 1) {
+    FitShape t = sh;
+    t.blocks = 1;
+    t.total_warps = sh.warps;
+    set_error("static fit scratch is %lld bytes; one CTA of %d warps needs %lld (history_size=%d, up to %d constants); "
+              "use sr_fit_lbfgs with a caller workspace",
+              (long long)kStaticFitScratchBytes, sh.warps, (long long)ws_bytes_for(t, o.history_size), o.history_size,
+              max_consts);
+    return SR_ERR_WORKSPACE;
+  }
+  void* scratch = nullptr;
+  rc = static_scratch_address(&scratch);
+  if (rc) return rc;
+  o.grid_blocks = (int32_t)blocks;
+  o.warps_per_block = sh.warps;
+  return sr_fit_lbfgs(X, N, n_x, Y, desc, meta, B, M, C_init, C_out, c_sb, c_sm, Y_final, iters_out, loss_out,
+                      evals_out, order, max_len, max_consts, &o, scratch, kStaticFitScratchBytes, status, stream);
+}

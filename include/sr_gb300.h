@@ -156,6 +156,30 @@ int sr_fit_lbfgs(const float *X_dev, int64_t N, int64_t n_x, const float *Y_dev,
                  int64_t workspace_bytes, int32_t *status_dev, void *stream);
 
 /*
+ * sr_fit_lbfgs without a caller workspace.  No counterpart in the reference: it is
+ * for callers that cannot allocate device memory for this library (a host whose
+ * device memory is all owned by its own pool and forbids other cudaMalloc calls,
+ * or a service that must not allocate on its request path).  The scratch (work
+ * counter and L-BFGS history rings) is a fixed 16 MiB device array inside the
+ * library, present on every device that loads it until the process exits.  The
+ * persistent grid is shrunk until its history fits; when even one CTA does not fit
+ * (very large history_size) the call fails with SR_ERR_WORKSPACE.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  Every call uses the same array and resets
+ * the work counter itself, so calls that overlap on the same GPU (for instance on
+ * two streams) race on it and must be serialised by the caller; each device has
+ * its own array.  Arguments and results are those of sr_fit_lbfgs; nothing is
+ * allocated.
+ */
+int sr_fit_lbfgs_static_scratch(const float *X_dev, int64_t N, int64_t n_x, const float *Y_dev,
+                                const uint32_t *desc_dev, const int32_t *meta_dev, int64_t B,
+                                int64_t M, const float *C_init_dev, float *C_out_dev, int64_t c_sb,
+                                int64_t c_sm, float *Y_final_dev, int32_t *iters_out_dev,
+                                float *loss_out_dev, int32_t *evals_out_dev, const int32_t *order_dev,
+                                int32_t max_len, int32_t max_consts, const sr_fit_options *opt,
+                                int32_t *status_dev, void *stream);
+
+/*
  * create_constants support (reference symbolic_torch/utils.py:7-41).
  * sr_const_offsets: for a 2-D Ops view (R, Cc) with strides (s0, s1), writes
  * offsets_dev (R + 1) int64: the exclusive prefix count of LEARNABLE_CONSTANT
