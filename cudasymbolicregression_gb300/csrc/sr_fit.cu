@@ -108,7 +108,7 @@ __device__ __forceinline__ double wsum_d(double v) {
   return v;
 }
 
-// Per-problem context held in registers.
+// Parameter-slot vectors: slot j lives in lane j % 32, register j / 32.
 template <int SPL>
 struct Slots {
   float v[SPL];
@@ -145,108 +145,191 @@ __device__ __forceinline__ Slots<SPL> axpy(const Slots<SPL>& x, float a, const S
   return r;
 }
 
+// phi0 + (c * a) * dphi0 in float32, each operation rounded on its own as the
+// reference's tensor arithmetic does.
+__device__ __forceinline__ float armijo(float phi0, float c, float a, float dphi0) {
+  return __fadd_rn(phi0, __fmul_rn(__fmul_rn(c, a), dphi0));
+}
+
+constexpr int kMaxRegVars = 4;  // X rows of up to this many variables are held in registers
+
+// Value of variable `var` at the lane's point: from registers when n_x is small.
+template <int V>
+__device__ __forceinline__ float var_value(const float (&xr)[V][kMaxRegVars], int v, int var, bool in_regs,
+                                           const float* __restrict__ X, int64_t nn, int64_t n_x) {
+  if (in_regs) {
+    float r = xr[v][0];
+    r = var == 1 ? xr[v][1] : r;
+    r = var == 2 ? xr[v][2] : r;
+    r = var == 3 ? xr[v][3] : r;
+    return r;
+  }
+  return __ldg(X + nn * n_x + var);
+}
+
 // ---------------------------------------------------------------------------------
-// closure: loss and gradient at the constants xt.
+// One pass over the problem's points at the constants published in S.cnode.
+// kGrad: loss + gradient (forward, residual, reverse sweep); otherwise forward only,
+// writing the root values to Y_final.
+//
+// Forward: node k's children are read from the shared-memory node table, except the
+// node just before it (the most common child in a postfix tape), whose value is
+// still in a register.  Reverse: the contribution a node makes to the node right
+// before it is likewise carried in registers into the next iteration instead of a
+// shared-memory read-modify-write; contributions are still added in the reference's
+// order (parents from the last to the first, child 0 before child 1).
 // ---------------------------------------------------------------------------------
-template <int V, int SPL>
-__device__ __noinline__ float closure(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P, const Slots<SPL>& xt,
-                         Slots<SPL>& grad, int& err) {
-  const int lane = P.lane;
-  // publish the trial constants to their nodes; clear the per-lane gradient sums
-#pragma unroll
-  for (int s = 0; s < SPL; ++s)
-    if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = xt.v[s];
-  for (int j = 0; j < P.K; ++j) S.gl[j * 32 + lane] = 0.0;
-  __syncwarp();
-  const int R = P.root;
+template <int V, bool kGrad>
+__device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int R, int K, int lane,
+                                           int& err) {
   const int64_t N = A.N;
   const float invN = 1.0f / (float)N;
-  const float* Yrow = A.Y ? A.Y + P.b * N : nullptr;
+  const float* __restrict__ Yrow = A.Y ? A.Y + b * N : nullptr;
+  const bool xin = A.n_x <= kMaxRegVars;
   double loss_part = 0.0;
   for (int64_t base = 0; base < N; base += 32 * V) {
     int64_t nn[V];
     bool valid[V];
+    float xr[V][kMaxRegVars];
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       const int64_t n = base + v * 32 + lane;
       valid[v] = n < N;
       nn[v] = valid[v] ? n : N - 1;
+#pragma unroll
+      for (int j = 0; j < kMaxRegVars; ++j) xr[v][j] = (xin && j < A.n_x) ? __ldg(A.X + nn[v] * A.n_x + j) : 0.f;
     }
-    // forward
+    // ---- forward ----
+    float prev[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) prev[v] = 0.f;
+    uint32_t dn = S.tape[0];
     for (int k = 0; k <= R; ++k) {
-      const uint32_t d = S.tape[k];
+      const uint32_t d = dn;
+      if (k < R) dn = S.tape[k + 1];
       const int code = code_of(d);
-      float* out = S.vals + k * (32 * V);
+      float r[V];
       if (code == VAR) {
         const int var = child0(d);
 #pragma unroll
-        for (int v = 0; v < V; ++v) out[v * 32 + lane] = __ldg(A.X + nn[v] * A.n_x + var);
+        for (int v = 0; v < V; ++v) r[v] = var_value<V>(xr, v, var, xin, A.X, nn[v], A.n_x);
       } else if (code == LEARNABLE) {
         const float c = S.cnode[k];
 #pragma unroll
-        for (int v = 0; v < V; ++v) out[v * 32 + lane] = c;
+        for (int v = 0; v < V; ++v) r[v] = c;
       } else {
-        const float* a = S.vals + child0(d) * (32 * V);
-        const float* bb = S.vals + child1(d) * (32 * V);
+        const int c0 = child0(d), c1 = child1(d);
+        const bool p0 = c0 == k - 1, p1 = c1 == k - 1;
 #pragma unroll
-        for (int v = 0; v < V; ++v) out[v * 32 + lane] = node_value<float>(code, a[v * 32 + lane], bb[v * 32 + lane], 0.f, 0.f);
+        for (int v = 0; v < V; ++v) {
+          const float a = p0 ? prev[v] : S.vals[c0 * (32 * V) + v * 32 + lane];
+          const float bb = p1 ? prev[v] : S.vals[c1 * (32 * V) + v * 32 + lane];
+          r[v] = node_value<float>(code, a, bb, 0.f, 0.f);
+        }
       }
-      S.adj[k * (32 * V) + 0 * 32 + lane] = 0.f;
 #pragma unroll
-      for (int v = 1; v < V; ++v) S.adj[k * (32 * V) + v * 32 + lane] = 0.f;
+      for (int v = 0; v < V; ++v) {
+        S.vals[k * (32 * V) + v * 32 + lane] = r[v];
+        if (kGrad) S.adj[k * (32 * V) + v * 32 + lane] = 0.f;
+        prev[v] = r[v];
+      }
     }
-    // residuals and the root adjoint: (2 (f - y)) * (1/N), as autograd forms it
+    if constexpr (!kGrad) {
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        if (valid[v]) A.Y_final[b * N + nn[v]] = prev[v];
+      continue;
+    } else {
+    // ---- residuals: root adjoint (2 (f - y)) * (1/N), as autograd forms it ----
+    float g_root[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      const float f = S.vals[R * (32 * V) + v * 32 + lane];
       float groot = 0.f;
       if (valid[v]) {
         if (A.objective == 0) {
-          const float r = f - __ldg(Yrow + nn[v]);
-          loss_part += (double)(r * r);
-          groot = __fmul_rn(r * 2.0f, invN);
+          const float rr = prev[v] - __ldg(Yrow + nn[v]);
+          loss_part += (double)(rr * rr);
+          groot = __fmul_rn(rr * 2.0f, invN);
         } else {
-          loss_part += (double)f;
+          loss_part += (double)prev[v];
           groot = invN;
         }
       }
-      S.adj[R * (32 * V) + v * 32 + lane] = groot;
+      g_root[v] = groot;
     }
-    // reverse sweep
+    // ---- reverse sweep ----
+    // carry*: contributions to node k-1 produced while processing node k
+    float cin0[V], cin1[V];
+    bool hin0 = false, hin1 = false;
+#pragma unroll
+    for (int v = 0; v < V; ++v) { cin0[v] = 0.f; cin1[v] = 0.f; }
+    uint32_t dn2 = S.tape[R];
     for (int k = R; k >= 0; --k) {
-      const uint32_t d = S.tape[k];
+      const uint32_t d = dn2;
+      if (k > 0) dn2 = S.tape[k - 1];
       const int code = code_of(d);
-      const float* gk = S.adj + k * (32 * V);
+      float g[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        float gv = (k == R) ? g_root[v] : S.adj[k * (32 * V) + v * 32 + lane];
+        if (hin0) gv = __fadd_rn(gv, cin0[v]);
+        if (hin1) gv = __fadd_rn(gv, cin1[v]);
+        g[v] = gv;
+      }
+      hin0 = hin1 = false;
       if (code == LEARNABLE) {
         const int slot = S.node_slot[k];
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const float g = gk[v * 32 + lane];
-          if (valid[v] && g != 0.f) S.gl[slot * 32 + lane] += (double)g;
-        }
+        for (int v = 0; v < V; ++v)
+          if (valid[v] && g[v] != 0.f) S.gl[slot * 32 + lane] += (double)g[v];
         continue;
       }
       if (code == VAR || code == ZERO || (code >= C1 && code <= E_) || code == FLOOR || code == CEIL) continue;
       const int c0 = child0(d), c1 = child1(d);
-      float* A0 = S.adj + c0 * (32 * V);
-      float* A1 = S.adj + c1 * (32 * V);
-      const float* av = S.vals + c0 * (32 * V);
-      const float* bv = S.vals + c1 * (32 * V);
-      const float* kv = S.vals + k * (32 * V);
+      const bool t0 = c0 == k - 1, t1 = c1 == k - 1;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         const int i = v * 32 + lane;
         bool a0, a1;
         float o0, o1;
-        const int e = node_adjoint<float>(code, gk[i], av[i], bv[i], kv[i], a0, o0, a1, o1);
-        if (valid[v]) {
-          if (e && !err) err = e;
-          if (a0) A0[i] = __fadd_rn(A0[i], o0);
-          if (a1) A1[i] = __fadd_rn(A1[i], o1);
+        const int e = node_adjoint<float>(code, g[v], S.vals[c0 * (32 * V) + i], S.vals[c1 * (32 * V) + i],
+                                          S.vals[k * (32 * V) + i], a0, o0, a1, o1);
+        if (!valid[v]) { a0 = a1 = false; o0 = o1 = 0.f; }
+        if (e && valid[v] && !err) err = e;
+        // the flags depend only on the opcode and g; they are per lane here
+        if (a0) {
+          if (t0) cin0[v] = o0;
+          else S.adj[c0 * (32 * V) + i] = __fadd_rn(S.adj[c0 * (32 * V) + i], o0);
+        } else if (t0) {
+          cin0[v] = 0.f;
+        }
+        if (a1) {
+          if (t1) cin1[v] = o1;
+          else S.adj[c1 * (32 * V) + i] = __fadd_rn(S.adj[c1 * (32 * V) + i], o1);
+        } else if (t1) {
+          cin1[v] = 0.f;
         }
       }
+      // a lane without a contribution carries +0, which leaves its sum unchanged
+      hin0 = t0;
+      hin1 = t1;
     }
+    }  // kGrad
   }
+  return kGrad ? (float)(wsum_d(loss_part) / (double)N) : 0.f;
+}
+
+// Closure: publish the trial constants, run the pass, reduce the gradient.
+template <int V, int SPL>
+__device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P,
+                                         const Slots<SPL>& xt, Slots<SPL>& grad, int& err) {
+  const int lane = P.lane;
+#pragma unroll
+  for (int s = 0; s < SPL; ++s)
+    if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = xt.v[s];
+  for (int j = 0; j < P.K; ++j) S.gl[j * 32 + lane] = 0.0;
+  __syncwarp();
+  const float loss = tape_pass<V, true>(A, S, P.b, P.root, P.K, lane, err);
   __syncwarp();
   // gradient of each real slot: the lane owning the slot sums the 32 lane partials
 #pragma unroll
@@ -255,64 +338,14 @@ __device__ __noinline__ float closure(const FitArgs& A, const WarpSmem& S, const
     if (P.real(s)) {
       const int j = s * 32 + lane;
       double acc = 0.0;
+#pragma unroll 8
       for (int l = 0; l < 32; ++l) acc += S.gl[j * 32 + l];
       gv = (float)acc;
     }
     grad.v[s] = gv;
   }
   __syncwarp();
-  return (float)(wsum_d(loss_part) / (double)N);
-}
-
-// Forward only: root values of the final constants into Y_final.
-template <int V, int SPL>
-__device__ void final_forward(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P, const Slots<SPL>& x) {
-  const int lane = P.lane;
-#pragma unroll
-  for (int s = 0; s < SPL; ++s)
-    if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = x.v[s];
-  __syncwarp();
-  const int R = P.root;
-  const int64_t N = A.N;
-  for (int64_t base = 0; base < N; base += 32 * V) {
-    int64_t nn[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      const int64_t n = base + v * 32 + lane;
-      nn[v] = n < N ? n : N - 1;
-    }
-    for (int k = 0; k <= R; ++k) {
-      const uint32_t d = S.tape[k];
-      const int code = code_of(d);
-      float* out = S.vals + k * (32 * V);
-      if (code == VAR) {
-        const int var = child0(d);
-#pragma unroll
-        for (int v = 0; v < V; ++v) out[v * 32 + lane] = __ldg(A.X + nn[v] * A.n_x + var);
-      } else if (code == LEARNABLE) {
-        const float c = S.cnode[k];
-#pragma unroll
-        for (int v = 0; v < V; ++v) out[v * 32 + lane] = c;
-      } else {
-        const float* a = S.vals + child0(d) * (32 * V);
-        const float* bb = S.vals + child1(d) * (32 * V);
-#pragma unroll
-        for (int v = 0; v < V; ++v) out[v * 32 + lane] = node_value<float>(code, a[v * 32 + lane], bb[v * 32 + lane], 0.f, 0.f);
-      }
-    }
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      const int64_t n = base + v * 32 + lane;
-      if (n < N) A.Y_final[P.b * N + n] = S.vals[R * (32 * V) + v * 32 + lane];
-    }
-  }
-  __syncwarp();
-}
-
-// phi0 + (c * a) * dphi0 in float32, each operation rounded on its own as the
-// reference's tensor arithmetic does.
-__device__ __forceinline__ float armijo(float phi0, float c, float a, float dphi0) {
-  return __fadd_rn(phi0, __fmul_rn(__fmul_rn(c, a), dphi0));
+  return loss;
 }
 
 // Evaluated point: value and gradient.
@@ -321,6 +354,12 @@ struct Point {
   float phi;
   Slots<SPL> g;
 };
+
+// Line-search phases of the per-problem state machine.  Every loop turn of the
+// kernel evaluates exactly one closure (one call site, inlined), then advances the
+// state; the transitions follow LBFGS_batch.step / _strong_wolfe /
+// _alpha_zoom_corrected / _backtracking_line_search for one column.
+enum Phase : int { PH_INIT = 0, PH_BRACKET, PH_ZOOM_LO, PH_ZOOM, PH_BACKTRACK, PH_UPDATE, PH_DONE };
 
 template <int V, int SPL>
 __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
@@ -333,6 +372,7 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
   float* ringY = ringS + (int64_t)A.hist * SPL * 32;
   double* alph = A.ws_scal + gwarp * (int64_t)2 * A.hist;
   double* rhos = alph + A.hist;
+  const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
 
   while (true) {
     int64_t idx = 0;
@@ -368,237 +408,299 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
     __syncwarp();
 
     const float* Cin = A.C_init + P.b * A.c_sb;
-    Slots<SPL> x, g;
+    Slots<SPL> x, g, p, xn;
 #pragma unroll
     for (int s = 0; s < SPL; ++s) {
       const int j = s * 32 + lane;
       x.v[s] = P.real(s) ? Cin[(int64_t)S.slot_node[j] * A.c_sm] : 0.f;
+      g.v[s] = 0.f;
+      p.v[s] = 0.f;
+      xn.v[s] = 0.f;
     }
-    int err = 0;
-    int evals = 1;
-    float f = closure<V, SPL>(A, S, P, x, g, err);
+    int err = 0, evals = 0;
+    float f = 0.f;
     bool poison = false;
-    int h = 0, head = 0;  // history length and index of the oldest pair
-    int it = 0;
-    for (it = 0; it < A.max_iter; ++it) {
-      const double gn = sqrt(dot(P, g, g));
-      if (gn < A.tol) break;
+    int h = 0, head = 0, it = 0;
+    // line-search state
+    int phase = PH_INIT;
+    int lsi = 0, zj = 0;
+    float phi0 = 0.f, dphi0 = 0.f, a_prev = 0.f, phi_prev = 0.f, a_i = 1.f, lo = 0.f, hi = 0.f, aj = 0.f, al = 1.f;
+    float alpha = 0.f;
+    Point<SPL> prevpt, plo, acc;
+    acc.phi = 0.f;
+    prevpt.phi = 0.f;
+    plo.phi = 0.f;
+#pragma unroll
+    for (int s = 0; s < SPL; ++s) { prevpt.g.v[s] = 0.f; plo.g.v[s] = 0.f; acc.g.v[s] = 0.f; }
 
-      // ---- two-loop recursion (lbfgs_batch.py:65-103) ----
-      Slots<SPL> q = g, p;
-      if (h > 0) {
-        for (int i = h - 1; i >= 0; --i) {
-          const int slot = (head + i) % A.hist;
-          Slots<SPL> si, yi;
+    while (phase != PH_DONE) {
+      // ---- trial point of this turn ----
+      Slots<SPL> xt;
+      switch (phase) {
+        case PH_INIT: xt = x; break;
+        case PH_BRACKET: xt = axpy(x, a_i, p); break;
+        case PH_ZOOM_LO: xt = axpy(x, 0.f, p); break;
+        case PH_ZOOM: aj = __fdiv_rn(__fadd_rn(lo, hi), 2.0f); xt = axpy(x, aj, p); break;
+        case PH_BACKTRACK: xt = axpy(x, al, p); break;
+        default: xt = xn; break;  // PH_UPDATE
+      }
+      Point<SPL> cur;
+      cur.phi = closure<V, SPL>(A, S, P, xt, cur.g, err);
+      ++evals;
+
+      // ---- advance the state machine ----
+      bool ls_finished = false, known = false;
+      bool begin_iter = false;
+      if (phase == PH_INIT) {
+        f = cur.phi;
+        g = cur.g;
+        begin_iter = true;
+      } else if (phase == PH_BRACKET) {
+        const float dphi = (float)dot(P, cur.g, p);
+        const bool bad = (cur.phi > armijo(phi0, c1, a_i, dphi0)) || (lsi > 0 && cur.phi >= phi_prev);
+        const bool good = fabsf(dphi) <= __fmul_rn(c2, fabsf(dphi0));
+        const bool passed = dphi >= 0.f;
+        if (good) {
+          alpha = a_i;
+          acc = cur;
+          known = true;
+          ls_finished = true;
+        } else if (bad || passed) {
+          lo = bad ? a_prev : a_i;
+          hi = bad ? a_i : a_prev;
+          zj = 0;
+          if (!bad) {
+            plo = cur;
+            phase = PH_ZOOM;
+          } else if (lsi > 0) {
+            plo = prevpt;
+            phase = PH_ZOOM;
+          } else {
+            // alpha_lo = 0: the point x + 0*p is x unless p holds inf/NaN
+            const Slots<SPL> x0 = axpy(x, 0.f, p);
+            bool same = true;
 #pragma unroll
-          for (int s = 0; s < SPL; ++s) {
-            si.v[s] = ringS[slot * SPL * 32 + s * 32 + lane];
-            yi.v[s] = ringY[slot * SPL * 32 + s * 32 + lane];
+            for (int s = 0; s < SPL; ++s)
+              if (P.real(s) && __float_as_uint(x0.v[s]) != __float_as_uint(x.v[s])) same = false;
+            same = __all_sync(0xffffffffu, same);
+            if (same) {
+              plo.phi = f;
+              plo.g = g;
+              phase = PH_ZOOM;
+            } else {
+              phase = PH_ZOOM_LO;
+            }
           }
-          const double rho = 1.0 / __dadd_rn(dot(P, yi, si), A.eps);
-          const double al = __dmul_rn(rho, dot(P, si, q));
+        } else {
+          a_prev = a_i;
+          phi_prev = cur.phi;
+          prevpt = cur;
+          a_i = __fadd_rn(a_i, __fmul_rn(__fsub_rn(amax, a_i), 0.8f));
+          ++lsi;
+          if (lsi >= A.ls_max) {  // unfinished bracket: the next extrapolated step, not evaluated
+            alpha = a_i;
+            known = false;
+            ls_finished = true;
+          }
+        }
+      } else if (phase == PH_ZOOM_LO) {
+        plo = cur;
+        phase = PH_ZOOM;
+      } else if (phase == PH_ZOOM) {
+        const float dphij = (float)dot(P, cur.g, p);
+        const bool zbad = (cur.phi > armijo(phi0, c1, aj, dphi0)) || (cur.phi >= plo.phi);
+        const bool zgood = fabsf(dphij) <= __fmul_rn(c2, fabsf(dphi0));
+        bool zdone = false;
+        if (zgood) {
+          alpha = aj;
+          acc = cur;
+          zdone = true;
+        }
+        if (!zdone) {
+          const float thi = zbad ? aj : hi;
+          const bool cond3 = __fmul_rn(dphij, __fsub_rn(thi, lo)) >= 0.f;
+          hi = (!zbad && cond3) ? lo : thi;
+          if (!zbad) {
+            lo = aj;
+            plo = cur;
+          }
+        }
+        if (!zdone && fabsf(__fsub_rn(hi, lo)) < 1e-9f) {
+          alpha = aj;
+          acc = cur;
+          zdone = true;
+        }
+        ++zj;
+        if (!zdone && zj >= 10) {
+          alpha = lo;
+          acc = plo;
+          zdone = true;
+        }
+        if (zdone) {
+          known = true;
+          ls_finished = true;
+        }
+      } else if (phase == PH_BACKTRACK) {
+        if (cur.phi <= armijo(f, 1e-4f, al, dphi0)) {
+          alpha = al;
+          acc = cur;
+          known = true;
+          ls_finished = true;
+        } else {
+          al = al * 0.5f;
+          ++lsi;
+          if (lsi >= A.ls_max) {
+            alpha = al;
+            known = false;
+            ls_finished = true;
+          }
+        }
+      }
+
+      // ---- end of the line search: the update x += alpha p ----
+      Slots<SPL> sv;
+      bool finish_iter = false;
+      Point<SPL> nxt;
+      if (phase == PH_UPDATE) {
+        nxt = cur;
+        finish_iter = true;
+      } else if (ls_finished) {
 #pragma unroll
-          for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dsub_rn((double)q.v[s], __dmul_rn(al, (double)yi.v[s]));
-          if (lane == 0) { alph[i] = al; rhos[i] = rho; }
+        for (int s = 0; s < SPL; ++s) {
+          sv.v[s] = P.active(s) ? __fmul_rn(alpha, p.v[s]) : 0.f;
+          xn.v[s] = __fadd_rn(x.v[s], sv.v[s]);
+        }
+        if (known) {
+          nxt = acc;
+          finish_iter = true;
+        } else {
+          phase = PH_UPDATE;
+        }
+      }
+      if (finish_iter) {
+        if (phase == PH_UPDATE) {  // the step of the line search that ended in the previous turn
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) sv.v[s] = P.active(s) ? __fmul_rn(alpha, p.v[s]) : 0.f;
+        }
+        if (P.has_virtual) {
+          bool vnan = false;
+#pragma unroll
+          for (int s = 0; s < SPL; ++s)
+            if (s * 32 + lane == P.K && isnan(sv.v[s])) vnan = true;
+          poison = poison || __any_sync(0xffffffffu, vnan);
+        }
+        // push (s, y): drop the oldest pair when the history is full
+        int slot;
+        if (h < A.hist) {
+          slot = (head + h) % A.hist;
+          ++h;
+        } else {
+          slot = head;
+          head = (head + 1) % A.hist;
+        }
+#pragma unroll
+        for (int s = 0; s < SPL; ++s) {
+          ringS[slot * SPL * 32 + s * 32 + lane] = sv.v[s];
+          ringY[slot * SPL * 32 + s * 32 + lane] = P.active(s) ? __fsub_rn(nxt.g.v[s], g.v[s]) : 0.f;
         }
         __syncwarp();
-        {
-          const int slot = (head + h - 1) % A.hist;
-          Slots<SPL> sl, yl;
-#pragma unroll
-          for (int s = 0; s < SPL; ++s) {
-            sl.v[s] = ringS[slot * SPL * 32 + s * 32 + lane];
-            yl.v[s] = ringY[slot * SPL * 32 + s * 32 + lane];
-          }
-          const double gam = dot(P, sl, yl) / __dadd_rn(dot(P, yl, yl), A.eps);
-#pragma unroll
-          for (int s = 0; s < SPL; ++s) q.v[s] = (float)(gam * (double)q.v[s]);
-        }
-        for (int i = 0; i < h; ++i) {
-          const int slot = (head + i) % A.hist;
-          Slots<SPL> si, yi;
-#pragma unroll
-          for (int s = 0; s < SPL; ++s) {
-            si.v[s] = ringS[slot * SPL * 32 + s * 32 + lane];
-            yi.v[s] = ringY[slot * SPL * 32 + s * 32 + lane];
-          }
-          const double be = __dmul_rn(rhos[i], dot(P, yi, q));
-          const double coef = __dsub_rn(alph[i], be);
-#pragma unroll
-          for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dadd_rn((double)q.v[s], __dmul_rn((double)si.v[s], coef));
-        }
-      }
-#pragma unroll
-      for (int s = 0; s < SPL; ++s) p.v[s] = P.active(s) ? -q.v[s] : 0.f;
-
-      // ---- line search ----
-      float alpha;
-      bool known = false;
-      Point<SPL> acc;
-      acc.phi = 0.f;
-      if (A.ls_kind == 0) {
-        // strong Wolfe (lbfgs_batch.py:138-202) with zoom (lbfgs_batch.py:204-264)
-        const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
-        const float phi0 = f;
-        const float dphi0 = (float)dot(P, g, p);
-        float a_prev = 0.f, phi_prev = phi0, a_i = 1.f;
-        Slots<SPL> g_prev = g;
-        bool done = false;
-        alpha = 0.f;
-        for (int i = 0; i < A.ls_max && !done; ++i) {
-          Point<SPL> cur;
-          cur.phi = closure<V, SPL>(A, S, P, axpy(x, a_i, p), cur.g, err);
-          ++evals;
-          const float dphi = (float)dot(P, cur.g, p);
-          const bool bad = (cur.phi > armijo(phi0, c1, a_i, dphi0)) || (i > 0 && cur.phi >= phi_prev);
-          const bool good = fabsf(dphi) <= __fmul_rn(c2, fabsf(dphi0));
-          const bool passed = dphi >= 0.f;
-          if (good) {
-            alpha = a_i;
-            acc = cur;
-            known = true;
-            done = true;
-          } else if (bad || passed) {
-            float lo = bad ? a_prev : a_i, hi = bad ? a_i : a_prev;
-            Point<SPL> plo;
-            if (!bad) {
-              plo = cur;
-            } else if (i > 0) {
-              plo.phi = phi_prev;
-              plo.g = g_prev;
-            } else {
-              // alpha_lo = 0: the point x + 0*p is x unless p holds inf/NaN
-              const Slots<SPL> x0 = axpy(x, 0.f, p);
-              bool same = true;
-#pragma unroll
-              for (int s = 0; s < SPL; ++s)
-                if (P.real(s) && __float_as_uint(x0.v[s]) != __float_as_uint(x.v[s])) same = false;
-              same = __all_sync(0xffffffffu, same);
-              if (same) {
-                plo.phi = f;
-                plo.g = g;
-              } else {
-                plo.phi = closure<V, SPL>(A, S, P, x0, plo.g, err);
-                ++evals;
-              }
-            }
-            // zoom
-            float za = 0.f;
-            bool zdone = false;
-            Point<SPL> zacc;
-            for (int j = 0; j < 10 && !zdone; ++j) {
-              const float aj = __fdiv_rn(__fadd_rn(lo, hi), 2.0f);
-              Point<SPL> pj;
-              pj.phi = closure<V, SPL>(A, S, P, axpy(x, aj, p), pj.g, err);
-              ++evals;
-              const float dphij = (float)dot(P, pj.g, p);
-              const bool zbad = (pj.phi > armijo(phi0, c1, aj, dphi0)) || (pj.phi >= plo.phi);
-              const bool zgood = fabsf(dphij) <= __fmul_rn(c2, fabsf(dphi0));
-              if (zgood) {
-                za = aj;
-                zacc = pj;
-                zdone = true;
-              }
-              if (!zdone) {
-                const float thi = zbad ? aj : hi;
-                const bool cond3 = __fmul_rn(dphij, __fsub_rn(thi, lo)) >= 0.f;
-                hi = (!zbad && cond3) ? lo : thi;
-                if (!zbad) {
-                  lo = aj;
-                  plo = pj;
-                }
-              }
-              if (!zdone && fabsf(__fsub_rn(hi, lo)) < 1e-9f) {
-                za = aj;
-                zacc = pj;
-                zdone = true;
-              }
-            }
-            if (!zdone) {
-              za = lo;
-              zacc = plo;
-            }
-            alpha = za;
-            acc = zacc;
-            known = true;
-            done = true;
-          }
-          if (!done) {
-            a_prev = a_i;
-            phi_prev = cur.phi;
-            g_prev = cur.g;
-            a_i = __fadd_rn(a_i, __fmul_rn(__fsub_rn(amax, a_i), 0.8f));
-          }
-        }
-        if (!done) alpha = a_i;  // unfinished bracket: the next extrapolated step
-      } else {
-        // Armijo backtracking (lbfgs_batch.py:105-136)
-        const float gfp = (float)dot(P, g, p);
-        float al = 1.f;
-        for (int t = 0; t < A.ls_max; ++t) {
-          Point<SPL> cur;
-          cur.phi = closure<V, SPL>(A, S, P, axpy(x, al, p), cur.g, err);
-          ++evals;
-          if (cur.phi <= armijo(f, 1e-4f, al, gfp)) {
-            acc = cur;
-            known = true;
-            break;
-          }
-          al = al * 0.5f;
-        }
-        alpha = al;
-      }
-
-      // ---- update (lbfgs_batch.py:305-322) ----
-      Slots<SPL> sv, xn;
-#pragma unroll
-      for (int s = 0; s < SPL; ++s) {
-        sv.v[s] = P.active(s) ? __fmul_rn(alpha, p.v[s]) : 0.f;
-        xn.v[s] = __fadd_rn(x.v[s], sv.v[s]);
-      }
-      Point<SPL> nxt;
-      if (known) {
-        nxt = acc;
-      } else {
-        nxt.phi = closure<V, SPL>(A, S, P, xn, nxt.g, err);
-        ++evals;
-      }
-      if (P.has_virtual) {
-        const int vs = P.K;  // virtual slot index
-        bool vnan = false;
+        x = xn;
+        g = nxt.g;
+        f = nxt.phi;
+        ++it;
+        // all real slots NaN and the others poisoned: nothing can change any more
+        bool allnan = true;
 #pragma unroll
         for (int s = 0; s < SPL; ++s)
-          if (s * 32 + lane == vs && isnan(sv.v[s])) vnan = true;
-        poison = poison || __any_sync(0xffffffffu, vnan);
+          if (P.real(s) && !isnan(x.v[s])) allnan = false;
+        allnan = __all_sync(0xffffffffu, allnan);
+        if (P.K > 0 && allnan && (poison || !P.has_virtual)) {
+          it = A.max_iter;
+          phase = PH_DONE;
+        } else {
+          begin_iter = true;
+        }
       }
-      // push (s, y): drop the oldest pair when the history is full
-      int slot;
-      if (h < A.hist) {
-        slot = (head + h) % A.hist;
-        ++h;
-      } else {
-        slot = head;
-        head = (head + 1) % A.hist;
-      }
-#pragma unroll
-      for (int s = 0; s < SPL; ++s) {
-        ringS[slot * SPL * 32 + s * 32 + lane] = sv.v[s];
-        ringY[slot * SPL * 32 + s * 32 + lane] = P.active(s) ? __fsub_rn(nxt.g.v[s], g.v[s]) : 0.f;
-      }
-      __syncwarp();
-      x = xn;
-      g = nxt.g;
-      f = nxt.phi;
 
-      // all real slots NaN and the others poisoned: nothing can change any more
-      bool allnan = true;
+      // ---- start of an outer iteration: convergence test, direction, line search ----
+      if (begin_iter) {
+        if (it >= A.max_iter || sqrt(dot(P, g, g)) < A.tol) {
+          phase = PH_DONE;
+        } else {
+          // two-loop recursion (lbfgs_batch.py:65-103)
+          Slots<SPL> q = g;
+          if (h > 0) {
+            for (int i = h - 1; i >= 0; --i) {
+              const int sl = (head + i) % A.hist;
+              Slots<SPL> si, yi;
 #pragma unroll
-      for (int s = 0; s < SPL; ++s)
-        if (P.real(s) && !isnan(x.v[s])) allnan = false;
-      allnan = __all_sync(0xffffffffu, allnan);
-      if (P.K > 0 && allnan && (poison || !P.has_virtual)) {
-        it = A.max_iter;
-        break;
+              for (int s = 0; s < SPL; ++s) {
+                si.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
+                yi.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
+              }
+              const double rho = 1.0 / __dadd_rn(dot(P, yi, si), A.eps);
+              const double a = __dmul_rn(rho, dot(P, si, q));
+#pragma unroll
+              for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dsub_rn((double)q.v[s], __dmul_rn(a, (double)yi.v[s]));
+              if (lane == 0) {
+                alph[i] = a;
+                rhos[i] = rho;
+              }
+            }
+            __syncwarp();
+            {
+              const int sl = (head + h - 1) % A.hist;
+              Slots<SPL> sl_, yl_;
+#pragma unroll
+              for (int s = 0; s < SPL; ++s) {
+                sl_.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
+                yl_.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
+              }
+              const double gam = dot(P, sl_, yl_) / __dadd_rn(dot(P, yl_, yl_), A.eps);
+#pragma unroll
+              for (int s = 0; s < SPL; ++s) q.v[s] = (float)(gam * (double)q.v[s]);
+            }
+            for (int i = 0; i < h; ++i) {
+              const int sl = (head + i) % A.hist;
+              Slots<SPL> si, yi;
+#pragma unroll
+              for (int s = 0; s < SPL; ++s) {
+                si.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
+                yi.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
+              }
+              const double be = __dmul_rn(rhos[i], dot(P, yi, q));
+              const double coef = __dsub_rn(alph[i], be);
+#pragma unroll
+              for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dadd_rn((double)q.v[s], __dmul_rn((double)si.v[s], coef));
+            }
+          }
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) p.v[s] = P.active(s) ? -q.v[s] : 0.f;
+          phi0 = f;
+          dphi0 = (float)dot(P, g, p);
+          lsi = 0;
+          if (A.ls_kind == 0) {
+            a_prev = 0.f;
+            phi_prev = phi0;
+            a_i = 1.f;
+            phase = PH_BRACKET;
+            if (A.ls_max <= 0) {  // no bracket step: alpha = 1, not evaluated
+              alpha = a_i;
+#pragma unroll
+              for (int s = 0; s < SPL; ++s) xn.v[s] = __fadd_rn(x.v[s], P.active(s) ? __fmul_rn(alpha, p.v[s]) : 0.f);
+              phase = PH_UPDATE;
+            }
+          } else {
+            al = 1.f;
+            phase = PH_BACKTRACK;
+            if (A.ls_max <= 0) {
+              alpha = al;
+#pragma unroll
+              for (int s = 0; s < SPL; ++s) xn.v[s] = __fadd_rn(x.v[s], P.active(s) ? __fmul_rn(alpha, p.v[s]) : 0.f);
+              phase = PH_UPDATE;
+            }
+          }
+        }
       }
     }
 
@@ -619,7 +721,14 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
       if (A.loss_out) A.loss_out[P.b] = f;
       if (A.evals_out) A.evals_out[P.b] = evals;
     }
-    if (A.Y_final) final_forward<V, SPL>(A, S, P, x);
+    if (A.Y_final) {
+#pragma unroll
+      for (int s = 0; s < SPL; ++s)
+        if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = x.v[s];
+      __syncwarp();
+      int dummy = 0;
+      tape_pass<V, false>(A, S, P.b, P.root, P.K, lane, dummy);
+    }
     __syncwarp();
   }
 }
