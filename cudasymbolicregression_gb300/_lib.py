@@ -53,6 +53,8 @@ _SIGS = {
                       ctypes.POINTER(FitOptions), vp, i64, vp, vp], ctypes.c_int),
     "sr_fit_lbfgs_static_scratch": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, vp, vp,
                                      i32, i32, ctypes.POINTER(FitOptions), vp, vp], ctypes.c_int),
+    "sr_postfix_children": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
+    "sr_postfix_to_infix": ([vp, i64, i64, i32, vp, i64, vp, vp], ctypes.c_int),
     "sr_const_offsets": ([vp, i64, i64, i64, i64, vp, vp], ctypes.c_int),
     "sr_const_scatter": ([vp, i64, i64, i64, i64, vp, vp, vp, vp], ctypes.c_int),
 }

@@ -1,0 +1,215 @@
+// sr_notation.cu -- integer tape conversions used around the fitting path:
+//   * child table of left-packed postfix tapes   (reference get_postfix_children,
+//     src/pcfg_cuda.cu:1228-1300, src/pcfg.cpp:957-986)
+//   * postfix -> infix token ids with parentheses (reference postfix_to_infix,
+//     src/pcfg_cuda.cu:502-701, src/pcfg.cpp:790-826)
+// Both are bit-exact integer transformations with the reference's error codes and
+// stack limits (128 entries, 3 x 128 output tokens).  One thread owns one tape; a
+// warp's 32 tapes are read with 8-byte loads that stay in L1 across the row.
+#include <cstdint>
+
+#include "sr_common.cuh"
+#include "sr_ops.cuh"
+
+namespace sr {
+
+constexpr int kStackLimit = 128;  // the reference's HARD_MAX_LENGTH
+
+enum NotationCode : int64_t {
+  SYM_NEGATIVE = -1,  // a symbol < 0
+  SYM_TOO_LARGE = -2, // a symbol >= n_operators
+  PARSE_UNEXPECTED_TOKEN = 408,
+  PARSE_UNARY_MISSING = 404,
+  PARSE_BINARY_MISSING = 405,
+  PARSE_STACK_OVERFLOW = 406,
+  PARSE_MALFORMED = 407,
+  CONV_TOO_LONG = 501,
+  CONV_STACK_OVERFLOW = 504,
+  CONV_UNARY_MISSING = 505,
+  CONV_BINARY_MISSING = 506,
+  CONV_MULTIPLE_ROOTS = 508,
+  CONV_UNEXPECTED_TOKEN = 509,
+};
+
+// Symbols must lie in [0, n_operators): -1 / -2 flag the two ways to fail.
+__device__ __forceinline__ int64_t symbol_check(const int64_t* row, int64_t M, int64_t n_operators) {
+  int64_t flag = 0;
+  for (int64_t i = 0; i < M; ++i) {
+    const int64_t t = row[i];
+    if (t < 0) return SYM_NEGATIVE;
+    if (t >= n_operators) flag = SYM_TOO_LARGE;
+  }
+  return flag;
+}
+
+// Unary operators written f(x); the others (^2, ^3, ^4, ^5, ^-1) are written (x)^k.
+__device__ __forceinline__ bool functional_style(int64_t op) {
+  return (op >= SIN && op <= LOG) || (op >= SQRT && op <= NEG);
+}
+
+__global__ void postfix_children_kernel(const int64_t* __restrict__ ops, int64_t B, int64_t M, int64_t n_operators,
+                                        int64_t* __restrict__ ch, int64_t* __restrict__ err) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int64_t* row = ops + b * M;
+  int64_t* out = ch + b * M * 2;
+  for (int64_t i = 0; i < 2 * M; ++i) out[i] = -1;
+  int64_t e = symbol_check(row, M, n_operators);
+  if (e) {
+    err[b] = e;
+    return;
+  }
+  int stack[kStackLimit];
+  int sp = 0;
+  bool ended = false;
+  for (int64_t i = 0; i < M; ++i) {
+    const int64_t t = row[i];
+    if (t == NO_OP) {
+      ended = true;
+      continue;
+    }
+    if (ended) { e = PARSE_UNEXPECTED_TOKEN; break; }
+    const int ar = arity_of(t);
+    if (ar == 1) {
+      if (sp < 1) { e = PARSE_UNARY_MISSING; break; }
+      out[i * 2] = stack[--sp];
+    } else if (ar == 2) {
+      if (sp < 2) { e = PARSE_BINARY_MISSING; break; }
+      const int right = stack[--sp];
+      const int left = stack[--sp];
+      out[i * 2] = left;
+      out[i * 2 + 1] = right;
+    }
+    if (sp >= kStackLimit) { e = PARSE_STACK_OVERFLOW; break; }
+    stack[sp++] = (int)i;
+  }
+  if (!e && sp != 1) e = PARSE_MALFORMED;
+  err[b] = e;
+}
+
+// Right-to-left rendering: the output is built backwards from the end of a
+// 3 x 128 buffer.  An operator first emits ")" (and, for (x)^k forms, its own
+// token); once its right operand is complete a binary operator emits itself, once
+// its left operand is complete it emits "(".  A unary f emits "( f" when its operand
+// is complete, a (x)^k form emits "(".
+__global__ void postfix_to_infix_kernel(const int64_t* __restrict__ ops, int64_t B, int64_t M, int64_t n_operators,
+                                        int64_t lparen, int64_t rparen, int64_t* __restrict__ infix, int64_t M_out,
+                                        int64_t* __restrict__ err) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int64_t* row = ops + b * M;
+  int64_t* out = infix + b * M_out;
+  for (int64_t i = 0; i < M_out; ++i) out[i] = NO_OP;
+  int64_t e = symbol_check(row, M, n_operators);
+  if (e) {
+    err[b] = e;
+    return;
+  }
+  // shape check from the right: padding only at the end, one root
+  bool started = false;
+  int len = 0, balance = 0, roots = 0;
+  for (int64_t k = M - 1; k >= 0; --k) {
+    const int64_t t = row[k];
+    if (t == NO_OP) {
+      if (started) { err[b] = CONV_UNEXPECTED_TOKEN; return; }
+    } else {
+      started = true;
+      ++len;
+      balance += arity_of(t) - 1;
+      if (balance == -1) ++roots;
+    }
+  }
+  if (len == 0) { err[b] = 0; return; }
+  if (roots > 1) { err[b] = CONV_MULTIPLE_ROOTS; return; }
+
+  constexpr int kBuf = 3 * kStackLimit;
+  int32_t buf[kBuf];
+  int32_t opst[kStackLimit];
+  int8_t waiting_left[kStackLimit];
+  int top = kBuf - 1;  // next free slot, filled downwards
+  int sp = 0;
+#define SR_EMIT(tok)                                \
+  do {                                              \
+    if (top < 0) { err[b] = CONV_STACK_OVERFLOW; return; } \
+    buf[top--] = (int32_t)(tok);                    \
+  } while (0)
+  for (int k = len - 1; k >= 0; --k) {
+    const int64_t t = row[k];
+    const int ar = arity_of(t);
+    if (ar == 0) {
+      SR_EMIT(t);
+      bool done = true;
+      while (done && sp > 0) {
+        const int32_t parent = opst[sp - 1];
+        if (arity_of(parent) == 1) {
+          if (functional_style(parent)) {
+            if (top - 1 < 0) { err[b] = CONV_STACK_OVERFLOW; return; }
+            buf[top--] = (int32_t)lparen;
+            buf[top--] = parent;
+          } else {
+            SR_EMIT(lparen);
+          }
+          --sp;
+        } else if (!waiting_left[sp - 1]) {
+          SR_EMIT(parent);
+          waiting_left[sp - 1] = 1;
+          done = false;
+        } else {
+          SR_EMIT(lparen);
+          --sp;
+        }
+      }
+    } else {
+      if (sp >= kStackLimit) { err[b] = CONV_STACK_OVERFLOW; return; }
+      opst[sp] = (int32_t)t;
+      waiting_left[sp] = 0;
+      if (ar == 1 && !functional_style(t)) SR_EMIT(t);
+      SR_EMIT(rparen);
+      ++sp;
+    }
+  }
+#undef SR_EMIT
+  if (sp > 0) {
+    err[b] = arity_of(opst[sp - 1]) == 1 ? CONV_UNARY_MISSING : CONV_BINARY_MISSING;
+    return;
+  }
+  const int n = kBuf - 1 - top;
+  if (n > M_out) { err[b] = CONV_TOO_LONG; return; }
+  for (int i = 0; i < n; ++i) out[i] = buf[top + 1 + i];
+  err[b] = 0;
+}
+
+}  // namespace sr
+
+extern "C" {
+
+int sr_postfix_children(const int64_t* ops, int64_t B, int64_t M, int32_t n_vars, int64_t* ch, int64_t* err,
+                        void* stream) {
+  using namespace sr;
+  if (B < 0 || M < 0 || n_vars < 0 || (B > 0 && (!ops || !ch || !err))) {
+    set_error("invalid arguments");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
+  if (B == 0) return SR_OK;
+  const int threads = 128;
+  postfix_children_kernel<<<(unsigned)((B + threads - 1) / threads), threads, 0, as_stream(stream)>>>(
+      ops, B, M, (int64_t)VAR + n_vars, ch, err);
+  return launch_check("postfix_children_kernel");
+}
+
+int sr_postfix_to_infix(const int64_t* ops, int64_t B, int64_t M, int32_t n_vars, int64_t* infix, int64_t M_out,
+                        int64_t* err, void* stream) {
+  using namespace sr;
+  if (B < 0 || M < 0 || M_out < 0 || n_vars < 0 || (B > 0 && (!ops || !err || (M_out > 0 && !infix)))) {
+    set_error("invalid arguments");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
+  if (B == 0) return SR_OK;
+  const int threads = 128;
+  const int64_t lparen = (int64_t)VAR + n_vars, rparen = lparen + 1;
+  postfix_to_infix_kernel<<<(unsigned)((B + threads - 1) / threads), threads, 0, as_stream(stream)>>>(
+      ops, B, M, (int64_t)VAR + n_vars, lparen, rparen, infix, M_out, err);
+  return launch_check("postfix_to_infix_kernel");
+}
+
+}  // extern "C"

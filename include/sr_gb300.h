@@ -193,6 +193,25 @@ int sr_const_scatter(const int64_t *ops_dev, int64_t R, int64_t Cc, int64_t s0, 
                      const int64_t *offsets_dev, const float *values_dev, float *out_dev,
                      void *stream);
 
+/*
+ * Child table of left-packed postfix tapes: ch (B, M, 2) int64 (-1 = no child) and
+ * err (B) int64 per tape: 0, the reference's codes 404/405/406/407/408, or -1 / -2
+ * when a symbol is negative / not below VAR_START_ID + n_vars.  Replaces
+ * get_postfix_children (reference src/pcfg_cuda.cu:1228-1300, src/pcfg.cpp:957-986).
+ * ops (B, M) int64 contiguous.
+ */
+int sr_postfix_children(const int64_t *ops_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *ch_dev,
+                        int64_t *err_dev, void *stream);
+
+/*
+ * Postfix tapes to infix token ids with parentheses: infix (B, M_out) int64, NO_OP
+ * padded; "(" = VAR_START_ID + n_vars, ")" = "(" + 1.  err (B) int64: 0, the
+ * reference's codes 501/504/505/506/508/509, or -1 / -2 as above.  Replaces
+ * postfix_to_infix (reference src/pcfg_cuda.cu:502-701, src/pcfg.cpp:790-826).
+ */
+int sr_postfix_to_infix(const int64_t *ops_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *infix_dev,
+                        int64_t M_out, int64_t *err_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -260,6 +260,92 @@ def case_rosenbrock(st):
                         x_backtracking=res["backtracking"])
 
 
+NOTATION_GRAMMAR = """E -> E + F [0.2]
+E -> E - F [0.2]
+E -> F [0.6]
+F -> F * T [0.2]
+F -> F / T [0.2]
+F -> T [0.6]
+T -> ( E ) P [0.1]
+T -> R ( E ) [0.3]
+T -> V [0.4]
+T -> ( E ) [0.2]
+V -> X_0 [0.2]
+V -> X_1 [0.2]
+V -> C [0.3]
+V -> 5 [0.3]
+R -> sin [0.2]
+R -> cos [0.2]
+R -> exp [0.2]
+R -> sqrt [0.2]
+R -> log [0.2]
+P -> ^2 [0.25]
+P -> ^3 [0.25]
+P -> ^4 [0.25]
+P -> ^5 [0.25]
+"""
+
+
+def case_notation(st):
+    """get_postfix_children / postfix_to_infix / to_string on PCFG samples and on
+    generated tapes over every operator, plus the error messages of malformed rows."""
+    torch.manual_seed(3)
+    pcfg = st.ProbabilisticContextFreeGrammar(NOTATION_GRAMMAR, "E", 64, 2, torch.device("cpu"))
+    infix = pcfg.sample_infix(400)
+    post = pcfg.infix_to_postfix(infix)
+    ch = pcfg.get_postfix_children(post)
+    inf = pcfg.postfix_to_infix(post, 100)
+    strings = pcfg.to_string(inf)
+    tb = tapes.generate(300, 40, seed=21, mean_length=14, n_vars=2, unary=ALL_UNARY, binary=ALL_BINARY,
+                        p_const_leaf=0.3)
+    ops_all = tb.ops.copy()
+    consts = np.array([2, 3, 4, 5, 6, 7, 8], np.int64)
+    rng = np.random.default_rng(5)
+    hard = (ops_all == 1) & (rng.random(ops_all.shape) < 0.3)
+    ops_all[hard] = consts[rng.integers(0, 7, size=int(hard.sum()))]
+    ch_all = pcfg.get_postfix_children(torch.tensor(ops_all))
+    inf_all = pcfg.postfix_to_infix(torch.tensor(ops_all), 200)
+    strings_all = pcfg.to_string(inf_all)
+    V = int(Operator.VAR_START_ID)
+    bad_rows = {
+        "unary_missing": [10, V, 40, 0],
+        "binary_missing": [V, 40, 0, 0],
+        "noop_inside": [V, 0, V, 40],
+        "too_many": [V, V, V, 40],
+        "empty": [0, 0, 0, 0],
+        "negative": [V, -3, 40, 0],
+        "too_large": [V, V + 2, 40, 0],
+    }
+    out = {}
+    for name, row in bad_rows.items():
+        x = torch.tensor([row], dtype=torch.int64)
+        for fn, kw in (("children", {}), ("infix", {"max_infix_len": 10})):
+            try:
+                if fn == "children":
+                    r = pcfg.get_postfix_children(x)
+                else:
+                    r = pcfg.postfix_to_infix(x, 10)
+                out[f"{name}__{fn}"] = r.numpy()
+                out[f"{name}__{fn}_msg"] = np.array("")
+            except RuntimeError as e:
+                out[f"{name}__{fn}_msg"] = np.array(str(e))
+        out[f"{name}__row"] = np.array([row], np.int64)
+    # output exactly as long as the infix, and one token shorter
+    x = torch.tensor([[V, V + 1, 40, 10]], dtype=torch.int64)
+    full = pcfg.postfix_to_infix(x, 20)
+    n = int((full != 0).sum())
+    out["exact_len"] = pcfg.postfix_to_infix(x, n).numpy()
+    try:
+        pcfg.postfix_to_infix(x, n - 1)
+        out["short_msg"] = np.array("")
+    except RuntimeError as e:
+        out["short_msg"] = np.array(str(e))
+    out["exact_row"] = x.numpy()
+    np.savez_compressed(os.path.join(OUT, "notation.npz"), post=post.numpy(), ch=ch.numpy(), infix=inf.numpy(),
+                        strings=np.array(strings), ops_all=ops_all, ch_all=ch_all.numpy(), infix_all=inf_all.numpy(),
+                        strings_all=np.array(strings_all), **out)
+
+
 def main():
     st = build_ref.load_reference()
     torch.set_num_threads(1)
@@ -275,6 +361,7 @@ def main():
     case_optimize_ragged(st)
     case_optimize_ragged(st, B=48, max_iter=30, line_search="backtracking", name="optimize_ragged_bt")
     case_rosenbrock(st)
+    case_notation(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))
