@@ -750,9 +750,8 @@ static int fit_defaults(const sr_fit_options* o, sr_fit_options& r) {
     set_error("invalid fit options");
     return SR_ERR_INVALID_ARGUMENT;
   }
-  if (r.points_per_lane == 0) r.points_per_lane = 1;
-  if (r.points_per_lane != 1 && r.points_per_lane != 2 && r.points_per_lane != 4) {
-    set_error("points_per_lane must be 1, 2 or 4");
+  if (r.points_per_lane != 0 && r.points_per_lane != 1 && r.points_per_lane != 2 && r.points_per_lane != 4) {
+    set_error("points_per_lane must be 0 (automatic), 1, 2 or 4");
     return SR_ERR_INVALID_ARGUMENT;
   }
   return SR_OK;
@@ -791,8 +790,11 @@ static void* pick_kernel(int V, int SPL) {
   }
 }
 
+// Launch shape: points per lane (V) and warps per CTA.  Unless the caller fixes
+// them, every candidate is scored by the warps it keeps resident on an SM (shared
+// memory and registers both limit it), with two points per lane counted as worth
+// 1.6 warps (their independent chains hide latency within one warp).
 static int fit_shape(int64_t B, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
-  sh.V = o.points_per_lane;
   sh.SPL = spl_for(Kmax);
   if (!sh.SPL) {
     set_error("at most 127 learnable constants per tape are supported (got %d)", Kmax);
@@ -802,30 +804,48 @@ static int fit_shape(int64_t B, int Lmax, int Kmax, const sr_fit_options& o, Fit
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t wb = fit_warp_bytes(Lmax, Kmax, sh.V);
-  int warps = o.warps_per_block > 0 ? o.warps_per_block : 4;
-  if (warps > 8) warps = 8;  // __launch_bounds__(256)
-  while (warps > 1 && wb * warps > (size_t)optin) warps >>= 1;
-  if (wb * warps > (size_t)optin) {
+  const int vc[3] = {1, 2, 4};
+  const int wc[4] = {1, 2, 4, 8};
+  double best = -1.0;
+  int bestV = 0, bestW = 0, bestPerSm = 0;
+  for (int vi = 0; vi < 3; ++vi) {
+    const int V = vc[vi];
+    if (o.points_per_lane ? V != o.points_per_lane : V == 4) continue;
+    void* k = pick_kernel(V, sh.SPL);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+      set_error("fit kernel shared memory attribute failed");
+      return SR_ERR_CUDA;
+    }
+    const size_t wb = fit_warp_bytes(Lmax, Kmax, V);
+    for (int wi = 0; wi < 4; ++wi) {
+      const int w = wc[wi];
+      if (o.warps_per_block > 0 && w != (o.warps_per_block > 8 ? 8 : o.warps_per_block)) continue;
+      if (wb * w > (size_t)optin) continue;
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, w * 32, wb * w) != cudaSuccess || per_sm < 1)
+        continue;
+      const double score = per_sm * w * (V == 1 ? 1.0 : V == 2 ? 1.6 : 2.4) + 1e-3 * w;
+      if (score > best) {
+        best = score;
+        bestV = V;
+        bestW = w;
+        bestPerSm = per_sm;
+      }
+    }
+  }
+  if (best < 0) {
     set_error("tape of %d nodes does not fit in shared memory for the fit kernel", Lmax);
     return SR_ERR_UNSUPPORTED;
   }
-  sh.warps = warps;
-  sh.smem = wb * warps;
-  void* k = pick_kernel(sh.V, sh.SPL);
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem) != cudaSuccess) {
-    set_error("fit kernel shared memory attribute failed");
-    return SR_ERR_CUDA;
-  }
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, warps * 32, sh.smem) != cudaSuccess || per_sm < 1)
-    per_sm = 1;
-  int64_t blocks = o.grid_blocks > 0 ? o.grid_blocks : (int64_t)sms * per_sm;
-  const int64_t need = (B + warps - 1) / warps;
+  sh.V = bestV;
+  sh.warps = bestW;
+  sh.smem = fit_warp_bytes(Lmax, Kmax, bestV) * bestW;
+  int64_t blocks = o.grid_blocks > 0 ? o.grid_blocks : (int64_t)sms * bestPerSm;
+  const int64_t need = (B + bestW - 1) / bestW;
   if (blocks > need) blocks = need;
   if (blocks < 1) blocks = 1;
   sh.blocks = (int)blocks;
-  sh.total_warps = blocks * warps;
+  sh.total_warps = blocks * bestW;
   return SR_OK;
 }
 
@@ -987,6 +1007,7 @@ extern "C" int sr_fit_lbfgs_static_scratch(const float* X, int64_t N, int64_t n_
   if (rc) return rc;
   o.grid_blocks = (int32_t)blocks;
   o.warps_per_block = sh.warps;
+  o.points_per_lane = sh.V;
   return sr_fit_lbfgs(X, N, n_x, Y, desc, meta, B, M, C_init, C_out, c_sb, c_sm, Y_final, iters_out, loss_out,
                       evals_out, order, max_len, max_consts, &o, scratch, kStaticFitScratchBytes, status, stream);
 }

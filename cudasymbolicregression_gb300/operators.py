@@ -94,6 +94,7 @@ class ErrorCode(enum.IntEnum):
     PARSING_TREE_BINARY_OP_MISSING_OPERANDS = 405
     PARSING_TREE_CHILD_STACK_OVERFLOW = 406
     PARSING_TREE_MALFORMED_EXPRESSION = 407
+    PARSING_UNEXPECTED_TOKEN = 408
     CONVERSION_RESULTING_INFIX_TOO_LONG = 501
     CONVERSION_INTERNAL_STACK_OVERFLOW = 504
     CONVERSION_UNARY_OP_MISSING_OPERAND = 505
@@ -112,11 +113,21 @@ _MESSAGES = {
     102: "Validation failed: Operator arity does not match the number of children.",
     201: "Backward pass error: A non-zero gradient was passed to a NO_OP node.",
     204: "Backward pass error: Gradient for a/b where b = 0.",
+    301: "Generation failed: Internal stack exceeded capacity.",
+    302: "Generation failed: Produced expression exceeded maximum length.",
+    303: "Generation failed: Could not produce a valid expression within the max_tries limit.",
+    304: "Generation failed: No valid production rule found during sampling.",
+    401: "Parsing failed: Output queue overflowed (expression likely too complex).",
+    402: "Parsing failed: Operator stack overflowed (expression likely too complex).",
+    403: "Parsing failed: Mismatched or unbalanced parentheses.",
     404: "Parsing failed: Unary operator is missing an operand during tree construction.",
     405: "Parsing failed: Binary operator is missing one or both operands during tree construction.",
     406: "Parsing failed: Child stack overflowed during tree construction.",
     407: "Parsing failed: Malformed expression (e.g., too many operands).",
+    408: "Parsing failed: Unexpected token encountered during parsing.",
     501: "Conversion failed: Resulting infix expression is longer than the maximum allowed length.",
+    502: "Conversion failed: Resulting postfix expression is longer than the maximum allowed length.",
+    503: "Conversion failed: Resulting prefix expression is longer than the maximum allowed length.",
     505: "Conversion failed: Malformed input, unary operator is missing an operand.",
     506: "Conversion failed: Malformed input, binary operator is missing one or both operands.",
     507: "Conversion failed: Malformed input (e.g., too many operands).",

@@ -11,6 +11,8 @@ from __future__ import annotations
 from dataclasses import dataclass
 from typing import Literal, Optional, Tuple
 
+import ctypes
+
 import torch
 
 from . import _lib
@@ -31,7 +33,8 @@ class FitResult:
 def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, *,
          objective: int = 0, line_search_max_iter: int = 10, eps: float = 1e-10,
          warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
-         order: Optional[torch.Tensor] = None, want_y: bool = True, raise_errors: bool = True) -> FitResult:
+         order: Optional[torch.Tensor] = None, want_y: bool = True, raise_errors: bool = True,
+         class_width: int = 16) -> FitResult:
     if line_search_fn not in ("strong_wolfe", "backtracking"):
         raise ValueError(f"Invalid line_search_fn: {line_search_fn}. Choose 'strong_wolfe' or 'backtracking'.")
     if Ops.dim() != 2:
@@ -58,39 +61,55 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
                            objective=int(objective), warps_per_block=int(warps_per_block),
                            points_per_lane=int(points_per_lane), grid_blocks=int(grid_blocks))
     L = _lib.lib()
-    max_len = max(tapes.max_root, 1)
-    wsb = L.sr_fit_workspace_bytes(B, max_len, tapes.max_consts, opts)
-    if wsb < 0:
-        _lib.check(-1, "sr_fit_workspace_bytes")
-    ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)
     C_out = torch.empty((B, M), dtype=torch.float32, device=dev)
     Y_out = torch.empty((B, N), dtype=torch.float32, device=dev) if want_y else None
     iters = torch.empty(B, dtype=torch.int32, device=dev)
     loss = torch.empty(B, dtype=torch.float32, device=dev)
     evals = torch.empty(B, dtype=torch.int32, device=dev)
-    status = torch.empty(1, dtype=torch.int32, device=dev)
-    if order is None and B > 1:
+    Cin = C_init.to(torch.float32).contiguous()
+    lens = tapes.meta[:, 1] + 1
+    if order is None:
         # longest tapes first: the persistent warps then finish at about the same time
-        order = torch.argsort(tapes.meta[:, 1], descending=True, stable=True).to(torch.int32)
-    rc = _fit_call(L, Xc, N, nx, Y, tapes, B, M, C_init, C_out, Y_out, iters, loss, evals, order, max_len, opts, ws,
-                   status, dev)
-    _lib.check(rc, "sr_fit_lbfgs")
-    code = int(status.item())
+        order = torch.argsort(lens, descending=True, stable=True).to(torch.int32)
+        classes = _length_classes(lens, order, class_width) if class_width > 0 else [(0, B, max(tapes.max_root, 1))]
+    else:
+        order = order.to(device=dev, dtype=torch.int32).contiguous()
+        classes = [(0, B, max(tapes.max_root, 1))]
+    status = torch.zeros(max(len(classes), 1), dtype=torch.int32, device=dev)
+    for ci, (start, count, max_len) in enumerate(classes):
+        if count == 0:
+            continue
+        # one launch per class of tape lengths: the per-warp shared memory is sized
+        # for the class, so short tapes run with more resident warps
+        wsb = L.sr_fit_workspace_bytes(count, max_len, tapes.max_consts, opts)
+        if wsb < 0:
+            _lib.check(-1, "sr_fit_workspace_bytes")
+        ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)
+        optr = ctypes.c_void_p(order.data_ptr() + 4 * start)
+        rc = L.sr_fit_lbfgs(_lib.ptr(Xc), N, nx, _lib.ptr(Y), _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), count, M,
+                            _lib.ptr(Cin), _lib.ptr(C_out), M, 1, _lib.ptr(Y_out), _lib.ptr(iters), _lib.ptr(loss),
+                            _lib.ptr(evals), optr, max_len, tapes.max_consts, opts, _lib.ptr(ws), ws.numel(),
+                            ctypes.c_void_p(status.data_ptr() + 4 * ci), _lib.stream_ptr(dev))
+        _lib.check(rc, "sr_fit_lbfgs")
+    codes = [c for c in status.tolist() if c]
+    code = codes[0] if codes else 0
     if code and raise_errors:
         ctx = "input validation" if code in (101, 102) else "symbolic evaluation backward pass"
         raise RuntimeError(error_message(code, ctx))
     return FitResult(C=C_out, Y=Y_out, iters=iters, loss=loss, evals=evals)
 
 
-def _fit_call(L, Xc, N, nx, Y, tapes, B, M, C_init, C_out, Y_out, iters, loss, evals, order, max_len, opts, ws,
-              status, dev):
-    # The kernel reads C_init and writes C_out through the same (b, m) strides, so
-    # C_init is made contiguous like C_out.
-    Cin = C_init.to(torch.float32).contiguous()
-    return L.sr_fit_lbfgs(_lib.ptr(Xc), N, nx, _lib.ptr(Y), _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), B, M,
-                          _lib.ptr(Cin), _lib.ptr(C_out), M, 1, _lib.ptr(Y_out), _lib.ptr(iters), _lib.ptr(loss),
-                          _lib.ptr(evals), _lib.ptr(order), max_len, tapes.max_consts, opts, _lib.ptr(ws),
-                          ws.numel(), _lib.ptr(status), _lib.stream_ptr(dev))
+def _length_classes(lens: torch.Tensor, order: torch.Tensor, width: int):
+    """(start, count, max_len) of each class of tape lengths along ``order``
+    (longest first); class c holds lengths in ((c-1)*width, c*width].  One host sync."""
+    cls = (lens[order.long()] + width - 1) // width
+    counts = torch.bincount(cls).tolist()
+    classes, start = [], 0
+    for c in range(len(counts) - 1, 0, -1):
+        if counts[c]:
+            classes.append((start, counts[c], c * width))
+            start += counts[c]
+    return classes
 
 
 def optimize(
@@ -125,7 +144,9 @@ def optimize_ex(X, Y, Ops, Ch, C_init, max_iter=100, history_size=10, tolerance_
 
     Extra keywords: line_search_max_iter, eps, objective (0 = MSE against Y,
     1 = mean of the root value; Y may be None), warps_per_block, points_per_lane,
-    grid_blocks (kernel shape), order (processing order), want_y, raise_errors
+    grid_blocks (kernel shape), order (processing order), want_y, class_width
+    (tapes are fitted in launches per class of lengths this many nodes wide, 0 =
+    one launch), raise_errors
     (False: problems whose closures hit error 201/204 are reported through
     ``iters < 0`` instead of aborting the whole batch as the reference does).
     """
