@@ -65,40 +65,63 @@ struct FitArgs {
   int32_t* status;
 };
 
-// Shared memory of one warp.
+// Shared memory.  The CTA works on one problem at a time: the tape, the constants
+// published for the current trial point, the slot maps and the cross-warp
+// reduction buffers are shared; each warp owns the node table of its own points.
 struct WarpSmem {
-  uint32_t* tape;  // [Lmax]
-  float* cnode;    // [Lmax] constant value of each node for the point being evaluated
-  int* node_slot;  // [Lmax] slot of each LEARNABLE node
-  int* slot_node;  // [Kmax]
-  float* vals;     // [Lmax][32V]
-  float* adj;      // [Lmax][32V]
-  double* gl;      // [Kmax][32] per-lane gradient partial sums
+  uint32_t* tape;    // [Lmax]                      (CTA)
+  float* cnode;      // [Lmax] constant of each node (CTA)
+  int* node_slot;    // [Lmax] slot of each LEARNABLE node (CTA)
+  int* slot_node;    // [Kmax]                      (CTA)
+  double* red_g;     // [W][Kmax] per-warp gradient sums (CTA)
+  double* red_l;     // [W] per-warp loss sums      (CTA)
+  int* red_e;        // [W] per-warp error codes    (CTA)
+  long long* task;   // the CTA's current problem   (CTA)
+  float* vals;       // [Lmax][32V]                 (warp)
+  float* adj;        // [Lmax][32V]                 (warp)
+  double* gl;        // [Kmax][32] per-lane gradient partial sums (warp)
 };
 
-__host__ __device__ __forceinline__ size_t fit_warp_bytes(int Lmax, int Kmax, int V) {
-  return fit_align16((size_t)Lmax * 4) * 3 + fit_align16((size_t)(Kmax > 0 ? Kmax : 1) * 4) +
-         2 * (size_t)Lmax * 32 * V * 4 + (size_t)(Kmax > 0 ? Kmax : 1) * 32 * 8;
+__host__ __device__ __forceinline__ size_t fit_shared_bytes(int Lmax, int Kmax, int W) {
+  const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
+  return fit_align16((size_t)Lmax * 4) * 3 + fit_align16(K * 4) + fit_align16((size_t)W * K * 8) +
+         fit_align16((size_t)W * 8) + fit_align16((size_t)W * 4) + 16;
 }
 
-__device__ __forceinline__ WarpSmem carve(unsigned char* p, int Lmax, int Kmax, int V) {
+__host__ __device__ __forceinline__ size_t fit_warp_bytes(int Lmax, int Kmax, int V) {
+  return 2 * (size_t)Lmax * 32 * V * 4 + (size_t)(Kmax > 0 ? Kmax : 1) * 32 * 8;
+}
+
+__host__ __device__ __forceinline__ size_t fit_cta_bytes(int Lmax, int Kmax, int V, int W) {
+  return fit_shared_bytes(Lmax, Kmax, W) + (size_t)W * fit_warp_bytes(Lmax, Kmax, V);
+}
+
+__device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Kmax, int V, int W, int warp) {
   WarpSmem s;
-  const size_t l4 = fit_align16((size_t)Lmax * 4);
-  const size_t k4 = fit_align16((size_t)(Kmax > 0 ? Kmax : 1) * 4);
-  s.gl = reinterpret_cast<double*>(p);
-  p += (size_t)(Kmax > 0 ? Kmax : 1) * 32 * 8;
-  s.vals = reinterpret_cast<float*>(p);
-  p += (size_t)Lmax * 32 * V * 4;
-  s.adj = reinterpret_cast<float*>(p);
-  p += (size_t)Lmax * 32 * V * 4;
+  const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
+  unsigned char* p = base;
+  s.red_g = reinterpret_cast<double*>(p);
+  p += fit_align16((size_t)W * K * 8);
+  s.red_l = reinterpret_cast<double*>(p);
+  p += fit_align16((size_t)W * 8);
   s.tape = reinterpret_cast<uint32_t*>(p);
-  p += l4;
+  p += fit_align16((size_t)Lmax * 4);
   s.cnode = reinterpret_cast<float*>(p);
-  p += l4;
+  p += fit_align16((size_t)Lmax * 4);
   s.node_slot = reinterpret_cast<int*>(p);
-  p += l4;
+  p += fit_align16((size_t)Lmax * 4);
   s.slot_node = reinterpret_cast<int*>(p);
-  p += k4;
+  p += fit_align16(K * 4);
+  s.red_e = reinterpret_cast<int*>(p);
+  p += fit_align16((size_t)W * 4);
+  s.task = reinterpret_cast<long long*>(p);
+  p += 16;
+  unsigned char* w = base + fit_shared_bytes(Lmax, Kmax, W) + (size_t)warp * fit_warp_bytes(Lmax, Kmax, V);
+  s.gl = reinterpret_cast<double*>(w);
+  w += K * 32 * 8;
+  s.vals = reinterpret_cast<float*>(w);
+  w += (size_t)Lmax * 32 * V * 4;
+  s.adj = reinterpret_cast<float*>(w);
   return s;
 }
 
@@ -180,14 +203,15 @@ __device__ __forceinline__ float var_value(const float (&xr)[V][kMaxRegVars], in
 // order (parents from the last to the first, child 0 before child 1).
 // ---------------------------------------------------------------------------------
 template <int V, bool kGrad>
-__device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int R, int K, int lane,
-                                           int& err) {
+__device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int R, int K, int lane,
+                                            int warp, int W, int& err) {
   const int64_t N = A.N;
   const float invN = 1.0f / (float)N;
   const float* __restrict__ Yrow = A.Y ? A.Y + b * N : nullptr;
   const bool xin = A.n_x <= kMaxRegVars;
   double loss_part = 0.0;
-  for (int64_t base = 0; base < N; base += 32 * V) {
+  // this warp's chunks of 32V points: warp, warp + W, warp + 2W, ...
+  for (int64_t base = (int64_t)warp * 32 * V; base < N; base += (int64_t)W * 32 * V) {
     int64_t nn[V];
     bool valid[V];
     float xr[V][kMaxRegVars];
@@ -316,36 +340,47 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
     }
     }  // kGrad
   }
-  return kGrad ? (float)(wsum_d(loss_part) / (double)N) : 0.f;
+  return kGrad ? wsum_d(loss_part) : 0.0;
 }
 
-// Closure: publish the trial constants, run the pass, reduce the gradient.
+// Closure: publish the trial constants, run the pass over this warp's points,
+// reduce loss and gradient over the lanes and then over the CTA's warps in a
+// fixed order (every warp ends with the same bits).  Two CTA barriers.
 template <int V, int SPL>
-__device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P,
+__device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P, int warp, int W,
                                          const Slots<SPL>& xt, Slots<SPL>& grad, int& err) {
   const int lane = P.lane;
+  if (warp == 0) {
 #pragma unroll
-  for (int s = 0; s < SPL; ++s)
-    if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = xt.v[s];
+    for (int s = 0; s < SPL; ++s)
+      if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = xt.v[s];
+  }
   for (int j = 0; j < P.K; ++j) S.gl[j * 32 + lane] = 0.0;
+  __syncthreads();
+  const double lpart = tape_pass<V, true>(A, S, P.b, P.root, P.K, lane, warp, W, err);
   __syncwarp();
-  const float loss = tape_pass<V, true>(A, S, P.b, P.root, P.K, lane, err);
-  __syncwarp();
-  // gradient of each real slot: the lane owning the slot sums the 32 lane partials
+  for (int j = lane; j < P.K; j += 32) {
+    double acc = 0.0;
+#pragma unroll 8
+    for (int l = 0; l < 32; ++l) acc += S.gl[j * 32 + l];
+    S.red_g[warp * P.K + j] = acc;
+  }
+  if (lane == 0) S.red_l[warp] = lpart;
+  __syncthreads();
 #pragma unroll
   for (int s = 0; s < SPL; ++s) {
     float gv = 0.f;
     if (P.real(s)) {
       const int j = s * 32 + lane;
       double acc = 0.0;
-#pragma unroll 8
-      for (int l = 0; l < 32; ++l) acc += S.gl[j * 32 + l];
+      for (int w = 0; w < W; ++w) acc += S.red_g[w * P.K + j];
       gv = (float)acc;
     }
     grad.v[s] = gv;
   }
-  __syncwarp();
-  return loss;
+  double lt = 0.0;
+  for (int w = 0; w < W; ++w) lt += S.red_l[w];
+  return (float)(lt / (double)A.N);
 }
 
 // Evaluated point: value and gradient.
@@ -364,10 +399,9 @@ enum Phase : int { PH_INIT = 0, PH_BRACKET, PH_ZOOM_LO, PH_ZOOM, PH_BACKTRACK, P
 template <int V, int SPL>
 __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  const size_t wbytes = fit_warp_bytes(A.Lmax, A.Kmax, V);
-  const WarpSmem S = carve(smem + warp * wbytes, A.Lmax, A.Kmax, V);
-  const int64_t gwarp = (int64_t)blockIdx.x * nwarp + warp;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+  const WarpSmem S = carve(smem, A.Lmax, A.Kmax, V, W, warp);
+  const int64_t gwarp = (int64_t)blockIdx.x * W + warp;
   float* ringS = A.ws_vec + gwarp * (int64_t)2 * A.hist * SPL * 32;
   float* ringY = ringS + (int64_t)A.hist * SPL * 32;
   double* alph = A.ws_scal + gwarp * (int64_t)2 * A.hist;
@@ -375,9 +409,11 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
   const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
 
   while (true) {
-    int64_t idx = 0;
-    if (lane == 0) idx = atomicAdd(A.counter, 1);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
+    // the CTA takes the next problem from the queue
+    if (threadIdx.x == 0) *S.task = (long long)atomicAdd(A.counter, 1);
+    __syncthreads();
+    const int64_t idx = (int64_t)*S.task;
+    __syncthreads();
     if (idx >= A.B) break;
     Problem<SPL> P;
     P.b = A.order ? (int64_t)A.order[idx] : idx;
@@ -388,10 +424,10 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
     P.nslots = P.K + (P.has_virtual ? 1 : 0);
     const int L = P.root + 1;
 
-    // stage the tape, map learnable nodes to slots
-    for (int k = lane; k < L; k += 32) S.tape[k] = A.desc[P.b * A.M + k];
-    __syncwarp();
-    {
+    // stage the tape, map learnable nodes to slots (warp 0), visible to the CTA
+    if (warp == 0) {
+      for (int k = lane; k < L; k += 32) S.tape[k] = A.desc[P.b * A.M + k];
+      __syncwarp();
       int base = 0;
       for (int k0 = 0; k0 < L; k0 += 32) {
         const int k = k0 + lane;
@@ -405,7 +441,7 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
         base += __popc(m);
       }
     }
-    __syncwarp();
+    __syncthreads();
 
     const float* Cin = A.C_init + P.b * A.c_sb;
     Slots<SPL> x, g, p, xn;
@@ -445,7 +481,7 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
         default: xt = xn; break;  // PH_UPDATE
       }
       Point<SPL> cur;
-      cur.phi = closure<V, SPL>(A, S, P, xt, cur.g, err);
+      cur.phi = closure<V, SPL>(A, S, P, warp, W, xt, cur.g, err);
       ++evals;
 
       // ---- advance the state machine ----
@@ -608,7 +644,7 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
         g = nxt.g;
         f = nxt.phi;
         ++it;
-        // all real slots NaN and the others poisoned: nothing can change any more
+        // all real slots NaN and the others poisoned: nothing can change any more (the same in every warp)
         bool allnan = true;
 #pragma unroll
         for (int s = 0; s < SPL; ++s)
@@ -704,32 +740,37 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
       }
     }
 
-    // errors are found per lane (per data point): combine them for the problem
+    // errors are found per lane (per data point): combine them over the CTA
     err = __reduce_max_sync(0xffffffffu, err);
-    if (err && lane == 0) report(A.status, err);
-    // ---- outputs ----
-    const float qnan = __int_as_float(0x7fffffff);
-    float* Cout = A.C_out + P.b * A.c_sb;
-    for (int64_t k = lane; k < A.M; k += 32) Cout[k * A.c_sm] = poison ? qnan : Cin[k * A.c_sm];
-    __syncwarp();
+    if (lane == 0) S.red_e[warp] = err;
+    __syncthreads();
+    for (int w = 0; w < W; ++w) err = max(err, S.red_e[w]);
+    // ---- outputs (warp 0) ----
+    if (warp == 0) {
+      if (err && lane == 0) report(A.status, err);
+      const float qnan = __int_as_float(0x7fffffff);
+      float* Cout = A.C_out + P.b * A.c_sb;
+      for (int64_t k = lane; k < A.M; k += 32) Cout[k * A.c_sm] = poison ? qnan : Cin[k * A.c_sm];
+      __syncwarp();
 #pragma unroll
-    for (int s = 0; s < SPL; ++s)
-      if (P.real(s)) Cout[(int64_t)S.slot_node[s * 32 + lane] * A.c_sm] = x.v[s];
-    if (lane == 0) {
-      // a problem whose closures raised an error reports -code instead of its iterations
-      if (A.iters_out) A.iters_out[P.b] = err ? -err : it;
-      if (A.loss_out) A.loss_out[P.b] = f;
-      if (A.evals_out) A.evals_out[P.b] = evals;
-    }
-    if (A.Y_final) {
+      for (int s = 0; s < SPL; ++s)
+        if (P.real(s)) Cout[(int64_t)S.slot_node[s * 32 + lane] * A.c_sm] = x.v[s];
+      if (lane == 0) {
+        // a problem whose closures raised an error reports -code instead of its iterations
+        if (A.iters_out) A.iters_out[P.b] = err ? -err : it;
+        if (A.loss_out) A.loss_out[P.b] = f;
+        if (A.evals_out) A.evals_out[P.b] = evals;
+      }
 #pragma unroll
       for (int s = 0; s < SPL; ++s)
         if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = x.v[s];
-      __syncwarp();
-      int dummy = 0;
-      tape_pass<V, false>(A, S, P.b, P.root, P.K, lane, dummy);
     }
-    __syncwarp();
+    __syncthreads();
+    if (A.Y_final) {
+      int dummy = 0;
+      tape_pass<V, false>(A, S, P.b, P.root, P.K, lane, warp, W, dummy);
+    }
+    __syncthreads();
   }
 }
 
@@ -790,11 +831,13 @@ static void* pick_kernel(int V, int SPL) {
   }
 }
 
-// Launch shape: points per lane (V) and warps per CTA.  Unless the caller fixes
-// them, every candidate is scored by the warps it keeps resident on an SM (shared
-// memory and registers both limit it), with two points per lane counted as worth
-// 1.6 warps (their independent chains hide latency within one warp).
-static int fit_shape(int64_t B, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
+// Launch shape.  A CTA of W warps works on one problem, each warp on every W-th
+// chunk of 32V points, so an expensive problem (many closures) finishes W times
+// sooner and the tail of the persistent grid shrinks.  Unless the caller fixes
+// them, W keeps about 128 points per warp (1..8 warps) and V is the one of 1 and 2
+// that keeps more work resident per SM (resident warps, with a warp of two points
+// per lane counted as 1.6 warps: its independent chains hide latency).
+static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
   sh.SPL = spl_for(Kmax);
   if (!sh.SPL) {
     set_error("at most 127 learnable constants per tape are supported (got %d)", Kmax);
@@ -804,48 +847,51 @@ static int fit_shape(int64_t B, int Lmax, int Kmax, const sr_fit_options& o, Fit
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  int W = o.warps_per_block;
+  if (W <= 0) {
+    W = 1;
+    while (W < 8 && (int64_t)W * 2 * 128 <= N) W *= 2;
+  }
+  if (W > 8) W = 8;  // __launch_bounds__(256)
   const int vc[3] = {1, 2, 4};
-  const int wc[4] = {1, 2, 4, 8};
   double best = -1.0;
-  int bestV = 0, bestW = 0, bestPerSm = 0;
-  for (int vi = 0; vi < 3; ++vi) {
-    const int V = vc[vi];
-    if (o.points_per_lane ? V != o.points_per_lane : V == 4) continue;
-    void* k = pick_kernel(V, sh.SPL);
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
-      set_error("fit kernel shared memory attribute failed");
-      return SR_ERR_CUDA;
-    }
-    const size_t wb = fit_warp_bytes(Lmax, Kmax, V);
-    for (int wi = 0; wi < 4; ++wi) {
-      const int w = wc[wi];
-      if (o.warps_per_block > 0 && w != (o.warps_per_block > 8 ? 8 : o.warps_per_block)) continue;
-      if (wb * w > (size_t)optin) continue;
+  int bestV = 0, bestPerSm = 0;
+  for (int w = W; w >= 1 && best < 0; w >>= 1) {
+    for (int vi = 0; vi < 3; ++vi) {
+      const int V = vc[vi];
+      if (o.points_per_lane ? V != o.points_per_lane : V == 4) continue;
+      void* k = pick_kernel(V, sh.SPL);
+      if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+        set_error("fit kernel shared memory attribute failed");
+        return SR_ERR_CUDA;
+      }
+      const size_t cb = fit_cta_bytes(Lmax, Kmax, V, w);
+      if (cb > (size_t)optin) continue;
       int per_sm = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, w * 32, wb * w) != cudaSuccess || per_sm < 1)
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, w * 32, cb) != cudaSuccess || per_sm < 1)
         continue;
-      const double score = per_sm * w * (V == 1 ? 1.0 : V == 2 ? 1.6 : 2.4) + 1e-3 * w;
+      const double score = per_sm * w * (V == 1 ? 1.0 : V == 2 ? 1.6 : 2.4);
       if (score > best) {
         best = score;
         bestV = V;
-        bestW = w;
         bestPerSm = per_sm;
+        W = w;
       }
     }
+    if (best < 0 && o.warps_per_block > 0) break;
   }
   if (best < 0) {
     set_error("tape of %d nodes does not fit in shared memory for the fit kernel", Lmax);
     return SR_ERR_UNSUPPORTED;
   }
   sh.V = bestV;
-  sh.warps = bestW;
-  sh.smem = fit_warp_bytes(Lmax, Kmax, bestV) * bestW;
+  sh.warps = W;
+  sh.smem = fit_cta_bytes(Lmax, Kmax, bestV, W);
   int64_t blocks = o.grid_blocks > 0 ? o.grid_blocks : (int64_t)sms * bestPerSm;
-  const int64_t need = (B + bestW - 1) / bestW;
-  if (blocks > need) blocks = need;
+  if (blocks > B) blocks = B;  // one problem per CTA at a time
   if (blocks < 1) blocks = 1;
   sh.blocks = (int)blocks;
-  sh.total_warps = blocks * bestW;
+  sh.total_warps = blocks * W;
   return SR_OK;
 }
 
@@ -859,12 +905,14 @@ static int64_t ws_bytes_for(const FitShape& sh, int hist) {
 
 extern "C" {
 
-int64_t sr_fit_workspace_bytes(int64_t B, int32_t max_len, int32_t max_consts, const sr_fit_options* opt) {
+int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len, int32_t max_consts,
+                               const sr_fit_options* opt) {
   sr_fit_options o;
   if (sr::fit_defaults(opt, o)) return -1;
   sr::FitShape sh;
-  const int Lmax = max_len < 1 ? 1 : max_len;
-  if (sr::fit_shape(B, Lmax, max_consts, o, sh)) return -1;
+  // the same node-table size sr_fit_lbfgs uses
+  const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)(M < 1 ? 1 : M);
+  if (sr::fit_shape(B, N, Lmax, max_consts, o, sh)) return -1;
   return sr::ws_bytes_for(sh, o.history_size);
 }
 
@@ -890,7 +938,7 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   }
   FitShape sh;
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  rc = fit_shape(B, Lmax, max_consts, o, sh);
+  rc = fit_shape(B, N, Lmax, max_consts, o, sh);
   if (rc) return rc;
   const int64_t need = ws_bytes_for(sh, o.history_size);
   if (workspace_bytes < need) {
@@ -982,7 +1030,7 @@ extern "C" int sr_fit_lbfgs_static_scratch(const float* X, int64_t N, int64_t n_
   // grid until its history rings fit in the static array.
   FitShape sh;
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  rc = fit_shape(B, Lmax, max_consts, o, sh);
+  rc = fit_shape(B, N, Lmax, max_consts, o, sh);
   if (rc) return rc;
   int64_t blocks = sh.blocks;
   while (blocks >= 1) {

@@ -34,7 +34,7 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
          objective: int = 0, line_search_max_iter: int = 10, eps: float = 1e-10,
          warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
          order: Optional[torch.Tensor] = None, want_y: bool = True, raise_errors: bool = True,
-         class_width: int = 16) -> FitResult:
+         class_width: int = 0) -> FitResult:
     if line_search_fn not in ("strong_wolfe", "backtracking"):
         raise ValueError(f"Invalid line_search_fn: {line_search_fn}. Choose 'strong_wolfe' or 'backtracking'.")
     if Ops.dim() != 2:
@@ -81,7 +81,8 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
             continue
         # one launch per class of tape lengths: the per-warp shared memory is sized
         # for the class, so short tapes run with more resident warps
-        wsb = L.sr_fit_workspace_bytes(count, max_len, tapes.max_consts, opts)
+        max_len = min(max_len, M)
+        wsb = L.sr_fit_workspace_bytes(count, N, M, max_len, tapes.max_consts, opts)
         if wsb < 0:
             _lib.check(-1, "sr_fit_workspace_bytes")
         ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)

@@ -122,19 +122,20 @@ typedef struct sr_fit_options {
   int32_t line_search_max_iter; /* 10 */
   double eps;                   /* 1e-10 */
   int32_t objective;            /* 0 = mean squared error vs Y, 1 = mean of the root value */
-  int32_t warps_per_block;      /* problems per CTA (0 = library default) */
-  int32_t points_per_lane;      /* data points per lane per pass: 1, 2 or 4 (0 = default) */
+  int32_t warps_per_block;      /* warps sharing one problem's points (0 = automatic) */
+  int32_t points_per_lane;      /* data points per lane per pass: 1, 2 or 4 (0 = automatic) */
   int32_t grid_blocks;          /* persistent CTAs (0 = one wave over all SMs) */
 } sr_fit_options;
 
 /* Bytes of device workspace sr_fit_lbfgs needs for this problem set
- * (max_len / max_consts as passed to sr_fit_lbfgs). */
-int64_t sr_fit_workspace_bytes(int64_t B, int32_t max_len, int32_t max_consts, const sr_fit_options *opt);
+ * (B, N, M, max_len, max_consts and opt as passed to sr_fit_lbfgs). */
+int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len, int32_t max_consts,
+                               const sr_fit_options *opt);
 
 /*
  * Fused batched L-BFGS fit of the learnable constants of every tape: one
- * persistent kernel in which each warp owns one problem at a time and runs the
- * whole optimisation (closure = forward + adjoint over all N points, two-loop
+ * persistent kernel in which each CTA owns one problem at a time (its warps split
+ * the data points) and runs the whole optimisation (closure = forward + adjoint over all N points, two-loop
  * recursion, strong-Wolfe or backtracking line search, history update) on chip.
  * Follows optimize() and LBFGS_batch per problem (reference
  * symbolic_torch/optimization.py:9-112, symbolic_torch/lbfgs_batch.py:61-326).

@@ -57,7 +57,8 @@ def test_static_scratch_matches_workspace_entry_point_twice(history):
     lib = L.lib()
     opts = L.FitOptions(max_iter=40, history_size=history, tolerance_grad=1e-7, line_search=0, line_search_max_iter=10,
                         eps=1e-10, objective=0, warps_per_block=0, points_per_lane=0, grid_blocks=0)
-    wsb = lib.sr_fit_workspace_bytes(tp.B, max(tp.max_root, 1), tp.max_consts, ctypes.byref(opts))
+    wsb = lib.sr_fit_workspace_bytes(tp.B, X.shape[0], tp.M, max(tp.max_root, 1), tp.max_consts,
+                                     ctypes.byref(opts))
     ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)
     ref = _call(L, lib.sr_fit_lbfgs, X, Y, tp, C, _outputs(tp.B, tp.M, X.shape[0], dev), opts, ws)
     for _ in range(2):  # the array keeps the previous call's contents; results must not depend on them
