@@ -34,6 +34,7 @@ class FitOptions(ctypes.Structure):
         ("warps_per_block", i32),
         ("points_per_lane", i32),
         ("grid_blocks", i32),
+        ("max_operators", i32),
     ]
 
 

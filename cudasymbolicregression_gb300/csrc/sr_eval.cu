@@ -91,12 +91,14 @@ __global__ void __launch_bounds__(256) tape_compile_kernel(const int64_t* __rest
     if (err) report(status, err);
     if (kStage) {
       const int root = count > 0 ? count - 1 : 0;
-      int kroot = 0, kall = 0;
+      int kroot = 0, kall = 0, nops = 0;
       for (int64_t m0 = 0; m0 < M; m0 += 32) {
         const int64_t m = m0 + lane;
-        const bool lc = m < M && ops[b * ops_sb + m * ops_sm] == LEARNABLE;
+        const int64_t op = m < M ? ops[b * ops_sb + m * ops_sm] : -1;
+        const bool lc = op == LEARNABLE;
         kall += __popc(__ballot_sync(0xffffffffu, lc));
         kroot += __popc(__ballot_sync(0xffffffffu, lc && m <= root));
+        nops += __popc(__ballot_sync(0xffffffffu, m <= root && (op == NO_OP || arity_of(op) >= 1)));
       }
       if (lane == 0) {
         meta[b * 4 + 0] = last + 1;
@@ -107,6 +109,7 @@ __global__ void __launch_bounds__(256) tape_compile_kernel(const int64_t* __rest
         atomicMax(status + 1, last + 1);
         atomicMax(status + 2, root + 1);
         atomicMax(status + 3, kroot);
+        atomicMax(status + 4, nops);
       }
     }
   }
@@ -362,7 +365,7 @@ static int launch_compile(const int64_t* ops, const int64_t* ch, int64_t B, int6
     return SR_ERR_UNSUPPORTED;
   }
   cudaStream_t st = as_stream(stream);
-  rc = cuda_check(cudaMemsetAsync(status, 0, (kStage ? 4 : 1) * sizeof(int32_t), st), "status reset");
+  rc = cuda_check(cudaMemsetAsync(status, 0, (kStage ? 8 : 1) * sizeof(int32_t), st), "status reset");
   if (rc || B == 0) return rc;
   const int threads = 256;
   int64_t blocks = (B + 7) / 8;

@@ -59,6 +59,7 @@ struct FitArgs {
   int max_iter, hist, ls_kind, ls_max, objective;
   double tol, eps;
   int Lmax, Kmax;
+  int Imax;         // rows of the per-warp node tables: largest count of operator nodes
   float* ws_vec;    // per warp: 2 * hist * SPL*32 floats (s and y rings)
   double* ws_scal;  // per warp: 2 * hist doubles (alpha, rho)
   int* counter;
@@ -70,33 +71,37 @@ struct FitArgs {
 // reduction buffers are shared; each warp owns the node table of its own points.
 struct WarpSmem {
   uint32_t* tape;    // [Lmax]                      (CTA)
-  float* cnode;      // [Lmax] constant of each node (CTA)
-  int* node_slot;    // [Lmax] slot of each LEARNABLE node (CTA)
+  uint32_t* pop;     // [Lmax] operator nodes: opcode | arity << 8              (CTA)
+  uint32_t* popnd;   // [Lmax] operator nodes: operand 0 | operand 1 << 16       (CTA)
+  float* cval;       // [Kmax] value of each constant slot at the trial point    (CTA)
+  int* info;         // [4] operator-node count, root operand                    (CTA)
+  int* node_slot;    // [Lmax] slot of a LEARNABLE node / row of an operator node (CTA)
   int* slot_node;    // [Kmax]                      (CTA)
   double* red_g;     // [W][Kmax] per-warp gradient sums (CTA)
   double* red_l;     // [W] per-warp loss sums      (CTA)
   int* red_e;        // [W] per-warp error codes    (CTA)
   long long* task;   // the CTA's current problem   (CTA)
-  float* vals;       // [Lmax][32V]                 (warp)
-  float* adj;        // [Lmax][32V]                 (warp)
-  double* gl;        // [Kmax][32] per-lane gradient partial sums (warp)
+  float* vals;       // [Imax][32V] values of the operator nodes (warp)
+  float* adj;        // [Imax][32V] their adjoints              (warp)
+  float* gl;         // [Kmax][32] per-lane gradient partial sums (warp)
 };
 
 __host__ __device__ __forceinline__ size_t fit_shared_bytes(int Lmax, int Kmax, int W) {
   const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
-  return fit_align16((size_t)Lmax * 4) * 3 + fit_align16(K * 4) + fit_align16((size_t)W * K * 8) +
-         fit_align16((size_t)W * 8) + fit_align16((size_t)W * 4) + 16;
+  return fit_align16((size_t)Lmax * 4) * 5 + fit_align16(K * 4) * 2 + fit_align16((size_t)W * K * 8) +
+         fit_align16((size_t)W * 8) + fit_align16((size_t)W * 4) + 16 + 16;
 }
 
-__host__ __device__ __forceinline__ size_t fit_warp_bytes(int Lmax, int Kmax, int V) {
-  return 2 * (size_t)Lmax * 32 * V * 4 + (size_t)(Kmax > 0 ? Kmax : 1) * 32 * 8;
+__host__ __device__ __forceinline__ size_t fit_warp_bytes(int Imax, int Kmax, int V) {
+  return 2 * (size_t)(Imax > 0 ? Imax : 1) * 32 * V * 4 + (size_t)(Kmax > 0 ? Kmax : 1) * 32 * 4;
 }
 
-__host__ __device__ __forceinline__ size_t fit_cta_bytes(int Lmax, int Kmax, int V, int W) {
-  return fit_shared_bytes(Lmax, Kmax, W) + (size_t)W * fit_warp_bytes(Lmax, Kmax, V);
+__host__ __device__ __forceinline__ size_t fit_cta_bytes(int Lmax, int Imax, int Kmax, int V, int W) {
+  return fit_shared_bytes(Lmax, Kmax, W) + (size_t)W * fit_warp_bytes(Imax, Kmax, V);
 }
 
-__device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Kmax, int V, int W, int warp) {
+__device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Imax, int Kmax, int V, int W,
+                                          int warp) {
   WarpSmem s;
   const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
   unsigned char* p = base;
@@ -106,8 +111,7 @@ __device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Kma
   p += fit_align16((size_t)W * 8);
   s.tape = reinterpret_cast<uint32_t*>(p);
   p += fit_align16((size_t)Lmax * 4);
-  s.cnode = reinterpret_cast<float*>(p);
-  p += fit_align16((size_t)Lmax * 4);
+  p += fit_align16((size_t)Lmax * 4);  // (unused row kept for alignment of the layout below)
   s.node_slot = reinterpret_cast<int*>(p);
   p += fit_align16((size_t)Lmax * 4);
   s.slot_node = reinterpret_cast<int*>(p);
@@ -116,11 +120,20 @@ __device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Kma
   p += fit_align16((size_t)W * 4);
   s.task = reinterpret_cast<long long*>(p);
   p += 16;
-  unsigned char* w = base + fit_shared_bytes(Lmax, Kmax, W) + (size_t)warp * fit_warp_bytes(Lmax, Kmax, V);
-  s.gl = reinterpret_cast<double*>(w);
-  w += K * 32 * 8;
+  s.pop = reinterpret_cast<uint32_t*>(p);
+  p += fit_align16((size_t)Lmax * 4);
+  s.popnd = reinterpret_cast<uint32_t*>(p);
+  p += fit_align16((size_t)Lmax * 4);
+  s.cval = reinterpret_cast<float*>(p);
+  p += fit_align16(K * 4);
+  s.info = reinterpret_cast<int*>(p);
+  p += 16;
+  const int I = Imax > 0 ? Imax : 1;
+  unsigned char* w = base + fit_shared_bytes(Lmax, Kmax, W) + (size_t)warp * fit_warp_bytes(Imax, Kmax, V);
+  s.gl = reinterpret_cast<float*>(w);
+  w += K * 32 * 4;
   s.vals = reinterpret_cast<float*>(w);
-  w += (size_t)Lmax * 32 * V * 4;
+  w += (size_t)I * 32 * V * 4;
   s.adj = reinterpret_cast<float*>(w);
   return s;
 }
@@ -191,26 +204,68 @@ __device__ __forceinline__ float var_value(const float (&xr)[V][kMaxRegVars], in
 }
 
 // ---------------------------------------------------------------------------------
-// One pass over the problem's points at the constants published in S.cnode.
+// Operator-node program.  Before the first closure of a problem its tape (nodes up
+// to the root) is rewritten as a list of operator nodes (arity >= 1, plus NO_OP
+// nodes, whose value NaN and adjoint check matter); every leaf becomes an operand
+// descriptor inside its parent.  16-bit operand descriptor:
+//   bit 15 = 0: operator node, bits 0..14 = its row
+//   bit 15 = 1: leaf, bits 12..14 = kind (0 zero, 1 variable, 2 constant slot,
+//               3 fixed constant), bits 0..11 = variable index / slot / opcode
+// The interpreter thus loops over operator nodes only, keeps node values and
+// adjoints for them only, reads variables from registers and constants from the
+// slot table, and sends the adjoint of a learnable leaf straight to its slot.
+// ---------------------------------------------------------------------------------
+constexpr uint32_t kLeaf = 0x8000u;
+enum LeafKind : uint32_t { LK_ZERO = 0, LK_VAR = 1, LK_CONST = 2, LK_FIXED = 3 };
+
+__device__ __forceinline__ bool is_operator_node(int code) { return code == NO_OP || arity_of(code) >= 1; }
+
+__device__ __forceinline__ uint32_t leaf_operand(uint32_t d, int slot) {
+  const int code = code_of(d);
+  if (code == VAR) return kLeaf | (LK_VAR << 12) | (uint32_t)child0(d);
+  if (code == LEARNABLE) return kLeaf | (LK_CONST << 12) | (uint32_t)slot;
+  if (code >= C1 && code <= E_) return kLeaf | (LK_FIXED << 12) | (uint32_t)code;
+  return kLeaf | (LK_ZERO << 12);
+}
+
+// Value of a leaf operand at the lane's point v.
+template <int V>
+__device__ __forceinline__ float leaf_value(uint32_t od, const float (&xr)[V][kMaxRegVars], int v, bool xin,
+                                            const float* __restrict__ X, int64_t nn, int64_t n_x,
+                                            const float* __restrict__ cval) {
+  const uint32_t kind = (od >> 12) & 7u, pay = od & 0xfffu;
+  if (kind == LK_VAR) return var_value<V>(xr, v, (int)pay, xin, X, nn, n_x);
+  if (kind == LK_CONST) return cval[pay];
+  if (kind == LK_FIXED) return node_value<float>((int)pay, 0.f, 0.f, 0.f, 0.f);
+  return 0.f;
+}
+
+// ---------------------------------------------------------------------------------
+// One pass over the problem's points at the constants published in S.cval.
 // kGrad: loss + gradient (forward, residual, reverse sweep); otherwise forward only,
 // writing the root values to Y_final.
 //
-// Forward: node k's children are read from the shared-memory node table, except the
-// node just before it (the most common child in a postfix tape), whose value is
-// still in a register.  Reverse: the contribution a node makes to the node right
-// before it is likewise carried in registers into the next iteration instead of a
-// shared-memory read-modify-write; contributions are still added in the reference's
-// order (parents from the last to the first, child 0 before child 1).
+// Forward: an operand that is the previous operator node (the most common case in
+// a postfix tape) comes from a register, other operator operands from the warp's
+// node table.  Reverse: the contribution to the previous operator node is carried
+// in registers into the next iteration instead of a shared-memory read-modify-write;
+// contributions are added in the reference's order (parents from the last to the
+// first, child 0 before child 1).
 // ---------------------------------------------------------------------------------
 template <int V, bool kGrad>
-__device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int R, int K, int lane,
-                                            int warp, int W, int& err) {
+__device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int lane, int warp, int W,
+                                            int& err) {
   const int64_t N = A.N;
   const float invN = 1.0f / (float)N;
   const float* __restrict__ Yrow = A.Y ? A.Y + b * N : nullptr;
   const bool xin = A.n_x <= kMaxRegVars;
-  double loss_part = 0.0;
-  // this warp's chunks of 32V points: warp, warp + W, warp + 2W, ...
+  const int nI = S.info[0];              // operator nodes
+  const uint32_t root_od = (uint32_t)S.info[1];
+  const bool root_leaf = (root_od & kLeaf) != 0;
+  const float* __restrict__ cval = S.cval;
+  // per-lane partial sums stay in float (a lane sees N / (32 V W) points); the
+  // cross-lane and cross-warp reductions are done in double
+  float loss_part = 0.f;
   for (int64_t base = (int64_t)warp * 32 * V; base < N; base += (int64_t)W * 32 * V) {
     int64_t nn[V];
     bool valid[V];
@@ -223,45 +278,48 @@ __device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S,
 #pragma unroll
       for (int j = 0; j < kMaxRegVars; ++j) xr[v][j] = (xin && j < A.n_x) ? __ldg(A.X + nn[v] * A.n_x + j) : 0.f;
     }
-    // ---- forward ----
+    // ---- forward over the operator nodes ----
     float prev[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) prev[v] = 0.f;
-    uint32_t dn = S.tape[0];
-    for (int k = 0; k <= R; ++k) {
-      const uint32_t d = dn;
-      if (k < R) dn = S.tape[k + 1];
-      const int code = code_of(d);
+    uint32_t opn = nI > 0 ? S.pop[0] : 0u, odn = nI > 0 ? S.popnd[0] : 0u;
+    for (int i = 0; i < nI; ++i) {
+      const uint32_t op = opn, od = odn;
+      if (i + 1 < nI) {
+        opn = S.pop[i + 1];
+        odn = S.popnd[i + 1];
+      }
+      const int code = (int)(op & 0xffu), ar = (int)(op >> 8);
+      const uint32_t o0 = od & 0xffffu, o1 = od >> 16;
       float r[V];
-      if (code == VAR) {
-        const int var = child0(d);
 #pragma unroll
-        for (int v = 0; v < V; ++v) r[v] = var_value<V>(xr, v, var, xin, A.X, nn[v], A.n_x);
-      } else if (code == LEARNABLE) {
-        const float c = S.cnode[k];
-#pragma unroll
-        for (int v = 0; v < V; ++v) r[v] = c;
-      } else {
-        const int c0 = child0(d), c1 = child1(d);
-        const bool p0 = c0 == k - 1, p1 = c1 == k - 1;
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const float a = p0 ? prev[v] : S.vals[c0 * (32 * V) + v * 32 + lane];
-          const float bb = p1 ? prev[v] : S.vals[c1 * (32 * V) + v * 32 + lane];
-          r[v] = node_value<float>(code, a, bb, 0.f, 0.f);
+      for (int v = 0; v < V; ++v) {
+        float a = 0.f, bb = 0.f;
+        if (ar >= 1) {
+          if (o0 & kLeaf) a = leaf_value<V>(o0, xr, v, xin, A.X, nn[v], A.n_x, cval);
+          else a = ((int)o0 == i - 1) ? prev[v] : S.vals[o0 * (32 * V) + v * 32 + lane];
         }
+        if (ar == 2) {
+          if (o1 & kLeaf) bb = leaf_value<V>(o1, xr, v, xin, A.X, nn[v], A.n_x, cval);
+          else bb = ((int)o1 == i - 1) ? prev[v] : S.vals[o1 * (32 * V) + v * 32 + lane];
+        }
+        r[v] = node_value<float>(code, a, bb, 0.f, 0.f);
       }
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        S.vals[k * (32 * V) + v * 32 + lane] = r[v];
-        if (kGrad) S.adj[k * (32 * V) + v * 32 + lane] = 0.f;
+        S.vals[i * (32 * V) + v * 32 + lane] = r[v];
+        if (kGrad) S.adj[i * (32 * V) + v * 32 + lane] = 0.f;
         prev[v] = r[v];
       }
     }
+    float fval[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+      fval[v] = root_leaf ? leaf_value<V>(root_od, xr, v, xin, A.X, nn[v], A.n_x, cval) : prev[v];
     if constexpr (!kGrad) {
 #pragma unroll
       for (int v = 0; v < V; ++v)
-        if (valid[v]) A.Y_final[b * N + nn[v]] = prev[v];
+        if (valid[v]) A.Y_final[b * N + nn[v]] = fval[v];
       continue;
     } else {
     // ---- residuals: root adjoint (2 (f - y)) * (1/N), as autograd forms it ----
@@ -271,65 +329,96 @@ __device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S,
       float groot = 0.f;
       if (valid[v]) {
         if (A.objective == 0) {
-          const float rr = prev[v] - __ldg(Yrow + nn[v]);
-          loss_part += (double)(rr * rr);
+          const float rr = fval[v] - __ldg(Yrow + nn[v]);
+          loss_part = __fadd_rn(loss_part, __fmul_rn(rr, rr));
           groot = __fmul_rn(rr * 2.0f, invN);
         } else {
-          loss_part += (double)prev[v];
+          loss_part = __fadd_rn(loss_part, fval[v]);
           groot = invN;
         }
       }
       g_root[v] = groot;
     }
-    // ---- reverse sweep ----
-    // carry*: contributions to node k-1 produced while processing node k
+    if (root_leaf) {  // a leaf root: its adjoint goes straight to its slot
+      if (((root_od >> 12) & 7u) == LK_CONST) {
+        const int slot = (int)(root_od & 0xfffu);
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+          if (valid[v] && g_root[v] != 0.f) S.gl[slot * 32 + lane] = __fadd_rn(S.gl[slot * 32 + lane], g_root[v]);
+      }
+    }
+    // ---- reverse sweep over the operator nodes ----
+    // cin*: contributions to operator node i-1 produced while processing node i
     float cin0[V], cin1[V];
     bool hin0 = false, hin1 = false;
 #pragma unroll
     for (int v = 0; v < V; ++v) { cin0[v] = 0.f; cin1[v] = 0.f; }
-    uint32_t dn2 = S.tape[R];
-    for (int k = R; k >= 0; --k) {
-      const uint32_t d = dn2;
-      if (k > 0) dn2 = S.tape[k - 1];
-      const int code = code_of(d);
+    uint32_t opp = nI > 0 ? S.pop[nI - 1] : 0u, odp = nI > 0 ? S.popnd[nI - 1] : 0u;
+    for (int i = nI - 1; i >= 0; --i) {
+      const uint32_t op = opp, od = odp;
+      if (i > 0) {
+        opp = S.pop[i - 1];
+        odp = S.popnd[i - 1];
+      }
+      const int code = (int)(op & 0xffu), ar = (int)(op >> 8);
       float g[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        float gv = (k == R) ? g_root[v] : S.adj[k * (32 * V) + v * 32 + lane];
+        float gv = (!root_leaf && i == nI - 1) ? g_root[v] : S.adj[i * (32 * V) + v * 32 + lane];
         if (hin0) gv = __fadd_rn(gv, cin0[v]);
         if (hin1) gv = __fadd_rn(gv, cin1[v]);
         g[v] = gv;
       }
       hin0 = hin1 = false;
-      if (code == LEARNABLE) {
-        const int slot = S.node_slot[k];
+      if (code == NO_OP) {
 #pragma unroll
         for (int v = 0; v < V; ++v)
-          if (valid[v] && g[v] != 0.f) S.gl[slot * 32 + lane] += (double)g[v];
+          if (valid[v] && g[v] != 0.f && !err) err = ERR_GRAD_ON_NO_OP;
         continue;
       }
-      if (code == VAR || code == ZERO || (code >= C1 && code <= E_) || code == FLOOR || code == CEIL) continue;
-      const int c0 = child0(d), c1 = child1(d);
-      const bool t0 = c0 == k - 1, t1 = c1 == k - 1;
+      if (code == FLOOR || code == CEIL) continue;
+      const uint32_t o0 = od & 0xffffu, o1 = od >> 16;
+      const bool t0 = !(o0 & kLeaf) && (int)o0 == i - 1;
+      const bool t1 = ar == 2 && !(o1 & kLeaf) && (int)o1 == i - 1;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        const int i = v * 32 + lane;
+        const int li = v * 32 + lane;
+        const float a = (o0 & kLeaf) ? leaf_value<V>(o0, xr, v, xin, A.X, nn[v], A.n_x, cval)
+                                     : S.vals[o0 * (32 * V) + li];
+        float bb = 0.f;
+        if (ar == 2)
+          bb = (o1 & kLeaf) ? leaf_value<V>(o1, xr, v, xin, A.X, nn[v], A.n_x, cval) : S.vals[o1 * (32 * V) + li];
         bool a0, a1;
-        float o0, o1;
-        const int e = node_adjoint<float>(code, g[v], S.vals[c0 * (32 * V) + i], S.vals[c1 * (32 * V) + i],
-                                          S.vals[k * (32 * V) + i], a0, o0, a1, o1);
-        if (!valid[v]) { a0 = a1 = false; o0 = o1 = 0.f; }
+        float r0, r1;
+        const int e = node_adjoint<float>(code, g[v], a, bb, S.vals[i * (32 * V) + li], a0, r0, a1, r1);
+        if (!valid[v]) { a0 = a1 = false; r0 = r1 = 0.f; }
         if (e && valid[v] && !err) err = e;
-        // the flags depend only on the opcode and g; they are per lane here
         if (a0) {
-          if (t0) cin0[v] = o0;
-          else S.adj[c0 * (32 * V) + i] = __fadd_rn(S.adj[c0 * (32 * V) + i], o0);
+          if (o0 & kLeaf) {
+            // a learnable leaf receives its (single) contribution straight into its slot
+            if (((o0 >> 12) & 7u) == LK_CONST && r0 != 0.f) {
+              const int slot = (int)(o0 & 0xfffu);
+              S.gl[slot * 32 + lane] = __fadd_rn(S.gl[slot * 32 + lane], r0);
+            }
+          } else if (t0) {
+            cin0[v] = r0;
+          } else {
+            S.adj[o0 * (32 * V) + li] = __fadd_rn(S.adj[o0 * (32 * V) + li], r0);
+          }
         } else if (t0) {
           cin0[v] = 0.f;
         }
         if (a1) {
-          if (t1) cin1[v] = o1;
-          else S.adj[c1 * (32 * V) + i] = __fadd_rn(S.adj[c1 * (32 * V) + i], o1);
+          if (o1 & kLeaf) {
+            if (((o1 >> 12) & 7u) == LK_CONST && r1 != 0.f) {
+              const int slot = (int)(o1 & 0xfffu);
+              S.gl[slot * 32 + lane] = __fadd_rn(S.gl[slot * 32 + lane], r1);
+            }
+          } else if (t1) {
+            cin1[v] = r1;
+          } else {
+            S.adj[o1 * (32 * V) + li] = __fadd_rn(S.adj[o1 * (32 * V) + li], r1);
+          }
         } else if (t1) {
           cin1[v] = 0.f;
         }
@@ -340,7 +429,7 @@ __device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S,
     }
     }  // kGrad
   }
-  return kGrad ? wsum_d(loss_part) : 0.0;
+  return kGrad ? wsum_d((double)loss_part) : 0.0;
 }
 
 // Closure: publish the trial constants, run the pass over this warp's points,
@@ -353,17 +442,14 @@ __device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, co
   if (warp == 0) {
 #pragma unroll
     for (int s = 0; s < SPL; ++s)
-      if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = xt.v[s];
+      if (P.real(s)) S.cval[s * 32 + lane] = xt.v[s];
   }
-  for (int j = 0; j < P.K; ++j) S.gl[j * 32 + lane] = 0.0;
+  for (int j = 0; j < P.K; ++j) S.gl[j * 32 + lane] = 0.f;
   __syncthreads();
-  const double lpart = tape_pass<V, true>(A, S, P.b, P.root, P.K, lane, warp, W, err);
-  __syncwarp();
-  for (int j = lane; j < P.K; j += 32) {
-    double acc = 0.0;
-#pragma unroll 8
-    for (int l = 0; l < 32; ++l) acc += S.gl[j * 32 + l];
-    S.red_g[warp * P.K + j] = acc;
+  const double lpart = tape_pass<V, true>(A, S, P.b, lane, warp, W, err);
+  for (int j = 0; j < P.K; ++j) {
+    const double t = wsum_d((double)S.gl[j * 32 + lane]);
+    if (lane == 0) S.red_g[warp * P.K + j] = t;
   }
   if (lane == 0) S.red_l[warp] = lpart;
   __syncthreads();
@@ -397,10 +483,10 @@ struct Point {
 enum Phase : int { PH_INIT = 0, PH_BRACKET, PH_ZOOM_LO, PH_ZOOM, PH_BACKTRACK, PH_UPDATE, PH_DONE };
 
 template <int V, int SPL>
-__global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
+__global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
-  const WarpSmem S = carve(smem, A.Lmax, A.Kmax, V, W, warp);
+  const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, warp);
   const int64_t gwarp = (int64_t)blockIdx.x * W + warp;
   float* ringS = A.ws_vec + gwarp * (int64_t)2 * A.hist * SPL * 32;
   float* ringY = ringS + (int64_t)A.hist * SPL * 32;
@@ -424,21 +510,53 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
     P.nslots = P.K + (P.has_virtual ? 1 : 0);
     const int L = P.root + 1;
 
-    // stage the tape, map learnable nodes to slots (warp 0), visible to the CTA
+    // stage the tape; number the constant slots and the operator nodes; write the
+    // operator-node program (warp 0), visible to the CTA
     if (warp == 0) {
       for (int k = lane; k < L; k += 32) S.tape[k] = A.desc[P.b * A.M + k];
       __syncwarp();
-      int base = 0;
+      int nslot = 0, nop = 0;
       for (int k0 = 0; k0 < L; k0 += 32) {
         const int k = k0 + lane;
-        const bool lc = k < L && code_of(S.tape[k]) == LEARNABLE;
-        const unsigned m = __ballot_sync(0xffffffffu, lc);
+        const int code = k < L ? code_of(S.tape[k]) : -1;
+        const bool lc = code == LEARNABLE;
+        const bool opn = k < L && is_operator_node(code);
+        const unsigned mc = __ballot_sync(0xffffffffu, lc);
+        const unsigned mo = __ballot_sync(0xffffffffu, opn);
+        const unsigned below = (1u << lane) - 1u;
         if (lc) {
-          const int slot = base + __popc(m & ((1u << lane) - 1u));
+          const int slot = nslot + __popc(mc & below);
           S.node_slot[k] = slot;
           S.slot_node[slot] = k;
         }
-        base += __popc(m);
+        if (opn) S.node_slot[k] = nop + __popc(mo & below);
+        nslot += __popc(mc);
+        nop += __popc(mo);
+      }
+      __syncwarp();
+      for (int k = lane; k < L; k += 32) {
+        const uint32_t d = S.tape[k];
+        const int code = code_of(d);
+        if (!is_operator_node(code)) continue;
+        const int ar = arity_of(code);
+        uint32_t od0 = 0, od1 = 0;
+        if (ar >= 1) {
+          const uint32_t c = S.tape[child0(d)];
+          od0 = is_operator_node(code_of(c)) ? (uint32_t)S.node_slot[child0(d)] : leaf_operand(c, S.node_slot[child0(d)]);
+        }
+        if (ar == 2) {
+          const uint32_t c = S.tape[child1(d)];
+          od1 = is_operator_node(code_of(c)) ? (uint32_t)S.node_slot[child1(d)] : leaf_operand(c, S.node_slot[child1(d)]);
+        }
+        const int row = S.node_slot[k];
+        S.pop[row] = (uint32_t)code | ((uint32_t)ar << 8);
+        S.popnd[row] = od0 | (od1 << 16);
+      }
+      if (lane == 0) {
+        const int R = P.root;
+        const uint32_t rd = S.tape[R];
+        S.info[0] = nop;
+        S.info[1] = (int)(is_operator_node(code_of(rd)) ? (uint32_t)S.node_slot[R] : leaf_operand(rd, S.node_slot[R]));
       }
     }
     __syncthreads();
@@ -763,12 +881,12 @@ __global__ void __launch_bounds__(256) fit_lbfgs_kernel(FitArgs A) {
       }
 #pragma unroll
       for (int s = 0; s < SPL; ++s)
-        if (P.real(s)) S.cnode[S.slot_node[s * 32 + lane]] = x.v[s];
+        if (P.real(s)) S.cval[s * 32 + lane] = x.v[s];
     }
     __syncthreads();
     if (A.Y_final) {
       int dummy = 0;
-      tape_pass<V, false>(A, S, P.b, P.root, P.K, lane, warp, W, dummy);
+      tape_pass<V, false>(A, S, P.b, lane, warp, W, dummy);
     }
     __syncthreads();
   }
@@ -785,6 +903,7 @@ static int fit_defaults(const sr_fit_options* o, sr_fit_options& r) {
   r.warps_per_block = 0;
   r.points_per_lane = 0;
   r.grid_blocks = 0;
+  r.max_operators = 0;
   if (o) r = *o;
   if (r.max_iter < 0 || r.history_size < 1 || r.line_search < 0 || r.line_search > 1 || r.line_search_max_iter < 0 ||
       r.objective < 0 || r.objective > 1) {
@@ -806,7 +925,7 @@ static int spl_for(int Kmax) {
 }
 
 struct FitShape {
-  int V, SPL, warps, blocks;
+  int V, SPL, warps, blocks, Imax;
   size_t smem;
   int64_t total_warps;
 };
@@ -838,6 +957,8 @@ static void* pick_kernel(int V, int SPL) {
 // that keeps more work resident per SM (resident warps, with a warp of two points
 // per lane counted as 1.6 warps: its independent chains hide latency).
 static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
+  const int Imax = (o.max_operators > 0 && o.max_operators < Lmax) ? o.max_operators : Lmax;
+  sh.Imax = Imax;
   sh.SPL = spl_for(Kmax);
   if (!sh.SPL) {
     set_error("at most 127 learnable constants per tape are supported (got %d)", Kmax);
@@ -865,7 +986,7 @@ static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_opti
         set_error("fit kernel shared memory attribute failed");
         return SR_ERR_CUDA;
       }
-      const size_t cb = fit_cta_bytes(Lmax, Kmax, V, w);
+      const size_t cb = fit_cta_bytes(Lmax, Imax, Kmax, V, w);
       if (cb > (size_t)optin) continue;
       int per_sm = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, w * 32, cb) != cudaSuccess || per_sm < 1)
@@ -886,7 +1007,7 @@ static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_opti
   }
   sh.V = bestV;
   sh.warps = W;
-  sh.smem = fit_cta_bytes(Lmax, Kmax, bestV, W);
+  sh.smem = fit_cta_bytes(Lmax, Imax, Kmax, bestV, W);
   int64_t blocks = o.grid_blocks > 0 ? o.grid_blocks : (int64_t)sms * bestPerSm;
   if (blocks > B) blocks = B;  // one problem per CTA at a time
   if (blocks < 1) blocks = 1;
@@ -954,7 +1075,7 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   A.order = order;
   A.max_iter = o.max_iter; A.hist = o.history_size; A.ls_kind = o.line_search; A.ls_max = o.line_search_max_iter;
   A.objective = o.objective; A.tol = o.tolerance_grad; A.eps = o.eps;
-  A.Lmax = Lmax; A.Kmax = max_consts;
+  A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax;
   A.counter = reinterpret_cast<int*>(ws);
   const int64_t vec = sh.total_warps * 2LL * o.history_size * sh.SPL * 32 * (int64_t)sizeof(float);
   A.ws_vec = reinterpret_cast<float*>(ws + 256);

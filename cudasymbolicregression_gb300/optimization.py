@@ -59,7 +59,8 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
                            line_search=0 if line_search_fn == "strong_wolfe" else 1,
                            line_search_max_iter=int(line_search_max_iter), eps=float(eps),
                            objective=int(objective), warps_per_block=int(warps_per_block),
-                           points_per_lane=int(points_per_lane), grid_blocks=int(grid_blocks))
+                           points_per_lane=int(points_per_lane), grid_blocks=int(grid_blocks),
+                           max_operators=int(max(tapes.max_operators, 1)))
     L = _lib.lib()
     C_out = torch.empty((B, M), dtype=torch.float32, device=dev)
     Y_out = torch.empty((B, N), dtype=torch.float32, device=dev) if want_y else None

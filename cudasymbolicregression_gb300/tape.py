@@ -25,6 +25,7 @@ class CompiledTapes:
     max_len: int        # largest L_eff
     max_root: int       # largest root + 1
     max_consts: int     # largest number of constants up to the root
+    max_operators: int  # largest number of operator nodes (arity >= 1 or NO_OP) up to the root
     _order: torch.Tensor | None = None
 
     @property
@@ -44,7 +45,7 @@ def compile_tapes(ops_bm: torch.Tensor, ch_bm: torch.Tensor, n_vars: int, valida
     B, M = ops_bm.shape
     L = _lib.lib()
     st = _lib.stream_ptr(dev)
-    stats = torch.zeros(4, dtype=torch.int32, device=dev)
+    stats = torch.zeros(8, dtype=torch.int32, device=dev)
     sb, sm = ops_bm.stride()
     cb, cm, ci = ch_bm.stride()
     if validate_only:
@@ -62,4 +63,5 @@ def compile_tapes(ops_bm: torch.Tensor, ch_bm: torch.Tensor, n_vars: int, valida
     s = stats.tolist()
     if s[0]:
         raise RuntimeError(error_message(s[0], "input validation"))
-    return CompiledTapes(desc=desc, meta=meta, B=B, M=M, max_len=s[1], max_root=s[2], max_consts=s[3])
+    return CompiledTapes(desc=desc, meta=meta, B=B, M=M, max_len=s[1], max_root=s[2], max_consts=s[3],
+                         max_operators=s[4])

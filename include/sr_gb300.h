@@ -59,9 +59,10 @@ int sr_validate(const int64_t *ops_dev, const int64_t *ch_dev, int64_t B, int64_
 /*
  * Validation plus staging of the tapes into the compact node encoding used by
  * every kernel here (one pass over Ops/Ch).  desc_dev (B, M) uint32 and
- * meta_dev (B, 4) int32 are outputs.  stats_dev is int32[4], zeroed by the call:
+ * meta_dev (B, 4) int32 are outputs.  stats_dev is int32[8], zeroed by the call:
  * stats[0] = status as in sr_validate, stats[1] = largest L_eff, stats[2] = largest
- * root + 1, stats[3] = largest number of constants up to the root.
+ * root + 1, stats[3] = largest number of constants up to the root, stats[4] =
+ * largest number of operator nodes (arity >= 1 or NO_OP) up to the root.
  * Covers the validation of validate_inputs (reference src/symbolic_evaluation.cpp:7-37)
  * and the root/constant-mask bookkeeping of optimize
  * (reference symbolic_torch/optimization.py:51-61).
@@ -125,6 +126,9 @@ typedef struct sr_fit_options {
   int32_t warps_per_block;      /* warps sharing one problem's points (0 = automatic) */
   int32_t points_per_lane;      /* data points per lane per pass: 1, 2 or 4 (0 = automatic) */
   int32_t grid_blocks;          /* persistent CTAs (0 = one wave over all SMs) */
+  int32_t max_operators;        /* largest number of operator nodes (arity >= 1 or NO_OP) up to a
+                                   root, stats[4] of sr_tape_compile; sizes the node tables
+                                   (0 = max_len) */
 } sr_fit_options;
 
 /* Bytes of device workspace sr_fit_lbfgs needs for this problem set
