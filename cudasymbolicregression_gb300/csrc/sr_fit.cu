@@ -1,16 +1,19 @@
 // sr_fit.cu -- fused batched L-BFGS fit of the learnable constants.
 //
-// One persistent kernel.  Each warp takes one problem (one tape, one target row)
-// from a work queue and runs the complete optimisation for it on chip:
+// One persistent kernel.  Each CTA takes one problem (one tape, one target row)
+// from a work queue and runs the complete optimisation for it on chip, its warps
+// splitting the N points:
 //
-//   closure(x)  forward sweep over the tape for all N points (lanes over points,
-//               node values in shared memory), residuals against Y, then the
-//               reverse (adjoint) sweep; the gradient of every constant is summed
-//               per lane in double and reduced in a fixed order, so results are
-//               bit-reproducible run to run.
+//   closure(x)  forward sweep over the tape for the warp's points (lanes over
+//               points, operator-node values in shared memory), residuals against
+//               Y, then the reverse (adjoint) sweep; the gradient of every constant
+//               is summed per lane in float, over the lanes by a butterfly and over
+//               the warps in a fixed order, so results are bit-reproducible run to
+//               run and the same in every warp.
 //   direction   two-loop recursion over the last `history_size` (s, y) pairs held in
-//               the warp's slice of the workspace; dots, rho, alpha, beta, gamma in
-//               double, vectors in float (one slot per lane).
+//               warp 0's slice of the workspace, broadcast to the CTA through shared
+//               memory; dots, rho, alpha, beta, gamma in double, vectors in float
+//               (one slot per lane).
 //   line search strong Wolfe (bracket + bisection zoom) or Armijo backtracking, with
 //               the reference's acceptance rules and float32 scalar arithmetic.
 //
@@ -69,6 +72,15 @@ struct FitArgs {
 // Shared memory.  The CTA works on one problem at a time: the tape, the constants
 // published for the current trial point, the slot maps and the cross-warp
 // reduction buffers are shared; each warp owns the node table of its own points.
+// Float pair (hi, lo) with |lo| <= ulp(hi)/2: an error-free sum (Knuth's TwoSum on
+// the high parts, the low parts and the rounding error added, then Dekker's
+// renormalisation) keeps about 48 significant bits on the FP32 pipe.  The result
+// does not depend on the operand order, so a butterfly leaves every lane with the
+// same bits.
+struct F2 {
+  float hi, lo;
+};
+
 struct WarpSmem {
   uint32_t* tape;    // [Lmax]                      (CTA)
   uint32_t* pop;     // [Lmax] operator nodes: opcode | arity << 8              (CTA)
@@ -77,8 +89,9 @@ struct WarpSmem {
   int* info;         // [4] operator-node count, root operand                    (CTA)
   int* node_slot;    // [Lmax] slot of a LEARNABLE node / row of an operator node (CTA)
   int* slot_node;    // [Kmax]                      (CTA)
-  double* red_g;     // [W][Kmax] per-warp gradient sums (CTA)
-  double* red_l;     // [W] per-warp loss sums      (CTA)
+  F2* red_g;         // [W][Kmax] per-warp gradient sums (CTA)
+  F2* red_l;         // [W] per-warp loss sums      (CTA)
+  float* pvec;       // [128] search direction computed by warp 0 (CTA)
   int* red_e;        // [W] per-warp error codes    (CTA)
   long long* task;   // the CTA's current problem   (CTA)
   float* vals;       // [Imax][32V] values of the operator nodes (warp)
@@ -89,7 +102,7 @@ struct WarpSmem {
 __host__ __device__ __forceinline__ size_t fit_shared_bytes(int Lmax, int Kmax, int W) {
   const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
   return fit_align16((size_t)Lmax * 4) * 5 + fit_align16(K * 4) * 2 + fit_align16((size_t)W * K * 8) +
-         fit_align16((size_t)W * 8) + fit_align16((size_t)W * 4) + 16 + 16;
+         fit_align16((size_t)W * 8) + fit_align16((size_t)W * 4) + 16 + 16 + 512;
 }
 
 __host__ __device__ __forceinline__ size_t fit_warp_bytes(int Imax, int Kmax, int V) {
@@ -105,10 +118,12 @@ __device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Ima
   WarpSmem s;
   const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
   unsigned char* p = base;
-  s.red_g = reinterpret_cast<double*>(p);
+  s.red_g = reinterpret_cast<F2*>(p);
   p += fit_align16((size_t)W * K * 8);
-  s.red_l = reinterpret_cast<double*>(p);
+  s.red_l = reinterpret_cast<F2*>(p);
   p += fit_align16((size_t)W * 8);
+  s.pvec = reinterpret_cast<float*>(p);
+  p += 512;
   s.tape = reinterpret_cast<uint32_t*>(p);
   p += fit_align16((size_t)Lmax * 4);
   p += fit_align16((size_t)Lmax * 4);  // (unused row kept for alignment of the layout below)
@@ -136,6 +151,26 @@ __device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Ima
   w += (size_t)I * 32 * V * 4;
   s.adj = reinterpret_cast<float*>(w);
   return s;
+}
+
+// Sum of two float pairs (see F2).
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bv = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bv)), __fsub_rn(b.hi, bv));
+  const float lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+  const float h = __fadd_rn(s, lo);
+  return F2{h, __fsub_rn(lo, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ F2 warp_sum_f2(float v) {
+  F2 a{v, 0.f};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const F2 b{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+    a = f2_add(a, b);
+  }
+  return a;
 }
 
 __device__ __forceinline__ double wsum_d(double v) {
@@ -253,7 +288,7 @@ __device__ __forceinline__ float leaf_value(uint32_t od, const float (&xr)[V][kM
 // first, child 0 before child 1).
 // ---------------------------------------------------------------------------------
 template <int V, bool kGrad>
-__device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int lane, int warp, int W,
+__device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int lane, int warp, int W,
                                             int& err) {
   const int64_t N = A.N;
   const float invN = 1.0f / (float)N;
@@ -263,8 +298,7 @@ __device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S,
   const uint32_t root_od = (uint32_t)S.info[1];
   const bool root_leaf = (root_od & kLeaf) != 0;
   const float* __restrict__ cval = S.cval;
-  // per-lane partial sums stay in float (a lane sees N / (32 V W) points); the
-  // cross-lane and cross-warp reductions are done in double
+  // per-lane partial sums in float (a lane sees N / (32 V W) points)
   float loss_part = 0.f;
   for (int64_t base = (int64_t)warp * 32 * V; base < N; base += (int64_t)W * 32 * V) {
     int64_t nn[V];
@@ -429,12 +463,14 @@ __device__ __forceinline__ double tape_pass(const FitArgs& A, const WarpSmem& S,
     }
     }  // kGrad
   }
-  return kGrad ? wsum_d((double)loss_part) : 0.0;
+  return loss_part;
 }
 
 // Closure: publish the trial constants, run the pass over this warp's points,
-// reduce loss and gradient over the lanes and then over the CTA's warps in a
-// fixed order (every warp ends with the same bits).  Two CTA barriers.
+// reduce loss and gradient over the lanes (butterfly) and then over the CTA's
+// warps in a fixed order, in float pairs on the FP32 pipe (GB300's FP64 rate is a
+// small fraction of its FP32 rate); every warp ends with the same bits.  Two CTA
+// barriers.
 template <int V, int SPL>
 __device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P, int warp, int W,
                                          const Slots<SPL>& xt, Slots<SPL>& grad, int& err) {
@@ -446,27 +482,25 @@ __device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, co
   }
   for (int j = 0; j < P.K; ++j) S.gl[j * 32 + lane] = 0.f;
   __syncthreads();
-  const double lpart = tape_pass<V, true>(A, S, P.b, lane, warp, W, err);
+  const F2 lsum = warp_sum_f2(tape_pass<V, true>(A, S, P.b, lane, warp, W, err));
   for (int j = 0; j < P.K; ++j) {
-    const double t = wsum_d((double)S.gl[j * 32 + lane]);
+    const F2 t = warp_sum_f2(S.gl[j * 32 + lane]);
     if (lane == 0) S.red_g[warp * P.K + j] = t;
   }
-  if (lane == 0) S.red_l[warp] = lpart;
+  if (lane == 0) S.red_l[warp] = lsum;
   __syncthreads();
 #pragma unroll
   for (int s = 0; s < SPL; ++s) {
-    float gv = 0.f;
+    F2 acc{0.f, 0.f};
     if (P.real(s)) {
       const int j = s * 32 + lane;
-      double acc = 0.0;
-      for (int w = 0; w < W; ++w) acc += S.red_g[w * P.K + j];
-      gv = (float)acc;
+      for (int w = 0; w < W; ++w) acc = f2_add(acc, S.red_g[w * P.K + j]);
     }
-    grad.v[s] = gv;
+    grad.v[s] = acc.hi;
   }
-  double lt = 0.0;
-  for (int w = 0; w < W; ++w) lt += S.red_l[w];
-  return (float)(lt / (double)A.N);
+  F2 lt{0.f, 0.f};
+  for (int w = 0; w < W; ++w) lt = f2_add(lt, S.red_l[w]);
+  return __fdiv_rn(lt.hi, (float)A.N);
 }
 
 // Evaluated point: value and gradient.
@@ -487,10 +521,10 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, warp);
-  const int64_t gwarp = (int64_t)blockIdx.x * W + warp;
-  float* ringS = A.ws_vec + gwarp * (int64_t)2 * A.hist * SPL * 32;
+  // history rings and two-loop scalars of this CTA (used by warp 0)
+  float* ringS = A.ws_vec + (int64_t)blockIdx.x * 2 * A.hist * SPL * 32;
   float* ringY = ringS + (int64_t)A.hist * SPL * 32;
-  double* alph = A.ws_scal + gwarp * (int64_t)2 * A.hist;
+  double* alph = A.ws_scal + (int64_t)blockIdx.x * 2 * A.hist;
   double* rhos = alph + A.hist;
   const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
 
@@ -752,10 +786,12 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
           slot = head;
           head = (head + 1) % A.hist;
         }
+        if (warp == 0) {  // only warp 0 computes directions
 #pragma unroll
-        for (int s = 0; s < SPL; ++s) {
-          ringS[slot * SPL * 32 + s * 32 + lane] = sv.v[s];
-          ringY[slot * SPL * 32 + s * 32 + lane] = P.active(s) ? __fsub_rn(nxt.g.v[s], g.v[s]) : 0.f;
+          for (int s = 0; s < SPL; ++s) {
+            ringS[slot * SPL * 32 + s * 32 + lane] = sv.v[s];
+            ringY[slot * SPL * 32 + s * 32 + lane] = P.active(s) ? __fsub_rn(nxt.g.v[s], g.v[s]) : 0.f;
+          }
         }
         __syncwarp();
         x = xn;
@@ -781,9 +817,9 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
         if (it >= A.max_iter || sqrt(dot(P, g, g)) < A.tol) {
           phase = PH_DONE;
         } else {
-          // two-loop recursion (lbfgs_batch.py:65-103)
+          // two-loop recursion (lbfgs_batch.py:65-103), by warp 0 for the CTA
           Slots<SPL> q = g;
-          if (h > 0) {
+          if (warp == 0 && h > 0) {
             for (int i = h - 1; i >= 0; --i) {
               const int sl = (head + i) % A.hist;
               Slots<SPL> si, yi;
@@ -828,8 +864,13 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
               for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dadd_rn((double)q.v[s], __dmul_rn((double)si.v[s], coef));
             }
           }
+          if (warp == 0) {
 #pragma unroll
-          for (int s = 0; s < SPL; ++s) p.v[s] = P.active(s) ? -q.v[s] : 0.f;
+            for (int s = 0; s < SPL; ++s) S.pvec[s * 32 + lane] = P.active(s) ? -q.v[s] : 0.f;
+          }
+          __syncthreads();
+#pragma unroll
+          for (int s = 0; s < SPL; ++s) p.v[s] = S.pvec[s * 32 + lane];
           phi0 = f;
           dphi0 = (float)dot(P, g, p);
           lsi = 0;
@@ -927,7 +968,6 @@ static int spl_for(int Kmax) {
 struct FitShape {
   int V, SPL, warps, blocks, Imax;
   size_t smem;
-  int64_t total_warps;
 };
 
 template <int V, int SPL>
@@ -953,7 +993,7 @@ static void* pick_kernel(int V, int SPL) {
 // Launch shape.  A CTA of W warps works on one problem, each warp on every W-th
 // chunk of 32V points, so an expensive problem (many closures) finishes W times
 // sooner and the tail of the persistent grid shrinks.  Unless the caller fixes
-// them, W keeps about 128 points per warp (1..8 warps) and V is the one of 1 and 2
+// them, W keeps about 64 points per warp (1..8 warps) and V is the one of 1 and 2
 // that keeps more work resident per SM (resident warps, with a warp of two points
 // per lane counted as 1.6 warps: its independent chains hide latency).
 static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
@@ -971,7 +1011,7 @@ static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_opti
   int W = o.warps_per_block;
   if (W <= 0) {
     W = 1;
-    while (W < 8 && (int64_t)W * 2 * 128 <= N) W *= 2;
+    while (W < 8 && (int64_t)W * 2 * 64 <= N) W *= 2;
   }
   if (W > 8) W = 8;  // __launch_bounds__(256)
   const int vc[3] = {1, 2, 4};
@@ -1012,13 +1052,12 @@ static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_opti
   if (blocks > B) blocks = B;  // one problem per CTA at a time
   if (blocks < 1) blocks = 1;
   sh.blocks = (int)blocks;
-  sh.total_warps = blocks * W;
   return SR_OK;
 }
 
 static int64_t ws_bytes_for(const FitShape& sh, int hist) {
-  const int64_t vec = sh.total_warps * 2LL * hist * sh.SPL * 32 * (int64_t)sizeof(float);
-  const int64_t scal = sh.total_warps * 2LL * hist * (int64_t)sizeof(double);
+  const int64_t vec = (int64_t)sh.blocks * 2LL * hist * sh.SPL * 32 * (int64_t)sizeof(float);
+  const int64_t scal = (int64_t)sh.blocks * 2LL * hist * (int64_t)sizeof(double);
   return 256 + fit_align16((size_t)vec) + fit_align16((size_t)scal);
 }
 
@@ -1077,7 +1116,7 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   A.objective = o.objective; A.tol = o.tolerance_grad; A.eps = o.eps;
   A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax;
   A.counter = reinterpret_cast<int*>(ws);
-  const int64_t vec = sh.total_warps * 2LL * o.history_size * sh.SPL * 32 * (int64_t)sizeof(float);
+  const int64_t vec = (int64_t)sh.blocks * 2LL * o.history_size * sh.SPL * 32 * (int64_t)sizeof(float);
   A.ws_vec = reinterpret_cast<float*>(ws + 256);
   A.ws_scal = reinterpret_cast<double*>(ws + 256 + fit_align16((size_t)vec));
   A.status = status;
@@ -1157,14 +1196,12 @@ extern "C" int sr_fit_lbfgs_static_scratch(const float* X, int64_t N, int64_t n_
   while (blocks >= 1) {
     FitShape t = sh;
     t.blocks = (int)blocks;
-    t.total_warps = blocks * sh.warps;
     if (ws_bytes_for(t, o.history_size) <= kStaticFitScratchBytes) break;
     blocks = blocks > 8 ? blocks * 3 / 4 : blocks - 1;
   }
   if (blocks < 1) {
     FitShape t = sh;
     t.blocks = 1;
-    t.total_warps = sh.warps;
     set_error("static fit scratch is %lld bytes; one CTA of %d warps needs %lld (history_size=%d, up to %d constants); "
               "use sr_fit_lbfgs with a caller workspace",
               (long long)kStaticFitScratchBytes, sh.warps, (long long)ws_bytes_for(t, o.history_size), o.history_size,
