@@ -20,6 +20,12 @@ Seeded synthetic data (no dataset is involved).
 restated) and prints its line.
 Multi-GPU: one process per GPU; every rank fits its own batch of B problems
 (independent seeds, no collective), value = all problems / max time.
+
+--workload eval measures the evaluation path instead (B=65536 tapes of padded
+length 64 over {+,-,*,/,sin,cos,exp,log,X0..X3,C}, mean length about 20,
+N=1024, X ~ U[-3, 3], C ~ N(0, 1)): one step is evaluate() forward plus the
+adjoint of a dense gradient that is 1 on every root row (the gradient of the sum
+of root outputs), value = algorithmic HBM bytes / step time.
 """
 from __future__ import annotations
 
@@ -42,6 +48,15 @@ METRIC = "expressions fitted/s at fixed final MSE, warm-start vs plain fused, 1 
 UNIT = "expressions/s"
 B_DEFAULT, N_DEFAULT, M_DEFAULT = 16384, 512, 64
 MAX_ITER = 200
+EVAL_METRIC = "evaluation forward+adjoint throughput (algorithmic HBM bytes)"
+EVAL_B, EVAL_N = 65536, 1024
+
+# DRAM bytes (read + write) of one launch of the dominant kernel on the default
+# workloads, from ncu captures of a 4x / 16x smaller batch scaled by the number of
+# problems (profiles/fit_lbfgs_ragged_B16384_N512.txt,
+# profiles/eval_forward_B4096_N1024.txt).
+FIT_TRAFFIC_BYTES = {(16384, 512): 4 * (10722048 + 24576)}
+EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000)}
 
 
 def peaks():
@@ -168,34 +183,26 @@ def workloads_cpu_fit(args):
     return workloads.ragged_fit(B=args.B, N=args.N, M=M_DEFAULT, seed=args.seed, root_eval=roots)
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--B", type=int, default=B_DEFAULT)
-    ap.add_argument("--N", type=int, default=N_DEFAULT)
-    ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--cpu-sample", type=int, default=48)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-e2e", action="store_true")
-    args = ap.parse_args()
-
-    rank, world, local = dist_env()
+def barrier(world):
     if world > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    if args.impl == "reference":
-        run_reference(args, rank)
-        return
+        dist.barrier()
 
+
+def max_over_ranks(x, world, dev):
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return x
+
+
+def run_fit(args, rank, world, local):
     import cudasymbolicregression_gb300 as sr
     from cudasymbolicregression_gb300 import workloads
 
     dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
     wl = workloads.ragged_fit(B=args.B, N=args.N, M=M_DEFAULT, seed=args.seed + 1000 * rank)
     Xd = torch.tensor(wl.X, device=dev)
     Yd = torch.tensor(wl.Y, device=dev)
@@ -204,39 +211,34 @@ def main():
     Cd = torch.tensor(wl.C, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def step():
-        return sr.optimize_ex(Xd, Yd, Od, Chd, Cd, max_iter=MAX_ITER, raise_errors=False)
+    def step(kev=None):
+        return sr.optimize_ex(Xd, Yd, Od, Chd, Cd, max_iter=MAX_ITER, raise_errors=False, kernel_events=kev)
 
     for _ in range(args.warmup):
         r = step()
     torch.cuda.synchronize()
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-
-    evs = []
-    barrier()
+    evs, kevs = [], []
+    barrier(world)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed")
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush.fill_(1.0)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            kev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             e0.record()
-            r = step()
+            r = step(kev)
             e1.record()
             evs.append((e0, e1))
+            kevs.append(kev)
         torch.cuda.synchronize()
-    barrier()
-    times = [a.elapsed_time(b) / 1000.0 for a, b in evs]
-    t_step = sum(times) / len(times)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    torch.cuda.nvtx.range_pop()
+    barrier(world)
+    t_step = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in evs)
+    t_kernel = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in kevs)
+    t_step = max_over_ranks(t_step, world, dev)
     value = args.B * world / t_step
 
     # quality and work accounting from the last step
@@ -244,7 +246,7 @@ def main():
     evals = r.evals.cpu().numpy().astype(np.float64)
     loss = r.loss.cpu().numpy()
     flops = float((wl.flops_per_closure() * evals).sum())
-    achieved_tflops = flops / t_step / 1e12
+    achieved_tflops = flops / t_kernel / 1e12
     pk, pk_kind = peaks()
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = sm_count * 128 * 2 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
@@ -280,6 +282,7 @@ def main():
 
     if rank == 0:
         fin = np.isfinite(loss)
+        traffic = FIT_TRAFFIC_BYTES.get((args.B, args.N))
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -288,8 +291,10 @@ def main():
                                        "tol 1e-7, plain randn init",
                            "B": args.B, "N": args.N, "M": M_DEFAULT, "l2": "flushed (256 MiB write) between steps"},
                 "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                             "frac": achieved_tflops / fp32_peak, "traffic": None,
-                             "peak_kind": f"nominal {sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz ({pk_kind} clock)"},
+                             "frac": achieved_tflops / fp32_peak, "traffic": traffic,
+                             "kernel": "fit_lbfgs_kernel", "kernel_ms": t_kernel * 1000.0,
+                             "peak_kind": f"nominal: {sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz "
+                                          f"({pk_kind} clock); no measured FP32 peak exists"},
                 "quality": {"median_final_mse": float(np.median(loss[fin])) if fin.any() else None,
                             "error_problems": int((iters < 0).sum()),
                             "nan_fraction": float(1 - fin.mean()), "mean_iters": float(iters.mean()),
@@ -301,6 +306,215 @@ def main():
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
+
+
+def eval_bytes(ops: np.ndarray, N: int):
+    """Algorithmic HBM bytes per tape of the forward (cache written once, node words,
+    tape summary and constants read once) and of the adjoint (dense gradient read
+    once, gradient of C written once, node words and constants read once)."""
+    B, M = ops.shape
+    fwd = 4 * M * N + 4 * M + 16 + 4 * M
+    bwd = 4 * M * N + 4 * M + 4 * M + 16 + 4 * M
+    return fwd * B, bwd * B
+
+
+def cpu_eval_sample(wl, chunk: int, seconds: float = 10.0):
+    """The CPU oracle port of the reference's forward + adjoint over consecutive
+    chunks of the workload's tapes (wrapping around) until `seconds` have passed;
+    returns algorithmic GB/s, seconds and tapes processed."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the checker / CPU baseline only
+    oracle.build()
+    B, M = wl.ops.shape
+    N = wl.X.shape[0]
+    chunk = min(chunk, B)
+    gout = np.zeros((chunk, M, N), np.float32)
+    done, nbytes, start, t_total = 0, 0, 0, 0.0
+    while t_total < seconds:
+        idx = np.arange(start, start + chunk) % B
+        ops, ch, C = wl.ops[idx], wl.ch[idx], wl.C[idx]
+        gout[:] = 0.0
+        gout[np.arange(chunk), np.maximum((ops != 0).sum(1) - 1, 0)] = 1.0
+        t0 = time.perf_counter()
+        oracle.eval_fwd(wl.X, ops, ch, C)
+        oracle.eval_bwd(wl.X, ops, ch, C, gout, want_gx=False)
+        t_total += time.perf_counter() - t0
+        fb, bb = eval_bytes(ops, N)
+        nbytes += fb + bb
+        done += chunk
+        start = (start + chunk) % B
+    return nbytes / t_total / 1e9, t_total, done, oracle.num_threads()
+
+
+def run_eval(args, rank, world, local):
+    import cudasymbolicregression_gb300 as sr
+    from cudasymbolicregression_gb300 import _lib, workloads
+    from cudasymbolicregression_gb300.tape import compile_tapes
+
+    dev = torch.device("cuda", local)
+    B = args.B if args.B != B_DEFAULT else EVAL_B
+    N = args.N if args.N != N_DEFAULT else EVAL_N
+    wl = workloads.eval_batch(B=B, N=N, M=M_DEFAULT, seed=args.seed + 1000 * rank, device=str(dev))
+    M = M_DEFAULT
+    Xd = torch.tensor(wl.X, device=dev)
+    Od = torch.tensor(wl.ops, device=dev)
+    Chd = torch.tensor(wl.ch, device=dev)
+    Cd = torch.tensor(wl.C, device=dev).requires_grad_(True)
+    root = torch.tensor(np.maximum((wl.ops != 0).sum(1) - 1, 0), device=dev)
+    G = torch.zeros((B, M, N), dtype=torch.float32, device=dev)
+    G[torch.arange(B, device=dev), root] = 1.0
+    fwd_bytes, bwd_bytes = eval_bytes(wl.ops, N)
+
+    def step():
+        out = sr.evaluation.evaluate(Xd, Od, Chd, Cd)
+        gC, = torch.autograd.grad(out, Cd, G)
+        return gC
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = []
+    barrier(world)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed")
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step()
+            e1.record()
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    barrier(world)
+    t_step = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in evs)
+    t_step = max_over_ranks(t_step, world, dev)
+    value = (fwd_bytes + bwd_bytes) * world / t_step / 1e9
+
+    # the two kernels alone, through the C ABI, on the launching stream
+    tapes = compile_tapes(Od, Chd, Xd.shape[1])
+    L = _lib.lib()
+    st = _lib.stream_ptr(dev)
+    cache = torch.empty((B, M, N), dtype=torch.float32, device=dev)
+    gCk = torch.empty((B, M), dtype=torch.float32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    Cp = Cd.detach()
+
+    def fwd_k():
+        _lib.check(L.sr_eval_forward_f32(_lib.ptr(Xd), N, Xd.shape[1], _lib.ptr(tapes.desc), _lib.ptr(tapes.meta),
+                                         _lib.ptr(tapes.order), B, M, tapes.max_len, _lib.ptr(Cp), M, 1,
+                                         _lib.ptr(cache), st), "sr_eval_forward_f32")
+
+    def bwd_k():
+        _lib.check(L.sr_eval_backward_f32(_lib.ptr(Xd), N, Xd.shape[1], _lib.ptr(tapes.desc), _lib.ptr(tapes.meta),
+                                          _lib.ptr(tapes.order), B, M, tapes.max_len, _lib.ptr(Cp), M, 1, _lib.ptr(G),
+                                          _lib.ptr(gCk), None, _lib.ptr(status), st), "sr_eval_backward_f32")
+
+    ktimes = {}
+    for name, fn in (("eval_forward_kernel", fwd_k), ("eval_backward_kernel", bwd_k)):
+        for _ in range(3):
+            fn()
+        ts = []
+        for _ in range(max(3, args.steps)):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            ts.append((e0, e1))
+        torch.cuda.synchronize()
+        ktimes[name] = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in ts)
+    assert int(status.item()) == 0
+    del cache
+
+    e2e = None
+    if not args.no_e2e:
+        hX = torch.tensor(wl.X).pin_memory()
+        hO = torch.tensor(wl.ops).pin_memory()
+        hCh = torch.tensor(wl.ch).pin_memory()
+        hC = torch.tensor(wl.C).pin_memory()
+        h2d = sum(t.numel() * t.element_size() for t in (hX, hO, hCh, hC))
+        ts = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Xh, Oh, Chh = (t.to(dev, non_blocking=True) for t in (hX, hO, hCh))
+            Ch_ = hC.to(dev, non_blocking=True).requires_grad_(True)
+            out = sr.evaluation.evaluate(Xh, Oh, Chh, Ch_)
+            rt = (Oh != 0).sum(1) - 1
+            loss = out.gather(1, rt.clamp(min=0).view(-1, 1, 1).expand(-1, 1, N)).sum()
+            loss.backward()
+            gC_h, loss_h = Ch_.grad.cpu(), loss.detach().cpu()
+            ts.append(time.perf_counter() - t0)
+            del out, loss
+        d2h = gC_h.numel() * 4 + loss_h.numel() * 4
+        e2e = {"value": (fwd_bytes + bwd_bytes) * world / statistics.median(ts) / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "path": "evaluate() + loss=sum of root outputs + loss.backward() from pinned host buffers"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, ntapes, threads = cpu_eval_sample(wl, args.cpu_eval_sample)
+        cpu = {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
+               "sample": f"{ntapes} tapes in chunks of {args.cpu_eval_sample}, forward + adjoint ({dt:.1f} s)"}
+
+    if rank == 0:
+        pk, pk_kind = peaks()
+        hbm = float(pk["hbm_gbs"])
+        dom = max(ktimes, key=ktimes.get)
+        dom_bytes = bwd_bytes if dom == "eval_backward_kernel" else fwd_bytes
+        ach = dom_bytes / ktimes[dom] / 1e9
+        line = {"metric": EVAL_METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"eval forward+adjoint: B={B} tapes, M={M}, N={N}, n_vars=4, mean length ~20, "
+                                       "dense root-row gradient", "B": B, "N": N, "M": M,
+                           "l2": f"inputs larger than L2 (cache {B * M * N * 4 / 1e9:.1f} GB)"},
+                "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                             "traffic": EVAL_TRAFFIC_BYTES.get((dom, B, N)), "kernel": dom, "peak_kind": pk_kind},
+                "kernels": {k: {"ms": v * 1000.0,
+                                "GB/s": (bwd_bytes if k == "eval_backward_kernel" else fwd_bytes) / v / 1e9}
+                            for k, v in ktimes.items()},
+                "expressions_per_s": B * world / t_step,
+                "gpu_launches": 3 * args.steps,
+                "clocks": clk.summary()}
+        if e2e:
+            line["e2e"] = e2e
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="fit", choices=["fit", "eval"])
+    ap.add_argument("--B", type=int, default=B_DEFAULT)
+    ap.add_argument("--N", type=int, default=N_DEFAULT)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=512)
+    ap.add_argument("--cpu-eval-sample", type=int, default=4096)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        torch.cuda.set_device(local)
+        if args.workload == "fit":
+            run_fit(args, rank, world, local)
+        else:
+            run_eval(args, rank, world, local)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

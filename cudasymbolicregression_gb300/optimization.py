@@ -34,7 +34,7 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
          objective: int = 0, line_search_max_iter: int = 10, eps: float = 1e-10,
          warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
          order: Optional[torch.Tensor] = None, want_y: bool = True, raise_errors: bool = True,
-         class_width: int = 0) -> FitResult:
+         class_width: int = 0, kernel_events=None) -> FitResult:
     if line_search_fn not in ("strong_wolfe", "backtracking"):
         raise ValueError(f"Invalid line_search_fn: {line_search_fn}. Choose 'strong_wolfe' or 'backtracking'.")
     if Ops.dim() != 2:
@@ -77,6 +77,8 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
         order = order.to(device=dev, dtype=torch.int32).contiguous()
         classes = [(0, B, max(tapes.max_root, 1))]
     status = torch.zeros(max(len(classes), 1), dtype=torch.int32, device=dev)
+    if kernel_events is not None:
+        kernel_events[0].record()
     for ci, (start, count, max_len) in enumerate(classes):
         if count == 0:
             continue
@@ -93,6 +95,8 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
                             _lib.ptr(evals), optr, max_len, tapes.max_consts, opts, _lib.ptr(ws), ws.numel(),
                             ctypes.c_void_p(status.data_ptr() + 4 * ci), _lib.stream_ptr(dev))
         _lib.check(rc, "sr_fit_lbfgs")
+    if kernel_events is not None:
+        kernel_events[1].record()
     codes = [c for c in status.tolist() if c]
     code = codes[0] if codes else 0
     if code and raise_errors:
@@ -150,6 +154,8 @@ def optimize_ex(X, Y, Ops, Ch, C_init, max_iter=100, history_size=10, tolerance_
     (tapes are fitted in launches per class of lengths this many nodes wide, 0 =
     one launch), raise_errors
     (False: problems whose closures hit error 201/204 are reported through
-    ``iters < 0`` instead of aborting the whole batch as the reference does).
+    ``iters < 0`` instead of aborting the whole batch as the reference does),
+    kernel_events (a pair of torch.cuda.Event recorded on the current stream just
+    before the first and just after the last fit-kernel launch).
     """
     return _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, **kw)
