@@ -1,31 +1,39 @@
-"""Benchmark: expressions fitted per second by the fused batched L-BFGS kernel.
+"""Benchmark: expressions fitted per second, warm-started vs plain fused fit.
 
-Workload (one "step"): the ragged batched L-BFGS configuration -- B=16384 tapes of
-uniform length 3..64 with 0..8 learnable constants, n_variables=2, N=512 points,
-X ~ U[-3, 3], targets = hidden random expressions + N(0, 0.01^2) noise, history 10,
-max_iter=200, strong Wolfe, tolerance_grad=1e-7 -- fitted by one optimize() call.
-Seeded synthetic data (no dataset is involved).
+Default workload (one "step" = one fit of the whole batch): the learned warm start
+evaluated on held-out problems -- B=65536 ragged problems (tapes of uniform length
+3..64 over {+,-,*,/,sin,cos,exp,log}, 0..8 learnable constants, n_variables=2,
+N=512 points, X ~ U[-3, 3], each target a hidden random expression + N(0, 0.01^2)
+noise), fitted with history 10, max_iter=200, strong Wolfe, tolerance_grad=1e-7.
+Before timing, the warm-start network is trained (untimed) on the fits of
+`--train-sets` x 65536 other problems: first on the constants the plain fit found,
+then on the fit objective itself.  Two arms are timed on the same batch:
+  plain : optimize() from the randn constants;
+  warm  : the network's constants (features + 5 tensor-core GEMMs), gated per
+          problem against the randn start by one closure each (the plain start is
+          kept where its initial MSE is not higher), then optimize().
+Seeded synthetic data; no dataset is involved.
 
-`value`   = B / (device time of one step), inputs resident in HBM, L2 flushed
-            between steps (a 256 MiB buffer is rewritten before each timed step).
-`e2e`     = the same through optimize() from pinned host buffers, host->device
-            copies of X, Y, Ops, Ch, C_init and the device->host copy of
-            C_final, Y_final inside the timed region.
+`value`   = B / (device time of one warm step), inputs resident in HBM, L2 flushed
+            (256 MiB write) before each step; `plain` holds the plain arm.
+`quality` = per arm: median final MSE over the problems the plain arm leaves finite
+            (a non-finite result counts as +inf), mean / median iterations, share of
+            problems that stop before max_iter, mean closures.
+`e2e`     = the warm arm through the public API from pinned host buffers (H2D of X,
+            Y, Ops, Ch, C_init and D2H of C_final, Y_final inside the timed region).
 `roofline`= the fit kernel's algorithmic FP32 rate (op table in
             cudasymbolicregression_gb300/workloads.py) over its CUDA-event time.
-`cpu_baseline` = the CPU oracle port of the reference's optimize() on a bounded
-            sample of the same problems, all host threads.
+`cpu_baseline` = the CPU oracle port of the reference's optimize() (plain start; the
+            reference has no warm start) on the first 512 problems, all host threads.
 
---impl reference runs only that CPU port (the reference's own CPU path,
-restated) and prints its line.
-Multi-GPU: one process per GPU; every rank fits its own batch of B problems
-(independent seeds, no collective), value = all problems / max time.
-
---workload eval measures the evaluation path instead (B=65536 tapes of padded
-length 64 over {+,-,*,/,sin,cos,exp,log,X0..X3,C}, mean length about 20,
-N=1024, X ~ U[-3, 3], C ~ N(0, 1)): one step is evaluate() forward plus the
-adjoint of a dense gradient that is 1 on every root row (the gradient of the sum
-of root outputs), value = algorithmic HBM bytes / step time.
+Other workloads: --workload ragged (the plain fit of B=16384 such problems),
+--workload readme (the README problem: expressions from its small grammar fitted to
+2.5 cos(X_0) - 1.5, warm vs plain), --workload eval (evaluate forward + adjoint of a
+dense root-row gradient at B=65536, M=64, N=1024; value = algorithmic HBM bytes /
+step time).
+--impl reference runs only the CPU port (the reference's own CPU path, restated).
+Multi-GPU: one process per GPU; every rank fits its own batch (independent seeds, no
+collective), value = all problems / max time over ranks.
 """
 from __future__ import annotations
 
@@ -46,16 +54,16 @@ import torch  # noqa: E402
 
 METRIC = "expressions fitted/s at fixed final MSE, warm-start vs plain fused, 1 GB300"
 UNIT = "expressions/s"
-B_DEFAULT, N_DEFAULT, M_DEFAULT = 16384, 512, 64
+M_DEFAULT = 64
 MAX_ITER = 200
 EVAL_METRIC = "evaluation forward+adjoint throughput (algorithmic HBM bytes)"
-EVAL_B, EVAL_N = 65536, 1024
+DEFAULTS = {"warmstart": (65536, 512), "ragged": (16384, 512), "readme": (65536, 100), "eval": (65536, 1024)}
 
 # DRAM bytes (read + write) of one launch of the dominant kernel on the default
 # workloads, from ncu captures of a 4x / 16x smaller batch scaled by the number of
 # problems (profiles/fit_lbfgs_ragged_B16384_N512.txt,
 # profiles/eval_forward_B4096_N1024.txt).
-FIT_TRAFFIC_BYTES = {(16384, 512): 4 * (10722048 + 24576)}
+FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10722048 + 24576)}
 EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000)}
 
 
@@ -130,48 +138,21 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_sample_run(wl, n_sample: int, threads: int | None = None):
-    """The CPU oracle port of optimize() on the first n_sample problems."""
+def cpu_sample_run(wl, n_sample: int, max_iter: int = MAX_ITER):
+    """The CPU oracle port of optimize() (plain start) on the first n_sample problems."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # the checker / CPU baseline only
     oracle.build()
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
-    idx = np.arange(min(n_sample, wl.B))
+    idx = np.arange(min(n_sample, wl.ops.shape[0]))
     t0 = time.perf_counter()
-    r = oracle.optimize(wl.X, wl.Y[idx], wl.ops[idx], wl.ch[idx], wl.C[idx], max_iter=MAX_ITER, dot_mode=0)
+    r = oracle.optimize(wl.X, wl.Y[idx], wl.ops[idx], wl.ch[idx], wl.C[idx], max_iter=max_iter, dot_mode=0)
     dt = time.perf_counter() - t0
     return len(idx) / dt, dt, oracle.num_threads(), r
 
 
-def run_reference(args, rank):
-    if rank != 0:
-        return
-    from cudasymbolicregression_gb300 import workloads
-    wl = workloads_cpu_fit(args)
-    n = args.cpu_sample
-    vals = []
-    cores = os.cpu_count()
-    for i in range(args.warmup + args.steps):
-        v, dt, threads, _ = cpu_sample_run(wl, n)
-        if i >= args.warmup:
-            vals.append(v)
-    value = statistics.median(vals)
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * n / value, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"ragged batched L-BFGS, B={args.B}, N={args.N}, M={M_DEFAULT}, "
-                                   f"max_iter={MAX_ITER}, strong_wolfe (CPU sample of {n} problems)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"first {n} problems of the workload, full max_iter={MAX_ITER}"},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "host_cores": cores}
-    print(json.dumps(line), flush=True)
-
-
-def workloads_cpu_fit(args):
-    """The same seeded workload, hidden targets evaluated by the CPU port (the
-    reference arm runs no GPU code)."""
+def cpu_fit_workload(args, B, N):
+    """The first problems of the benchmark's workload, built on the host only (the
+    reference arm runs no GPU code): the same seeds as the GPU batch."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from cudasymbolicregression_gb300 import workloads
@@ -180,7 +161,58 @@ def workloads_cpu_fit(args):
         cache = oracle.eval_fwd(X, ops, ch, C)
         root = np.maximum((ops != 0).sum(1) - 1, 0)
         return cache[np.arange(ops.shape[0]), root]
-    return workloads.ragged_fit(B=args.B, N=args.N, M=M_DEFAULT, seed=args.seed, root_eval=roots)
+    if args.workload == "readme":
+        return workloads.readme_fit(B=min(B, args.cpu_sample), N=N, seed=args.seed)
+    if args.workload == "ragged":
+        return workloads.ragged_fit(B=B, N=N, M=M_DEFAULT, seed=args.seed, root_eval=roots)
+    return workloads.ragged_fit_chunks(B=B, N=N, M=M_DEFAULT, seed=args.seed, n_chunks=1, root_eval=roots)
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    B, N = args.B, args.N
+    if args.workload == "eval":
+        from cudasymbolicregression_gb300 import tapes
+        rng = np.random.default_rng(args.seed)
+        X = rng.uniform(-3, 3, (N, 4)).astype(np.float32)
+        n = min(B, args.cpu_eval_sample)
+        tb = tapes.generate(n, M_DEFAULT, seed=args.seed + 1, mean_length=20.0, n_vars=4, p_const_leaf=0.2)
+
+        class _W:
+            pass
+        wl = _W()
+        wl.X, wl.ops, wl.ch = X, tb.ops, tb.ch
+        wl.C = rng.standard_normal((n, M_DEFAULT)).astype(np.float32)
+        vals = []
+        for i in range(args.warmup + args.steps):
+            v, dt, ntapes, threads = cpu_eval_sample(wl, n, seconds=2.0)
+            if i >= args.warmup:
+                vals.append(v)
+        value, unit, sample = statistics.median(vals), "GB/s", f"{n} tapes per pass, forward + adjoint"
+        metric, workload = EVAL_METRIC, f"eval forward+adjoint: M={M_DEFAULT}, N={N}, n_vars=4 (CPU sample)"
+        ms = None
+    else:
+        wl = cpu_fit_workload(args, B, N)
+        n = args.cpu_sample
+        vals = []
+        threads = 1
+        for i in range(args.warmup + args.steps):
+            v, dt, threads, _ = cpu_sample_run(wl, n, max_iter=MAX_ITER if args.workload != "readme" else 100)
+            if i >= args.warmup:
+                vals.append(v)
+        value, unit = statistics.median(vals), UNIT
+        sample = f"first {n} problems of the workload, plain start, full max_iter"
+        metric, workload = METRIC, f"{args.workload}: B={B}, N={N} (CPU sample of {n} problems)"
+        ms = 1000.0 * n / value
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload},
+            "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "host_cores": os.cpu_count()}
+    print(json.dumps(line), flush=True)
 
 
 def barrier(world):
@@ -198,109 +230,181 @@ def max_over_ranks(x, world, dev):
     return x
 
 
+def timed_steps(step, steps, flush):
+    """CUDA-event time of each call of step(kernel_events) (L2 flushed before each)."""
+    evs, kevs, r = [], [], None
+    for _ in range(steps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        kev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        e0.record()
+        r = step(kev)
+        e1.record()
+        evs.append((e0, e1))
+        kevs.append(kev)
+    torch.cuda.synchronize()
+    t = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in evs)
+    tk = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in kevs)
+    return t, tk, r
+
+
+def fit_quality(r, ref_finite, max_iter):
+    """Quality of one arm: median final MSE over the reference arm's finite problems
+    (non-finite results count as +inf), iterations and closures."""
+    loss = r.loss.cpu().numpy()
+    it = r.iters.cpu().numpy()
+    lf = np.where(np.isfinite(loss), loss, np.inf)[ref_finite]
+    return {"median_final_mse": float(np.median(lf)) if lf.size else None,
+            "p25_final_mse": float(np.percentile(lf, 25)) if lf.size else None,
+            "finite_fraction": float(np.isfinite(loss).mean()), "error_problems": int((it < 0).sum()),
+            "mean_iters": float(it.mean()), "median_iters": float(np.median(it)),
+            "stopped_before_max_iter": float(((it >= 0) & (it < max_iter)).mean()),
+            "mean_closures": float(r.evals.float().mean())}
+
+
+def train_warm_start(args, dev, n_vars):
+    """The warm-start network trained (untimed) on the fits of other problems."""
+    from cudasymbolicregression_gb300 import warmstart, workloads
+    T = lambda a: torch.tensor(a, device=dev)  # noqa: E731
+    probs, data = [], warmstart.TrainingSet([], [], [], [], [])
+    t0 = time.perf_counter()
+    for s in range(args.train_sets):
+        if args.workload == "readme":
+            wl = workloads.readme_fit(B=16384, seed=10_000 + s)
+            mi = 100
+        else:
+            wl = workloads.ragged_fit(B=65536, N=args.N, M=M_DEFAULT, seed=10_000 + s, device=str(dev))
+            mi = MAX_ITER
+        X, Y, O, Ch, C = T(wl.X), T(wl.Y), T(wl.ops), T(wl.ch), T(wl.C)
+        tgt, msk, _ = warmstart.fitted_examples(X, Y, O, Ch, C, max_iter=mi)
+        probs.append((X, Y, O, Ch, C))
+        data.X.append(X)
+        data.Y.append(Y)
+        data.ops.append(O)
+        data.target.append(tgt)
+        data.mask.append(msk)
+    t_data = time.perf_counter() - t0
+    net = warmstart.WarmStartMLP(device=dev, seed=args.seed, n_vars=n_vars)
+    s1 = warmstart.train(net, data, epochs=args.train_epochs, batch=2048, lr=2e-3)
+    s2 = warmstart.train_fit_objective(net, probs, epochs=args.train_epochs, batch=2048, lr=5e-4)
+    torch.cuda.synchronize()
+    info = {"training_problems": int(sum(p[2].shape[0] for p in probs)), "data_s": round(t_data, 1),
+            "train_s": round(time.perf_counter() - t0 - t_data, 1), "steps": s1.steps + s2.steps,
+            "objective": "constants of the plain fits, then the normalised fit MSE of the predictions"}
+    return net, info
+
+
 def run_fit(args, rank, world, local):
     import cudasymbolicregression_gb300 as sr
-    from cudasymbolicregression_gb300 import workloads
+    from cudasymbolicregression_gb300 import warmstart, workloads
 
     dev = torch.device("cuda", local)
-    wl = workloads.ragged_fit(B=args.B, N=args.N, M=M_DEFAULT, seed=args.seed + 1000 * rank)
-    Xd = torch.tensor(wl.X, device=dev)
-    Yd = torch.tensor(wl.Y, device=dev)
-    Od = torch.tensor(wl.ops, device=dev)
-    Chd = torch.tensor(wl.ch, device=dev)
-    Cd = torch.tensor(wl.C, device=dev)
+    B, N = args.B, args.N
+    seed = args.seed + 1000 * rank
+    if args.workload == "readme":
+        wl = workloads.readme_fit(B=B, N=N, seed=seed)
+        n_vars, max_iter = 1, 100
+    elif args.workload == "ragged":
+        wl = workloads.ragged_fit(B=B, N=N, M=M_DEFAULT, seed=seed, device=str(dev))
+        n_vars, max_iter = 2, MAX_ITER
+    else:
+        wl = workloads.ragged_fit_chunks(B=B, N=N, M=M_DEFAULT, seed=seed, device=str(dev))
+        n_vars, max_iter = 2, MAX_ITER
+    warm = args.workload != "ragged"
+    Xd, Yd, Od, Chd, Cd = (torch.tensor(a, device=dev) for a in (wl.X, wl.Y, wl.ops, wl.ch, wl.C))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    net, train_info = train_warm_start(args, dev, n_vars) if warm else (None, None)
 
-    def step(kev=None):
-        return sr.optimize_ex(Xd, Yd, Od, Chd, Cd, max_iter=MAX_ITER, raise_errors=False, kernel_events=kev)
+    def plain_step(kev=None):
+        return sr.optimize_ex(Xd, Yd, Od, Chd, Cd, max_iter=max_iter, raise_errors=False, kernel_events=kev)
+
+    def warm_step(kev=None):
+        Cg = warmstart.gated_warm_start(net, Xd, Yd, Od, Chd, Cd)
+        return sr.optimize_ex(Xd, Yd, Od, Chd, Cg, max_iter=max_iter, raise_errors=False, kernel_events=kev)
 
     for _ in range(args.warmup):
-        r = step()
+        plain_step()
+        if warm:
+            warm_step()
     torch.cuda.synchronize()
-
-    evs, kevs = [], []
     barrier(world)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("timed")
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            kev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-            e0.record()
-            r = step(kev)
-            e1.record()
-            evs.append((e0, e1))
-            kevs.append(kev)
-        torch.cuda.synchronize()
+        t_plain, tk_plain, r_plain = timed_steps(plain_step, args.steps, flush)
+        if warm:
+            t_warm, tk_warm, r_warm = timed_steps(warm_step, args.steps, flush)
     torch.cuda.nvtx.range_pop()
     barrier(world)
-    t_step = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in evs)
-    t_kernel = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in kevs)
-    t_step = max_over_ranks(t_step, world, dev)
-    value = args.B * world / t_step
+    t_plain = max_over_ranks(t_plain, world, dev)
+    head_t, head_tk, head_r = (t_warm, tk_warm, r_warm) if warm else (t_plain, tk_plain, r_plain)
+    head_t = max_over_ranks(head_t, world, dev)
+    value = B * world / head_t
 
-    # quality and work accounting from the last step
-    iters = r.iters.cpu().numpy()
-    evals = r.evals.cpu().numpy().astype(np.float64)
-    loss = r.loss.cpu().numpy()
+    ref_finite = np.isfinite(r_plain.loss.cpu().numpy())
+    q_plain = fit_quality(r_plain, ref_finite, max_iter)
+    q_head = fit_quality(head_r, ref_finite, max_iter)
+    evals = head_r.evals.cpu().numpy().astype(np.float64)
     flops = float((wl.flops_per_closure() * evals).sum())
-    achieved_tflops = flops / t_kernel / 1e12
+    achieved_tflops = flops / head_tk / 1e12
     pk, pk_kind = peaks()
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = sm_count * 128 * 2 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
 
-    # end-to-end through the public API from pinned host buffers
     e2e = None
     if not args.no_e2e:
-        hX = torch.tensor(wl.X).pin_memory()
-        hY = torch.tensor(wl.Y).pin_memory()
-        hO = torch.tensor(wl.ops).pin_memory()
-        hCh = torch.tensor(wl.ch).pin_memory()
-        hC = torch.tensor(wl.C).pin_memory()
+        hX, hY, hO, hCh, hC = (torch.tensor(a).pin_memory() for a in (wl.X, wl.Y, wl.ops, wl.ch, wl.C))
         h2d = sum(t.numel() * t.element_size() for t in (hX, hY, hO, hCh, hC))
         e2e_times = []
-        for i in range(max(1, args.steps)):
+        for _ in range(max(1, args.steps)):
             flush.fill_(1.0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            re = sr.optimize_ex(hX.to(dev, non_blocking=True), hY.to(dev, non_blocking=True),
-                                hO.to(dev, non_blocking=True), hCh.to(dev, non_blocking=True),
-                                hC.to(dev, non_blocking=True), max_iter=MAX_ITER, raise_errors=False)
+            X_, Y_, O_, Ch_, C_ = (t.to(dev, non_blocking=True) for t in (hX, hY, hO, hCh, hC))
+            if warm:
+                C_ = warmstart.gated_warm_start(net, X_, Y_, O_, Ch_, C_)
+            re = sr.optimize_ex(X_, Y_, O_, Ch_, C_, max_iter=max_iter, raise_errors=False)
             Cf_h, Yf_h = re.C.cpu(), re.Y.cpu()
             e2e_times.append(time.perf_counter() - t0)
         d2h = Cf_h.numel() * 4 + Yf_h.numel() * 4
-        e2e = {"value": args.B * world / statistics.median(e2e_times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+        e2e = {"value": B * world / statistics.median(e2e_times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "arm": "warm" if warm else "plain"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, threads, _ = cpu_sample_run(wl, args.cpu_sample)
+        v, dt, threads, _ = cpu_sample_run(wl, args.cpu_sample, max_iter=max_iter)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {args.cpu_sample} problems, full max_iter={MAX_ITER} ({dt:.1f} s)"}
+               "sample": f"first {args.cpu_sample} problems, plain start, full max_iter={max_iter} ({dt:.1f} s)"}
 
     if rank == 0:
-        fin = np.isfinite(loss)
-        traffic = FIT_TRAFFIC_BYTES.get((args.B, args.N))
+        names = {"warmstart": f"learned warm start on held-out ragged problems: B={B}, tapes U[3,64] over "
+                              f"+-*/ sin cos exp log, 0..8 constants, n_vars=2, N={N}, history 10, "
+                              f"max_iter={max_iter}, strong_wolfe, tol 1e-7",
+                 "ragged": f"ragged batched L-BFGS: B={B} tapes U[3,64], 0..8 constants, n_vars=2, N={N}, "
+                           f"history 10, max_iter={max_iter}, strong_wolfe, tol 1e-7, plain randn init",
+                 "readme": f"README problem: B={B} expressions of the README grammar (infix <= 32 tokens), "
+                           f"N={N}, Y = 2.5 cos(X0) - 1.5, max_iter={max_iter}, strong_wolfe, tol 1e-7"}
+        launches_per_step = 2 + (13 if warm else 0)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True, "scaling": "weak",
+                "warmup": args.warmup, "ms_per_step": head_t * 1000.0, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": f"ragged batched L-BFGS: B={args.B} tapes, lengths U[3,64], 0..8 constants, "
-                                       f"n_vars=2, N={args.N}, history 10, max_iter={MAX_ITER}, strong_wolfe, "
-                                       "tol 1e-7, plain randn init",
-                           "B": args.B, "N": args.N, "M": M_DEFAULT, "l2": "flushed (256 MiB write) between steps"},
+                "config": {"workload": names[args.workload], "B": B, "N": N, "M": M_DEFAULT if args.workload != "readme" else 32,
+                           "arm": "warm" if warm else "plain", "l2": "flushed (256 MiB write) between steps"},
                 "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                             "frac": achieved_tflops / fp32_peak, "traffic": traffic,
-                             "kernel": "fit_lbfgs_kernel", "kernel_ms": t_kernel * 1000.0,
+                             "frac": achieved_tflops / fp32_peak,
+                             "traffic": FIT_TRAFFIC_BYTES.get((args.workload, B, N)),
+                             "kernel": "fit_lbfgs_kernel", "kernel_ms": head_tk * 1000.0,
                              "peak_kind": f"nominal: {sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz "
                                           f"({pk_kind} clock); no measured FP32 peak exists"},
-                "quality": {"median_final_mse": float(np.median(loss[fin])) if fin.any() else None,
-                            "error_problems": int((iters < 0).sum()),
-                            "nan_fraction": float(1 - fin.mean()), "mean_iters": float(iters.mean()),
-                            "mean_closures": float(evals.mean())},
-                "gpu_launches": 2 * args.steps,
+                "quality": q_head,
+                "gpu_launches": launches_per_step * args.steps,
                 "clocks": clk.summary()}
+        if warm:
+            line["plain"] = {"value": B * world / t_plain, "ms_per_step": t_plain * 1000.0, "quality": q_plain,
+                             "kernel_ms": tk_plain * 1000.0}
+            line["warm_vs_plain"] = (B * world / head_t) / (B * world / t_plain)
+            line["fixed_final_mse"] = bool(q_head["median_final_mse"] <= q_plain["median_final_mse"] * 1.0001)
+            line["warm_start_training"] = train_info
         if e2e:
             line["e2e"] = e2e
         if cpu:
@@ -352,8 +456,7 @@ def run_eval(args, rank, world, local):
     from cudasymbolicregression_gb300.tape import compile_tapes
 
     dev = torch.device("cuda", local)
-    B = args.B if args.B != B_DEFAULT else EVAL_B
-    N = args.N if args.N != N_DEFAULT else EVAL_N
+    B, N = args.B, args.N
     wl = workloads.eval_batch(B=B, N=N, M=M_DEFAULT, seed=args.seed + 1000 * rank, device=str(dev))
     M = M_DEFAULT
     Xd = torch.tensor(wl.X, device=dev)
@@ -492,15 +595,20 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="fit", choices=["fit", "eval"])
-    ap.add_argument("--B", type=int, default=B_DEFAULT)
-    ap.add_argument("--N", type=int, default=N_DEFAULT)
+    ap.add_argument("--workload", default="warmstart", choices=list(DEFAULTS))
+    ap.add_argument("--B", type=int, default=None)
+    ap.add_argument("--N", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--train-sets", type=int, default=4)
+    ap.add_argument("--train-epochs", type=int, default=8)
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--cpu-eval-sample", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    dB, dN = DEFAULTS[args.workload]
+    args.B = dB if args.B is None else args.B
+    args.N = dN if args.N is None else args.N
 
     rank, world, local = dist_env()
     if world > 1:
@@ -511,10 +619,10 @@ def main():
         run_reference(args, rank)
     else:
         torch.cuda.set_device(local)
-        if args.workload == "fit":
-            run_fit(args, rank, world, local)
-        else:
+        if args.workload == "eval":
             run_eval(args, rank, world, local)
+        else:
+            run_fit(args, rank, world, local)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

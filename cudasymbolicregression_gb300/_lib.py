@@ -38,6 +38,30 @@ class FitOptions(ctypes.Structure):
     ]
 
 
+class MlpEpilogue(ctypes.Structure):
+    """Mirror of ``sr_mlp_epilogue``."""
+    _fields_ = [
+        ("epilogue", i32),
+        ("splits", i32),
+        ("bias", vp),
+        ("gate", vp),
+        ("ld_gate", i64),
+        ("out", vp),
+        ("ld_out", i64),
+        ("out_col0", i64),
+        ("out_t", vp),
+        ("ld_out_t", i64),
+        ("out_t_row0", i64),
+        ("out_f32", vp),
+        ("ld_out_f32", i64),
+        ("split_stride", i64),
+    ]
+
+
+MLP_EPI_RELU, MLP_EPI_LINEAR, MLP_EPI_F32, MLP_EPI_RELU_GRAD, MLP_EPI_SPLIT_F32 = 0, 1, 2, 3, 4
+MLP_VOCAB, MLP_EMB, MLP_FEATS, MLP_PROJ, MLP_IN = 64, 64, 32, 28, 128
+MLP_TIMEOUT = 601
+
 _SIGS = {
     "sr_last_error": ([], ctypes.c_char_p),
     "sr_version": ([], ctypes.c_char_p),
@@ -58,6 +82,16 @@ _SIGS = {
     "sr_postfix_to_infix": ([vp, i64, i64, i32, vp, i64, vp, vp], ctypes.c_int),
     "sr_const_offsets": ([vp, i64, i64, i64, i64, vp, vp], ctypes.c_int),
     "sr_const_scatter": ([vp, i64, i64, i64, i64, vp, vp, vp, vp], ctypes.c_int),
+    "sr_mlp_gemm": ([vp, i64, i64, i64, vp, i64, i64, ctypes.POINTER(MlpEpilogue), vp, vp], ctypes.c_int),
+    "sr_mlp_gemm_splits_used": ([i64, i32], ctypes.c_int),
+    "sr_mlp_random_features": ([vp, i64, i64, vp, vp, vp, vp], ctypes.c_int),
+    "sr_mlp_features": ([vp, i64, i64, i64, i64, vp, i64, vp, vp, vp, i64, vp, vp, vp, vp], ctypes.c_int),
+    "sr_mlp_loss": ([vp, i64, i64, vp, vp, i32, ctypes.c_float, vp, vp, i64, vp, i64, vp], ctypes.c_int),
+    "sr_mlp_colsum": ([vp, i64, i64, i64, vp, vp], ctypes.c_int),
+    "sr_mlp_output_grad": ([vp, i64, i32, i64, ctypes.c_float, vp, i64, vp, i64, vp], ctypes.c_int),
+    "sr_mlp_reduce_splits": ([vp, i32, i64, i64, vp, vp], ctypes.c_int),
+    "sr_mlp_adam": ([vp, vp, vp, vp, i64, i64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                     ctypes.c_float, i32, vp, vp, vp], ctypes.c_int),
 }
 
 

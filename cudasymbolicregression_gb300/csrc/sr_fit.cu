@@ -206,6 +206,28 @@ __device__ __forceinline__ double dot(const Problem<SPL>& P, const Slots<SPL>& a
   return wsum_d(acc);
 }
 
+// Dot product of two slot vectors with float-pair accumulation (TwoProduct by
+// FMA, then pair sums): about 48 significant bits on the FP32 pipe, rounded to
+// float.  Used for the line-search slope g.p and the gradient norm; the curvature
+// dots of the two-loop recursion stay in double.
+template <int SPL>
+__device__ __forceinline__ float dot_f2(const Problem<SPL>& P, const Slots<SPL>& a, const Slots<SPL>& b) {
+  F2 acc{0.f, 0.f};
+#pragma unroll
+  for (int s = 0; s < SPL; ++s) {
+    if (P.active(s)) {
+      const float pr = __fmul_rn(a.v[s], b.v[s]);
+      acc = f2_add(acc, F2{pr, __fmaf_rn(a.v[s], b.v[s], -pr)});
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const F2 t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
+    acc = f2_add(acc, t);
+  }
+  return acc.hi;
+}
+
 // x + a * p, rounded as two separate float operations (never fused), so that the
 // trial point and the later update x += a*p give identical bits.
 template <int SPL>
@@ -644,7 +666,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
         g = cur.g;
         begin_iter = true;
       } else if (phase == PH_BRACKET) {
-        const float dphi = (float)dot(P, cur.g, p);
+        const float dphi = dot_f2(P, cur.g, p);
         const bool bad = (cur.phi > armijo(phi0, c1, a_i, dphi0)) || (lsi > 0 && cur.phi >= phi_prev);
         const bool good = fabsf(dphi) <= __fmul_rn(c2, fabsf(dphi0));
         const bool passed = dphi >= 0.f;
@@ -695,7 +717,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
         plo = cur;
         phase = PH_ZOOM;
       } else if (phase == PH_ZOOM) {
-        const float dphij = (float)dot(P, cur.g, p);
+        const float dphij = dot_f2(P, cur.g, p);
         const bool zbad = (cur.phi > armijo(phi0, c1, aj, dphi0)) || (cur.phi >= plo.phi);
         const bool zgood = fabsf(dphij) <= __fmul_rn(c2, fabsf(dphi0));
         bool zdone = false;
@@ -814,7 +836,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
 
       // ---- start of an outer iteration: convergence test, direction, line search ----
       if (begin_iter) {
-        if (it >= A.max_iter || sqrt(dot(P, g, g)) < A.tol) {
+        if (it >= A.max_iter || sqrt((double)dot_f2(P, g, g)) < A.tol) {
           phase = PH_DONE;
         } else {
           // two-loop recursion (lbfgs_batch.py:65-103), by warp 0 for the CTA
@@ -872,7 +894,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
 #pragma unroll
           for (int s = 0; s < SPL; ++s) p.v[s] = S.pvec[s * 32 + lane];
           phi0 = f;
-          dphi0 = (float)dot(P, g, p);
+          dphi0 = dot_f2(P, g, p);
           lsi = 0;
           if (A.ls_kind == 0) {
             a_prev = 0.f;

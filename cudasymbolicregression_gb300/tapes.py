@@ -141,7 +141,8 @@ def _exp_under_div(ops: np.ndarray, ch: np.ndarray) -> np.ndarray:
 def generate(B: int, M: int = 64, *, seed: int = 0, lengths=None, mean_length: float | None = None,
              n_vars: int = 4, binary=BIN_DEFAULT, unary=UN_DEFAULT, const_counts=None,
              p_const_leaf: float = 0.2, X_screen: np.ndarray | None = None,
-             C_screen: np.ndarray | None = None, no_exp_in_denominator: bool = False) -> TapeBatch:
+             C_screen: np.ndarray | None = None, no_exp_in_denominator: bool = False,
+             screen_fn=None) -> TapeBatch:
     """Draw B postfix tapes of padded length M.
 
     lengths: (B,) int array of exact tape lengths, or None to draw them from a
@@ -151,6 +152,8 @@ def generate(B: int, M: int = 64, *, seed: int = 0, lengths=None, mean_length: f
       probability ``p_const_leaf`` and otherwise a uniform variable.
     X_screen/C_screen: rows used to reject exact-zero denominators (None skips).
     no_exp_in_denominator: also redraw tapes with EXP under a DIV denominator.
+    screen_fn(ops, ch, X_screen, C) -> (B,) bool: the zero-denominator test
+      (default: a float32 numpy evaluation).
     """
     rng = np.random.default_rng(seed)
     if lengths is None:
@@ -188,7 +191,7 @@ def generate(B: int, M: int = 64, *, seed: int = 0, lengths=None, mean_length: f
             break
         if X_screen is not None:
             Cs = np.zeros((nb, M), np.float32) if C_screen is None else np.asarray(C_screen, np.float32)[todo]
-            bad |= _screen_eval(o, c, np.asarray(X_screen, np.float32), Cs)
+            bad |= (screen_fn or _screen_eval)(o, c, np.asarray(X_screen, np.float32), Cs)
         todo = todo[bad]
         if todo.size == 0:
             break

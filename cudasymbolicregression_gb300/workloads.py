@@ -68,18 +68,24 @@ def _gpu_roots(X, ops, ch, C, device="cuda"):
 
 
 def ragged_fit(B: int = 16384, N: int = 512, M: int = 64, n_vars: int = 2, seed: int = 0,
-               device: str = "cuda", root_eval=None) -> FitWorkload:
+               device: str = "cuda", root_eval=None, X: np.ndarray | None = None) -> FitWorkload:
     """root_eval(X, ops, ch, C) -> (B, N) root values of the hidden targets
-    (default: the library's forward kernel on ``device``)."""
-    root_eval = root_eval or (lambda X_, o, c, C_: _gpu_roots(X_, o, c, C_, device))
+    (default: the library's forward kernel on ``device``, which then also screens
+    the tapes for zero denominators; with a root_eval given, everything runs on the
+    host)."""
+    screen = None
+    if root_eval is None:
+        root_eval = lambda X_, o, c, C_: _gpu_roots(X_, o, c, C_, device)  # noqa: E731
+        screen = lambda o, c, Xs_, Cs_: _gpu_zero_denominators(Xs_, o, c, Cs_, device)  # noqa: E731
     rng = np.random.default_rng(seed)
-    X = rng.uniform(-3, 3, (N, n_vars)).astype(np.float32)
+    Xd = rng.uniform(-3, 3, (N, n_vars)).astype(np.float32)
+    X = Xd if X is None else np.asarray(X, np.float32)
     C = rng.standard_normal((B, M)).astype(np.float32)
     lengths = rng.integers(3, M + 1, size=B)
     kc = rng.integers(0, 9, size=B)
     Xs = X[rng.choice(N, size=min(N, 32), replace=False)]
     tb = tapes.generate(B, M, seed=seed + 1, lengths=lengths, const_counts=kc, n_vars=n_vars,
-                        X_screen=Xs, C_screen=C, no_exp_in_denominator=True)
+                        X_screen=Xs, C_screen=C, no_exp_in_denominator=True, screen_fn=screen)
     # hidden target expressions
     Y = np.zeros((B, N), np.float32)
     todo = np.arange(B)
@@ -89,7 +95,7 @@ def ragged_fit(B: int = 16384, N: int = 512, M: int = 64, n_vars: int = 2, seed:
         hk = rng.integers(0, 9, size=nb)
         Ch_ = rng.standard_normal((nb, M)).astype(np.float32)
         hid = tapes.generate(nb, M, seed=seed + 100 + attempt, lengths=hl, const_counts=hk, n_vars=n_vars,
-                             X_screen=Xs, C_screen=Ch_)
+                             X_screen=Xs, C_screen=Ch_, screen_fn=screen)
         yh = np.asarray(root_eval(X, hid.ops, hid.ch, Ch_), np.float32)
         ok = np.isfinite(yh).all(1) & (np.abs(yh).max(1) < 1e4)
         Y[todo[ok]] = yh[ok]
@@ -99,6 +105,24 @@ def ragged_fit(B: int = 16384, N: int = 512, M: int = 64, n_vars: int = 2, seed:
     Y[todo] = 0.0
     Y = (Y + 0.01 * rng.standard_normal((B, N))).astype(np.float32)
     return FitWorkload(X=X, Y=Y, ops=tb.ops, ch=tb.ch, C=C, name=f"ragged_fit_B{B}_N{N}_M{M}")
+
+
+def ragged_fit_chunks(B: int, N: int = 512, M: int = 64, n_vars: int = 2, seed: int = 0, chunk: int = 4096,
+                      n_chunks: int | None = None, device: str = "cuda", root_eval=None) -> FitWorkload:
+    """The ragged workload built from chunks of `chunk` problems with seeds
+    seed * 1000 + i that share one X (drawn from `seed`): the first chunks of a large
+    batch are the same problems as a small batch, so a bounded CPU sample and the
+    GPU batch can be compared problem by problem.  n_chunks limits how many are built."""
+    X = np.random.default_rng(seed).uniform(-3, 3, (N, n_vars)).astype(np.float32)
+    total = (B + chunk - 1) // chunk if n_chunks is None else n_chunks
+    parts = []
+    for i in range(total):
+        b = min(chunk, B - i * chunk)
+        parts.append(ragged_fit(B=b, N=N, M=M, n_vars=n_vars, seed=seed * 1000 + i, device=device,
+                                root_eval=root_eval, X=X))
+    cat = lambda k: np.concatenate([getattr(p, k) for p in parts])  # noqa: E731
+    return FitWorkload(X=X, Y=cat("Y"), ops=cat("ops"), ch=cat("ch"), C=cat("C"),
+                       name=f"ragged_fit_B{B}_N{N}_M{M}_chunks{chunk}")
 
 
 @dataclass
@@ -147,3 +171,59 @@ def eval_batch(B: int = 65536, N: int = 1024, M: int = 64, n_vars: int = 4, seed
         ops[bad] = nb.ops
         ch[bad] = nb.ch
     return EvalWorkload(X=X, ops=ops, ch=ch, C=C)
+
+
+def _readme_expression(rng: np.random.Generator, max_infix: int):
+    """One postfix expression from the grammar
+    E -> E + T (0.4) | T (0.6);  T -> F * T (0.4) | F (0.6);  F -> R(V) (0.3) | V (0.7);
+    R -> sin (0.5) | cos (0.5);  V -> X_0 (0.5) | C (0.5),
+    with its infix token count (parentheses included); None when the infix is longer
+    than max_infix."""
+    X0, C = 50, int(Operator.LEARNABLE_CONSTANT)
+    SIN, COS, ADD, MUL = int(Operator.SIN), int(Operator.COS), int(Operator.ADD), int(Operator.MUL)
+
+    def V():
+        return [X0 if rng.random() < 0.5 else C], 1
+
+    def F():
+        if rng.random() < 0.3:
+            r = SIN if rng.random() < 0.5 else COS
+            v, n = V()
+            return v + [r], n + 3
+        return V()
+
+    def T():
+        post, n = F()
+        rest = []
+        while rng.random() < 0.4:  # T -> F * T: right-nested products
+            f, m = F()
+            rest.append(f)
+            n += m + 1
+        for f in rest:
+            post = post + f
+        return post + [MUL] * len(rest), n
+
+    post, n = T()
+    while rng.random() < 0.4:  # E -> E + T: left-nested sums
+        t, m = T()
+        post = post + t + [ADD]
+        n += m + 1
+    return (post, n) if n <= max_infix else None
+
+
+def readme_fit(B: int = 1024, N: int = 100, M: int = 32, seed: int = 0) -> FitWorkload:
+    """The README problem: expressions from the grammar above (infix capped at M
+    tokens), X = 2 randn(N, 1), every target row 2.5 cos(X_0) - 1.5, C ~ N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    X = (2.0 * rng.standard_normal((N, 1))).astype(np.float32)
+    ops = np.zeros((B, M), np.int64)
+    for b in range(B):
+        e = None
+        while e is None:
+            e = _readme_expression(rng, M)
+        ops[b, :len(e[0])] = e[0]
+    arity = np.where(ops == 0, -1, np.where(ops >= 50, 0, np.where(ops == 1, 0, np.where(ops >= 40, 2, 1))))
+    ch = tapes._children(arity.astype(np.int8))
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    Y = np.tile((2.5 * np.cos(X[:, 0]) - 1.5).astype(np.float32), (B, 1))
+    return FitWorkload(X=X, Y=Y, ops=ops, ch=ch, C=C, name=f"readme_fit_B{B}_N{N}_M{M}")

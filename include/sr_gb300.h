@@ -217,6 +217,103 @@ int sr_postfix_children(const int64_t *ops_dev, int64_t B, int64_t M, int32_t n_
 int sr_postfix_to_infix(const int64_t *ops_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *infix_dev,
                         int64_t M_out, int64_t *err_dev, void *stream);
 
+/* ---- Warm-start network ---------------------------------------------------------
+ * No reference counterpart: the learned part of the fit.  A BF16 MLP with fp32
+ * accumulation predicts starting constants from a tape (bag of tokens through a
+ * 64-wide embedding) and 32 features of its target row.  bf16 tensors are passed
+ * as uint16_t bit patterns.  Layer widths are padded to multiples of 64. */
+#define SR_MLP_VOCAB 64  /* token bins: operator codes 0..63 (larger codes share bin 63) */
+#define SR_MLP_EMB 64    /* embedding width */
+#define SR_MLP_FEATS 32  /* target features: 4 moments + SR_MLP_PROJ projections */
+#define SR_MLP_PROJ 28   /* random features of X */
+#define SR_MLP_IN 128    /* first hidden layer input: embedding | features | zero padding */
+#define SR_MLP_TIMEOUT 601 /* status: a GEMM wait on the tensor-core pipeline ran out */
+
+#define SR_MLP_EPI_RELU 0       /* bf16 out = relu(acc + bias), row-major and/or transposed */
+#define SR_MLP_EPI_LINEAR 1     /* bf16 out = acc + bias (bias may be NULL) */
+#define SR_MLP_EPI_F32 2        /* fp32 out_f32 = acc + bias (bias may be NULL) */
+#define SR_MLP_EPI_RELU_GRAD 3  /* bf16 out = acc where gate > 0, else 0 (ReLU adjoint) */
+#define SR_MLP_EPI_SPLIT_F32 4  /* fp32 partial sums: the K range is cut into `splits` pieces,
+                                   piece s written at out_f32 + s * split_stride (no bias) */
+
+typedef struct {
+  int32_t epilogue;         /* SR_MLP_EPI_* */
+  int32_t splits;           /* SR_MLP_EPI_SPLIT_F32 only */
+  const float *bias_dev;    /* [n] or NULL */
+  const uint16_t *gate_dev; /* RELU_GRAD: bf16 [rows][ld_gate] */
+  int64_t ld_gate;
+  uint16_t *out_dev;        /* bf16 row-major: row r, column c at out[r * ld_out + out_col0 + c]; or NULL */
+  int64_t ld_out, out_col0;
+  uint16_t *out_t_dev;      /* bf16 transposed: out_t[(out_t_row0 + c) * ld_out_t + r]; or NULL */
+  int64_t ld_out_t, out_t_row0;
+  float *out_f32_dev;       /* fp32 row-major [rows][ld_out_f32] (per split) */
+  int64_t ld_out_f32, split_stride;
+} sr_mlp_epilogue;
+
+/*
+ * D[rows][n] = A[rows][k] . W[n][k]^T on the tensor cores (tcgen05, bf16 operands
+ * staged by TMA, fp32 accumulation in TMEM), followed by the epilogue.  k a positive
+ * multiple of 64; n 64, 128 or 256; lda, ldw >= k and multiples of 8; A and W
+ * 16-byte aligned.  status_dev receives SR_MLP_TIMEOUT if a pipeline wait ran out.
+ */
+int sr_mlp_gemm(const uint16_t *A_dev, int64_t rows, int64_t k, int64_t lda, const uint16_t *W_dev, int64_t n,
+                int64_t ldw, const sr_mlp_epilogue *epi, int32_t *status_dev, void *stream);
+
+/* Number of K pieces sr_mlp_gemm uses for SR_MLP_EPI_SPLIT_F32 with this k and request. */
+int sr_mlp_gemm_splits_used(int64_t k, int32_t splits);
+
+/* phi (N, SR_MLP_PROJ) = sqrt(2) cos(omega_j . x_n + beta_j); omega (SR_MLP_PROJ, n_x), beta (SR_MLP_PROJ). */
+int sr_mlp_random_features(const float *X_dev, int64_t N, int64_t n_x, const float *omega_dev,
+                           const float *beta_dev, float *phi_dev, void *stream);
+
+/*
+ * Network inputs of B problems: hist (B, SR_MLP_VOCAB) bf16 token frequencies of each
+ * tape (counts / number of non-NO_OP tokens) and its transpose hist_t (SR_MLP_VOCAB,
+ * ld_t); columns SR_MLP_EMB.. of x0 (B, SR_MLP_IN) and rows SR_MLP_EMB.. of x0_t
+ * (SR_MLP_IN, ld_t) get the 32 target features of Y (B, N) then zeros: asinh(mean),
+ * log(std + 1e-3), skewness, asinh(excess kurtosis), and the means of the standardised
+ * target times each random feature phi (N, SR_MLP_PROJ).  feats (B, 32) fp32 or NULL.
+ */
+int sr_mlp_features(const int64_t *ops_dev, int64_t B, int64_t M, int64_t ops_sb, int64_t ops_sm,
+                    const float *Y_dev, int64_t N, const float *phi_dev, uint16_t *hist_dev,
+                    uint16_t *hist_t_dev, int64_t ld_t, uint16_t *x0_dev, uint16_t *x0_t_dev,
+                    float *feats_dev, void *stream);
+
+/*
+ * Squared-error loss on the first n_out output columns where mask > 0:
+ * row_loss (rows) = sum_j mask (out - target)^2 (or NULL), and the bf16 output
+ * gradient scale * 2 * mask * (out - target) into d_out (rows, ld_d) (zero in columns
+ * n_out..ld_d-1) and, if not NULL, its transpose d_out_t (ld_d rows, ld_dt).
+ */
+int sr_mlp_loss(const float *out_dev, int64_t rows, int64_t ld_out, const float *target_dev,
+                const float *mask_dev, int32_t n_out, float scale, float *row_loss_dev, uint16_t *d_out_dev,
+                int64_t ld_d, uint16_t *d_out_t_dev, int64_t ld_dt, void *stream);
+
+/*
+ * An output gradient computed outside the network: d_out (rows, ld_d) bf16 =
+ * scale * g (rows, n_out; row stride ld_g), zero in columns n_out..ld_d-1 and in rows
+ * where g is not finite; its transpose into d_out_t (ld_d rows, ld_dt) if not NULL.
+ */
+int sr_mlp_output_grad(const float *g_dev, int64_t rows, int32_t n_out, int64_t ld_g, float scale,
+                       uint16_t *d_out_dev, int64_t ld_d, uint16_t *d_out_t_dev, int64_t ld_dt, void *stream);
+
+/* out (n) = row sums of the bf16 matrix xt (n, ld) over its first `rows` columns. */
+int sr_mlp_colsum(const uint16_t *xt_dev, int64_t n, int64_t rows, int64_t ld, float *out_dev, void *stream);
+
+/* out (count) = sum over s < splits of part[s * split_stride + i], in order. */
+int sr_mlp_reduce_splits(const float *part_dev, int32_t splits, int64_t count, int64_t split_stride,
+                         float *out_dev, void *stream);
+
+/*
+ * One Adam step (decoupled weight decay, bias correction for `step` >= 1) on fp32
+ * weights w (rows, cols) with gradient g and moments m, v; then bf16 copies into
+ * w_bf16 (rows, cols) and w_t_bf16 (cols, rows) where not NULL.  lr = 0 only
+ * refreshes the bf16 copies (g, m, v unused).
+ */
+int sr_mlp_adam(float *w_dev, const float *g_dev, float *m_dev, float *v_dev, int64_t rows, int64_t cols,
+                float lr, float beta1, float beta2, float eps, float weight_decay, int32_t step,
+                uint16_t *w_bf16_dev, uint16_t *w_t_bf16_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
