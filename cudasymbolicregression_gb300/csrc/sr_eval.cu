@@ -216,46 +216,125 @@ __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__
 // grad_C is deterministic.
 // ------------------------------------------------------------------------------------
 
-// True in every lane when one of count values at p is nonzero (NaN counts as nonzero).
+// ---- padding rows: any nonzero output gradient on a NO_OP row is error 201 ----------
+// One CTA per tape (grid-stride): rows L..M-1 of its (M, N) gradient block are one
+// contiguous range, read with 16-byte streaming loads, four in flight per thread.
+// Launched before the adjoint kernel so that 201 takes precedence, as in the
+// reference, whose reverse loop meets the padding rows first.
 template <typename T>
-__device__ __forceinline__ bool warp_any_nonzero(const T* p, size_t count, int lane) {
-  bool nz = false;
+__global__ void __launch_bounds__(256) padding_check_kernel(const T* __restrict__ gout,
+                                                            const int32_t* __restrict__ meta, int64_t B,
+                                                            int64_t M, int64_t N, int32_t* __restrict__ status) {
   constexpr int kVec = 16 / sizeof(T);
-  size_t head = (size_t)((16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15) / sizeof(T);
-  if (reinterpret_cast<uintptr_t>(p) % sizeof(T)) head = count;
-  if (head > count) head = count;
-  for (size_t i = lane; i < head; i += 32) nz |= __ldcs(p + i) != T(0);
-  const size_t nvec = (count - head) / kVec;
-  const float4* q = reinterpret_cast<const float4*>(p + head);
-  for (size_t i = lane; i < nvec; i += 32) {
-    const float4 v = __ldcs(q + i);
-    if (sizeof(T) == 4) {
-      nz |= (v.x != 0.f) | (v.y != 0.f) | (v.z != 0.f) | (v.w != 0.f);
-    } else {
-      const double* d = reinterpret_cast<const double*>(&v);
-      nz |= (d[0] != 0.0) | (d[1] != 0.0);
+  for (int64_t b = blockIdx.x; b < B; b += gridDim.x) {
+    // the whole CTA stops once any error is recorded (uniform decision)
+    if (__syncthreads_or(threadIdx.x == 0 && *reinterpret_cast<volatile int32_t*>(status) != 0)) return;
+    const int64_t L = meta[b * 4];
+    const T* p = gout + (size_t)b * M * N + (size_t)L * N;
+    const size_t count = (size_t)(M - L) * N;
+    size_t head = (size_t)((16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15) / sizeof(T);
+    if (reinterpret_cast<uintptr_t>(p) % sizeof(T)) head = count;  // unaligned element type: scalar path
+    if (head > count) head = count;
+    bool nz = false;
+    for (size_t i = threadIdx.x; i < head; i += blockDim.x) nz |= __ldcs(p + i) != T(0);
+    const size_t nvec = (count - head) / kVec;
+    const float4* q = reinterpret_cast<const float4*>(p + head);
+    size_t i = threadIdx.x;
+    for (; i + 3 * blockDim.x < nvec; i += 4 * blockDim.x) {
+      float4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = __ldcs(q + i + u * blockDim.x);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (sizeof(T) == 4) {
+          nz |= (v[u].x != 0.f) | (v[u].y != 0.f) | (v[u].z != 0.f) | (v[u].w != 0.f);
+        } else {
+          const double* d = reinterpret_cast<const double*>(&v[u]);
+          nz |= (d[0] != 0.0) | (d[1] != 0.0);
+        }
+      }
     }
+    for (; i < nvec; i += blockDim.x) {
+      const float4 v = __ldcs(q + i);
+      if (sizeof(T) == 4) {
+        nz |= (v.x != 0.f) | (v.y != 0.f) | (v.z != 0.f) | (v.w != 0.f);
+      } else {
+        const double* d = reinterpret_cast<const double*>(&v);
+        nz |= (d[0] != 0.0) | (d[1] != 0.0);
+      }
+    }
+    for (size_t j = head + nvec * kVec + threadIdx.x; j < count; j += blockDim.x) nz |= __ldcs(p + j) != T(0);
+    if (__syncthreads_or(nz) && threadIdx.x == 0) report(status, ERR_GRAD_ON_NO_OP);
   }
-  for (size_t i = head + nvec * kVec + lane; i < count; i += 32) nz |= __ldcs(p + i) != T(0);
-  return __any_sync(0xffffffffu, nz);
 }
 
+// ---- asynchronous staging of output-gradient rows -----------------------------------
+
+__device__ __forceinline__ void cp_async(void* dst_smem, const void* src, int cp_bytes, int src_bytes) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst_smem));
+  if (cp_bytes == 16) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+  } else if (cp_bytes == 8) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int kPending>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory"); }
+
+// Copies rows 0..L-1, points base..base+31 of the (L, N) gradient block G into
+// buf[k][32] (zero beyond N).  vec16: rows start 16-byte aligned, so each lane moves
+// 16 bytes (E = 16 / sizeof(T) points; E rows per instruction); otherwise one element
+// per lane and row.
+template <typename T>
+__device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N, int64_t base, int lane, bool vec16) {
+  if (vec16) {
+    constexpr int E = 16 / sizeof(T);
+    constexpr int kLanesPerRow = 32 / E;
+    const int r0 = lane / kLanesPerRow, p = (lane % kLanesPerRow) * E;
+    const int64_t left = N - (base + p);
+    const int bytes = left >= E ? 16 : (left > 0 ? (int)left * (int)sizeof(T) : 0);
+    for (int k = r0; k < L; k += E) {
+      const T* src = bytes ? G + (size_t)k * N + base + p : G;
+      cp_async(buf + k * 32 + p, src, 16, bytes);
+    }
+  } else {
+    const int64_t n = base + lane;
+    const int bytes = n < N ? (int)sizeof(T) : 0;
+    for (int k = 0; k < L; ++k) {
+      const T* src = bytes ? G + (size_t)k * N + n : G;
+      cp_async(buf + k * 32 + lane, src, (int)sizeof(T), bytes);
+    }
+  }
+  cp_async_commit();
+}
+
+// ------------------------------------------------------------------------------------
+// Adjoint.  One warp per tape (persistent, longest first), 32 points per chunk.  The
+// output-gradient rows of chunk c+1 are staged into shared memory with cp.async while
+// chunk c is processed (two buffers), node values are recomputed (the saved cache is
+// never read), and the gradient of each constant is summed over points in a fixed
+// order (per chunk a butterfly, then in chunk order), so grad_C is deterministic.
+// ------------------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(256) eval_backward_kernel(
     const T* __restrict__ X, int64_t N, int64_t n_x, const uint32_t* __restrict__ desc,
     const int32_t* __restrict__ meta, const int32_t* __restrict__ order, int64_t B, int64_t M, int Lmax,
     const T* __restrict__ C, int64_t c_sb, int64_t c_sm, const T* __restrict__ gout, T* __restrict__ gC,
-    T* __restrict__ gX, int32_t* __restrict__ status) {
+    T* __restrict__ gX, int32_t* __restrict__ status, bool vec16) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const size_t tbytes = align16((size_t)Lmax * 4);
   const size_t vbytes = (size_t)Lmax * 32 * sizeof(T);
-  const size_t per_warp = tbytes + 2 * vbytes + align16((size_t)Lmax * sizeof(T));
+  const size_t per_warp = tbytes + 3 * vbytes + align16((size_t)Lmax * sizeof(T));
   unsigned char* base_ptr = smem + warp * per_warp;
   uint32_t* tape = reinterpret_cast<uint32_t*>(base_ptr);
   T* vals = reinterpret_cast<T*>(base_ptr + tbytes);
-  T* adj = reinterpret_cast<T*>(base_ptr + tbytes + vbytes);
-  T* gsum = reinterpret_cast<T*>(base_ptr + tbytes + 2 * vbytes);
+  T* const adj0 = reinterpret_cast<T*>(base_ptr + tbytes + vbytes);
+  T* const adj1 = reinterpret_cast<T*>(base_ptr + tbytes + 2 * vbytes);
+  T* gsum = reinterpret_cast<T*>(base_ptr + tbytes + 3 * vbytes);
   for (int64_t ti = (int64_t)blockIdx.x * nwarp + warp; ti < B; ti += (int64_t)gridDim.x * nwarp) {
     const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
@@ -263,25 +342,27 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
       tape[k] = desc[b * M + k];
       gsum[k] = T(0);
     }
-    __syncwarp();
     const T* Crow = C + b * c_sb;
     const T* G = gout + (size_t)b * M * N;
     int err = 0;
-    for (int64_t base = 0; base < N; base += 32) {
+    const int64_t nchunks = (N + 31) / 32;
+    stage_rows<T>(adj0, G, L, N, 0, lane, vec16);
+    __syncwarp();
+    for (int64_t c = 0; c < nchunks; ++c) {
+      const int64_t base = c * 32;
       const int64_t n = base + lane;
       const bool valid = n < N;
       const int64_t nn = valid ? n : N - 1;
-      // adjoint seeds 0 + grad_out (the reference's zeros_like(cache).add_(grad_output)),
-      // loaded four rows at a time so the loads are in flight together
-      int k = 0;
-      for (; k + 4 <= L; k += 4) {
-        T g4[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) g4[j] = valid ? __ldcs(G + (size_t)(k + j) * N + nn) : T(0);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) adj[(k + j) * 32 + lane] = M_<T>::add(T(0), g4[j]);
+      T* adj = (c & 1) ? adj1 : adj0;
+      if (c + 1 < nchunks) {
+        stage_rows<T>((c & 1) ? adj0 : adj1, G, L, N, base + 32, lane, vec16);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
       }
-      for (; k < L; ++k) adj[k * 32 + lane] = valid ? M_<T>::add(T(0), __ldcs(G + (size_t)k * N + nn)) : T(0);
+      __syncwarp();
+      // adjoint seeds 0 + grad_out (the reference's zeros_like(cache).add_(grad_output))
+      for (int k = 0; k < L; ++k) adj[k * 32 + lane] = M_<T>::add(T(0), adj[k * 32 + lane]);
       forward_points<T>(tape, L, vals, X, n_x, nn, valid, Crow, c_sm, lane, nullptr, N);
       for (int kk = L - 1; kk >= 0; --kk) {
         const uint32_t d = tape[kk];
@@ -307,10 +388,8 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
           if (a1) adj[c1 * 32 + lane] = M_<T>::add(adj[c1 * 32 + lane], o1);
         }
       }
+      __syncwarp();  // every lane is done with this buffer before it is refilled
     }
-    __syncwarp();
-    // rows after the last real node are NO_OP nodes: any nonzero gradient there is error 201
-    if (warp_any_nonzero(G + (size_t)L * N, (size_t)(M - L) * N, lane)) err = ERR_GRAD_ON_NO_OP;
     err = __reduce_max_sync(0xffffffffu, err);
     if (err && lane == 0) report(status, err);
     // gradient row: constant nodes get their sums, everything else 0
@@ -441,15 +520,23 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
   if (!desc || !meta || !C || !gC || (N > 0 && !gout)) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
   if (N == 0) return cuda_check(cudaMemsetAsync(gC, 0, sizeof(T) * B * M, st), "grad_C reset");
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  const size_t per_warp = align16((size_t)Lmax * 4) + 2 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
+  // padding rows first (error 201 takes precedence)
+  int64_t pblocks = (int64_t)device_sm_count() * 8;
+  if (pblocks > B) pblocks = B;
+  padding_check_kernel<T><<<(unsigned)pblocks, 256, 0, st>>>(gout, meta, B, M, N, status);
+  rc = launch_check("padding_check_kernel");
+  if (rc) return rc;
+  const size_t per_warp = align16((size_t)Lmax * 4) + 3 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
   Shape sh;
   auto kern = eval_backward_kernel<T>;
   if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, B, sh)) {
     set_error("tape of %d nodes does not fit in shared memory", Lmax);
     return SR_ERR_UNSUPPORTED;
   }
+  // 16-byte staging needs every (tape, row, 32-point chunk) start 16-byte aligned
+  const bool vec16 = (reinterpret_cast<uintptr_t>(gout) % 16 == 0) && (N % (16 / (int64_t)sizeof(T)) == 0);
   kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, Lmax, C, c_sb, c_sm,
-                                                           gout, gC, gX, status);
+                                                           gout, gC, gX, status, vec16);
   return launch_check("eval_backward_kernel");
 }
 
