@@ -63,6 +63,7 @@ struct FitArgs {
   double tol, eps;
   int Lmax, Kmax;
   int Imax;         // rows of the per-warp node tables: largest count of operator nodes
+  int VR;           // rows of the per-warp table for variables (distinct variables of a tape)
   float* ws_vec;    // per warp: 2 * hist * SPL*32 floats (s and y rings)
   double* ws_scal;  // per warp: 2 * hist doubles (alpha, rho)
   int* counter;
@@ -83,37 +84,57 @@ struct F2 {
 
 struct WarpSmem {
   uint32_t* tape;    // [Lmax]                      (CTA)
-  uint32_t* pop;     // [Lmax] operator nodes: opcode | arity << 8              (CTA)
-  uint32_t* popnd;   // [Lmax] operator nodes: operand 0 | operand 1 << 16       (CTA)
-  float* cval;       // [Kmax] value of each constant slot at the trial point    (CTA)
-  int* info;         // [4] operator-node count, root operand                    (CTA)
-  int* node_slot;    // [Lmax] slot of a LEARNABLE node / row of an operator node (CTA)
+  uint32_t* pcode;   // [Lmax] opcode of each operator node of the program       (CTA)
+  uint32_t* psa;     // [Lmax] operand 0 source word (see the program notes)     (CTA)
+  uint32_t* psb;     // [Lmax] operand 1 source word                             (CTA)
+  uint32_t* pda;     // [Lmax] operand 0 adjoint destination (byte offset)        (CTA)
+  uint32_t* pdb;     // [Lmax] operand 1 adjoint destination                      (CTA)
+  int* rowvar;       // [VR] variable held in each variable row                  (CTA)
+  int* info;         // [8] operator nodes, root row, variable rows, root source, root destination (CTA)
+  int* node_slot;    // [Lmax] slot of a LEARNABLE node / row of an operator node / row of a variable (CTA)
   int* slot_node;    // [Kmax]                      (CTA)
   F2* red_g;         // [W][Kmax] per-warp gradient sums (CTA)
   F2* red_l;         // [W] per-warp loss sums      (CTA)
   float* pvec;       // [128] search direction computed by warp 0 (CTA)
   int* red_e;        // [W] per-warp error codes    (CTA)
   long long* task;   // the CTA's current problem   (CTA)
-  float* vals;       // [Imax][32V] values of the operator nodes (warp)
-  float* adj;        // [Imax][32V] their adjoints              (warp)
-  float* gl;         // [Kmax][32] per-lane gradient partial sums (warp)
+  unsigned char* wb; // this warp's table base (warp):
+  float* bc;         //   [1 + Kmax + Lmax] broadcast values: 0, constants, fixed constants
+  float* vals;       //   [Imax + VR][32V] operator-node values, then variable values
+  float* adj;        //   [Imax + 1][32V] operator-node adjoints, then a sink row
+  float* gl;         //   [Kmax][32V] per-lane, per-point gradient partial sums
 };
 
-__host__ __device__ __forceinline__ size_t fit_shared_bytes(int Lmax, int Kmax, int W) {
+// Per-warp table layout (byte offsets from the warp's base), V points per lane,
+// rows of RW = 32 V floats.
+struct WarpLayout {
+  uint32_t vals, adj, sink, gl, bytes;
+};
+
+__host__ __device__ __forceinline__ WarpLayout warp_layout(int Lmax, int Imax, int Kmax, int V, int VR) {
+  const uint32_t K = (uint32_t)(Kmax > 0 ? Kmax : 1), I = (uint32_t)(Imax > 0 ? Imax : 1);
+  const uint32_t RW = 32u * (uint32_t)V * 4u;  // bytes per row
+  WarpLayout w;
+  w.vals = (uint32_t)((4u * (1u + K + (uint32_t)Lmax) + 127u) & ~127u);
+  w.adj = w.vals + (I + (uint32_t)VR) * RW;
+  w.sink = w.adj + I * RW;
+  w.gl = w.sink + RW;
+  w.bytes = w.gl + K * RW;
+  return w;
+}
+
+__host__ __device__ __forceinline__ size_t fit_shared_bytes(int Lmax, int Kmax, int W, int VR) {
   const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
-  return fit_align16((size_t)Lmax * 4) * 5 + fit_align16(K * 4) * 2 + fit_align16((size_t)W * K * 8) +
-         fit_align16((size_t)W * 8) + fit_align16((size_t)W * 4) + 16 + 16 + 512;
+  return fit_align16((size_t)Lmax * 4) * 8 + fit_align16(K * 4) + fit_align16((size_t)W * K * 8) +
+         fit_align16((size_t)W * 8) + fit_align16((size_t)W * 4) + fit_align16((size_t)VR * 4) + 32 + 16 + 512 +
+         128;  // + alignment of the warp tables
 }
 
-__host__ __device__ __forceinline__ size_t fit_warp_bytes(int Imax, int Kmax, int V) {
-  return 2 * (size_t)(Imax > 0 ? Imax : 1) * 32 * V * 4 + (size_t)(Kmax > 0 ? Kmax : 1) * 32 * 4;
+__host__ __device__ __forceinline__ size_t fit_cta_bytes(int Lmax, int Imax, int Kmax, int V, int W, int VR) {
+  return fit_shared_bytes(Lmax, Kmax, W, VR) + (size_t)W * warp_layout(Lmax, Imax, Kmax, V, VR).bytes;
 }
 
-__host__ __device__ __forceinline__ size_t fit_cta_bytes(int Lmax, int Imax, int Kmax, int V, int W) {
-  return fit_shared_bytes(Lmax, Kmax, W) + (size_t)W * fit_warp_bytes(Imax, Kmax, V);
-}
-
-__device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Imax, int Kmax, int V, int W,
+__device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Imax, int Kmax, int V, int W, int VR,
                                           int warp) {
   WarpSmem s;
   const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
@@ -126,7 +147,6 @@ __device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Ima
   p += 512;
   s.tape = reinterpret_cast<uint32_t*>(p);
   p += fit_align16((size_t)Lmax * 4);
-  p += fit_align16((size_t)Lmax * 4);  // (unused row kept for alignment of the layout below)
   s.node_slot = reinterpret_cast<int*>(p);
   p += fit_align16((size_t)Lmax * 4);
   s.slot_node = reinterpret_cast<int*>(p);
@@ -135,21 +155,28 @@ __device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Ima
   p += fit_align16((size_t)W * 4);
   s.task = reinterpret_cast<long long*>(p);
   p += 16;
-  s.pop = reinterpret_cast<uint32_t*>(p);
+  s.pcode = reinterpret_cast<uint32_t*>(p);
   p += fit_align16((size_t)Lmax * 4);
-  s.popnd = reinterpret_cast<uint32_t*>(p);
+  s.psa = reinterpret_cast<uint32_t*>(p);
   p += fit_align16((size_t)Lmax * 4);
-  s.cval = reinterpret_cast<float*>(p);
-  p += fit_align16(K * 4);
+  s.psb = reinterpret_cast<uint32_t*>(p);
+  p += fit_align16((size_t)Lmax * 4);
+  s.pda = reinterpret_cast<uint32_t*>(p);
+  p += fit_align16((size_t)Lmax * 4);
+  s.pdb = reinterpret_cast<uint32_t*>(p);
+  p += fit_align16((size_t)Lmax * 4);
+  s.rowvar = reinterpret_cast<int*>(p);
+  p += fit_align16((size_t)VR * 4);
   s.info = reinterpret_cast<int*>(p);
-  p += 16;
-  const int I = Imax > 0 ? Imax : 1;
-  unsigned char* w = base + fit_shared_bytes(Lmax, Kmax, W) + (size_t)warp * fit_warp_bytes(Imax, Kmax, V);
-  s.gl = reinterpret_cast<float*>(w);
-  w += K * 32 * 4;
-  s.vals = reinterpret_cast<float*>(w);
-  w += (size_t)I * 32 * V * 4;
-  s.adj = reinterpret_cast<float*>(w);
+  p += 32;
+  const WarpLayout L = warp_layout(Lmax, Imax, Kmax, V, VR);
+  unsigned char* t = base + fit_shared_bytes(Lmax, Kmax, W, VR) - 128;
+  t = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(t) + 127) & ~uintptr_t(127));
+  s.wb = t + (size_t)warp * L.bytes;
+  s.bc = reinterpret_cast<float*>(s.wb);
+  s.vals = reinterpret_cast<float*>(s.wb + L.vals);
+  s.adj = reinterpret_cast<float*>(s.wb + L.adj);
+  s.gl = reinterpret_cast<float*>(s.wb + L.gl);
   return s;
 }
 
@@ -263,51 +290,60 @@ __device__ __forceinline__ float var_value(const float (&xr)[V][kMaxRegVars], in
 // ---------------------------------------------------------------------------------
 // Operator-node program.  Before the first closure of a problem its tape (nodes up
 // to the root) is rewritten as a list of operator nodes (arity >= 1, plus NO_OP
-// nodes, whose value NaN and adjoint check matter); every leaf becomes an operand
-// descriptor inside its parent.  16-bit operand descriptor:
-//   bit 15 = 0: operator node, bits 0..14 = its row
-//   bit 15 = 1: leaf, bits 12..14 = kind (0 zero, 1 variable, 2 constant slot,
-//               3 fixed constant), bits 0..11 = variable index / slot / opcode
-// The interpreter thus loops over operator nodes only, keeps node values and
-// adjoints for them only, reads variables from registers and constants from the
-// slot table, and sends the adjoint of a learnable leaf straight to its slot.
+// nodes, whose value NaN and adjoint check matter).  Leaves are not executed: every
+// operand is a precomputed address in the warp's table,
+//   source word  = byte offset (bits 0..23) | lane stride in bytes (bits 24..31):
+//                  an operator node's row or a variable's row (stride 4: one value
+//                  per lane and point) or a broadcast entry (stride 0: 0, a
+//                  constant slot, a fixed constant),
+//   destination  = byte offset of the row that receives the operand's adjoint: the
+//                  operator node's adjoint row, the constant slot's partial-sum
+//                  row, or a sink row for variables and fixed constants.
+// So the interpreter fetches and stores operands without branching on their kind;
+// only the opcode dispatch remains (warp-uniform).
 // ---------------------------------------------------------------------------------
-constexpr uint32_t kLeaf = 0x8000u;
-enum LeafKind : uint32_t { LK_ZERO = 0, LK_VAR = 1, LK_CONST = 2, LK_FIXED = 3 };
-
 __device__ __forceinline__ bool is_operator_node(int code) { return code == NO_OP || arity_of(code) >= 1; }
 
-__device__ __forceinline__ uint32_t leaf_operand(uint32_t d, int slot) {
-  const int code = code_of(d);
-  if (code == VAR) return kLeaf | (LK_VAR << 12) | (uint32_t)child0(d);
-  if (code == LEARNABLE) return kLeaf | (LK_CONST << 12) | (uint32_t)slot;
-  if (code >= C1 && code <= E_) return kLeaf | (LK_FIXED << 12) | (uint32_t)code;
-  return kLeaf | (LK_ZERO << 12);
+__device__ __forceinline__ bool is_fixed_leaf(int code) { return code >= C1 && code <= E_; }
+
+// Source word and destination of operand node c (operator row / slot / variable row
+// numbers in node_slot).
+__device__ __forceinline__ void operand_words(const uint32_t* tape, const int* node_slot, int c, int Kmax, int Imax,
+                                              const WarpLayout& L, uint32_t RW, uint32_t& src, uint32_t& dst) {
+  const int code = code_of(tape[c]);
+  if (is_operator_node(code)) {
+    src = (L.vals + (uint32_t)node_slot[c] * RW) | (4u << 24);
+    dst = L.adj + (uint32_t)node_slot[c] * RW;
+  } else if (code == VAR) {
+    src = (L.vals + (uint32_t)(Imax + node_slot[c]) * RW) | (4u << 24);
+    dst = L.sink;
+  } else if (code == LEARNABLE) {
+    src = 4u * (1u + (uint32_t)node_slot[c]);
+    dst = L.gl + (uint32_t)node_slot[c] * RW;
+  } else if (is_fixed_leaf(code)) {
+    src = 4u * (1u + (uint32_t)Kmax + (uint32_t)c);
+    dst = L.sink;
+  } else {
+    src = 0u;  // the zero entry
+    dst = L.sink;
+  }
 }
 
-// Value of a leaf operand at the lane's point v.
 template <int V>
-__device__ __forceinline__ float leaf_value(uint32_t od, const float (&xr)[V][kMaxRegVars], int v, bool xin,
-                                            const float* __restrict__ X, int64_t nn, int64_t n_x,
-                                            const float* __restrict__ cval) {
-  const uint32_t kind = (od >> 12) & 7u, pay = od & 0xfffu;
-  if (kind == LK_VAR) return var_value<V>(xr, v, (int)pay, xin, X, nn, n_x);
-  if (kind == LK_CONST) return cval[pay];
-  if (kind == LK_FIXED) return node_value<float>((int)pay, 0.f, 0.f, 0.f, 0.f);
-  return 0.f;
+__device__ __forceinline__ float lds_src(const unsigned char* wb, uint32_t w, int li) {
+  return *reinterpret_cast<const float*>(wb + (w & 0xffffffu) + (uint32_t)li * (w >> 24));
+}
+
+__device__ __forceinline__ float* row_ptr(unsigned char* wb, uint32_t off, int li) {
+  return reinterpret_cast<float*>(wb + off) + li;
 }
 
 // ---------------------------------------------------------------------------------
-// One pass over the problem's points at the constants published in S.cval.
-// kGrad: loss + gradient (forward, residual, reverse sweep); otherwise forward only,
-// writing the root values to Y_final.
-//
-// Forward: an operand that is the previous operator node (the most common case in
-// a postfix tape) comes from a register, other operator operands from the warp's
-// node table.  Reverse: the contribution to the previous operator node is carried
-// in registers into the next iteration instead of a shared-memory read-modify-write;
-// contributions are added in the reference's order (parents from the last to the
-// first, child 0 before child 1).
+// One pass over the problem's points at the constants in the warp's broadcast
+// entries.  kGrad: loss + gradient (forward, residual, reverse sweep); otherwise
+// forward only, writing the root values to Y_final.  Adjoint contributions are added
+// in the reference's order (parents from the last to the first, child 0 before
+// child 1).
 // ---------------------------------------------------------------------------------
 template <int V, bool kGrad>
 __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int lane, int warp, int W,
@@ -317,9 +353,12 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
   const float* __restrict__ Yrow = A.Y ? A.Y + b * N : nullptr;
   const bool xin = A.n_x <= kMaxRegVars;
   const int nI = S.info[0];              // operator nodes
-  const uint32_t root_od = (uint32_t)S.info[1];
-  const bool root_leaf = (root_od & kLeaf) != 0;
-  const float* __restrict__ cval = S.cval;
+  const int root_row = S.info[1];        // the root's operator row, or -1 for a leaf root
+  const int nvr = S.info[2];             // variable rows in use
+  const uint32_t root_src = (uint32_t)S.info[3], root_dst = (uint32_t)S.info[4];
+  const uint32_t sink = (uint32_t)S.info[5];  // adjoints of variables and fixed constants go nowhere
+  const uint32_t RW = 32u * V;           // floats per row
+  unsigned char* wb = S.wb;
   // per-lane partial sums in float (a lane sees N / (32 V W) points)
   float loss_part = 0.f;
   for (int64_t base = (int64_t)warp * 32 * V; base < N; base += (int64_t)W * 32 * V) {
@@ -334,52 +373,43 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
 #pragma unroll
       for (int j = 0; j < kMaxRegVars; ++j) xr[v][j] = (xin && j < A.n_x) ? __ldg(A.X + nn[v] * A.n_x + j) : 0.f;
     }
+    // variable rows of this chunk
+    for (int r = 0; r < nvr; ++r) {
+      const int var = S.rowvar[r];
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        S.vals[(A.Imax + r) * RW + v * 32 + lane] = var_value<V>(xr, v, var, xin, A.X, nn[v], A.n_x);
+    }
+    __syncwarp();
     // ---- forward over the operator nodes ----
-    float prev[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) prev[v] = 0.f;
-    uint32_t opn = nI > 0 ? S.pop[0] : 0u, odn = nI > 0 ? S.popnd[0] : 0u;
+    uint32_t cn = nI > 0 ? S.pcode[0] : 0u, san = nI > 0 ? S.psa[0] : 0u, sbn = nI > 0 ? S.psb[0] : 0u;
     for (int i = 0; i < nI; ++i) {
-      const uint32_t op = opn, od = odn;
+      const int code = (int)cn;
+      const uint32_t sa = san, sb = sbn;
       if (i + 1 < nI) {
-        opn = S.pop[i + 1];
-        odn = S.popnd[i + 1];
-      }
-      const int code = (int)(op & 0xffu), ar = (int)(op >> 8);
-      const uint32_t o0 = od & 0xffffu, o1 = od >> 16;
-      float r[V];
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        float a = 0.f, bb = 0.f;
-        if (ar >= 1) {
-          if (o0 & kLeaf) a = leaf_value<V>(o0, xr, v, xin, A.X, nn[v], A.n_x, cval);
-          else a = ((int)o0 == i - 1) ? prev[v] : S.vals[o0 * (32 * V) + v * 32 + lane];
-        }
-        if (ar == 2) {
-          if (o1 & kLeaf) bb = leaf_value<V>(o1, xr, v, xin, A.X, nn[v], A.n_x, cval);
-          else bb = ((int)o1 == i - 1) ? prev[v] : S.vals[o1 * (32 * V) + v * 32 + lane];
-        }
-        r[v] = node_value<float>(code, a, bb, 0.f, 0.f);
+        cn = S.pcode[i + 1];
+        san = S.psa[i + 1];
+        sbn = S.psb[i + 1];
       }
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        S.vals[i * (32 * V) + v * 32 + lane] = r[v];
-        if (kGrad) S.adj[i * (32 * V) + v * 32 + lane] = 0.f;
-        prev[v] = r[v];
+        const int li = v * 32 + lane;
+        const float r = node_value<float>(code, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li), 0.f, 0.f);
+        S.vals[i * RW + li] = r;
+        if (kGrad) S.adj[i * RW + li] = 0.f;
       }
     }
     float fval[V];
 #pragma unroll
-    for (int v = 0; v < V; ++v)
-      fval[v] = root_leaf ? leaf_value<V>(root_od, xr, v, xin, A.X, nn[v], A.n_x, cval) : prev[v];
+    for (int v = 0; v < V; ++v) fval[v] = lds_src<V>(wb, root_src, v * 32 + lane);
     if constexpr (!kGrad) {
 #pragma unroll
       for (int v = 0; v < V; ++v)
         if (valid[v]) A.Y_final[b * N + nn[v]] = fval[v];
+      __syncwarp();
       continue;
     } else {
     // ---- residuals: root adjoint (2 (f - y)) * (1/N), as autograd forms it ----
-    float g_root[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       float groot = 0.f;
@@ -393,96 +423,47 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
           groot = invN;
         }
       }
-      g_root[v] = groot;
-    }
-    if (root_leaf) {  // a leaf root: its adjoint goes straight to its slot
-      if (((root_od >> 12) & 7u) == LK_CONST) {
-        const int slot = (int)(root_od & 0xfffu);
-#pragma unroll
-        for (int v = 0; v < V; ++v)
-          if (valid[v] && g_root[v] != 0.f) S.gl[slot * 32 + lane] = __fadd_rn(S.gl[slot * 32 + lane], g_root[v]);
+      const int li = v * 32 + lane;
+      if (root_row >= 0) {
+        S.adj[root_row * RW + li] = groot;  // the seed of the root (the forward wrote 0)
+      } else if (groot != 0.f) {
+        float* d = row_ptr(wb, root_dst, li);  // a leaf root: its slot's row, or the sink
+        *d = __fadd_rn(*d, groot);
       }
     }
     // ---- reverse sweep over the operator nodes ----
-    // cin*: contributions to operator node i-1 produced while processing node i
-    float cin0[V], cin1[V];
-    bool hin0 = false, hin1 = false;
-#pragma unroll
-    for (int v = 0; v < V; ++v) { cin0[v] = 0.f; cin1[v] = 0.f; }
-    uint32_t opp = nI > 0 ? S.pop[nI - 1] : 0u, odp = nI > 0 ? S.popnd[nI - 1] : 0u;
+    uint32_t cp = 0u, sap = 0u, sbp = 0u, dap = 0u, dbp = 0u;
+    if (nI > 0) {
+      cp = S.pcode[nI - 1]; sap = S.psa[nI - 1]; sbp = S.psb[nI - 1]; dap = S.pda[nI - 1]; dbp = S.pdb[nI - 1];
+    }
     for (int i = nI - 1; i >= 0; --i) {
-      const uint32_t op = opp, od = odp;
+      const int code = (int)cp;
+      const uint32_t sa = sap, sb = sbp, da = dap, db = dbp;
       if (i > 0) {
-        opp = S.pop[i - 1];
-        odp = S.popnd[i - 1];
+        cp = S.pcode[i - 1]; sap = S.psa[i - 1]; sbp = S.psb[i - 1]; dap = S.pda[i - 1]; dbp = S.pdb[i - 1];
       }
-      const int code = (int)(op & 0xffu), ar = (int)(op >> 8);
-      float g[V];
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        float gv = (!root_leaf && i == nI - 1) ? g_root[v] : S.adj[i * (32 * V) + v * 32 + lane];
-        if (hin0) gv = __fadd_rn(gv, cin0[v]);
-        if (hin1) gv = __fadd_rn(gv, cin1[v]);
-        g[v] = gv;
-      }
-      hin0 = hin1 = false;
-      if (code == NO_OP) {
-#pragma unroll
-        for (int v = 0; v < V; ++v)
-          if (valid[v] && g[v] != 0.f && !err) err = ERR_GRAD_ON_NO_OP;
-        continue;
-      }
-      if (code == FLOOR || code == CEIL) continue;
-      const uint32_t o0 = od & 0xffffu, o1 = od >> 16;
-      const bool t0 = !(o0 & kLeaf) && (int)o0 == i - 1;
-      const bool t1 = ar == 2 && !(o1 & kLeaf) && (int)o1 == i - 1;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         const int li = v * 32 + lane;
-        const float a = (o0 & kLeaf) ? leaf_value<V>(o0, xr, v, xin, A.X, nn[v], A.n_x, cval)
-                                     : S.vals[o0 * (32 * V) + li];
-        float bb = 0.f;
-        if (ar == 2)
-          bb = (o1 & kLeaf) ? leaf_value<V>(o1, xr, v, xin, A.X, nn[v], A.n_x, cval) : S.vals[o1 * (32 * V) + li];
+        const float g = S.adj[i * RW + li];
         bool a0, a1;
         float r0, r1;
-        const int e = node_adjoint<float>(code, g[v], a, bb, S.vals[i * (32 * V) + li], a0, r0, a1, r1);
-        if (!valid[v]) { a0 = a1 = false; r0 = r1 = 0.f; }
-        if (e && valid[v] && !err) err = e;
-        if (a0) {
-          if (o0 & kLeaf) {
-            // a learnable leaf receives its (single) contribution straight into its slot
-            if (((o0 >> 12) & 7u) == LK_CONST && r0 != 0.f) {
-              const int slot = (int)(o0 & 0xfffu);
-              S.gl[slot * 32 + lane] = __fadd_rn(S.gl[slot * 32 + lane], r0);
-            }
-          } else if (t0) {
-            cin0[v] = r0;
-          } else {
-            S.adj[o0 * (32 * V) + li] = __fadd_rn(S.adj[o0 * (32 * V) + li], r0);
+        const int e = node_adjoint<float>(code, g, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li), S.vals[i * RW + li],
+                                          a0, r0, a1, r1);
+        if (valid[v]) {
+          if (e && !err) err = e;
+          if (a0 && da != sink) {
+            float* d = row_ptr(wb, da, li);
+            *d = __fadd_rn(*d, r0);
           }
-        } else if (t0) {
-          cin0[v] = 0.f;
-        }
-        if (a1) {
-          if (o1 & kLeaf) {
-            if (((o1 >> 12) & 7u) == LK_CONST && r1 != 0.f) {
-              const int slot = (int)(o1 & 0xfffu);
-              S.gl[slot * 32 + lane] = __fadd_rn(S.gl[slot * 32 + lane], r1);
-            }
-          } else if (t1) {
-            cin1[v] = r1;
-          } else {
-            S.adj[o1 * (32 * V) + li] = __fadd_rn(S.adj[o1 * (32 * V) + li], r1);
+          if (a1 && db != sink) {
+            float* d = row_ptr(wb, db, li);
+            *d = __fadd_rn(*d, r1);
           }
-        } else if (t1) {
-          cin1[v] = 0.f;
         }
       }
-      // a lane without a contribution carries +0, which leaves its sum unchanged
-      hin0 = t0;
-      hin1 = t1;
     }
+    __syncwarp();
     }  // kGrad
   }
   return loss_part;
@@ -497,16 +478,21 @@ template <int V, int SPL>
 __device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, const Problem<SPL>& P, int warp, int W,
                                          const Slots<SPL>& xt, Slots<SPL>& grad, int& err) {
   const int lane = P.lane;
-  if (warp == 0) {
+  // every warp holds the same trial point: each publishes it into its own broadcast entries
 #pragma unroll
-    for (int s = 0; s < SPL; ++s)
-      if (P.real(s)) S.cval[s * 32 + lane] = xt.v[s];
+  for (int s = 0; s < SPL; ++s)
+    if (P.real(s)) S.bc[1 + s * 32 + lane] = xt.v[s];
+  for (int j = 0; j < P.K; ++j) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) S.gl[j * 32 * V + v * 32 + lane] = 0.f;
   }
-  for (int j = 0; j < P.K; ++j) S.gl[j * 32 + lane] = 0.f;
-  __syncthreads();
+  __syncthreads();  // also: every warp has read the previous closure's reduction buffers
   const F2 lsum = warp_sum_f2(tape_pass<V, true>(A, S, P.b, lane, warp, W, err));
   for (int j = 0; j < P.K; ++j) {
-    const F2 t = warp_sum_f2(S.gl[j * 32 + lane]);
+    float part = S.gl[j * 32 * V + lane];
+#pragma unroll
+    for (int v = 1; v < V; ++v) part = __fadd_rn(part, S.gl[j * 32 * V + v * 32 + lane]);
+    const F2 t = warp_sum_f2(part);
     if (lane == 0) S.red_g[warp * P.K + j] = t;
   }
   if (lane == 0) S.red_l[warp] = lsum;
@@ -542,7 +528,7 @@ template <int V, int SPL>
 __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
-  const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, warp);
+  const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, A.VR, warp);
   // history rings and two-loop scalars of this CTA (used by warp 0)
   float* ringS = A.ws_vec + (int64_t)blockIdx.x * 2 * A.hist * SPL * 32;
   float* ringY = ringS + (int64_t)A.hist * SPL * 32;
@@ -566,8 +552,8 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
     P.nslots = P.K + (P.has_virtual ? 1 : 0);
     const int L = P.root + 1;
 
-    // stage the tape; number the constant slots and the operator nodes; write the
-    // operator-node program (warp 0), visible to the CTA
+    // stage the tape; number the constant slots, the operator nodes and the
+    // variables; write the operator-node program (warp 0), visible to the CTA
     if (warp == 0) {
       for (int k = lane; k < L; k += 32) S.tape[k] = A.desc[P.b * A.M + k];
       __syncwarp();
@@ -589,33 +575,56 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
         nslot += __popc(mc);
         nop += __popc(mo);
       }
+      if (lane == 0) {  // one row per distinct variable, in order of first use
+        int nvr = 0;
+        for (int k = 0; k < L; ++k) {
+          const uint32_t d = S.tape[k];
+          if (code_of(d) != VAR) continue;
+          const int var = child0(d);
+          int r = 0;
+          while (r < nvr && S.rowvar[r] != var) ++r;
+          if (r == nvr) S.rowvar[nvr++] = var;
+          S.node_slot[k] = r;
+        }
+        S.info[2] = nvr;
+      }
       __syncwarp();
+      const WarpLayout WL = warp_layout(A.Lmax, A.Imax, A.Kmax, V, A.VR);
+      const uint32_t RWB = 32u * V * 4u;
       for (int k = lane; k < L; k += 32) {
         const uint32_t d = S.tape[k];
         const int code = code_of(d);
         if (!is_operator_node(code)) continue;
         const int ar = arity_of(code);
-        uint32_t od0 = 0, od1 = 0;
-        if (ar >= 1) {
-          const uint32_t c = S.tape[child0(d)];
-          od0 = is_operator_node(code_of(c)) ? (uint32_t)S.node_slot[child0(d)] : leaf_operand(c, S.node_slot[child0(d)]);
-        }
-        if (ar == 2) {
-          const uint32_t c = S.tape[child1(d)];
-          od1 = is_operator_node(code_of(c)) ? (uint32_t)S.node_slot[child1(d)] : leaf_operand(c, S.node_slot[child1(d)]);
-        }
+        uint32_t sa = 0u, sb = 0u, da = WL.sink, db = WL.sink;
+        if (ar >= 1) operand_words(S.tape, S.node_slot, child0(d), A.Kmax, A.Imax, WL, RWB, sa, da);
+        if (ar == 2) operand_words(S.tape, S.node_slot, child1(d), A.Kmax, A.Imax, WL, RWB, sb, db);
         const int row = S.node_slot[k];
-        S.pop[row] = (uint32_t)code | ((uint32_t)ar << 8);
-        S.popnd[row] = od0 | (od1 << 16);
+        S.pcode[row] = (uint32_t)code;
+        S.psa[row] = sa;
+        S.psb[row] = sb;
+        S.pda[row] = da;
+        S.pdb[row] = db;
       }
       if (lane == 0) {
         const int R = P.root;
-        const uint32_t rd = S.tape[R];
+        uint32_t rs, rdst;
+        operand_words(S.tape, S.node_slot, R, A.Kmax, A.Imax, WL, RWB, rs, rdst);
         S.info[0] = nop;
-        S.info[1] = (int)(is_operator_node(code_of(rd)) ? (uint32_t)S.node_slot[R] : leaf_operand(rd, S.node_slot[R]));
+        S.info[1] = is_operator_node(code_of(S.tape[R])) ? S.node_slot[R] : -1;
+        S.info[3] = (int)rs;
+        S.info[4] = (int)rdst;
+        S.info[5] = (int)WL.sink;
       }
     }
     __syncthreads();
+    // this warp's broadcast entries: 0 and the fixed constants of the tape
+    if (lane == 0) S.bc[0] = 0.f;
+    for (int k = lane; k < L; k += 32) {
+      const int code = code_of(S.tape[k]);
+      if (is_fixed_leaf(code)) S.bc[1 + A.Kmax + k] = node_value<float>(code, 0.f, 0.f, 0.f, 0.f);
+    }
+    __syncwarp();
 
     const float* Cin = A.C_init + P.b * A.c_sb;
     Slots<SPL> x, g, p, xn;
@@ -942,10 +951,11 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
         if (A.loss_out) A.loss_out[P.b] = f;
         if (A.evals_out) A.evals_out[P.b] = evals;
       }
-#pragma unroll
-      for (int s = 0; s < SPL; ++s)
-        if (P.real(s)) S.cval[s * 32 + lane] = x.v[s];
     }
+    // the final constants into every warp's broadcast entries for the Y_final pass
+#pragma unroll
+    for (int s = 0; s < SPL; ++s)
+      if (P.real(s)) S.bc[1 + s * 32 + lane] = x.v[s];
     __syncthreads();
     if (A.Y_final) {
       int dummy = 0;
@@ -988,7 +998,7 @@ static int spl_for(int Kmax) {
 }
 
 struct FitShape {
-  int V, SPL, warps, blocks, Imax;
+  int V, SPL, warps, blocks, Imax, VR;
   size_t smem;
 };
 
@@ -1017,10 +1027,12 @@ static void* pick_kernel(int V, int SPL) {
 // sooner and the tail of the persistent grid shrinks.  Unless the caller fixes
 // them, W keeps about 64 points per warp (1..8 warps) and V is the one of 1 and 2
 // that keeps more work resident per SM (resident warps, with a warp of two points
-// per lane counted as 1.6 warps: its independent chains hide latency).
-static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
+// per lane counted as 1.6 warps: its independent chains hide latency).  The warp
+// tables hold a row per distinct variable of a tape: VR = min(n_x, Lmax) rows.
+static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
   const int Imax = (o.max_operators > 0 && o.max_operators < Lmax) ? o.max_operators : Lmax;
   sh.Imax = Imax;
+  sh.VR = (int)(n_x < 1 ? 1 : (n_x < Lmax ? n_x : Lmax));
   sh.SPL = spl_for(Kmax);
   if (!sh.SPL) {
     set_error("at most 127 learnable constants per tape are supported (got %d)", Kmax);
@@ -1048,7 +1060,7 @@ static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_opti
         set_error("fit kernel shared memory attribute failed");
         return SR_ERR_CUDA;
       }
-      const size_t cb = fit_cta_bytes(Lmax, Imax, Kmax, V, w);
+      const size_t cb = fit_cta_bytes(Lmax, Imax, Kmax, V, w, sh.VR);
       if (cb > (size_t)optin) continue;
       int per_sm = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, w * 32, cb) != cudaSuccess || per_sm < 1)
@@ -1069,7 +1081,7 @@ static int fit_shape(int64_t B, int64_t N, int Lmax, int Kmax, const sr_fit_opti
   }
   sh.V = bestV;
   sh.warps = W;
-  sh.smem = fit_cta_bytes(Lmax, Imax, Kmax, bestV, W);
+  sh.smem = fit_cta_bytes(Lmax, Imax, Kmax, bestV, W, sh.VR);
   int64_t blocks = o.grid_blocks > 0 ? o.grid_blocks : (int64_t)sms * bestPerSm;
   if (blocks > B) blocks = B;  // one problem per CTA at a time
   if (blocks < 1) blocks = 1;
@@ -1092,9 +1104,11 @@ int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len,
   sr_fit_options o;
   if (sr::fit_defaults(opt, o)) return -1;
   sr::FitShape sh;
-  // the same node-table size sr_fit_lbfgs uses
+  // the same node-table size sr_fit_lbfgs uses; one variable row gives the smallest
+  // tables, hence the most resident CTAs: an upper bound for any n_x (sr_fit_lbfgs
+  // shrinks its grid to the workspace it is given)
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)(M < 1 ? 1 : M);
-  if (sr::fit_shape(B, N, Lmax, max_consts, o, sh)) return -1;
+  if (sr::fit_shape(B, N, 1, Lmax, max_consts, o, sh)) return -1;
   return sr::ws_bytes_for(sh, o.history_size);
 }
 
@@ -1120,8 +1134,11 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   }
   FitShape sh;
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  rc = fit_shape(B, N, Lmax, max_consts, o, sh);
+  rc = fit_shape(B, N, n_x, Lmax, max_consts, o, sh);
   if (rc) return rc;
+  // fewer persistent CTAs only lengthen each one's share of the queue
+  while (sh.blocks > 1 && ws_bytes_for(sh, o.history_size) > workspace_bytes)
+    sh.blocks = sh.blocks > 8 ? sh.blocks * 3 / 4 : sh.blocks - 1;
   const int64_t need = ws_bytes_for(sh, o.history_size);
   if (workspace_bytes < need) {
     set_error("workspace too small: %lld < %lld bytes", (long long)workspace_bytes, (long long)need);
@@ -1136,7 +1153,7 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   A.order = order;
   A.max_iter = o.max_iter; A.hist = o.history_size; A.ls_kind = o.line_search; A.ls_max = o.line_search_max_iter;
   A.objective = o.objective; A.tol = o.tolerance_grad; A.eps = o.eps;
-  A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax;
+  A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.VR = sh.VR;
   A.counter = reinterpret_cast<int*>(ws);
   const int64_t vec = (int64_t)sh.blocks * 2LL * o.history_size * sh.SPL * 32 * (int64_t)sizeof(float);
   A.ws_vec = reinterpret_cast<float*>(ws + 256);
@@ -1212,7 +1229,7 @@ extern "C" int sr_fit_lbfgs_static_scratch(const float* X, int64_t N, int64_t n_
   // grid until its history rings fit in the static array.
   FitShape sh;
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  rc = fit_shape(B, N, Lmax, max_consts, o, sh);
+  rc = fit_shape(B, N, n_x, Lmax, max_consts, o, sh);
   if (rc) return rc;
   int64_t blocks = sh.blocks;
   while (blocks >= 1) {
