@@ -230,6 +230,13 @@ __device__ __forceinline__ double dot(const Problem<SPL>& P, const Slots<SPL>& a
 #pragma unroll
   for (int s = 0; s < SPL; ++s)
     if (P.active(s)) acc += (double)a.v[s] * (double)b.v[s];
+  if (SPL == 1 && P.nslots <= 16) {
+    // only lanes below 2^k hold terms: the butterfly steps above 2^(k-1) would add
+    // exact zeros, so lane 0 ends with the same sum after the lower steps alone
+    const int width = P.nslots <= 4 ? 4 : (P.nslots <= 8 ? 8 : 16);
+    for (int o = width >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return __shfl_sync(0xffffffffu, acc, 0);
+  }
   return wsum_d(acc);
 }
 
@@ -640,6 +647,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
     float f = 0.f;
     bool poison = false;
     int h = 0, head = 0, it = 0;
+    double last_sy = 0.0, last_yy = 0.0;  // warp 0: s.y and y.y of the newest history pair
     // line-search state
     int phase = PH_INIT;
     int lsi = 0, zj = 0;
@@ -818,11 +826,17 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
           head = (head + 1) % A.hist;
         }
         if (warp == 0) {  // only warp 0 computes directions
+          Slots<SPL> yv;
 #pragma unroll
           for (int s = 0; s < SPL; ++s) {
+            yv.v[s] = P.active(s) ? __fsub_rn(nxt.g.v[s], g.v[s]) : 0.f;
             ringS[slot * SPL * 32 + s * 32 + lane] = sv.v[s];
-            ringY[slot * SPL * 32 + s * 32 + lane] = P.active(s) ? __fsub_rn(nxt.g.v[s], g.v[s]) : 0.f;
+            ringY[slot * SPL * 32 + s * 32 + lane] = yv.v[s];
           }
+          // curvature of the new pair, computed once: rho of its slot, and s.y, y.y for gamma
+          last_sy = dot(P, yv, sv);
+          last_yy = dot(P, yv, yv);
+          if (lane == 0) rhos[slot] = 1.0 / __dadd_rn(last_sy, A.eps);
         }
         __syncwarp();
         x = xn;
@@ -859,25 +873,14 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
                 si.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
                 yi.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
               }
-              const double rho = 1.0 / __dadd_rn(dot(P, yi, si), A.eps);
-              const double a = __dmul_rn(rho, dot(P, si, q));
+              const double a = __dmul_rn(rhos[sl], dot(P, si, q));
 #pragma unroll
               for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dsub_rn((double)q.v[s], __dmul_rn(a, (double)yi.v[s]));
-              if (lane == 0) {
-                alph[i] = a;
-                rhos[i] = rho;
-              }
+              if (lane == 0) alph[i] = a;
             }
             __syncwarp();
             {
-              const int sl = (head + h - 1) % A.hist;
-              Slots<SPL> sl_, yl_;
-#pragma unroll
-              for (int s = 0; s < SPL; ++s) {
-                sl_.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
-                yl_.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
-              }
-              const double gam = dot(P, sl_, yl_) / __dadd_rn(dot(P, yl_, yl_), A.eps);
+              const double gam = last_sy / __dadd_rn(last_yy, A.eps);
 #pragma unroll
               for (int s = 0; s < SPL; ++s) q.v[s] = (float)(gam * (double)q.v[s]);
             }
@@ -889,7 +892,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
                 si.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
                 yi.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
               }
-              const double be = __dmul_rn(rhos[i], dot(P, yi, q));
+              const double be = __dmul_rn(rhos[sl], dot(P, yi, q));
               const double coef = __dsub_rn(alph[i], be);
 #pragma unroll
               for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dadd_rn((double)q.v[s], __dmul_rn((double)si.v[s], coef));
