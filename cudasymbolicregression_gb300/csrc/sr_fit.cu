@@ -476,8 +476,60 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
   return loss_part;
 }
 
+// Sums over the 32 lanes of KP per-lane values at once (the per-slot gradient
+// partials and the loss partial) by recursive halving: at each step a lane keeps
+// half of its values and receives its partner's partial sums of that half, so KP
+// values need KP - 1 + 5 - log2(KP) pair exchanges instead of 5 KP.  Every slot's
+// total ends in the lanes whose high bits spell it; f2_add does not depend on the
+// operand order, so the result is deterministic.
+template <int KP>
+__device__ __forceinline__ void reduce_slots(const float* __restrict__ gl, int V, int K, float loss_part, int lane,
+                                             F2* __restrict__ out_g, F2* __restrict__ out_l) {
+  F2 x[KP];
+#pragma unroll
+  for (int j = 0; j < KP; ++j) {
+    float part = 0.f;
+    if (j < K) {
+      part = gl[j * 32 * V + lane];
+      for (int v = 1; v < V; ++v) part = __fadd_rn(part, gl[j * 32 * V + v * 32 + lane]);
+    } else if (j == K) {
+      part = loss_part;
+    }
+    x[j] = F2{part, 0.f};
+  }
+  int slot = 0;
+  int n = KP;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    if (n > 1) {
+      const bool up = (lane & o) != 0;
+      const int h = n >> 1;
+#pragma unroll
+      for (int t = 0; t < KP / 2; ++t) {
+        if (t < h) {
+          const F2 send = up ? x[t] : x[t + h];
+          const F2 keep = up ? x[t + h] : x[t];
+          const F2 recv{__shfl_xor_sync(0xffffffffu, send.hi, o), __shfl_xor_sync(0xffffffffu, send.lo, o)};
+          x[t] = f2_add(keep, recv);
+        }
+      }
+      slot = slot * 2 + (up ? 1 : 0);
+      n = h;
+    } else {
+      const F2 recv{__shfl_xor_sync(0xffffffffu, x[0].hi, o), __shfl_xor_sync(0xffffffffu, x[0].lo, o)};
+      x[0] = f2_add(x[0], recv);
+    }
+  }
+  // lanes with the same high bits hold the same total: the lowest of them writes it
+  constexpr int kGroup = 32 / KP;
+  if ((lane & (kGroup - 1)) == 0) {
+    if (slot < K) out_g[slot] = x[0];
+    else if (slot == K) *out_l = x[0];
+  }
+}
+
 // Closure: publish the trial constants, run the pass over this warp's points,
-// reduce loss and gradient over the lanes (butterfly) and then over the CTA's
+// reduce loss and gradient over the lanes (recursive halving) and then over the CTA's
 // warps in a fixed order, in float pairs on the FP32 pipe (GB300's FP64 rate is a
 // small fraction of its FP32 rate); every warp ends with the same bits.  Two CTA
 // barriers.
@@ -494,15 +546,26 @@ __device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, co
     for (int v = 0; v < V; ++v) S.gl[j * 32 * V + v * 32 + lane] = 0.f;
   }
   __syncthreads();  // also: every warp has read the previous closure's reduction buffers
-  const F2 lsum = warp_sum_f2(tape_pass<V, true>(A, S, P.b, lane, warp, W, err));
-  for (int j = 0; j < P.K; ++j) {
-    float part = S.gl[j * 32 * V + lane];
+  const float lpart = tape_pass<V, true>(A, S, P.b, lane, warp, W, err);
+  F2* out_g = S.red_g + warp * P.K;
+  if (P.K < 32) {
+    if (P.K < 1) reduce_slots<1>(S.gl, V, P.K, lpart, lane, out_g, S.red_l + warp);
+    else if (P.K < 2) reduce_slots<2>(S.gl, V, P.K, lpart, lane, out_g, S.red_l + warp);
+    else if (P.K < 4) reduce_slots<4>(S.gl, V, P.K, lpart, lane, out_g, S.red_l + warp);
+    else if (P.K < 8) reduce_slots<8>(S.gl, V, P.K, lpart, lane, out_g, S.red_l + warp);
+    else if (P.K < 16) reduce_slots<16>(S.gl, V, P.K, lpart, lane, out_g, S.red_l + warp);
+    else reduce_slots<32>(S.gl, V, P.K, lpart, lane, out_g, S.red_l + warp);
+  } else {
+    const F2 lsum = warp_sum_f2(lpart);
+    for (int j = 0; j < P.K; ++j) {
+      float part = S.gl[j * 32 * V + lane];
 #pragma unroll
-    for (int v = 1; v < V; ++v) part = __fadd_rn(part, S.gl[j * 32 * V + v * 32 + lane]);
-    const F2 t = warp_sum_f2(part);
-    if (lane == 0) S.red_g[warp * P.K + j] = t;
+      for (int v = 1; v < V; ++v) part = __fadd_rn(part, S.gl[j * 32 * V + v * 32 + lane]);
+      const F2 t = warp_sum_f2(part);
+      if (lane == 0) out_g[j] = t;
+    }
+    if (lane == 0) S.red_l[warp] = lsum;
   }
-  if (lane == 0) S.red_l[warp] = lsum;
   __syncthreads();
 #pragma unroll
   for (int s = 0; s < SPL; ++s) {
