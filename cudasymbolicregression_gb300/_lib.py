@@ -73,6 +73,14 @@ _SIGS = {
                              ctypes.c_int),
     "sr_eval_backward_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp],
                              ctypes.c_int),
+    "sr_eval_forward_multi_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp],
+                                  ctypes.c_int),
+    "sr_eval_forward_multi_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp],
+                                  ctypes.c_int),
+    "sr_eval_backward_multi_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp, vp, vp,
+                                    vp], ctypes.c_int),
+    "sr_eval_backward_multi_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp, vp, vp,
+                                    vp], ctypes.c_int),
     "sr_fit_workspace_bytes": ([i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions)], i64),
     "sr_fit_lbfgs": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, vp, vp, i32, i32,
                       ctypes.POINTER(FitOptions), vp, i64, vp, vp], ctypes.c_int),

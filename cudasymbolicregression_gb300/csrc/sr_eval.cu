@@ -147,12 +147,13 @@ __device__ __forceinline__ void warp_fill_nan(T* p, size_t count, int lane) {
 }
 
 // Node values of one tape at the 32 points nn (one per lane) into vals[k][lane];
-// with `out` also streamed to the cache rows as they are produced.
+// with `out` also streamed to the cache as they are produced (node k, point n at
+// out[k * out_rs + n * out_es]).
 template <typename T>
 __device__ __forceinline__ void forward_points(const uint32_t* __restrict__ tape, int L, T* __restrict__ vals,
                                                const T* __restrict__ X, int64_t n_x, int64_t nn, bool valid,
                                                const T* __restrict__ Crow, int64_t c_sm, int lane,
-                                               T* __restrict__ out, int64_t N) {
+                                               T* __restrict__ out, int64_t out_rs, int64_t out_es = 1) {
   for (int k = 0; k < L; ++k) {
     const uint32_t d = tape[k];
     const int code = code_of(d);
@@ -165,18 +166,20 @@ __device__ __forceinline__ void forward_points(const uint32_t* __restrict__ tape
       r = node_value<T>(code, vals[child0(d) * 32 + lane], vals[child1(d) * 32 + lane], T(0), T(0));
     }
     vals[k * 32 + lane] = r;
-    if (out && valid) __stcs(out + (size_t)k * N + nn, r);
+    if (out && valid) __stcs(out + (size_t)k * out_rs + nn * out_es, r);
   }
 }
 
-template <typename T>
+template <typename T, bool kMulti>
 __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__ X, int64_t N, int64_t n_x,
                                                            const uint32_t* __restrict__ desc,
                                                            const int32_t* __restrict__ meta,
                                                            const int32_t* __restrict__ order, int64_t B,
                                                            int64_t M, int Lmax, const T* __restrict__ C,
-                                                           int64_t c_sb, int64_t c_sm, T* __restrict__ cache) {
+                                                           int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K_,
+                                                           T* __restrict__ cache) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const int64_t K = kMulti ? K_ : 1;  // one constant set: the strides fold at compile time
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const size_t tbytes = align16((size_t)Lmax * 4);
   const size_t per_warp = tbytes + (size_t)Lmax * 32 * sizeof(T);
@@ -190,19 +193,23 @@ __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__
     const int L = meta[b * 4];
     for (int k = lane; k < L; k += 32) tape[k] = desc[b * M + k];
     __syncwarp();
-    const T* Crow = C + b * c_sb;
-    T* out = cache + (size_t)b * M * N;
+    // K constant sets: the cache is (B, M, N, K), set kk of node k, point n at
+    // ((b M + k) N + n) K + kk
+    T* out = cache + (size_t)b * M * N * K;
     const int64_t n0 = sl * kSlice, n1 = min(N, n0 + kSlice);
-    for (int64_t base = n0; base < n1; base += 32) {
-      const int64_t n = base + lane;
-      const bool valid = n < n1;
-      forward_points<T>(tape, L, vals, X, n_x, valid ? n : n1 - 1, valid, Crow, c_sm, lane, out, N);
+    for (int64_t kk = 0; kk < K; ++kk) {
+      const T* Crow = C + b * c_sb + kk * c_sk;
+      for (int64_t base = n0; base < n1; base += 32) {
+        const int64_t n = base + lane;
+        const bool valid = n < n1;
+        forward_points<T>(tape, L, vals, X, n_x, valid ? n : n1 - 1, valid, Crow, c_sm, lane, out + kk, N * K, K);
+      }
     }
     // rows after the last real node: NaN (one contiguous block when the unit spans all points)
     if (nslices == 1) {
-      warp_fill_nan(out + (size_t)L * N, (size_t)(M - L) * N, lane);
+      warp_fill_nan(out + (size_t)L * N * K, (size_t)(M - L) * N * K, lane);
     } else {
-      for (int64_t k = L; k < M; ++k) warp_fill_nan(out + (size_t)k * N + n0, (size_t)(n1 - n0), lane);
+      for (int64_t k = L; k < M; ++k) warp_fill_nan(out + ((size_t)k * N + n0) * K, (size_t)(n1 - n0) * K, lane);
     }
     __syncwarp();
   }
@@ -284,12 +291,13 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int kPending>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory"); }
 
-// Copies rows 0..L-1, points base..base+31 of the (L, N) gradient block G into
-// buf[k][32] (zero beyond N).  vec16: rows start 16-byte aligned, so each lane moves
-// 16 bytes (E = 16 / sizeof(T) points; E rows per instruction); otherwise one element
-// per lane and row.
+// Copies rows 0..L-1, points base..base+31 of the gradient block G (node k, point n
+// at G[k * rs + n * es]) into buf[k][32] (zero beyond N).  vec16 (es == 1, rows
+// 16-byte aligned): each lane moves 16 bytes (E = 16 / sizeof(T) points; E rows per
+// instruction); otherwise one element per lane and row.
 template <typename T>
-__device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N, int64_t base, int lane, bool vec16) {
+__device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N, int64_t rs, int64_t es,
+                                           int64_t base, int lane, bool vec16) {
   if (vec16) {
     constexpr int E = 16 / sizeof(T);
     constexpr int kLanesPerRow = 32 / E;
@@ -297,14 +305,14 @@ __device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N,
     const int64_t left = N - (base + p);
     const int bytes = left >= E ? 16 : (left > 0 ? (int)left * (int)sizeof(T) : 0);
     for (int k = r0; k < L; k += E) {
-      const T* src = bytes ? G + (size_t)k * N + base + p : G;
+      const T* src = bytes ? G + (size_t)k * rs + base + p : G;
       cp_async(buf + k * 32 + p, src, 16, bytes);
     }
   } else {
     const int64_t n = base + lane;
     const int bytes = n < N ? (int)sizeof(T) : 0;
     for (int k = 0; k < L; ++k) {
-      const T* src = bytes ? G + (size_t)k * N + n : G;
+      const T* src = bytes ? G + (size_t)k * rs + n * es : G;
       cp_async(buf + k * 32 + lane, src, (int)sizeof(T), bytes);
     }
   }
@@ -318,13 +326,14 @@ __device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N,
 // never read), and the gradient of each constant is summed over points in a fixed
 // order (per chunk a butterfly, then in chunk order), so grad_C is deterministic.
 // ------------------------------------------------------------------------------------
-template <typename T>
+template <typename T, bool kMulti>
 __global__ void __launch_bounds__(256) eval_backward_kernel(
     const T* __restrict__ X, int64_t N, int64_t n_x, const uint32_t* __restrict__ desc,
     const int32_t* __restrict__ meta, const int32_t* __restrict__ order, int64_t B, int64_t M, int Lmax,
-    const T* __restrict__ C, int64_t c_sb, int64_t c_sm, const T* __restrict__ gout, T* __restrict__ gC,
-    T* __restrict__ gX, int32_t* __restrict__ status, bool vec16) {
+    const T* __restrict__ C, int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K_, const T* __restrict__ gout,
+    T* __restrict__ gC, T* __restrict__ gX, int32_t* __restrict__ status, bool vec16) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const int64_t K = kMulti ? K_ : 1;  // one constant set: the strides fold at compile time
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const size_t tbytes = align16((size_t)Lmax * 4);
   const size_t vbytes = (size_t)Lmax * 32 * sizeof(T);
@@ -338,15 +347,17 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
   for (int64_t ti = (int64_t)blockIdx.x * nwarp + warp; ti < B; ti += (int64_t)gridDim.x * nwarp) {
     const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
-    for (int k = lane; k < L; k += 32) {
-      tape[k] = desc[b * M + k];
-      gsum[k] = T(0);
-    }
-    const T* Crow = C + b * c_sb;
-    const T* G = gout + (size_t)b * M * N;
+    for (int k = lane; k < L; k += 32) tape[k] = desc[b * M + k];
     int err = 0;
     const int64_t nchunks = (N + 31) / 32;
-    stage_rows<T>(adj0, G, L, N, 0, lane, vec16);
+    // K constant sets, one after the other: grad_out is (B, M, N, K), set kk of
+    // node k, point n at ((b M + k) N + n) K + kk
+    for (int64_t kk = 0; kk < K; ++kk) {
+    for (int k = lane; k < L; k += 32) gsum[k] = T(0);
+    const T* Crow = C + b * c_sb + kk * c_sk;
+    const T* G = gout + (size_t)b * M * N * K + kk;
+    const int64_t rs = N * K;
+    stage_rows<T>(adj0, G, L, N, rs, K, 0, lane, vec16);
     __syncwarp();
     for (int64_t c = 0; c < nchunks; ++c) {
       const int64_t base = c * 32;
@@ -355,7 +366,7 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
       const int64_t nn = valid ? n : N - 1;
       T* adj = (c & 1) ? adj1 : adj0;
       if (c + 1 < nchunks) {
-        stage_rows<T>((c & 1) ? adj0 : adj1, G, L, N, base + 32, lane, vec16);
+        stage_rows<T>((c & 1) ? adj0 : adj1, G, L, N, rs, K, base + 32, lane, vec16);
         cp_async_wait<1>();
       } else {
         cp_async_wait<0>();
@@ -364,13 +375,13 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
       // adjoint seeds 0 + grad_out (the reference's zeros_like(cache).add_(grad_output))
       for (int k = 0; k < L; ++k) adj[k * 32 + lane] = M_<T>::add(T(0), adj[k * 32 + lane]);
       forward_points<T>(tape, L, vals, X, n_x, nn, valid, Crow, c_sm, lane, nullptr, N);
-      for (int kk = L - 1; kk >= 0; --kk) {
-        const uint32_t d = tape[kk];
+      for (int kk2 = L - 1; kk2 >= 0; --kk2) {
+        const uint32_t d = tape[kk2];
         const int code = code_of(d);
-        const T g = adj[kk * 32 + lane];
+        const T g = adj[kk2 * 32 + lane];
         if (code == LEARNABLE) {
           const T part = warp_sum((valid && g != T(0)) ? g : T(0));
-          if (lane == 0) gsum[kk] = M_<T>::add(gsum[kk], part);
+          if (lane == 0) gsum[kk2] = M_<T>::add(gsum[kk2], part);
           continue;
         }
         if (code == VAR) {
@@ -380,7 +391,7 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
         const int c0 = child0(d), c1 = child1(d);
         bool a0, a1;
         T o0, o1;
-        const int e = node_adjoint<T>(code, g, vals[c0 * 32 + lane], vals[c1 * 32 + lane], vals[kk * 32 + lane], a0,
+        const int e = node_adjoint<T>(code, g, vals[c0 * 32 + lane], vals[c1 * 32 + lane], vals[kk2 * 32 + lane], a0,
                                       o0, a1, o1);
         if (valid) {
           if (e && !err) err = e;
@@ -390,15 +401,17 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
       }
       __syncwarp();  // every lane is done with this buffer before it is refilled
     }
-    err = __reduce_max_sync(0xffffffffu, err);
-    if (err && lane == 0) report(status, err);
-    // gradient row: constant nodes get their sums, everything else 0
-    T* gCrow = gC + (size_t)b * M;
+    // gradient row of this set: constant nodes get their sums, everything else 0
+    T* gCrow = gC + (size_t)b * M * K + kk;
     for (int64_t k = lane; k < M; k += 32) {
       T val = T(0);
       if (k < L && code_of(tape[k]) == LEARNABLE) val = gsum[k];
-      gCrow[k] = val;
+      gCrow[k * K] = val;
     }
+    __syncwarp();
+    }  // sets
+    err = __reduce_max_sync(0xffffffffu, err);
+    if (err && lane == 0) report(status, err);
     __syncwarp();
   }
 }
@@ -484,59 +497,61 @@ static bool pick_shape(const void* kern, size_t per_warp, int64_t work_items, Sh
 template <typename T>
 static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                           const int32_t* order, int64_t B, int64_t M, int32_t max_len, const T* C, int64_t c_sb,
-                          int64_t c_sm, T* cache, void* stream) {
+                          int64_t c_sm, int64_t c_sk, int64_t K, T* cache, void* stream) {
   int rc = check_tape_args(B, M);
   if (rc) return rc;
-  if (N < 0 || n_x < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
-  if (B == 0 || M == 0 || N == 0) return SR_OK;
+  if (N < 0 || n_x < 0 || K < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (B == 0 || M == 0 || N == 0 || K == 0) return SR_OK;
   if (!X && n_x > 0) { set_error("null X"); return SR_ERR_INVALID_ARGUMENT; }
   if (!desc || !meta || !C || !cache) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
   const size_t per_warp = align16((size_t)Lmax * 4) + (size_t)Lmax * 32 * sizeof(T);
   Shape sh;
-  auto kern = eval_forward_kernel<T>;
+  auto kern = K == 1 ? eval_forward_kernel<T, false> : eval_forward_kernel<T, true>;
   const int64_t units = B * ((N + kSlice - 1) / kSlice);
   if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, units, sh)) {
     set_error("tape of %d nodes does not fit in shared memory", Lmax);
     return SR_ERR_UNSUPPORTED;
   }
   kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, as_stream(stream)>>>(X, N, n_x, desc, meta, order, B, M, Lmax,
-                                                                          C, c_sb, c_sm, cache);
+                                                                          C, c_sb, c_sm, c_sk, K, cache);
   return launch_check("eval_forward_kernel");
 }
 
 template <typename T>
 static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                            const int32_t* order, int64_t B, int64_t M, int32_t max_len, const T* C, int64_t c_sb,
-                           int64_t c_sm, const T* gout, T* gC, T* gX, int32_t* status, void* stream) {
+                           int64_t c_sm, int64_t c_sk, int64_t K, const T* gout, T* gC, T* gX, int32_t* status,
+                           void* stream) {
   int rc = check_tape_args(B, M);
   if (rc) return rc;
-  if (N < 0 || n_x < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (N < 0 || n_x < 0 || K < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
   if (!status) { set_error("null status"); return SR_ERR_INVALID_ARGUMENT; }
   cudaStream_t st = as_stream(stream);
   rc = cuda_check(cudaMemsetAsync(status, 0, sizeof(int32_t), st), "status reset");
   if (rc) return rc;
-  if (B == 0 || M == 0) return SR_OK;
+  if (B == 0 || M == 0 || K == 0) return SR_OK;
   if (!desc || !meta || !C || !gC || (N > 0 && !gout)) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
-  if (N == 0) return cuda_check(cudaMemsetAsync(gC, 0, sizeof(T) * B * M, st), "grad_C reset");
+  if (N == 0) return cuda_check(cudaMemsetAsync(gC, 0, sizeof(T) * B * M * K, st), "grad_C reset");
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
   // padding rows first (error 201 takes precedence)
   int64_t pblocks = (int64_t)device_sm_count() * 8;
   if (pblocks > B) pblocks = B;
-  padding_check_kernel<T><<<(unsigned)pblocks, 256, 0, st>>>(gout, meta, B, M, N, status);
+  padding_check_kernel<T><<<(unsigned)pblocks, 256, 0, st>>>(gout, meta, B, M, N * K, status);
   rc = launch_check("padding_check_kernel");
   if (rc) return rc;
   const size_t per_warp = align16((size_t)Lmax * 4) + 3 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
   Shape sh;
-  auto kern = eval_backward_kernel<T>;
+  auto kern = K == 1 ? eval_backward_kernel<T, false> : eval_backward_kernel<T, true>;
   if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, B, sh)) {
     set_error("tape of %d nodes does not fit in shared memory", Lmax);
     return SR_ERR_UNSUPPORTED;
   }
   // 16-byte staging needs every (tape, row, 32-point chunk) start 16-byte aligned
-  const bool vec16 = (reinterpret_cast<uintptr_t>(gout) % 16 == 0) && (N % (16 / (int64_t)sizeof(T)) == 0);
+  const bool vec16 =
+      K == 1 && (reinterpret_cast<uintptr_t>(gout) % 16 == 0) && (N % (16 / (int64_t)sizeof(T)) == 0);
   kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, Lmax, C, c_sb, c_sm,
-                                                           gout, gC, gX, status, vec16);
+                                                           c_sk, K, gout, gC, gX, status, vec16);
   return launch_check("eval_backward_kernel");
 }
 
@@ -567,27 +582,56 @@ int sr_tape_compile(const int64_t* ops, const int64_t* ch, int64_t B, int64_t M,
 int sr_eval_forward_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                         const int32_t* order, int64_t B, int64_t M, int32_t max_len, const float* C, int64_t c_sb,
                         int64_t c_sm, float* cache, void* stream) {
-  return sr::launch_forward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, cache, stream);
+  return sr::launch_forward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, 0, 1, cache, stream);
 }
 
 int sr_eval_forward_f64(const double* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                         const int32_t* order, int64_t B, int64_t M, int32_t max_len, const double* C, int64_t c_sb,
                         int64_t c_sm, double* cache, void* stream) {
-  return sr::launch_forward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, cache, stream);
+  return sr::launch_forward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, 0, 1, cache, stream);
 }
 
 int sr_eval_backward_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                          const int32_t* order, int64_t B, int64_t M, int32_t max_len, const float* C, int64_t c_sb,
                          int64_t c_sm, const float* gout, float* gC, float* gX, int32_t* status, void* stream) {
-  return sr::launch_backward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, gout, gC, gX, status,
-                                    stream);
+  return sr::launch_backward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, 0, 1, gout, gC, gX,
+                                    status, stream);
 }
 
 int sr_eval_backward_f64(const double* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                          const int32_t* order, int64_t B, int64_t M, int32_t max_len, const double* C, int64_t c_sb,
                          int64_t c_sm, const double* gout, double* gC, double* gX, int32_t* status, void* stream) {
-  return sr::launch_backward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, gout, gC, gX,
+  return sr::launch_backward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, 0, 1, gout, gC, gX,
                                      status, stream);
+}
+
+int sr_eval_forward_multi_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
+                              const int32_t* order, int64_t B, int64_t M, int32_t max_len, const float* C,
+                              int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, float* cache, void* stream) {
+  return sr::launch_forward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, c_sk, K, cache, stream);
+}
+
+int sr_eval_forward_multi_f64(const double* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
+                              const int32_t* order, int64_t B, int64_t M, int32_t max_len, const double* C,
+                              int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, double* cache, void* stream) {
+  return sr::launch_forward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, c_sk, K, cache,
+                                    stream);
+}
+
+int sr_eval_backward_multi_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
+                               const int32_t* order, int64_t B, int64_t M, int32_t max_len, const float* C,
+                               int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const float* gout, float* gC,
+                               float* gX, int32_t* status, void* stream) {
+  return sr::launch_backward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, c_sk, K, gout, gC, gX,
+                                    status, stream);
+}
+
+int sr_eval_backward_multi_f64(const double* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
+                               const int32_t* order, int64_t B, int64_t M, int32_t max_len, const double* C,
+                               int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const double* gout, double* gC,
+                               double* gX, int32_t* status, void* stream) {
+  return sr::launch_backward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, c_sk, K, gout, gC,
+                                     gX, status, stream);
 }
 
 }  // extern "C"

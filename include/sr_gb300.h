@@ -131,6 +131,34 @@ typedef struct sr_fit_options {
                                    (0 = max_len) */
 } sr_fit_options;
 
+/*
+ * Evaluation with K constant sets per tape (the reference's
+ * evaluate_multiple_constant_backend, src/symbolic_evaluation.cpp:171-305, with the
+ * per-position kernels src/evaluation_kernels_cuda.cu:761-1343, here one launch):
+ * C (B, M, K) through (b, m, set) strides; cache (B, M, N, K) contiguous, NO_OP rows
+ * NaN.  The adjoint takes grad_out (B, M, N, K) contiguous and writes grad_C
+ * (B, M, K) contiguous and, if not NULL, adds into grad_X (N, n_x) summed over the
+ * sets; status as for sr_eval_backward_f32.
+ */
+int sr_eval_forward_multi_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
+                              const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
+                              int32_t max_len, const float *C_dev, int64_t c_sb, int64_t c_sm, int64_t c_sk,
+                              int64_t K, float *cache_dev, void *stream);
+int sr_eval_forward_multi_f64(const double *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
+                              const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
+                              int32_t max_len, const double *C_dev, int64_t c_sb, int64_t c_sm, int64_t c_sk,
+                              int64_t K, double *cache_dev, void *stream);
+int sr_eval_backward_multi_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
+                               const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
+                               int32_t max_len, const float *C_dev, int64_t c_sb, int64_t c_sm, int64_t c_sk,
+                               int64_t K, const float *grad_out_dev, float *grad_C_dev, float *grad_X_dev,
+                               int32_t *status_dev, void *stream);
+int sr_eval_backward_multi_f64(const double *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
+                               const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
+                               int32_t max_len, const double *C_dev, int64_t c_sb, int64_t c_sm, int64_t c_sk,
+                               int64_t K, const double *grad_out_dev, double *grad_C_dev, double *grad_X_dev,
+                               int32_t *status_dev, void *stream);
+
 /* Bytes of device workspace sr_fit_lbfgs needs for this problem set
  * (B, N, M, max_len, max_consts and opt as passed to sr_fit_lbfgs). */
 int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len, int32_t max_consts,

@@ -111,6 +111,30 @@ def eval_bwd(X, ops, ch, C, gout, dtype=np.float32, want_gx=True):
     return gC, gX, err
 
 
+def eval_fwd_multi(X, ops, ch, C3, dtype=np.float32):
+    """evaluate_multiple: (B,M,N,K) node values for K constant sets C3 (B,M,K).  The
+    reference evaluates every set with the single-set operator policies
+    (src/evaluation_kernels_cpu.cpp multiple-constant kernels), so each set is one
+    single-set evaluation here."""
+    C3 = np.asarray(C3)
+    return np.stack([eval_fwd(X, ops, ch, C3[:, :, k], dtype) for k in range(C3.shape[2])], axis=3)
+
+
+def eval_bwd_multi(X, ops, ch, C3, gout4, dtype=np.float32, want_gx=True):
+    """Adjoint of evaluate_multiple for a dense (B,M,N,K) output gradient ->
+    (gC (B,M,K), gX (N,nx) summed over the sets, first error code)."""
+    C3 = np.asarray(C3)
+    gout4 = np.asarray(gout4)
+    gCs, gX, err = [], None, 0
+    for k in range(C3.shape[2]):
+        gC, gx, e = eval_bwd(X, ops, ch, C3[:, :, k], gout4[..., k], dtype, want_gx)
+        gCs.append(gC)
+        err = err or e
+        if want_gx:
+            gX = gx if gX is None else gX + gx
+    return np.stack(gCs, axis=2), gX, err
+
+
 def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_grad=1e-7,
              line_search_fn="strong_wolfe", line_search_max_iter=10, dot_mode=1):
     """Per-problem restatement of ``symbolic_torch.optimize``.

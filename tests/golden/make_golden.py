@@ -346,9 +346,37 @@ def case_notation(st):
                         strings_all=np.array(strings_all), **out)
 
 
+def case_multiple(st):
+    """evaluate_multiple: K=3 constant sets, dense output gradient on every node
+    (reference tests/test_evaluation_multiple_constants.py pattern)."""
+    rng = np.random.default_rng(77)
+    B, M, N, n_vars, K = 64, 24, 33, 3, 3
+    X = rng.uniform(-3, 3, (N, n_vars)).astype(np.float32)
+    tb = tapes.generate(B, M, seed=78, mean_length=10, n_vars=n_vars, p_const_leaf=0.35)
+    ops, ch = tb.ops, tb.ch
+    C = rng.standard_normal((B, M, K)).astype(np.float32)
+    Xt = torch.tensor(X, requires_grad=True)
+    Ct = torch.tensor(C, requires_grad=True)
+    out = st.evaluation.evaluate_multiple(Xt, torch.tensor(ops), torch.tensor(ch), Ct)
+    cache = out.detach().numpy().copy()
+    gout = rng.standard_normal(cache.shape).astype(np.float32)
+    gout[np.isnan(cache)] = 0.0
+    for b in range(B):  # no gradient into tapes whose DIV denominators hit exact zeros
+        for k in range(M):
+            if ops[b, k] == int(Operator.DIV) and (cache[b, ch[b, k, 1]] == 0).any():
+                gout[b] = 0.0
+    out.backward(torch.tensor(gout))
+    np.savez_compressed(os.path.join(OUT, "multiple.npz"), X=X, ops=ops, ch=ch, C=C, cache=cache, gout=gout,
+                        gC=Ct.grad.numpy().copy(), gX=Xt.grad.numpy().copy())
+
+
 def main():
     st = build_ref.load_reference()
     torch.set_num_threads(1)
+    if len(sys.argv) > 1:  # selected cases only, e.g. `make_golden.py multiple`
+        for name in sys.argv[1:]:
+            globals()["case_" + name](st)
+        return
     rng = np.random.default_rng(2024)
     case_single_ops(st, rng)
     case_random_dags(st, rng, "random_dags", B=160, M=24, N=37, n_vars=3, seed=11,
@@ -362,6 +390,7 @@ def main():
     case_optimize_ragged(st, B=48, max_iter=30, line_search="backtracking", name="optimize_ragged_bt")
     case_rosenbrock(st)
     case_notation(st)
+    case_multiple(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

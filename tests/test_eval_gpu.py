@@ -281,3 +281,86 @@ def test_create_constants_large(B):
     ref = torch.zeros(m.shape, device="cuda")
     ref[m] = torch.randn(int(m.sum()), device="cuda")
     assert torch.equal(mine, ref)
+
+
+# ---- evaluate_multiple (K constant sets) --------------------------------------------
+
+def test_multiple_vs_reference_golden(golden):
+    """evaluate_multiple against the reference's own outputs: every set node by node
+    (exact operations bit for bit), gradients per set and the X gradient summed over
+    the sets."""
+    sr = _sr()
+    g = golden("multiple")
+    X = cuda(g["X"]).requires_grad_(True)
+    C = cuda(g["C"]).requires_grad_(True)
+    out = sr.evaluation.evaluate_multiple(X, cuda(g["ops"]), cuda(g["ch"]), C)
+    assert out.shape == g["cache"].shape
+    got = out.detach().cpu().numpy()
+    for k in range(g["C"].shape[2]):
+        check_local(g["X"], g["ops"], g["ch"], g["C"][:, :, k], got[..., k])
+    ref64 = oracle.eval_fwd_multi(g["X"], g["ops"], g["ch"], g["C"], dtype=np.float64)
+    check_accuracy(got, g["cache"], ref64)
+    out.backward(cuda(g["gout"]))
+    gC64, gX64, err = oracle.eval_bwd_multi(g["X"], g["ops"], g["ch"], g["C"], g["gout"], dtype=np.float64)
+    assert err == 0
+    check_accuracy(C.grad.cpu().numpy(), g["gC"], gC64, rtol=1e-5, atol=1e-5, min_frac_tight=0.99)
+    check_accuracy(X.grad.cpu().numpy(), g["gX"], gX64, rtol=1e-4, atol=1e-4, min_frac_tight=0.9)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_multiple_equals_single_per_set(dtype):
+    """Set k of evaluate_multiple is evaluate() with C[..., k], bit for bit, and so are
+    the per-set constant gradients; the X gradient is the sum over the sets."""
+    sr = _sr()
+    from cudasymbolicregression_gb300 import tapes
+    rng = np.random.default_rng(21)
+    B, M, N, K = 90, 32, 77, 4
+    X = rng.uniform(-3, 3, (N, 2))
+    tb = tapes.generate(B, M, seed=22, mean_length=12, n_vars=2, p_const_leaf=0.3, X_screen=X.astype(np.float32))
+    C = rng.standard_normal((B, M, K))
+    Xt = cuda(X, dtype)
+    ops, ch = cuda(tb.ops), cuda(tb.ch)
+    Cm = cuda(C, dtype).requires_grad_(True)
+    Xm = Xt.clone().requires_grad_(True)
+    out = sr.evaluation.evaluate_multiple(Xm, ops, ch, Cm)
+    root = np.maximum((tb.ops != 0).sum(1) - 1, 0)
+    gout = np.zeros(out.shape)
+    gout[np.arange(B), root] = rng.standard_normal((B, N, K))
+    out.backward(cuda(gout, dtype))
+    gx_sum = torch.zeros_like(Xt)
+    for k in range(K):
+        Ck = cuda(C[:, :, k], dtype).requires_grad_(True)
+        Xk = Xt.clone().requires_grad_(True)
+        single = sr.evaluation.evaluate(Xk, ops, ch, Ck)
+        assert torch.equal(torch.nan_to_num(single, nan=7.0), torch.nan_to_num(out[..., k].detach(), nan=7.0))
+        single.backward(cuda(gout[..., k], dtype))
+        assert torch.equal(torch.nan_to_num(Ck.grad, nan=7.0), torch.nan_to_num(Cm.grad[..., k], nan=7.0))
+        gx_sum += Xk.grad
+    torch.testing.assert_close(Xm.grad, gx_sum, rtol=1e-5, atol=1e-5, equal_nan=True)
+
+
+def test_multiple_backend_layout_and_errors(golden):
+    """M-first entry point (M, N, B, K) (reference src/symbolic_evaluation.cpp:171-202),
+    its argument checks and the backward error context."""
+    sr = _sr()
+    g = golden("multiple")
+    X, ops, ch, C = cuda(g["X"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"])
+    out = sr.evaluation.evaluate_multiple_constant_backend(X, ops.permute(1, 0), ch.permute(1, 0, 2),
+                                                           C.permute(1, 0, 2))
+    B, M, K = g["C"].shape
+    assert out.shape == (M, X.shape[0], B, K)
+    direct = sr.evaluation.evaluate_multiple(X, ops, ch, C)
+    assert torch.equal(torch.nan_to_num(out.permute(2, 0, 1, 3), nan=3.0), torch.nan_to_num(direct, nan=3.0))
+    with pytest.raises(RuntimeError, match="C must be a 3D tensor for multiple constant evaluation"):
+        sr.evaluation.evaluate_multiple(X, ops, ch, C[:, :, 0])
+    with pytest.raises(RuntimeError, match="must have the same batch size"):
+        sr.evaluation.evaluate_multiple(X, ops, ch, C[:-1])
+    e = golden("errors")
+    o, c = cuda(e["noop_grad__ops"]), cuda(e["noop_grad__ch"])
+    Xe = cuda(e["noop_grad__X"]).requires_grad_(True)
+    Ce = torch.zeros(o.shape + (2,), device="cuda").requires_grad_(True)
+    y = sr.evaluation.evaluate_multiple(Xe, o, c, Ce)
+    gy = torch.zeros_like(y)
+    gy[:, -1] = 1.0
+    with pytest.raises(RuntimeError, match="multiple constants"):
+        y.backward(gy)

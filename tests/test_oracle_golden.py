@@ -29,6 +29,20 @@ def test_backward(golden, name):
         np.testing.assert_allclose(mine[fin], ref[fin], rtol=1e-5, atol=1e-5 * max(1.0, np.abs(ref[fin]).max(initial=0)))
 
 
+def test_multiple_constants_against_reference(golden):
+    """evaluate_multiple (reference symbolic_torch/evaluation.py:36-65): every set is
+    a single-set evaluation; gradients per set, X gradient summed over the sets."""
+    g = golden("multiple")
+    cache = oracle.eval_fwd_multi(g["X"], g["ops"], g["ch"], g["C"])
+    assert np.array_equal(cache, g["cache"], equal_nan=True)
+    gC, gX, err = oracle.eval_bwd_multi(g["X"], g["ops"], g["ch"], g["C"], g["gout"])
+    assert err == 0
+    for mine, ref in ((gC, g["gC"]), (gX, g["gX"])):
+        assert np.array_equal(np.isnan(mine), np.isnan(ref))
+        fin = np.isfinite(ref)
+        np.testing.assert_allclose(mine[fin], ref[fin], rtol=1e-5, atol=1e-5 * max(1.0, np.abs(ref[fin]).max(initial=0)))
+
+
 def test_single_op_x_gradients_per_row(golden):
     g = golden("single_ops")
     B = g["ops"].shape[0]
