@@ -14,7 +14,7 @@ Every compute entry point runs hand-written sm_103a kernels from
 """
 from . import evaluation
 from .operators import MAX_ARITY, NULL_CHILD, ErrorCode, Operator, get_arity, is_valid_op
-from .optimization import FitResult, optimize, optimize_ex
+from .optimization import FitPlan, FitResult, optimize, optimize_ex
 from .utils import create_constants
 
 __all__ = [
@@ -25,6 +25,7 @@ __all__ = [
     "optimize",
     "optimize_ex",
     "FitResult",
+    "FitPlan",
     "get_arity",
     "is_valid_op",
     "MAX_ARITY",

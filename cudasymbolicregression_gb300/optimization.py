@@ -30,11 +30,51 @@ class FitResult:
     evals: torch.Tensor    # (B,) int32 closures (forward + adjoint passes) evaluated
 
 
+# Launch shapes (points per lane V, warps per CTA W) the autotuner tries, and its
+# decisions per problem class: (N, n_x, longest tape, most constants, line search).
+_TUNE_CANDIDATES = ((1, 2), (1, 4), (1, 8), (2, 2), (2, 4), (2, 8))
+_TUNED: dict = {}
+
+
+def _autotune(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, key, sample=2048,
+              tune_iter=20, **kw):
+    """Time every candidate launch shape on a seeded random sample of the problems
+    (at most `tune_iter` iterations each) and return the fastest (V, W)."""
+    if key in _TUNED:
+        return _TUNED[key]
+    B = Ops.shape[0]
+    g = torch.Generator().manual_seed(1234)
+    idx = torch.randperm(B, generator=g)[:min(B, sample)].to(Ops.device)
+    Xs, Ys, Os, Cs, C0 = X, Y[idx] if Y is not None else None, Ops[idx], Ch[idx], C_init[idx]
+    N = X.shape[0]
+    best, best_t = None, float("inf")
+    for V, W in _TUNE_CANDIDATES:
+        if W * 32 * V > 2 * max(N, 32):
+            continue  # more points per CTA than the data has
+        try:
+            times = []
+            for rep in range(2):  # the first run also builds the program caches
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                _fit(Xs, Ys, Os, Cs, C0, min(max_iter, tune_iter), history_size, tolerance_grad, line_search_fn,
+                     points_per_lane=V, warps_per_block=W, raise_errors=False, want_y=False, **kw)
+                e1.record()
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+            t = times[-1]
+        except RuntimeError:
+            continue  # the shape does not fit (shared memory)
+        if t < best_t:
+            best, best_t = (V, W), t
+    _TUNED[key] = best if best is not None else (0, 0)
+    return _TUNED[key]
+
+
 def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, *,
          objective: int = 0, line_search_max_iter: int = 10, eps: float = 1e-10,
          warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
          order: Optional[torch.Tensor] = None, want_y: bool = True, raise_errors: bool = True,
-         class_width: int = 0, kernel_events=None) -> FitResult:
+         class_width: int = 0, kernel_events=None, autotune: bool = False) -> FitResult:
     if line_search_fn not in ("strong_wolfe", "backtracking"):
         raise ValueError(f"Invalid line_search_fn: {line_search_fn}. Choose 'strong_wolfe' or 'backtracking'.")
     if Ops.dim() != 2:
@@ -54,6 +94,11 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
         Y = Y.to(torch.float32).contiguous()
     tapes = compile_tapes(Ops, Ch, nx)
     Xc = X.contiguous()
+    if autotune and warps_per_block == 0 and points_per_lane == 0:
+        key = (N, nx, tapes.max_root, tapes.max_consts, line_search_fn, objective)
+        points_per_lane, warps_per_block = _autotune(
+            X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, key, objective=objective,
+            line_search_max_iter=line_search_max_iter, eps=eps)
     opts = _lib.FitOptions(max_iter=int(max_iter), history_size=int(history_size),
                            tolerance_grad=float(tolerance_grad),
                            line_search=0 if line_search_fn == "strong_wolfe" else 1,
@@ -156,6 +201,92 @@ def optimize_ex(X, Y, Ops, Ch, C_init, max_iter=100, history_size=10, tolerance_
     (False: problems whose closures hit error 201/204 are reported through
     ``iters < 0`` instead of aborting the whole batch as the reference does),
     kernel_events (a pair of torch.cuda.Event recorded on the current stream just
-    before the first and just after the last fit-kernel launch).
+    before the first and just after the last fit-kernel launch), autotune (time the
+    candidate launch shapes on a sample of the batch once per problem class and use
+    the fastest; the choice is cached for the process).
     """
     return _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, **kw)
+
+
+class FitPlan:
+    """A fit of fixed tapes and data whose launches can be replayed and captured in a
+    CUDA graph: validation, staging, ordering and every allocation happen once here
+    (one host synchronisation); ``run`` then only enqueues the status/counter resets
+    and the fused fit kernel on the current stream, so a sequence of fits of the same
+    expressions from different starting constants (multi-start, warm-start rounds)
+    costs one graph replay each.
+
+    plan = FitPlan(X, Y, Ops, Ch, max_iter=100)
+    plan.C_in.copy_(C0); plan.run()            # or: g = plan.capture(); ...; g.replay()
+    plan.result()                              # FitResult (reads the status once)
+    """
+
+    def __init__(self, X, Y, Ops, Ch, max_iter=100, history_size=10, tolerance_grad=1e-7,
+                 line_search_fn="strong_wolfe", *, objective: int = 0, line_search_max_iter: int = 10,
+                 eps: float = 1e-10, warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
+                 want_y: bool = True):
+        if line_search_fn not in ("strong_wolfe", "backtracking"):
+            raise ValueError(f"Invalid line_search_fn: {line_search_fn}. Choose 'strong_wolfe' or 'backtracking'.")
+        B, M = Ops.shape
+        _check_backend_inputs(X, Ops.permute(1, 0), Ch.permute(1, 0, 2),
+                              torch.empty((M, B), dtype=X.dtype, device=X.device))
+        if X.dtype != torch.float32:
+            raise RuntimeError("optimize runs in float32: X and C_init must be float32")
+        dev = X.device
+        N, nx = X.shape
+        self.B, self.M, self.N, self.nx = B, M, N, nx
+        self.X = X.contiguous()
+        self.Y = None if Y is None else Y.to(torch.float32).contiguous()
+        self.tapes = compile_tapes(Ops, Ch, nx)
+        self.order = torch.argsort(self.tapes.meta[:, 1] + 1, descending=True, stable=True).to(torch.int32)
+        self.opts = _lib.FitOptions(max_iter=int(max_iter), history_size=int(history_size),
+                                    tolerance_grad=float(tolerance_grad),
+                                    line_search=0 if line_search_fn == "strong_wolfe" else 1,
+                                    line_search_max_iter=int(line_search_max_iter), eps=float(eps),
+                                    objective=int(objective), warps_per_block=int(warps_per_block),
+                                    points_per_lane=int(points_per_lane), grid_blocks=int(grid_blocks),
+                                    max_operators=int(max(self.tapes.max_operators, 1)))
+        L = _lib.lib()
+        self.max_len = min(max(self.tapes.max_root, 1), M)
+        wsb = L.sr_fit_workspace_bytes(B, N, M, self.max_len, self.tapes.max_consts, self.opts)
+        if wsb < 0:
+            _lib.check(-1, "sr_fit_workspace_bytes")
+        self.ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)
+        self.C_in = torch.zeros((B, M), dtype=torch.float32, device=dev)
+        self.C_out = torch.empty((B, M), dtype=torch.float32, device=dev)
+        self.Y_out = torch.empty((B, N), dtype=torch.float32, device=dev) if want_y else None
+        self.iters = torch.empty(B, dtype=torch.int32, device=dev)
+        self.loss = torch.empty(B, dtype=torch.float32, device=dev)
+        self.evals = torch.empty(B, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def run(self) -> None:
+        """Enqueue one fit from self.C_in on the current stream (no synchronisation)."""
+        L = _lib.lib()
+        rc = L.sr_fit_lbfgs(_lib.ptr(self.X), self.N, self.nx, _lib.ptr(self.Y), _lib.ptr(self.tapes.desc),
+                            _lib.ptr(self.tapes.meta), self.B, self.M, _lib.ptr(self.C_in), _lib.ptr(self.C_out),
+                            self.M, 1, _lib.ptr(self.Y_out), _lib.ptr(self.iters), _lib.ptr(self.loss),
+                            _lib.ptr(self.evals), _lib.ptr(self.order), self.max_len, self.tapes.max_consts, self.opts,
+                            _lib.ptr(self.ws), self.ws.numel(), _lib.ptr(self.status),
+                            _lib.stream_ptr(self.X.device))
+        _lib.check(rc, "sr_fit_lbfgs")
+
+    def capture(self) -> torch.cuda.CUDAGraph:
+        """A CUDA graph of ``run`` (one warm-up run first, on a side stream)."""
+        s = torch.cuda.Stream(device=self.X.device)
+        s.wait_stream(torch.cuda.current_stream(self.X.device))
+        with torch.cuda.stream(s):
+            self.run()
+        torch.cuda.current_stream(self.X.device).wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run()
+        return g
+
+    def result(self, raise_errors: bool = True) -> FitResult:
+        """The outputs of the last run (reads the status word once)."""
+        code = int(self.status.item())
+        if code and raise_errors:
+            ctx = "input validation" if code in (101, 102) else "symbolic evaluation backward pass"
+            raise RuntimeError(error_message(code, ctx))
+        return FitResult(C=self.C_out, Y=self.Y_out, iters=self.iters, loss=self.loss, evals=self.evals)

@@ -364,3 +364,72 @@ def test_multiple_backend_layout_and_errors(golden):
     gy[:, -1] = 1.0
     with pytest.raises(RuntimeError, match="multiple constants"):
         y.backward(gy)
+
+
+def test_gradients_match_central_finite_differences_fp64():
+    """The adjoint in float64 against central finite differences (h = 1e-3) of the
+    float64 forward: loss = sum of root outputs, gradient w.r.t. C, tapes over
+    {+,-,*,/,sin,cos,exp,log,X0..X3,C} with X ~ U[-3, 3] and C ~ N(0, 1).  The
+    differences at h and h/2 give a Richardson estimate and its truncation error,
+    which (with the rounding error of the differences) is the tolerance.  Only
+    entries where the function is smooth at the scale of h are compared: no division
+    by a value below 0.05 at any point, a loss below 1e6, and a change over h no
+    larger than ten times the loss (elsewhere the root oscillates or blows up within
+    h and the difference quotient is meaningless; the CPU oracle shows the same
+    picture there, so those entries say nothing about this kernel)."""
+    sr = _sr()
+    from cudasymbolicregression_gb300 import tapes
+    rng = np.random.default_rng(31)
+    B, M, N, nx, h = 2048, 64, 64, 4, 1e-3
+    X = rng.uniform(-3, 3, (N, nx))
+    C = rng.standard_normal((B, M))
+    tb = tapes.generate(B, M, seed=32, mean_length=20, n_vars=nx, p_const_leaf=0.2,
+                        X_screen=X.astype(np.float32), C_screen=C.astype(np.float32))
+    ops, ch = cuda(tb.ops), cuda(tb.ch)
+    Xt = cuda(X, torch.float64)
+    root = torch.tensor(np.maximum((tb.ops != 0).sum(1) - 1, 0)).cuda()
+
+    def loss_rows(Cn):
+        with torch.no_grad():
+            out = sr.evaluation.evaluate(Xt, ops, ch, cuda(Cn, torch.float64))
+        return out[torch.arange(B).cuda(), root].sum(1).cpu().numpy()
+
+    Ct = cuda(C, torch.float64).requires_grad_(True)
+    out = sr.evaluation.evaluate(Xt, ops, ch, Ct)
+    gout = torch.zeros_like(out)
+    gout[torch.arange(B).cuda(), root] = 1.0
+    out.backward(gout)
+    g = Ct.grad.cpu().numpy()
+    L0 = loss_rows(C)
+    # a difference quotient only means something where the function is smooth at the
+    # scale of h: leave out tapes that divide by a value near zero at some point (the
+    # root then oscillates or blows up within h) and tapes whose loss is huge
+    vals = out.detach().cpu().numpy()
+    smooth = np.abs(L0) < 1e6
+    from cudasymbolicregression_gb300.operators import Operator
+    for b_, k_ in zip(*np.nonzero(tb.ops == int(Operator.DIV))):
+        den = vals[b_, tb.ch[b_, k_, 1]]
+        if np.nanmin(np.abs(den)) < 0.05:
+            smooth[b_] = False
+    is_c = tb.ops == 1
+    rank = np.cumsum(is_c, 1) - 1
+    checked = agree = 0
+    with np.errstate(invalid="ignore", over="ignore"):
+        for j in range(int(is_c.sum(1).max())):
+            rows, cols = np.nonzero(is_c & (rank == j))
+            fds = []
+            for step in (h, h / 2):
+                Cp, Cm = C.copy(), C.copy()
+                Cp[rows, cols] += step
+                Cm[rows, cols] -= step
+                fds.append(((loss_rows(Cp) - loss_rows(Cm)) / (2 * step))[rows])
+            f1, f2 = fds
+            rich = (4 * f2 - f1) / 3
+            ad = g[rows, cols]
+            ok = smooth[rows] & np.isfinite(L0[rows]) & np.isfinite(f1) & np.isfinite(f2) & np.isfinite(ad)
+            ok &= np.abs(ad) * h <= 10 * (np.abs(L0[rows]) + 1)  # changes within h stay small
+            tol = 1e-6 * np.maximum(np.abs(ad), 1.0) + 4 * np.abs(f1 - f2) + 1e-12 * np.abs(L0[rows]) / (h / 2)
+            checked += int(ok.sum())
+            agree += int((np.abs(rich - ad) <= tol)[ok].sum())
+    assert checked > 200
+    assert agree / checked >= 0.99, (agree, checked)

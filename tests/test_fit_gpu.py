@@ -240,3 +240,41 @@ def test_kernel_shapes_agree(golden, ppl, wpb):
                        points_per_lane=ppl, warps_per_block=wpb, raise_errors=False)
     close = rel_close(mse(r.Y.cpu().numpy(), g["Y"]), mse(base.Y.cpu().numpy(), g["Y"]), 1e-4)
     assert close.mean() >= 0.9
+
+
+def test_fit_plan_and_cuda_graph_replay(golden):
+    """FitPlan: the same results as optimize_ex, and a captured CUDA graph replays the
+    fit from new starting constants with identical results to a direct run."""
+    sr = _sr()
+    g = golden("optimize_ragged")
+    X, Y, ops, ch = cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"])
+    C0 = cuda(g["C"])
+    ref = sr.optimize_ex(X, Y, ops, ch, C0, max_iter=25, raise_errors=False)
+    plan = sr.FitPlan(X, Y, ops, ch, max_iter=25)
+    plan.C_in.copy_(C0)
+    plan.run()
+    r = plan.result(raise_errors=False)
+    for a, b in ((r.C, ref.C), (r.Y, ref.Y), (r.loss, ref.loss)):
+        assert torch.equal(torch.nan_to_num(a, nan=9.0), torch.nan_to_num(b, nan=9.0))
+    assert torch.equal(r.iters, ref.iters) and torch.equal(r.evals, ref.evals)
+    graph = plan.capture()
+    C1 = C0 + 0.25
+    ref1 = sr.optimize_ex(X, Y, ops, ch, C1, max_iter=25, raise_errors=False)
+    plan.C_in.copy_(C1)
+    graph.replay()
+    r1 = plan.result(raise_errors=False)
+    assert torch.equal(torch.nan_to_num(r1.C, nan=9.0), torch.nan_to_num(ref1.C, nan=9.0))
+    assert torch.equal(r1.iters, ref1.iters)
+
+
+def test_autotune_picks_a_shape_and_matches_it(golden):
+    sr = _sr()
+    from cudasymbolicregression_gb300 import optimization
+    g = golden("optimize_ragged")
+    X, Y, ops, ch, C = cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"])
+    r = sr.optimize_ex(X, Y, ops, ch, C, max_iter=20, raise_errors=False, autotune=True)
+    assert len(optimization._TUNED) >= 1
+    V, W = list(optimization._TUNED.values())[-1]
+    assert (V, W) in optimization._TUNE_CANDIDATES
+    r2 = sr.optimize_ex(X, Y, ops, ch, C, max_iter=20, raise_errors=False, points_per_lane=V, warps_per_block=W)
+    assert torch.equal(torch.nan_to_num(r.C, nan=9.0), torch.nan_to_num(r2.C, nan=9.0))
