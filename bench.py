@@ -262,6 +262,27 @@ def fit_quality(r, ref_finite, max_iter):
             "mean_closures": float(r.evals.float().mean())}
 
 
+def fp64_check(r, X, Y, ops, ch, sample=4096):
+    """The reported final MSE of a sample of finite problems against an FP64
+    evaluation of the same constants (the library's float64 forward kernel): the
+    median and largest relative difference."""
+    import cudasymbolicregression_gb300 as sr
+    loss = r.loss
+    idx = torch.nonzero(torch.isfinite(loss)).flatten()[:sample]
+    if idx.numel() == 0:
+        return None
+    o, c = ops[idx], ch[idx]
+    with torch.no_grad():
+        out = sr.evaluation.evaluate(X.double(), o, c, r.C[idx].double())
+        root = ((o != 0).sum(1) - 1).clamp(min=0)
+        f = out[torch.arange(idx.numel(), device=out.device), root]
+        mse64 = ((f - Y[idx].double()) ** 2).mean(1)
+    rel = ((loss[idx].double() - mse64).abs() / mse64.abs().clamp(min=1e-300)).cpu().numpy()
+    rel = rel[np.isfinite(rel)]
+    return {"problems": int(idx.numel()), "median_rel_diff": float(np.median(rel)) if rel.size else None,
+            "max_rel_diff": float(rel.max()) if rel.size else None}
+
+
 def train_warm_start(args, dev, n_vars):
     """The warm-start network trained (untimed) on the fits of other problems."""
     from cudasymbolicregression_gb300 import warmstart, workloads
@@ -344,6 +365,9 @@ def run_fit(args, rank, world, local):
     ref_finite = np.isfinite(r_plain.loss.cpu().numpy())
     q_plain = fit_quality(r_plain, ref_finite, max_iter)
     q_head = fit_quality(head_r, ref_finite, max_iter)
+    q_head["fp64_check"] = fp64_check(head_r, Xd, Yd, Od, Chd)
+    if warm:
+        q_plain["fp64_check"] = fp64_check(r_plain, Xd, Yd, Od, Chd)
     evals = head_r.evals.cpu().numpy().astype(np.float64)
     flops = float((wl.flops_per_closure() * evals).sum())
     achieved_tflops = flops / head_tk / 1e12

@@ -321,10 +321,10 @@ __device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N,
 
 // ------------------------------------------------------------------------------------
 // Adjoint.  One warp per tape (persistent, longest first), 32 points per chunk.  The
-// output-gradient rows of chunk c+1 are staged into shared memory with cp.async while
-// chunk c is processed (two buffers), node values are recomputed (the saved cache is
-// never read), and the gradient of each constant is summed over points in a fixed
-// order (per chunk a butterfly, then in chunk order), so grad_C is deterministic.
+// output-gradient rows of a chunk are staged into shared memory with cp.async and
+// land while the chunk's node values are recomputed (the saved cache is never read);
+// the gradient of each constant is summed over points in a fixed order (per chunk
+// a butterfly, then in chunk order), so grad_C is deterministic.
 // ------------------------------------------------------------------------------------
 template <typename T, bool kMulti>
 __global__ void __launch_bounds__(256) eval_backward_kernel(
@@ -337,13 +337,12 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const size_t tbytes = align16((size_t)Lmax * 4);
   const size_t vbytes = (size_t)Lmax * 32 * sizeof(T);
-  const size_t per_warp = tbytes + 3 * vbytes + align16((size_t)Lmax * sizeof(T));
+  const size_t per_warp = tbytes + 2 * vbytes + align16((size_t)Lmax * sizeof(T));
   unsigned char* base_ptr = smem + warp * per_warp;
   uint32_t* tape = reinterpret_cast<uint32_t*>(base_ptr);
   T* vals = reinterpret_cast<T*>(base_ptr + tbytes);
-  T* const adj0 = reinterpret_cast<T*>(base_ptr + tbytes + vbytes);
-  T* const adj1 = reinterpret_cast<T*>(base_ptr + tbytes + 2 * vbytes);
-  T* gsum = reinterpret_cast<T*>(base_ptr + tbytes + 3 * vbytes);
+  T* adj = reinterpret_cast<T*>(base_ptr + tbytes + vbytes);
+  T* gsum = reinterpret_cast<T*>(base_ptr + tbytes + 2 * vbytes);
   for (int64_t ti = (int64_t)blockIdx.x * nwarp + warp; ti < B; ti += (int64_t)gridDim.x * nwarp) {
     const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
@@ -357,24 +356,20 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
     const T* Crow = C + b * c_sb + kk * c_sk;
     const T* G = gout + (size_t)b * M * N * K + kk;
     const int64_t rs = N * K;
-    stage_rows<T>(adj0, G, L, N, rs, K, 0, lane, vec16);
     __syncwarp();
     for (int64_t c = 0; c < nchunks; ++c) {
       const int64_t base = c * 32;
       const int64_t n = base + lane;
       const bool valid = n < N;
       const int64_t nn = valid ? n : N - 1;
-      T* adj = (c & 1) ? adj1 : adj0;
-      if (c + 1 < nchunks) {
-        stage_rows<T>((c & 1) ? adj0 : adj1, G, L, N, rs, K, base + 32, lane, vec16);
-        cp_async_wait<1>();
-      } else {
-        cp_async_wait<0>();
-      }
-      __syncwarp();
-      // adjoint seeds 0 + grad_out (the reference's zeros_like(cache).add_(grad_output))
-      for (int k = 0; k < L; ++k) adj[k * 32 + lane] = M_<T>::add(T(0), adj[k * 32 + lane]);
+      // the adjoint seeds (grad_out rows of this chunk) are in flight while the node
+      // values are recomputed.  Seeding with the raw values instead of 0 + grad_out
+      // (the reference's zeros_like(cache).add_(grad_output)) can only flip the sign
+      // of a zero seed, which no output can see: a zero adjoint contributes nothing
+      stage_rows<T>(adj, G, L, N, rs, K, base, lane, vec16);
       forward_points<T>(tape, L, vals, X, n_x, nn, valid, Crow, c_sm, lane, nullptr, N);
+      cp_async_wait<0>();
+      __syncwarp();
       for (int kk2 = L - 1; kk2 >= 0; --kk2) {
         const uint32_t d = tape[kk2];
         const int code = code_of(d);
@@ -399,7 +394,7 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
           if (a1) adj[c1 * 32 + lane] = M_<T>::add(adj[c1 * 32 + lane], o1);
         }
       }
-      __syncwarp();  // every lane is done with this buffer before it is refilled
+      __syncwarp();  // every lane is done with the seeds before the next chunk's land
     }
     // gradient row of this set: constant nodes get their sums, everything else 0
     T* gCrow = gC + (size_t)b * M * K + kk;
@@ -478,15 +473,23 @@ struct Shape {
 
 static bool pick_shape(const void* kern, size_t per_warp, int64_t work_items, Shape& sh) {
   const int limit = max_dyn_smem();
-  int w = 8;
-  while (w > 1 && per_warp * w > (size_t)limit) w >>= 1;
-  if (per_warp * w > (size_t)limit) return false;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, limit) != cudaSuccess) return false;
+  // the CTA size (8, 4, 2 or 1 warps) that keeps the most warps resident per SM
+  int w = 0, per_sm = 0, best = 0;
+  for (int cand = 8; cand >= 1; cand >>= 1) {
+    if (per_warp * cand > (size_t)limit) continue;
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, cand * 32, per_warp * cand) != cudaSuccess)
+      continue;
+    if (blocks * cand > best) {
+      best = blocks * cand;
+      w = cand;
+      per_sm = blocks;
+    }
+  }
+  if (w == 0) return false;
   sh.warps = w;
   sh.smem = per_warp * w;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem) != cudaSuccess) return false;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, w * 32, sh.smem) != cudaSuccess || per_sm < 1)
-    per_sm = 1;
   int64_t blocks = (int64_t)device_sm_count() * per_sm;
   const int64_t need = (work_items + w - 1) / w;
   sh.blocks = blocks < need ? blocks : need;
@@ -540,7 +543,7 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
   padding_check_kernel<T><<<(unsigned)pblocks, 256, 0, st>>>(gout, meta, B, M, N * K, status);
   rc = launch_check("padding_check_kernel");
   if (rc) return rc;
-  const size_t per_warp = align16((size_t)Lmax * 4) + 3 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
+  const size_t per_warp = align16((size_t)Lmax * 4) + 2 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
   Shape sh;
   auto kern = K == 1 ? eval_backward_kernel<T, false> : eval_backward_kernel<T, true>;
   if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, B, sh)) {
