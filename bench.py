@@ -31,6 +31,12 @@ Other workloads: --workload ragged (the plain fit of B=16384 such problems),
 2.5 cos(X_0) - 1.5, warm vs plain), --workload eval (evaluate forward + adjoint of a
 dense root-row gradient at B=65536, M=64, N=1024; value = algorithmic HBM bytes /
 step time).
+--workload search (the full search round): every round samples B=262144 new
+expressions (tapes over {+,-,*,/,sin,cos,exp,log}, 3 variables, padded length 64) and
+fits them (max_iter=100) to N=2048 points of one hidden seeded 5-operator target, for
+--rounds rounds; the plain arm starts from randn, the warm arm from the gated
+network, which is trained online on every finished round's fits.  Reported per arm:
+wall-clock to the first MSE < 1e-6 and expressions fitted/s over all rounds.
 --impl reference runs only the CPU port (the reference's own CPU path, restated).
 Multi-GPU: one process per GPU; every rank fits its own batch (independent seeds, no
 collective), value = all problems / max time over ranks.
@@ -57,7 +63,8 @@ UNIT = "expressions/s"
 M_DEFAULT = 64
 MAX_ITER = 200
 EVAL_METRIC = "evaluation forward+adjoint throughput (algorithmic HBM bytes)"
-DEFAULTS = {"warmstart": (65536, 512), "ragged": (16384, 512), "readme": (65536, 100), "eval": (65536, 1024)}
+DEFAULTS = {"warmstart": (65536, 512), "ragged": (16384, 512), "readme": (65536, 100), "eval": (65536, 1024),
+            "search": (262144, 2048)}
 
 # DRAM bytes (read + write) of one launch of the dominant kernel on the default
 # workloads, from ncu captures of a 4x / 16x smaller batch scaled by the number of
@@ -613,6 +620,127 @@ def run_eval(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def search_target(X, seed, dev):
+    """A hidden target: a random tape with exactly five operator nodes and N(0, 1)
+    constants whose root values are finite and not constant, evaluated at X."""
+    import cudasymbolicregression_gb300 as sr
+    from cudasymbolicregression_gb300 import tapes
+    rng = np.random.default_rng(seed)
+    for attempt in range(1000):
+        tb = tapes.generate(64, M_DEFAULT, seed=seed * 1000 + attempt, lengths=rng.integers(6, 12, 64), n_vars=X.shape[1],
+                            p_const_leaf=0.3)
+        for b in range(64):
+            ops = tb.ops[b]
+            nop = int(((ops >= 10) & (ops < 50)).sum())
+            if nop != 5:
+                continue
+            C = rng.standard_normal((1, M_DEFAULT)).astype(np.float32)
+            with torch.no_grad():
+                out = sr.evaluation.evaluate(torch.tensor(X, device=dev), torch.tensor(ops[None], device=dev),
+                                             torch.tensor(tb.ch[b][None], device=dev), torch.tensor(C, device=dev))
+            y = out[0, int((ops != 0).sum()) - 1].cpu().numpy()
+            if np.isfinite(y).all() and y.std() > 1e-2 and np.abs(y).max() < 1e3:
+                return y.astype(np.float32), ops, tb.ch[b], C[0]
+    raise RuntimeError("no target found")
+
+
+def run_search(args, rank, world, local):
+    """Config 5: rounds of sampling + fitting against one hidden target, plain vs warm."""
+    import cudasymbolicregression_gb300 as sr
+    from cudasymbolicregression_gb300 import warmstart, workloads, tapes
+
+    dev = torch.device("cuda", local)
+    B, N, n_vars, max_iter = args.B, args.N, 3, 100
+    rng = np.random.default_rng(args.seed + 1000 * rank)
+    X = rng.uniform(-3, 3, (N, n_vars)).astype(np.float32)
+    y, t_ops, _, _ = search_target(X, args.seed + 17, dev)
+    Xd = torch.tensor(X, device=dev)
+    Yd = torch.tensor(y, device=dev).unsqueeze(0).expand(B, N).contiguous()
+    Xs = X[rng.choice(N, size=32, replace=False)]
+    net = warmstart.WarmStartMLP(device=dev, seed=args.seed, n_vars=n_vars)
+    arms = {"plain": {"t": 0.0, "first_hit_s": None, "best": float("inf"), "mean_closures": []},
+            "warm": {"t": 0.0, "first_hit_s": None, "best": float("inf"), "mean_closures": [], "train_s": 0.0}}
+    gen_s = 0.0
+    # one-time set-up (library load, kernel attributes, workspace sizes) off the clock
+    tw = tapes.generate(512, M_DEFAULT, seed=1, mean_length=8.0, n_vars=n_vars, p_const_leaf=0.3)
+    sr.optimize_ex(Xd, Yd[:512], torch.tensor(tw.ops, device=dev), torch.tensor(tw.ch, device=dev),
+                   torch.randn(512, M_DEFAULT, device=dev), max_iter=2, raise_errors=False)
+    warmstart.gated_warm_start(net, Xd, Yd[:512], torch.tensor(tw.ops, device=dev), torch.tensor(tw.ch, device=dev),
+                               torch.randn(512, M_DEFAULT, device=dev))
+    # the training step's first call loads torch's gather/scatter kernels (seconds, once per process)
+    warm_net = warmstart.WarmStartMLP(device=dev, seed=args.seed + 1, n_vars=n_vars)
+    warmstart.train_fit_objective(warm_net, [(Xd[:256], Yd[:512, :256].contiguous(), torch.tensor(tw.ops, device=dev),
+                                              torch.tensor(tw.ch, device=dev), torch.randn(512, M_DEFAULT, device=dev))],
+                                  epochs=1, batch=512, lr=5e-4)
+    torch.cuda.synchronize()
+    n_train = min(B, 16384)
+    n_pts = min(N, 256)
+    with ClockSampler(local) as clk:
+        for r in range(args.rounds):
+            t0 = time.perf_counter()
+            C0 = rng.standard_normal((B, M_DEFAULT)).astype(np.float32)
+            tb = tapes.generate(B, M_DEFAULT, seed=args.seed * 100 + r, mean_length=8.0, n_vars=n_vars,
+                                p_const_leaf=0.3, X_screen=Xs, C_screen=C0,
+                                screen_fn=lambda o, c, Xs_, Cs_: workloads._gpu_zero_denominators(Xs_, o, c, Cs_,
+                                                                                                   str(dev)))
+            O, Ch, C = (torch.tensor(a, device=dev) for a in (tb.ops, tb.ch, C0))
+            torch.cuda.synchronize()
+            gen_s += time.perf_counter() - t0
+            for name in ("plain", "warm"):
+                a = arms[name]
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                Cs = C if (name == "plain" or r == 0) else warmstart.gated_warm_start(net, Xd, Yd, O, Ch, C)
+                res = sr.optimize_ex(Xd, Yd, O, Ch, Cs, max_iter=max_iter, raise_errors=False)
+                e1.record()
+                e1.synchronize()
+                a["t"] += e0.elapsed_time(e1) / 1000.0
+                loss = res.loss
+                best = float(torch.where(torch.isfinite(loss), loss, torch.full_like(loss, float("inf"))).min())
+                a["best"] = min(a["best"], best)
+                if a["first_hit_s"] is None and best < 1e-6:
+                    a["first_hit_s"] = a["t"]
+                a["mean_closures"].append(float(res.evals.float().mean()))
+                if name == "plain":
+                    plain_res = res
+            # the warm arm's network learns from this round's plain fits (timed into the warm arm)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            # a sample of the round's problems; the fit objective on a subset of the points
+            sel = torch.randperm(B, device=dev)[:n_train]
+            tgt, msk = warmstart.constant_targets(O[sel], plain_res.C[sel])
+            ok = torch.isfinite(plain_res.loss[sel]) & (plain_res.iters[sel] >= 0)
+            ok &= ((tgt.abs() <= 10) | (msk == 0)).all(dim=1) & torch.isfinite(tgt).all(dim=1)
+            msk = msk * ok.unsqueeze(1).float()
+            data = warmstart.TrainingSet([Xd], [Yd[sel]], [O[sel]], [torch.nan_to_num(tgt) * msk], [msk])
+            warmstart.train(net, data, epochs=2, batch=4096, lr=2e-3)
+            warmstart.train_fit_objective(net, [(Xd[:n_pts], Yd[sel, :n_pts].contiguous(), O[sel], Ch[sel], C[sel])],
+                                          epochs=1, batch=4096, lr=5e-4)
+            torch.cuda.synchronize()
+            tr = time.perf_counter() - t1
+            arms["warm"]["train_s"] += tr
+            arms["warm"]["t"] += tr
+    if rank == 0:
+        total = B * args.rounds
+        out = {}
+        for name, a in arms.items():
+            out[name] = {"expressions_per_s": total / a["t"], "seconds": a["t"], "first_mse_below_1e-6_s": a["first_hit_s"],
+                         "best_mse": a["best"], "mean_closures_per_round": a["mean_closures"]}
+            if "train_s" in a:
+                out[name]["online_training_s"] = a["train_s"]
+        line = {"metric": METRIC, "value": out["warm"]["expressions_per_s"], "unit": UNIT, "n_gpus": world,
+                "steps": args.rounds, "warmup": 0, "ms_per_step": 1000.0 * arms["warm"]["t"] / args.rounds,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"full search round: {args.rounds} rounds of B={B} new expressions (mean length 8, "
+                                       f"padded 64, +-*/ sin cos exp log, 3 variables) fitted to N={N} points of one "
+                                       "hidden 5-operator target, max_iter=100; warm arm trained online after every round",
+                           "B": B, "N": N, "target_ops": [int(v) for v in t_ops[t_ops != 0]]},
+                "arms": out, "warm_vs_plain": out["warm"]["expressions_per_s"] / out["plain"]["expressions_per_s"],
+                "generation_s": gen_s, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -625,6 +753,7 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--train-sets", type=int, default=4)
     ap.add_argument("--train-epochs", type=int, default=8)
+    ap.add_argument("--rounds", type=int, default=10)
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--cpu-eval-sample", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -645,6 +774,8 @@ def main():
         torch.cuda.set_device(local)
         if args.workload == "eval":
             run_eval(args, rank, world, local)
+        elif args.workload == "search":
+            run_search(args, rank, world, local)
         else:
             run_fit(args, rank, world, local)
     if world > 1:
