@@ -70,7 +70,7 @@ DEFAULTS = {"warmstart": (65536, 512), "ragged": (16384, 512), "readme": (65536,
 # workloads, from ncu captures of a 4x / 16x smaller batch scaled by the number of
 # problems (profiles/fit_lbfgs_ragged_B16384_N512.txt,
 # profiles/eval_forward_B4096_N1024.txt).
-FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10722048 + 24576)}
+FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10780928 + 20224)}
 EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000)}
 
 
