@@ -12,13 +12,14 @@ Public API, mirroring the reference package ``symbolic_torch``:
 Every compute entry point runs hand-written sm_103a kernels from
 ``libsr_gb300.so`` on CUDA tensors; there is no CPU path.
 """
-from . import evaluation
+from . import evaluation, notation
 from .operators import MAX_ARITY, NULL_CHILD, ErrorCode, Operator, get_arity, is_valid_op
 from .optimization import FitPlan, FitResult, optimize, optimize_ex
 from .utils import create_constants
 
 __all__ = [
     "evaluation",
+    "notation",
     "Operator",
     "ErrorCode",
     "create_constants",
