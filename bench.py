@@ -71,6 +71,9 @@ DEFAULTS = {"warmstart": (65536, 512), "ragged": (16384, 512), "readme": (65536,
 # problems (profiles/fit_lbfgs_ragged_B16384_N512.txt,
 # profiles/eval_forward_B4096_N1024.txt).
 FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10780928 + 20224)}
+# Issue utilisation of the fit kernel from the same capture (smsp__issue_active, percent):
+# the binding resource of an interpreter whose instructions are mostly integer/control work.
+FIT_ISSUE_ACTIVE_PCT = 46.9
 EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000)}
 
 
@@ -425,6 +428,7 @@ def run_fit(args, rank, world, local):
                              "frac": achieved_tflops / fp32_peak,
                              "traffic": FIT_TRAFFIC_BYTES.get((args.workload, B, N)),
                              "kernel": "fit_lbfgs_kernel", "kernel_ms": head_tk * 1000.0,
+                             "issue_active_pct_ncu": FIT_ISSUE_ACTIVE_PCT,
                              "peak_kind": f"nominal: {sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz "
                                           f"({pk_kind} clock); no measured FP32 peak exists"},
                 "quality": q_head,
