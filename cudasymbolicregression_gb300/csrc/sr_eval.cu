@@ -320,14 +320,25 @@ __device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N,
 }
 
 // ------------------------------------------------------------------------------------
-// Adjoint.  One warp per tape (persistent, longest first), 32 points per chunk.  The
-// output-gradient rows of a chunk are staged into shared memory with cp.async and
-// land while the chunk's node values are recomputed (the saved cache is never read);
-// the gradient of each constant is summed over points in a fixed order (per chunk
-// a butterfly, then in chunk order), so grad_C is deterministic.
+// Adjoint.  One warp per tape (persistent, longest first), 32 points per chunk.
+// Per tape the warp compacts its nodes into an operator list (code, own row, child
+// rows in one word each) and lists of its constant and variable leaves; leaf values
+// live in their rows (fixed constants once per tape, learnable constants once per
+// constant set, variables once per chunk).  Per chunk the output-gradient rows are
+// staged into shared memory with cp.async while the operator nodes are recomputed
+// (the saved cache is never read); the reverse sweep then runs over the operator list
+// only, adding contributions into the children's rows in the reference's order
+// (parents from the last to the first, child 0 before child 1), and the leaves are
+// reduced afterwards: each constant's gradient summed over points in a fixed order
+// (per chunk a butterfly, then in chunk order), so grad_C is deterministic.
 // ------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ size_t backward_warp_bytes(int Lmax) {
+  return align16((size_t)Lmax * 4) * 5 + 2 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
+}
+
 template <typename T, bool kMulti>
-__global__ void __launch_bounds__(256) eval_backward_kernel(
+__global__ void __launch_bounds__(256, 1) eval_backward_kernel(
     const T* __restrict__ X, int64_t N, int64_t n_x, const uint32_t* __restrict__ desc,
     const int32_t* __restrict__ meta, const int32_t* __restrict__ order, int64_t B, int64_t M, int Lmax,
     const T* __restrict__ C, int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K_, const T* __restrict__ gout,
@@ -335,75 +346,128 @@ __global__ void __launch_bounds__(256) eval_backward_kernel(
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t K = kMulti ? K_ : 1;  // one constant set: the strides fold at compile time
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  const size_t tbytes = align16((size_t)Lmax * 4);
+  const size_t lb = align16((size_t)Lmax * 4);
   const size_t vbytes = (size_t)Lmax * 32 * sizeof(T);
-  const size_t per_warp = tbytes + 2 * vbytes + align16((size_t)Lmax * sizeof(T));
-  unsigned char* base_ptr = smem + warp * per_warp;
+  unsigned char* base_ptr = smem + warp * backward_warp_bytes<T>(Lmax);
   uint32_t* tape = reinterpret_cast<uint32_t*>(base_ptr);
-  T* vals = reinterpret_cast<T*>(base_ptr + tbytes);
-  T* adj = reinterpret_cast<T*>(base_ptr + tbytes + vbytes);
-  T* gsum = reinterpret_cast<T*>(base_ptr + tbytes + 2 * vbytes);
+  uint32_t* prog0 = reinterpret_cast<uint32_t*>(base_ptr + lb);      // code | row << 8 | child0 << 20
+  uint32_t* prog1 = reinterpret_cast<uint32_t*>(base_ptr + 2 * lb);  // child1
+  int* lcon = reinterpret_cast<int*>(base_ptr + 3 * lb);             // learnable leaves
+  int* lvar = reinterpret_cast<int*>(base_ptr + 4 * lb);             // variable leaves
+  T* vals = reinterpret_cast<T*>(base_ptr + 5 * lb);
+  T* adj = reinterpret_cast<T*>(base_ptr + 5 * lb + vbytes);
+  T* gsum = reinterpret_cast<T*>(base_ptr + 5 * lb + 2 * vbytes);
+  const unsigned below = (1u << lane) - 1u;
   for (int64_t ti = (int64_t)blockIdx.x * nwarp + warp; ti < B; ti += (int64_t)gridDim.x * nwarp) {
     const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
     for (int k = lane; k < L; k += 32) tape[k] = desc[b * M + k];
+    __syncwarp();
+    // compaction: operator nodes (NO_OP included: its value is NaN and its adjoint
+    // check matters), learnable and variable leaves; fixed leaves get their rows now
+    int nop = 0, ncon = 0, nvar = 0;
+    for (int k0 = 0; k0 < L; k0 += 32) {
+      const int k = k0 + lane;
+      const uint32_t d = k < L ? tape[k] : 0u;
+      const int code = k < L ? code_of(d) : -1;
+      const bool isop = k < L && (code == NO_OP || arity_of(code) >= 1);
+      const bool iscon = code == LEARNABLE, isvar = code == VAR;
+      const unsigned mo = __ballot_sync(0xffffffffu, isop);
+      const unsigned mc = __ballot_sync(0xffffffffu, iscon);
+      const unsigned mv = __ballot_sync(0xffffffffu, isvar);
+      if (isop) {
+        const int ar = arity_of(code);
+        const uint32_t c0 = ar >= 1 ? (uint32_t)child0(d) : (uint32_t)k;
+        const uint32_t c1 = ar == 2 ? (uint32_t)child1(d) : (uint32_t)k;
+        const int pos = nop + __popc(mo & below);
+        prog0[pos] = (uint32_t)code | ((uint32_t)k << 8) | (c0 << 20);
+        prog1[pos] = c1;
+      }
+      if (iscon) lcon[ncon + __popc(mc & below)] = k;
+      if (isvar) lvar[nvar + __popc(mv & below)] = k;
+      nop += __popc(mo);
+      ncon += __popc(mc);
+      nvar += __popc(mv);
+    }
+    for (int k = 0; k < L; ++k) {
+      const int code = code_of(tape[k]);
+      if (code != NO_OP && code != LEARNABLE && code != VAR && arity_of(code) == 0)
+        vals[k * 32 + lane] = node_value<T>(code, T(0), T(0), T(0), T(0));
+    }
     int err = 0;
     const int64_t nchunks = (N + 31) / 32;
     // K constant sets, one after the other: grad_out is (B, M, N, K), set kk of
     // node k, point n at ((b M + k) N + n) K + kk
     for (int64_t kk = 0; kk < K; ++kk) {
-    for (int k = lane; k < L; k += 32) gsum[k] = T(0);
-    const T* Crow = C + b * c_sb + kk * c_sk;
-    const T* G = gout + (size_t)b * M * N * K + kk;
-    const int64_t rs = N * K;
-    __syncwarp();
-    for (int64_t c = 0; c < nchunks; ++c) {
-      const int64_t base = c * 32;
-      const int64_t n = base + lane;
-      const bool valid = n < N;
-      const int64_t nn = valid ? n : N - 1;
-      // the adjoint seeds (grad_out rows of this chunk) are in flight while the node
-      // values are recomputed.  Seeding with the raw values instead of 0 + grad_out
-      // (the reference's zeros_like(cache).add_(grad_output)) can only flip the sign
-      // of a zero seed, which no output can see: a zero adjoint contributes nothing
-      stage_rows<T>(adj, G, L, N, rs, K, base, lane, vec16);
-      forward_points<T>(tape, L, vals, X, n_x, nn, valid, Crow, c_sm, lane, nullptr, N);
-      cp_async_wait<0>();
-      __syncwarp();
-      for (int kk2 = L - 1; kk2 >= 0; --kk2) {
-        const uint32_t d = tape[kk2];
-        const int code = code_of(d);
-        const T g = adj[kk2 * 32 + lane];
-        if (code == LEARNABLE) {
-          const T part = warp_sum((valid && g != T(0)) ? g : T(0));
-          if (lane == 0) gsum[kk2] = M_<T>::add(gsum[kk2], part);
-          continue;
-        }
-        if (code == VAR) {
-          if (gX && valid && g != T(0)) atomicAdd(gX + nn * n_x + child0(d), g);
-          continue;
-        }
-        const int c0 = child0(d), c1 = child1(d);
-        bool a0, a1;
-        T o0, o1;
-        const int e = node_adjoint<T>(code, g, vals[c0 * 32 + lane], vals[c1 * 32 + lane], vals[kk2 * 32 + lane], a0,
-                                      o0, a1, o1);
-        if (valid) {
-          if (e && !err) err = e;
-          if (a0) adj[c0 * 32 + lane] = M_<T>::add(adj[c0 * 32 + lane], o0);
-          if (a1) adj[c1 * 32 + lane] = M_<T>::add(adj[c1 * 32 + lane], o1);
-        }
+      for (int k = lane; k < L; k += 32) gsum[k] = T(0);
+      const T* Crow = C + b * c_sb + kk * c_sk;
+      for (int j = 0; j < ncon; ++j) {
+        const int k = lcon[j];
+        vals[k * 32 + lane] = __ldg(Crow + (int64_t)k * c_sm);
       }
-      __syncwarp();  // every lane is done with the seeds before the next chunk's land
-    }
-    // gradient row of this set: constant nodes get their sums, everything else 0
-    T* gCrow = gC + (size_t)b * M * K + kk;
-    for (int64_t k = lane; k < M; k += 32) {
-      T val = T(0);
-      if (k < L && code_of(tape[k]) == LEARNABLE) val = gsum[k];
-      gCrow[k * K] = val;
-    }
-    __syncwarp();
+      const T* G = gout + (size_t)b * M * N * K + kk;
+      const int64_t rs = N * K;
+      __syncwarp();
+      for (int64_t c = 0; c < nchunks; ++c) {
+        const int64_t base = c * 32;
+        const int64_t n = base + lane;
+        const bool valid = n < N;
+        const int64_t nn = valid ? n : N - 1;
+        // the adjoint seeds (grad_out rows of this chunk) are in flight while the node
+        // values are recomputed.  Seeding with the raw values instead of 0 + grad_out
+        // (the reference's zeros_like(cache).add_(grad_output)) can only flip the sign
+        // of a zero seed, which no output can see: a zero adjoint contributes nothing
+        stage_rows<T>(adj, G, L, N, rs, K, base, lane, vec16);
+        for (int j = 0; j < nvar; ++j) {
+          const int k = lvar[j];
+          vals[k * 32 + lane] = __ldg(X + nn * n_x + child0(tape[k]));
+        }
+        for (int i = 0; i < nop; ++i) {
+          const uint32_t w0 = prog0[i];
+          const int code = (int)(w0 & 0xffu), k = (int)((w0 >> 8) & 0xfffu), c0 = (int)(w0 >> 20);
+          const int c1 = (int)prog1[i];
+          vals[k * 32 + lane] = node_value<T>(code, vals[c0 * 32 + lane], vals[c1 * 32 + lane], T(0), T(0));
+        }
+        cp_async_wait<0>();
+        __syncwarp();
+        for (int i = nop - 1; i >= 0; --i) {
+          const uint32_t w0 = prog0[i];
+          const int code = (int)(w0 & 0xffu), k = (int)((w0 >> 8) & 0xfffu), c0 = (int)(w0 >> 20);
+          const int c1 = (int)prog1[i];
+          bool a0, a1;
+          T o0, o1;
+          const int e = node_adjoint<T>(code, adj[k * 32 + lane], vals[c0 * 32 + lane], vals[c1 * 32 + lane],
+                                        vals[k * 32 + lane], a0, o0, a1, o1);
+          if (valid) {
+            if (e && !err) err = e;
+            if (a0) adj[c0 * 32 + lane] = M_<T>::add(adj[c0 * 32 + lane], o0);
+            if (a1) adj[c1 * 32 + lane] = M_<T>::add(adj[c1 * 32 + lane], o1);
+          }
+        }
+        // leaves: every contribution from the parents has arrived
+        for (int j = 0; j < ncon; ++j) {
+          const int k = lcon[j];
+          const T g = adj[k * 32 + lane];
+          const T part = warp_sum((valid && g != T(0)) ? g : T(0));
+          if (lane == 0) gsum[k] = M_<T>::add(gsum[k], part);
+        }
+        if (gX) {
+          for (int j = 0; j < nvar; ++j) {
+            const int k = lvar[j];
+            const T g = adj[k * 32 + lane];
+            if (valid && g != T(0)) atomicAdd(gX + nn * n_x + child0(tape[k]), g);
+          }
+        }
+        __syncwarp();  // every lane is done with the seeds before the next chunk's land
+      }
+      // gradient row of this set: constant nodes get their sums, everything else 0
+      T* gCrow = gC + (size_t)b * M * K + kk;
+      for (int64_t k = lane; k < M; k += 32) {
+        T val = T(0);
+        if (k < L && code_of(tape[k]) == LEARNABLE) val = gsum[k];
+        gCrow[k * K] = val;
+      }
+      __syncwarp();
     }  // sets
     err = __reduce_max_sync(0xffffffffu, err);
     if (err && lane == 0) report(status, err);
@@ -543,7 +607,8 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
   padding_check_kernel<T><<<(unsigned)pblocks, 256, 0, st>>>(gout, meta, B, M, N * K, status);
   rc = launch_check("padding_check_kernel");
   if (rc) return rc;
-  const size_t per_warp = align16((size_t)Lmax * 4) + 2 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
+  const size_t per_warp = align16((size_t)Lmax * 4) * 5 + 2 * (size_t)Lmax * 32 * sizeof(T) +
+                          align16((size_t)Lmax * sizeof(T));
   Shape sh;
   auto kern = K == 1 ? eval_backward_kernel<T, false> : eval_backward_kernel<T, true>;
   if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, B, sh)) {
