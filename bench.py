@@ -232,12 +232,8 @@ def barrier(world):
 
 
 def max_over_ranks(x, world, dev):
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-    return x
+    from cudasymbolicregression_gb300 import sharding
+    return sharding.max_over_ranks(x, device=dev) if world > 1 else x
 
 
 def timed_steps(step, steps, flush):
@@ -700,8 +696,8 @@ def run_search(args, rank, world, local):
                 e1.record()
                 e1.synchronize()
                 a["t"] += e0.elapsed_time(e1) / 1000.0
-                loss = res.loss
-                best = float(torch.where(torch.isfinite(loss), loss, torch.full_like(loss, float("inf"))).min())
+                from cudasymbolicregression_gb300 import sharding
+                best, _ = sharding.best_over_ranks(res.loss, offset=rank * B, device=dev)  # over all ranks
                 a["best"] = min(a["best"], best)
                 if a["first_hit_s"] is None and best < 1e-6:
                     a["first_hit_s"] = a["t"]

@@ -1,0 +1,74 @@
+"""Multi-process host logic (world_size 2, gloo on CPU): sharding, the job's time as
+the slowest rank's, and the best expression over all ranks."""
+import os
+import socket
+
+import pytest
+import torch
+import torch.multiprocessing as mp
+
+from cudasymbolicregression_gb300 import sharding
+
+
+def test_shard_range_partitions_exactly():
+    for total in (0, 1, 7, 16384, 16385):
+        for world in (1, 2, 3, 8):
+            spans = [sharding.shard_range(total, r, world) for r in range(world)]
+            assert spans[0][0] == 0 and spans[-1][1] == total
+            for (a, b), (c, d) in zip(spans, spans[1:]):
+                assert b == c and b >= a
+            sizes = [b - a for a, b in spans]
+            assert max(sizes) - min(sizes) <= 1
+    with pytest.raises(ValueError):
+        sharding.shard_range(10, 2, 2)
+
+
+def test_single_process_fallbacks():
+    assert sharding.max_over_ranks(3.5) == 3.5
+    loss = torch.tensor([float("nan"), 2.0, 0.5, float("inf")])
+    assert sharding.best_over_ranks(loss, offset=10) == (0.5, 12)
+    assert sharding.best_over_ranks(torch.tensor([float("nan")]), offset=0) == (float("inf"), -1)
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, results):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        total = 1001
+        start, stop = sharding.shard_range(total, rank, world)
+        # every rank fits its slice; the losses are a known function of the global index
+        idx = torch.arange(start, stop, dtype=torch.float64)
+        loss = (idx - 637.0).abs() + 0.25
+        loss[::7] = float("nan")  # some problems end NaN
+        t = sharding.max_over_ranks(0.1 * (rank + 1))
+        best = sharding.best_over_ranks(loss.float(), offset=start)
+        none = sharding.best_over_ranks(torch.full((3,), float("nan")), offset=start)
+        results[rank] = (start, stop, t, best, none)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_ranks_gloo():
+    ctx = mp.get_context("spawn")
+    manager = ctx.Manager()
+    results = manager.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, results)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    r0, r1 = results[0], results[1]
+    assert r0[0] == 0 and r0[1] == r1[0] and r1[1] == 1001
+    assert r0[2] == pytest.approx(0.2) and r1[2] == pytest.approx(0.2)  # the slowest rank's time on both
+    assert r0[3] == r1[3] == (pytest.approx(0.25), 637)               # the global minimum and its index
+    assert r0[4] == r1[4] == (float("inf"), -1)
