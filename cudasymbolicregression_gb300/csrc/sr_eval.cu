@@ -291,80 +291,138 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int kPending>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory"); }
 
-// Copies rows 0..L-1, points base..base+31 of the gradient block G (node k, point n
-// at G[k * rs + n * es]) into buf[k][32] (zero beyond N).  vec16 (es == 1, rows
-// 16-byte aligned): each lane moves 16 bytes (E = 16 / sizeof(T) points; E rows per
-// instruction); otherwise one element per lane and row.
-template <typename T>
+// Copies rows 0..L-1, points base..base+32V-1 of the gradient block G (node k, point
+// n at G[k * rs + n * es]) into buf[k][32 V] (zero beyond N).  vec16 (es == 1, rows
+// 16-byte aligned): each lane moves 16 bytes (E = 16 / sizeof(T) points), 32 E / (32 V)
+// rows per instruction; otherwise one element per lane, point and row.
+template <typename T, int V>
 __device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N, int64_t rs, int64_t es,
                                            int64_t base, int lane, bool vec16) {
+  constexpr int RW = 32 * V;
   if (vec16) {
     constexpr int E = 16 / sizeof(T);
-    constexpr int kLanesPerRow = 32 / E;
+    constexpr int kLanesPerRow = RW / E;
+    static_assert(kLanesPerRow <= 32 && 32 % kLanesPerRow == 0, "row width");
+    constexpr int kRowsPerStep = 32 / kLanesPerRow;
     const int r0 = lane / kLanesPerRow, p = (lane % kLanesPerRow) * E;
     const int64_t left = N - (base + p);
     const int bytes = left >= E ? 16 : (left > 0 ? (int)left * (int)sizeof(T) : 0);
-    for (int k = r0; k < L; k += E) {
+    for (int k = r0; k < L; k += kRowsPerStep) {
       const T* src = bytes ? G + (size_t)k * rs + base + p : G;
-      cp_async(buf + k * 32 + p, src, 16, bytes);
+      cp_async(buf + k * RW + p, src, 16, bytes);
     }
   } else {
-    const int64_t n = base + lane;
-    const int bytes = n < N ? (int)sizeof(T) : 0;
-    for (int k = 0; k < L; ++k) {
-      const T* src = bytes ? G + (size_t)k * rs + n * es : G;
-      cp_async(buf + k * 32 + lane, src, (int)sizeof(T), bytes);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int64_t n = base + v * 32 + lane;
+      const int bytes = n < N ? (int)sizeof(T) : 0;
+      for (int k = 0; k < L; ++k) {
+        const T* src = bytes ? G + (size_t)k * rs + n * es : G;
+        cp_async(buf + k * RW + v * 32 + lane, src, (int)sizeof(T), bytes);
+      }
     }
   }
   cp_async_commit();
 }
 
 // ------------------------------------------------------------------------------------
-// Adjoint.  One warp per tape (persistent, longest first), 32 points per chunk.
-// Per tape the warp compacts its nodes into an operator list (code, own row, child
-// rows in one word each) and lists of its constant and variable leaves; leaf values
-// live in their rows (fixed constants once per tape, learnable constants once per
-// constant set, variables once per chunk).  Per chunk the output-gradient rows are
-// staged into shared memory with cp.async while the operator nodes are recomputed
-// (the saved cache is never read); the reverse sweep then runs over the operator list
-// only, adding contributions into the children's rows in the reference's order
-// (parents from the last to the first, child 0 before child 1), and the leaves are
-// reduced afterwards: each constant's gradient summed over points in a fixed order
-// (per chunk a butterfly, then in chunk order), so grad_C is deterministic.
+// Adjoint.  One warp per tape, 32 V points per chunk (V points per lane: the per-node
+// decode and dispatch serve V points).  The host launches one persistent grid per
+// class of tape lengths (Llo, Lhi], each sized for its class's shared memory, so short
+// tapes run at the occupancy their size allows; every grid scans the whole work order
+// and takes the tapes of its class.  Per tape the warp compiles its nodes into an
+// operator program (NO_OP nodes included: their value NaN and their adjoint check
+// matter) whose operands are precomputed addresses in the warp's shared memory:
+//   source word = byte offset (bits 0..23) | lane stride in bytes (bits 24..31): the
+//                 value row of an operator node or a variable leaf (stride sizeof(T))
+//                 or the broadcast entry of any other leaf (stride 0);
+//   adjoint destination = byte offset of the child's adjoint row.
+// Every node has an adjoint row.  Per chunk the output-gradient rows are staged into
+// them with cp.async while the operator nodes are recomputed (the saved cache is never
+// read); the reverse sweep then adds the contributions into the children's rows in the
+// reference's order (parents from the last to the first, child 0 before child 1), and
+// the leaves are reduced afterwards.  A learnable constant's operand is a broadcast
+// entry, so its value row is free and holds its per-lane gradient sums over the
+// chunks; one butterfly per constant and set ends the sum (a fixed order: grad_C is
+// deterministic).
 // ------------------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ size_t backward_warp_bytes(int Lmax) {
-  return align16((size_t)Lmax * 4) * 5 + 2 * (size_t)Lmax * 32 * sizeof(T) + align16((size_t)Lmax * sizeof(T));
+struct BwdLayout {
+  uint32_t pcode, psa, psb, prow, pda, pdb, lcon, lvar, bc, vals, adj, bytes;
+};
+
+template <typename T, int V>
+__host__ __device__ __forceinline__ BwdLayout backward_layout(int Lmax) {
+  const uint32_t lb = (uint32_t)align16((size_t)Lmax * 4);
+  BwdLayout l;
+  l.pcode = lb;  // the tape words sit at offset 0
+  l.psa = 2 * lb;
+  l.psb = 3 * lb;
+  l.prow = 4 * lb;
+  l.pda = 5 * lb;
+  l.pdb = 6 * lb;
+  l.lcon = 7 * lb;
+  l.lvar = 8 * lb;
+  l.bc = 9 * lb;
+  l.vals = l.bc + (uint32_t)align16((size_t)(Lmax + 1) * sizeof(T));
+  const uint32_t rows = (uint32_t)Lmax * 32u * V * (uint32_t)sizeof(T);
+  l.adj = l.vals + rows;
+  l.bytes = l.adj + rows;
+  return l;
 }
 
-template <typename T, bool kMulti>
-__global__ void __launch_bounds__(256, 1) eval_backward_kernel(
+template <typename T>
+__device__ __forceinline__ T lds_operand(const unsigned char* wb, uint32_t w, int li) {
+  return *reinterpret_cast<const T*>(wb + (w & 0xffffffu) + (uint32_t)li * (w >> 24));
+}
+
+template <typename T>
+__device__ __forceinline__ T* row_at(unsigned char* wb, uint32_t off, int li) {
+  return reinterpret_cast<T*>(wb + off) + li;
+}
+
+template <typename T, bool kMulti, int V>
+__global__ void __launch_bounds__(256, 4) eval_backward_kernel(
     const T* __restrict__ X, int64_t N, int64_t n_x, const uint32_t* __restrict__ desc,
-    const int32_t* __restrict__ meta, const int32_t* __restrict__ order, int64_t B, int64_t M, int Lmax,
+    const int32_t* __restrict__ meta, const int32_t* __restrict__ order, int64_t B, int64_t M, int Llo, int Lhi,
     const T* __restrict__ C, int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K_, const T* __restrict__ gout,
     T* __restrict__ gC, T* __restrict__ gX, int32_t* __restrict__ status, bool vec16) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t K = kMulti ? K_ : 1;  // one constant set: the strides fold at compile time
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  const size_t lb = align16((size_t)Lmax * 4);
-  const size_t vbytes = (size_t)Lmax * 32 * sizeof(T);
-  unsigned char* base_ptr = smem + warp * backward_warp_bytes<T>(Lmax);
-  uint32_t* tape = reinterpret_cast<uint32_t*>(base_ptr);
-  uint32_t* prog0 = reinterpret_cast<uint32_t*>(base_ptr + lb);      // code | row << 8 | child0 << 20
-  uint32_t* prog1 = reinterpret_cast<uint32_t*>(base_ptr + 2 * lb);  // child1
-  int* lcon = reinterpret_cast<int*>(base_ptr + 3 * lb);             // learnable leaves
-  int* lvar = reinterpret_cast<int*>(base_ptr + 4 * lb);             // variable leaves
-  T* vals = reinterpret_cast<T*>(base_ptr + 5 * lb);
-  T* adj = reinterpret_cast<T*>(base_ptr + 5 * lb + vbytes);
-  T* gsum = reinterpret_cast<T*>(base_ptr + 5 * lb + 2 * vbytes);
+  constexpr uint32_t RW = 32u * V;                       // elements per row
+  constexpr uint32_t RB = RW * (uint32_t)sizeof(T);      // bytes per row
+  constexpr uint32_t kRowStride = (uint32_t)sizeof(T) << 24;
+  const BwdLayout ly = backward_layout<T, V>(Lhi);
+  unsigned char* wb = smem + (size_t)warp * ly.bytes;
+  uint32_t* tape = reinterpret_cast<uint32_t*>(wb);
+  uint32_t* pcode = reinterpret_cast<uint32_t*>(wb + ly.pcode);
+  uint32_t* psa = reinterpret_cast<uint32_t*>(wb + ly.psa);
+  uint32_t* psb = reinterpret_cast<uint32_t*>(wb + ly.psb);
+  uint32_t* prow = reinterpret_cast<uint32_t*>(wb + ly.prow);
+  uint32_t* pda = reinterpret_cast<uint32_t*>(wb + ly.pda);
+  uint32_t* pdb = reinterpret_cast<uint32_t*>(wb + ly.pdb);
+  int* lcon = reinterpret_cast<int*>(wb + ly.lcon);
+  int* lvar = reinterpret_cast<int*>(wb + ly.lvar);
+  T* bc = reinterpret_cast<T*>(wb + ly.bc);
+  T* vals = reinterpret_cast<T*>(wb + ly.vals);
+  T* adj = reinterpret_cast<T*>(wb + ly.adj);
+  const uint32_t adj_delta = ly.adj - ly.vals;
   const unsigned below = (1u << lane) - 1u;
   for (int64_t ti = (int64_t)blockIdx.x * nwarp + warp; ti < B; ti += (int64_t)gridDim.x * nwarp) {
     const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
+    if (L <= Llo || L > Lhi) continue;  // another class's grid takes it (warp-uniform)
     for (int k = lane; k < L; k += 32) tape[k] = desc[b * M + k];
+    if (lane == 0) bc[0] = T(0);
     __syncwarp();
-    // compaction: operator nodes (NO_OP included: its value is NaN and its adjoint
-    // check matters), learnable and variable leaves; fixed leaves get their rows now
+    // source word of operand node c: its value row, or its broadcast entry
+    auto src_word = [&](int c) -> uint32_t {
+      const int cc = code_of(tape[c]);
+      if (cc == NO_OP || cc == VAR || arity_of(cc) >= 1) return (ly.vals + (uint32_t)c * RB) | kRowStride;
+      return ly.bc + (uint32_t)(1 + c) * (uint32_t)sizeof(T);
+    };
+    // compaction: operator nodes, learnable and variable leaves; the broadcast
+    // entries of fixed leaves (and of codes that evaluate to 0) now
     int nop = 0, ncon = 0, nvar = 0;
     for (int k0 = 0; k0 < L; k0 += 32) {
       const int k = k0 + lane;
@@ -377,11 +435,25 @@ __global__ void __launch_bounds__(256, 1) eval_backward_kernel(
       const unsigned mv = __ballot_sync(0xffffffffu, isvar);
       if (isop) {
         const int ar = arity_of(code);
-        const uint32_t c0 = ar >= 1 ? (uint32_t)child0(d) : (uint32_t)k;
-        const uint32_t c1 = ar == 2 ? (uint32_t)child1(d) : (uint32_t)k;
         const int pos = nop + __popc(mo & below);
-        prog0[pos] = (uint32_t)code | ((uint32_t)k << 8) | (c0 << 20);
-        prog1[pos] = c1;
+        const uint32_t own = ly.adj + (uint32_t)k * RB;  // never written through (arity < 2)
+        uint32_t sa = ly.bc, sb = ly.bc, da = own, db = own;
+        if (ar >= 1) {
+          sa = src_word(child0(d));
+          da = ly.adj + (uint32_t)child0(d) * RB;
+        }
+        if (ar == 2) {
+          sb = src_word(child1(d));
+          db = ly.adj + (uint32_t)child1(d) * RB;
+        }
+        pcode[pos] = (uint32_t)code;
+        psa[pos] = sa;
+        psb[pos] = sb;
+        prow[pos] = ly.vals + (uint32_t)k * RB;
+        pda[pos] = da;
+        pdb[pos] = db;
+      } else if (k < L && !iscon && !isvar) {
+        bc[1 + k] = node_value<T>(code, T(0), T(0), T(0), T(0));
       }
       if (iscon) lcon[ncon + __popc(mc & below)] = k;
       if (isvar) lvar[nvar + __popc(mv & below)] = k;
@@ -389,82 +461,108 @@ __global__ void __launch_bounds__(256, 1) eval_backward_kernel(
       ncon += __popc(mc);
       nvar += __popc(mv);
     }
-    for (int k = 0; k < L; ++k) {
-      const int code = code_of(tape[k]);
-      if (code != NO_OP && code != LEARNABLE && code != VAR && arity_of(code) == 0)
-        vals[k * 32 + lane] = node_value<T>(code, T(0), T(0), T(0), T(0));
-    }
     int err = 0;
-    const int64_t nchunks = (N + 31) / 32;
+    const int64_t nchunks = (N + RW - 1) / RW;
     // K constant sets, one after the other: grad_out is (B, M, N, K), set kk of
     // node k, point n at ((b M + k) N + n) K + kk
     for (int64_t kk = 0; kk < K; ++kk) {
-      for (int k = lane; k < L; k += 32) gsum[k] = T(0);
       const T* Crow = C + b * c_sb + kk * c_sk;
+      for (int j = lane; j < ncon; j += 32) bc[1 + lcon[j]] = __ldg(Crow + (int64_t)lcon[j] * c_sm);
       for (int j = 0; j < ncon; ++j) {
-        const int k = lcon[j];
-        vals[k * 32 + lane] = __ldg(Crow + (int64_t)k * c_sm);
+#pragma unroll
+        for (int v = 0; v < V; ++v) vals[lcon[j] * RW + v * 32 + lane] = T(0);
       }
       const T* G = gout + (size_t)b * M * N * K + kk;
       const int64_t rs = N * K;
       __syncwarp();
       for (int64_t c = 0; c < nchunks; ++c) {
-        const int64_t base = c * 32;
-        const int64_t n = base + lane;
-        const bool valid = n < N;
-        const int64_t nn = valid ? n : N - 1;
+        const int64_t base = c * RW;
+        int64_t nn[V];
+        bool valid[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const int64_t n = base + v * 32 + lane;
+          valid[v] = n < N;
+          nn[v] = valid[v] ? n : N - 1;
+        }
         // the adjoint seeds (grad_out rows of this chunk) are in flight while the node
         // values are recomputed.  Seeding with the raw values instead of 0 + grad_out
         // (the reference's zeros_like(cache).add_(grad_output)) can only flip the sign
         // of a zero seed, which no output can see: a zero adjoint contributes nothing
-        stage_rows<T>(adj, G, L, N, rs, K, base, lane, vec16);
+        stage_rows<T, V>(adj, G, L, N, rs, K, base, lane, vec16);
         for (int j = 0; j < nvar; ++j) {
           const int k = lvar[j];
-          vals[k * 32 + lane] = __ldg(X + nn * n_x + child0(tape[k]));
+          const int var = child0(tape[k]);
+#pragma unroll
+          for (int v = 0; v < V; ++v) vals[k * RW + v * 32 + lane] = __ldg(X + nn[v] * n_x + var);
         }
+        __syncwarp();
         for (int i = 0; i < nop; ++i) {
-          const uint32_t w0 = prog0[i];
-          const int code = (int)(w0 & 0xffu), k = (int)((w0 >> 8) & 0xfffu), c0 = (int)(w0 >> 20);
-          const int c1 = (int)prog1[i];
-          vals[k * 32 + lane] = node_value<T>(code, vals[c0 * 32 + lane], vals[c1 * 32 + lane], T(0), T(0));
+          const int code = (int)pcode[i];
+          const uint32_t sa = psa[i], sb = psb[i], pr = prow[i];
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            const int li = v * 32 + lane;
+            *row_at<T>(wb, pr, li) = node_value<T>(code, lds_operand<T>(wb, sa, li), lds_operand<T>(wb, sb, li), T(0), T(0));
+          }
         }
         cp_async_wait<0>();
         __syncwarp();
         for (int i = nop - 1; i >= 0; --i) {
-          const uint32_t w0 = prog0[i];
-          const int code = (int)(w0 & 0xffu), k = (int)((w0 >> 8) & 0xfffu), c0 = (int)(w0 >> 20);
-          const int c1 = (int)prog1[i];
-          bool a0, a1;
-          T o0, o1;
-          const int e = node_adjoint<T>(code, adj[k * 32 + lane], vals[c0 * 32 + lane], vals[c1 * 32 + lane],
-                                        vals[k * 32 + lane], a0, o0, a1, o1);
-          if (valid) {
-            if (e && !err) err = e;
-            if (a0) adj[c0 * 32 + lane] = M_<T>::add(adj[c0 * 32 + lane], o0);
-            if (a1) adj[c1 * 32 + lane] = M_<T>::add(adj[c1 * 32 + lane], o1);
+          const int code = (int)pcode[i];
+          const uint32_t sa = psa[i], sb = psb[i], pr = prow[i], da = pda[i], db = pdb[i];
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            const int li = v * 32 + lane;
+            bool a0, a1;
+            T o0, o1;
+            const int e = node_adjoint<T>(code, *row_at<T>(wb, pr + adj_delta, li), lds_operand<T>(wb, sa, li),
+                                          lds_operand<T>(wb, sb, li), *row_at<T>(wb, pr, li), a0, o0, a1, o1);
+            if (valid[v]) {
+              if (e && !err) err = e;
+              if (a0) { T* d = row_at<T>(wb, da, li); *d = M_<T>::add(*d, o0); }
+              if (a1) { T* d = row_at<T>(wb, db, li); *d = M_<T>::add(*d, o1); }
+            }
           }
         }
         // leaves: every contribution from the parents has arrived
         for (int j = 0; j < ncon; ++j) {
           const int k = lcon[j];
-          const T g = adj[k * 32 + lane];
-          const T part = warp_sum((valid && g != T(0)) ? g : T(0));
-          if (lane == 0) gsum[k] = M_<T>::add(gsum[k], part);
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            const T g = adj[k * RW + v * 32 + lane];
+            if (valid[v] && g != T(0)) vals[k * RW + v * 32 + lane] = M_<T>::add(vals[k * RW + v * 32 + lane], g);
+          }
         }
         if (gX) {
           for (int j = 0; j < nvar; ++j) {
             const int k = lvar[j];
-            const T g = adj[k * 32 + lane];
-            if (valid && g != T(0)) atomicAdd(gX + nn * n_x + child0(tape[k]), g);
+            const int var = child0(tape[k]);
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+              const T g = adj[k * RW + v * 32 + lane];
+              if (valid[v] && g != T(0)) atomicAdd(gX + nn[v] * n_x + var, g);
+            }
           }
         }
         __syncwarp();  // every lane is done with the seeds before the next chunk's land
       }
+      // the constants' sums (lane partials in point order, then a butterfly) replace
+      // their values in the broadcast entries
+      for (int j = 0; j < ncon; ++j) {
+        const int k = lcon[j];
+        T part = vals[k * RW + lane];
+#pragma unroll
+        for (int v = 1; v < V; ++v) part = M_<T>::add(part, vals[k * RW + v * 32 + lane]);
+        part = warp_sum(part);
+        if (lane == 0) bc[1 + k] = part;
+      }
+      __syncwarp();
       // gradient row of this set: constant nodes get their sums, everything else 0
       T* gCrow = gC + (size_t)b * M * K + kk;
       for (int64_t k = lane; k < M; k += 32) {
         T val = T(0);
-        if (k < L && code_of(tape[k]) == LEARNABLE) val = gsum[k];
+        if (k < L && code_of(tape[k]) == LEARNABLE) val = bc[1 + k];
         gCrow[k * K] = val;
       }
       __syncwarp();
@@ -585,6 +683,50 @@ static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* de
   return launch_check("eval_forward_kernel");
 }
 
+template <typename T, bool kMulti, int V>
+static int launch_backward_v(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
+                             const int32_t* order, int64_t B, int64_t M, int Llo, int Lhi, const T* C, int64_t c_sb,
+                             int64_t c_sm, int64_t c_sk, int64_t K, const T* gout, T* gC, T* gX, int32_t* status,
+                             bool vec16, cudaStream_t st) {
+  const size_t per_warp = backward_layout<T, V>(Lhi).bytes;
+  Shape sh;
+  auto kern = eval_backward_kernel<T, kMulti, V>;
+  if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, B, sh)) {
+    set_error("tape of %d nodes does not fit in shared memory", Lhi);
+    return SR_ERR_UNSUPPORTED;
+  }
+  kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb,
+                                                           c_sm, c_sk, K, gout, gC, gX, status, vec16);
+  return launch_check("eval_backward_kernel");
+}
+
+// Points per lane of the adjoint for tapes of up to Lhi nodes.  One: with two, the
+// node loop ran the points one after the other (their shared-memory rows may alias)
+// at half the warps, and the adjoint took 1.9x as long on a GB300.
+template <typename T>
+static int backward_points_per_lane(int64_t N, int Lhi) {
+  (void)N;
+  (void)Lhi;
+  return 1;
+}
+
+template <typename T>
+static int launch_backward_class(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
+                                 const int32_t* order, int64_t B, int64_t M, int Llo, int Lhi, const T* C,
+                                 int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const T* gout, T* gC, T* gX,
+                                 int32_t* status, bool vec16, cudaStream_t st) {
+  const int V = backward_points_per_lane<T>(N, Lhi);
+  if (K == 1)
+    return V == 2 ? launch_backward_v<T, false, 2>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk,
+                                                   K, gout, gC, gX, status, vec16, st)
+                  : launch_backward_v<T, false, 1>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk,
+                                                   K, gout, gC, gX, status, vec16, st);
+  return V == 2 ? launch_backward_v<T, true, 2>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K,
+                                                gout, gC, gX, status, vec16, st)
+                : launch_backward_v<T, true, 1>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K,
+                                                gout, gC, gX, status, vec16, st);
+}
+
 template <typename T>
 static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                            const int32_t* order, int64_t B, int64_t M, int32_t max_len, const T* C, int64_t c_sb,
@@ -607,20 +749,21 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
   padding_check_kernel<T><<<(unsigned)pblocks, 256, 0, st>>>(gout, meta, B, M, N * K, status);
   rc = launch_check("padding_check_kernel");
   if (rc) return rc;
-  const size_t per_warp = align16((size_t)Lmax * 4) * 5 + 2 * (size_t)Lmax * 32 * sizeof(T) +
-                          align16((size_t)Lmax * sizeof(T));
-  Shape sh;
-  auto kern = K == 1 ? eval_backward_kernel<T, false> : eval_backward_kernel<T, true>;
-  if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, B, sh)) {
-    set_error("tape of %d nodes does not fit in shared memory", Lmax);
-    return SR_ERR_UNSUPPORTED;
-  }
-  // 16-byte staging needs every (tape, row, 32-point chunk) start 16-byte aligned
+  // 16-byte staging needs every (tape, row, chunk) start 16-byte aligned
   const bool vec16 =
       K == 1 && (reinterpret_cast<uintptr_t>(gout) % 16 == 0) && (N % (16 / (int64_t)sizeof(T)) == 0);
-  kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, Lmax, C, c_sb, c_sm,
-                                                           c_sk, K, gout, gC, gX, status, vec16);
-  return launch_check("eval_backward_kernel");
+  // one persistent grid per class of tape lengths (Llo, Lhi]: (32, Lmax], (16, 32],
+  // [0, 16], as far as Lmax reaches
+  int cls[3][2], nc = 0;
+  if (Lmax > 32) { cls[nc][0] = 32; cls[nc][1] = Lmax; ++nc; }
+  if (Lmax > 16) { cls[nc][0] = 16; cls[nc][1] = Lmax < 32 ? Lmax : 32; ++nc; }
+  cls[nc][0] = -1; cls[nc][1] = Lmax < 16 ? Lmax : 16; ++nc;
+  for (int ci = 0; ci < nc; ++ci) {
+    rc = launch_backward_class<T>(X, N, n_x, desc, meta, order, B, M, cls[ci][0], cls[ci][1], C, c_sb, c_sm, c_sk, K,
+                                  gout, gC, gX, status, vec16, st);
+    if (rc) return rc;
+  }
+  return SR_OK;
 }
 
 }  // namespace sr
