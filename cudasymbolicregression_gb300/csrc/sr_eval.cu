@@ -146,30 +146,44 @@ __device__ __forceinline__ void warp_fill_nan(T* p, size_t count, int lane) {
   for (size_t i = head + nvec * kVec + lane; i < count; i += 32) __stcs(p + i, qnan);
 }
 
-// Node values of one tape at the 32 points nn (one per lane) into vals[k][lane];
-// with `out` also streamed to the cache as they are produced (node k, point n at
-// out[k * out_rs + n * out_es]).
+// Shared-memory layout of one warp of the forward kernel: the tape words, the
+// operator program (dense code | node << 8, two operand source words), the lists of
+// variable leaves and of broadcast leaves (learnable, fixed, codes that evaluate to
+// 0), the broadcast entries (entry 0 = 0, entry 1 + k = value of leaf k) and one
+// value row of 32 points per node.
+struct FwdLayout {
+  uint32_t pw, psa, psb, lvar, lbc, bc, vals, bytes;
+};
+
 template <typename T>
-__device__ __forceinline__ void forward_points(const uint32_t* __restrict__ tape, int L, T* __restrict__ vals,
-                                               const T* __restrict__ X, int64_t n_x, int64_t nn, bool valid,
-                                               const T* __restrict__ Crow, int64_t c_sm, int lane,
-                                               T* __restrict__ out, int64_t out_rs, int64_t out_es = 1) {
-  for (int k = 0; k < L; ++k) {
-    const uint32_t d = tape[k];
-    const int code = code_of(d);
-    T r;
-    if (code == VAR) {
-      r = __ldg(X + nn * n_x + child0(d));
-    } else if (code == LEARNABLE) {
-      r = __ldg(Crow + (int64_t)k * c_sm);
-    } else {
-      r = node_value<T>(code, vals[child0(d) * 32 + lane], vals[child1(d) * 32 + lane], T(0), T(0));
-    }
-    vals[k * 32 + lane] = r;
-    if (out && valid) __stcs(out + (size_t)k * out_rs + nn * out_es, r);
-  }
+__host__ __device__ __forceinline__ FwdLayout forward_layout(int Lmax) {
+  const uint32_t lb = (uint32_t)align16((size_t)Lmax * 4);
+  FwdLayout l;
+  l.pw = lb;  // the tape words sit at offset 0
+  l.psa = 2 * lb;
+  l.psb = 3 * lb;
+  l.lvar = 4 * lb;
+  l.lbc = 5 * lb;
+  l.bc = 6 * lb;
+  l.vals = l.bc + (uint32_t)align16((size_t)(Lmax + 1) * sizeof(T));
+  l.bytes = l.vals + (uint32_t)Lmax * 32u * (uint32_t)sizeof(T);
+  return l;
 }
 
+template <typename T>
+__device__ __forceinline__ T lds_operand(const unsigned char* wb, uint32_t w, int li) {
+  return *reinterpret_cast<const T*>(wb + (w & 0xffffffu) + (uint32_t)li * (w >> 24));
+}
+
+template <typename T>
+__device__ __forceinline__ T* row_at(unsigned char* wb, uint32_t off, int li) {
+  return reinterpret_cast<T*>(wb + off) + li;
+}
+
+// Per unit the warp compiles its tape into an operator program whose operands are
+// precomputed addresses (the value row of an operator node or variable leaf, or the
+// broadcast entry of any other leaf), so the point loop runs the leaves as plain
+// loads and stores and dispatches on the opcode for operator nodes only.
 template <typename T, bool kMulti>
 __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__ X, int64_t N, int64_t n_x,
                                                            const uint32_t* __restrict__ desc,
@@ -181,10 +195,19 @@ __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t K = kMulti ? K_ : 1;  // one constant set: the strides fold at compile time
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  const size_t tbytes = align16((size_t)Lmax * 4);
-  const size_t per_warp = tbytes + (size_t)Lmax * 32 * sizeof(T);
-  uint32_t* tape = reinterpret_cast<uint32_t*>(smem + warp * per_warp);
-  T* vals = reinterpret_cast<T*>(smem + warp * per_warp + tbytes);
+  constexpr uint32_t RB = 32u * (uint32_t)sizeof(T);
+  constexpr uint32_t kRowStride = (uint32_t)sizeof(T) << 24;
+  const FwdLayout ly = forward_layout<T>(Lmax);
+  unsigned char* wb = smem + (size_t)warp * ly.bytes;
+  uint32_t* tape = reinterpret_cast<uint32_t*>(wb);
+  uint32_t* pw = reinterpret_cast<uint32_t*>(wb + ly.pw);
+  uint32_t* psa = reinterpret_cast<uint32_t*>(wb + ly.psa);
+  uint32_t* psb = reinterpret_cast<uint32_t*>(wb + ly.psb);
+  int* lvar = reinterpret_cast<int*>(wb + ly.lvar);
+  int* lbc = reinterpret_cast<int*>(wb + ly.lbc);
+  T* bc = reinterpret_cast<T*>(wb + ly.bc);
+  T* vals = reinterpret_cast<T*>(wb + ly.vals);
+  const unsigned below = (1u << lane) - 1u;
   const int64_t nslices = (N + kSlice - 1) / kSlice;
   const int64_t units = B * nslices;
   for (int64_t u = (int64_t)blockIdx.x * nwarp + warp; u < units; u += (int64_t)gridDim.x * nwarp) {
@@ -192,17 +215,77 @@ __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__
     const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
     for (int k = lane; k < L; k += 32) tape[k] = desc[b * M + k];
+    if (lane == 0) bc[0] = T(0);
     __syncwarp();
+    auto src_word = [&](int c) -> uint32_t {
+      const int cc = code_of(tape[c]);
+      if (cc == NO_OP || cc == VAR || arity_of(cc) >= 1) return (ly.vals + (uint32_t)c * RB) | kRowStride;
+      return ly.bc + (uint32_t)(1 + c) * (uint32_t)sizeof(T);
+    };
+    int nop = 0, nvar = 0, nbc = 0;
+    for (int k0 = 0; k0 < L; k0 += 32) {
+      const int k = k0 + lane;
+      const uint32_t d = k < L ? tape[k] : 0u;
+      const int code = k < L ? code_of(d) : -1;
+      const bool isop = k < L && (code == NO_OP || arity_of(code) >= 1);
+      const bool isvar = code == VAR;
+      const bool isbc = k < L && !isop && !isvar;
+      const unsigned mo = __ballot_sync(0xffffffffu, isop);
+      const unsigned mv = __ballot_sync(0xffffffffu, isvar);
+      const unsigned mb = __ballot_sync(0xffffffffu, isbc);
+      if (isop) {
+        const int ar = arity_of(code);
+        const int pos = nop + __popc(mo & below);
+        pw[pos] = (uint32_t)dense_op(code) | ((uint32_t)k << 8);
+        psa[pos] = ar >= 1 ? src_word(child0(d)) : ly.bc;
+        psb[pos] = ar == 2 ? src_word(child1(d)) : ly.bc;
+      }
+      if (isvar) lvar[nvar + __popc(mv & below)] = k;
+      if (isbc) {
+        lbc[nbc + __popc(mb & below)] = k;
+        if (code != LEARNABLE) bc[1 + k] = node_value<T>(code, T(0), T(0), T(0), T(0));
+      }
+      nop += __popc(mo);
+      nvar += __popc(mv);
+      nbc += __popc(mb);
+    }
     // K constant sets: the cache is (B, M, N, K), set kk of node k, point n at
     // ((b M + k) N + n) K + kk
     T* out = cache + (size_t)b * M * N * K;
+    const int64_t rs = N * K;
     const int64_t n0 = sl * kSlice, n1 = min(N, n0 + kSlice);
     for (int64_t kk = 0; kk < K; ++kk) {
+      __syncwarp();  // every lane is done with the previous set's broadcast entries
       const T* Crow = C + b * c_sb + kk * c_sk;
+      for (int j = lane; j < nbc; j += 32) {
+        const int k = lbc[j];
+        if (code_of(tape[k]) == LEARNABLE) bc[1 + k] = __ldg(Crow + (int64_t)k * c_sm);
+      }
+      __syncwarp();
       for (int64_t base = n0; base < n1; base += 32) {
         const int64_t n = base + lane;
         const bool valid = n < n1;
-        forward_points<T>(tape, L, vals, X, n_x, valid ? n : n1 - 1, valid, Crow, c_sm, lane, out + kk, N * K, K);
+        const int64_t nn = valid ? n : n1 - 1;
+        T* o = out + kk + nn * K;  // node k of this point at o[k * rs]
+        for (int j = 0; j < nvar; ++j) {
+          const int k = lvar[j];
+          const T x = __ldg(X + nn * n_x + child0(tape[k]));
+          vals[k * 32 + lane] = x;
+          if (valid) __stcs(o + (int64_t)k * rs, x);
+        }
+        if (valid) {
+          for (int j = 0; j < nbc; ++j) {
+            const int k = lbc[j];
+            __stcs(o + (int64_t)k * rs, bc[1 + k]);
+          }
+        }
+        for (int i = 0; i < nop; ++i) {
+          const uint32_t w = pw[i];
+          const int k = (int)(w >> 8);
+          const T r = op_value<T>((int)(w & 0xffu), lds_operand<T>(wb, psa[i], lane), lds_operand<T>(wb, psb[i], lane));
+          vals[k * 32 + lane] = r;
+          if (valid) __stcs(o + (int64_t)k * rs, r);
+        }
       }
     }
     // rows after the last real node: NaN (one contiguous block when the unit spans all points)
@@ -370,16 +453,6 @@ __host__ __device__ __forceinline__ BwdLayout backward_layout(int Lmax) {
   return l;
 }
 
-template <typename T>
-__device__ __forceinline__ T lds_operand(const unsigned char* wb, uint32_t w, int li) {
-  return *reinterpret_cast<const T*>(wb + (w & 0xffffffu) + (uint32_t)li * (w >> 24));
-}
-
-template <typename T>
-__device__ __forceinline__ T* row_at(unsigned char* wb, uint32_t off, int li) {
-  return reinterpret_cast<T*>(wb + off) + li;
-}
-
 template <typename T, bool kMulti, int V>
 __global__ void __launch_bounds__(256, 4) eval_backward_kernel(
     const T* __restrict__ X, int64_t N, int64_t n_x, const uint32_t* __restrict__ desc,
@@ -446,7 +519,7 @@ __global__ void __launch_bounds__(256, 4) eval_backward_kernel(
           sb = src_word(child1(d));
           db = ly.adj + (uint32_t)child1(d) * RB;
         }
-        pcode[pos] = (uint32_t)code;
+        pcode[pos] = (uint32_t)dense_op(code);
         psa[pos] = sa;
         psb[pos] = sb;
         prow[pos] = ly.vals + (uint32_t)k * RB;
@@ -503,7 +576,7 @@ __global__ void __launch_bounds__(256, 4) eval_backward_kernel(
 #pragma unroll
           for (int v = 0; v < V; ++v) {
             const int li = v * 32 + lane;
-            *row_at<T>(wb, pr, li) = node_value<T>(code, lds_operand<T>(wb, sa, li), lds_operand<T>(wb, sb, li), T(0), T(0));
+            *row_at<T>(wb, pr, li) = op_value<T>(code, lds_operand<T>(wb, sa, li), lds_operand<T>(wb, sb, li));
           }
         }
         cp_async_wait<0>();
@@ -516,7 +589,7 @@ __global__ void __launch_bounds__(256, 4) eval_backward_kernel(
             const int li = v * 32 + lane;
             bool a0, a1;
             T o0, o1;
-            const int e = node_adjoint<T>(code, *row_at<T>(wb, pr + adj_delta, li), lds_operand<T>(wb, sa, li),
+            const int e = op_adjoint<T>(code, *row_at<T>(wb, pr + adj_delta, li), lds_operand<T>(wb, sa, li),
                                           lds_operand<T>(wb, sb, li), *row_at<T>(wb, pr, li), a0, o0, a1, o1);
             if (valid[v]) {
               if (e && !err) err = e;
@@ -670,7 +743,7 @@ static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* de
   if (!X && n_x > 0) { set_error("null X"); return SR_ERR_INVALID_ARGUMENT; }
   if (!desc || !meta || !C || !cache) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  const size_t per_warp = align16((size_t)Lmax * 4) + (size_t)Lmax * 32 * sizeof(T);
+  const size_t per_warp = forward_layout<T>(Lmax).bytes;
   Shape sh;
   auto kern = K == 1 ? eval_forward_kernel<T, false> : eval_forward_kernel<T, true>;
   const int64_t units = B * ((N + kSlice - 1) / kSlice);

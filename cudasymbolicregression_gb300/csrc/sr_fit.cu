@@ -405,7 +405,7 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         const int li = v * 32 + lane;
-        const float r = node_value<float>(code, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li), 0.f, 0.f);
+        const float r = op_value<float>(code, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li));
         S.vals[i * RW + li] = r;
         if (kGrad) S.adj[i * RW + li] = 0.f;
       }
@@ -459,7 +459,7 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
         const float g = S.adj[i * RW + li];
         bool a0, a1;
         float r0, r1;
-        const int e = node_adjoint<float>(code, g, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li), S.vals[i * RW + li],
+        const int e = op_adjoint<float>(code, g, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li), S.vals[i * RW + li],
                                           a0, r0, a1, r1);
         if (valid[v]) {
           if (e && !err) err = e;
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
         if (ar >= 1) operand_words(S.tape, S.node_slot, child0(d), A.Kmax, A.Imax, WL, RWB, sa, da);
         if (ar == 2) operand_words(S.tape, S.node_slot, child1(d), A.Kmax, A.Imax, WL, RWB, sb, db);
         const int row = S.node_slot[k];
-        S.pcode[row] = (uint32_t)code;
+        S.pcode[row] = (uint32_t)dense_op(code);
         S.psa[row] = sa;
         S.psb[row] = sb;
         S.pda[row] = da;

@@ -225,4 +225,43 @@ __device__ __forceinline__ int node_adjoint(int code, T g, T a, T b, T v, bool& 
   }
 }
 
+// ---- dense dispatch for operator nodes ---------------------------------------------
+// The interpreters' programs hold operator nodes only (NO_OP and arity >= 1), coded
+// densely: 0 = NO_OP, 1..22 = SIN..FIFTH, 23..27 = ADD..POW, so the per-node switch
+// has contiguous cases.  Each case calls the scalar rule above with a constant code,
+// which folds to that one rule.
+constexpr int kDenseOps = 28;
+
+__host__ __device__ __forceinline__ int dense_op(int code) {
+  return code == NO_OP ? 0 : (code >= ADD ? code - ADD + 23 : code - SIN + 1);
+}
+
+__host__ __device__ constexpr int op_of_dense(int d) { return d == 0 ? NO_OP : (d >= 23 ? ADD + d - 23 : SIN + d - 1); }
+
+#define SR_DENSE_CASES(X) \
+  X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17) X(18) \
+  X(19) X(20) X(21) X(22) X(23) X(24) X(25) X(26) X(27)
+
+template <typename T>
+__device__ __forceinline__ T op_value(int d, T a, T b) {
+  switch (d) {
+#define SR_VALUE_CASE(i) \
+  case i: return node_value<T>(op_of_dense(i), a, b, T(0), T(0));
+    SR_DENSE_CASES(SR_VALUE_CASE)
+#undef SR_VALUE_CASE
+    default: return T(0);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ int op_adjoint(int d, T g, T a, T b, T v, bool& add0, T& o0, bool& add1, T& o1) {
+  switch (d) {
+#define SR_ADJOINT_CASE(i) \
+  case i: return node_adjoint<T>(op_of_dense(i), g, a, b, v, add0, o0, add1, o1);
+    SR_DENSE_CASES(SR_ADJOINT_CASE)
+#undef SR_ADJOINT_CASE
+    default: add0 = add1 = false; o0 = o1 = T(0); return 0;
+  }
+}
+
 }  // namespace sr
