@@ -264,4 +264,41 @@ __device__ __forceinline__ int op_adjoint(int d, T g, T a, T b, T v, bool& add0,
   }
 }
 
+// V points at once: one dispatch, then the rule for every point (the operands are in
+// registers, so the points' chains interleave).
+template <typename T, int V>
+__device__ __forceinline__ void op_value_v(int d, const T (&a)[V], const T (&b)[V], T (&r)[V]) {
+  switch (d) {
+#define SR_VALUE_V_CASE(i)                                                           \
+  case i:                                                                            \
+    _Pragma("unroll") for (int q = 0; q < V; ++q) r[q] = node_value<T>(op_of_dense(i), a[q], b[q], T(0), T(0)); \
+    break;
+    SR_DENSE_CASES(SR_VALUE_V_CASE)
+#undef SR_VALUE_V_CASE
+    default:
+      _Pragma("unroll") for (int q = 0; q < V; ++q) r[q] = T(0);
+  }
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void op_adjoint_v(int d, const T (&g)[V], const T (&a)[V], const T (&b)[V],
+                                             const T (&v)[V], bool (&add0)[V], T (&o0)[V], bool (&add1)[V],
+                                             T (&o1)[V], int (&e)[V]) {
+  switch (d) {
+#define SR_ADJOINT_V_CASE(i)                                                                               \
+  case i:                                                                                                  \
+    _Pragma("unroll") for (int q = 0; q < V; ++q) e[q] =                                                   \
+        node_adjoint<T>(op_of_dense(i), g[q], a[q], b[q], v[q], add0[q], o0[q], add1[q], o1[q]);           \
+    break;
+    SR_DENSE_CASES(SR_ADJOINT_V_CASE)
+#undef SR_ADJOINT_V_CASE
+    default:
+      _Pragma("unroll") for (int q = 0; q < V; ++q) {
+        add0[q] = add1[q] = false;
+        o0[q] = o1[q] = T(0);
+        e[q] = 0;
+      }
+  }
+}
+
 }  // namespace sr

@@ -217,6 +217,35 @@ def test_backward_errors(golden):
         assert str(g[name + "__msg"]) in str(e.value)
 
 
+def test_backward_error_precedence():
+    """A gradient on a padding (NO_OP) row is reported as 201 even when other tapes of
+    the batch meet a zero denominator (204): the padding check and the adjoint run
+    concurrently, and 201 takes precedence whichever finds its error first."""
+    sr = _sr()
+    B, M, N = 4096, 8, 256
+    ops = torch.zeros(B, M, dtype=torch.int64)
+    ch = -torch.ones(B, M, 2, dtype=torch.int64)
+    ops[:, 0], ops[:, 1], ops[:, 2] = 1, 50, 43  # C / X0
+    ch[:, 2, 0], ch[:, 2, 1] = 0, 1
+    X = torch.linspace(-1, 1, N).reshape(N, 1)
+    X[N // 2] = 0.0
+    ops, ch, X = ops.cuda(), ch.cuda(), X.cuda()
+    for culprit in (0, B // 2, B - 1):
+        C = torch.ones(B, M, device="cuda").requires_grad_(True)
+        y = sr.evaluation.evaluate(X, ops, ch, C)
+        gout = torch.zeros_like(y)
+        gout[:, 2, :] = 1.0                      # every tape: a/b with b = 0 at one point
+        gout[culprit, M - 1, 3] = 1.0            # one tape: a gradient on a padding row
+        with pytest.raises(RuntimeError, match="A non-zero gradient was passed to a NO_OP node"):
+            y.backward(gout)
+    C = torch.ones(B, M, device="cuda").requires_grad_(True)
+    y = sr.evaluation.evaluate(X, ops, ch, C)
+    gout = torch.zeros_like(y)
+    gout[:, 2, :] = 1.0
+    with pytest.raises(RuntimeError, match=r"Gradient for a/b where b = 0"):
+        y.backward(gout)
+
+
 def test_ragged_batch_and_padding_rows():
     """Ragged tapes: rows after the last real node are NaN, NO_OP inside a tape is NaN."""
     sr = _sr()
