@@ -7,6 +7,8 @@ Public API, mirroring the reference package ``symbolic_torch``:
 * ``create_constants(ops, method='randn'|'range', **kw)``;
 * ``optimize(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad,
   line_search_fn)`` -- the fused batched L-BFGS kernel;
+* ``ProbabilisticContextFreeGrammar`` -- grammar sampling and infix parsing on
+  the device (``sample(B)`` gives postfix Ops and Ch for the fit);
 * ``Operator``, ``get_arity``, ``is_valid_op``.
 
 Every compute entry point runs hand-written sm_103a kernels from
@@ -15,11 +17,13 @@ Every compute entry point runs hand-written sm_103a kernels from
 from . import evaluation, notation
 from .operators import MAX_ARITY, NULL_CHILD, ErrorCode, Operator, get_arity, is_valid_op
 from .optimization import FitPlan, FitResult, optimize, optimize_ex
+from .pcfg import ProbabilisticContextFreeGrammar
 from .utils import create_constants
 
 __all__ = [
     "evaluation",
     "notation",
+    "ProbabilisticContextFreeGrammar",
     "Operator",
     "ErrorCode",
     "create_constants",

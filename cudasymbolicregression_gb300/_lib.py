@@ -88,6 +88,9 @@ _SIGS = {
                                      i32, i32, ctypes.POINTER(FitOptions), vp, vp], ctypes.c_int),
     "sr_postfix_children": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
     "sr_postfix_to_infix": ([vp, i64, i64, i32, vp, i64, vp, vp], ctypes.c_int),
+    "sr_pcfg_sample_infix": ([vp, vp, vp, vp, i32, i32, i64, i32, i32, ctypes.c_uint64, vp, vp, vp], ctypes.c_int),
+    "sr_infix_to_postfix": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
+    "sr_infix_to_prefix": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
     "sr_const_offsets": ([vp, i64, i64, i64, i64, vp, vp], ctypes.c_int),
     "sr_const_scatter": ([vp, i64, i64, i64, i64, vp, vp, vp, vp], ctypes.c_int),
     "sr_mlp_gemm": ([vp, i64, i64, i64, vp, i64, i64, ctypes.POINTER(MlpEpilogue), vp, vp], ctypes.c_int),

@@ -245,6 +245,34 @@ int sr_postfix_children(const int64_t *ops_dev, int64_t B, int64_t M, int32_t n_
 int sr_postfix_to_infix(const int64_t *ops_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *infix_dev,
                         int64_t M_out, int64_t *err_dev, void *stream);
 
+/* ---- Grammar sampling and infix parsing -------------------------------------------
+ * Sample B infix expressions (B, max_length) int64, NO_OP padded, from a grammar in
+ * the reference's CSR form: nt_rule_ptr (n_symbols + 1) int32, the rules of symbol s
+ * being nt_rule_ptr[s] .. nt_rule_ptr[s + 1] - 1; nt_rule_cum_probs (rules) float32
+ * cumulative per symbol, the last of each symbol 1.0; rhs_ptr (rules + 1) int32 and
+ * rhs_concat int32, the right-hand sides.  A seed fixes every expression (a
+ * SplitMix64 stream per expression).  err (B) int64: 0, 303 (max_tries exceeded) or
+ * 304 (no rule for the drawn number).  max_length <= 128.  Replaces sample_infix
+ * (reference src/pcfg.cpp:568-628, src/pcfg_cuda.cu:10-146).
+ */
+int sr_pcfg_sample_infix(const int32_t *nt_rule_ptr, const float *nt_rule_cum_probs, const int32_t *rhs_ptr,
+                         const int32_t *rhs_concat, int32_t n_symbols, int32_t start_symbol, int64_t B,
+                         int32_t max_length, int32_t max_tries, uint64_t seed, int64_t *out_dev,
+                         int64_t *err_dev, void *stream);
+
+/*
+ * Infix token rows (B, M) int64 (M <= 128; "(" = VAR_START_ID + n_vars, ")" = "(" + 1)
+ * to postfix (with the reference's tree check) or to prefix, (B, M) int64 NO_OP
+ * padded; a row with an error is all NO_OP.  err (B) int64: 0, the reference's codes
+ * 401..408, or -1 / -2 for a token below 0 / at or above the terminal limit.
+ * Replace infix_to_postfix and infix_to_prefix (reference src/pcfg.cpp:660-746,
+ * src/pcfg_cpu.cpp:121-448).
+ */
+int sr_infix_to_postfix(const int64_t *infix_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *postfix_dev,
+                        int64_t *err_dev, void *stream);
+int sr_infix_to_prefix(const int64_t *infix_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *prefix_dev,
+                       int64_t *err_dev, void *stream);
+
 /* ---- Warm-start network ---------------------------------------------------------
  * No reference counterpart: the learned part of the fit.  A BF16 MLP with fp32
  * accumulation predicts starting constants from a tape (bag of tokens through a

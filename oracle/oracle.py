@@ -62,6 +62,11 @@ def lib() -> ctypes.CDLL:
         L.sro_num_threads.restype = ctypes.c_int
         L.sro_node_fwd_f32.argtypes = [i64, vp, vp, vp, vp, vp, vp]
         L.sro_node_fwd_f32.restype = None
+        i32 = ctypes.c_int32
+        L.sro_pcfg_sample.argtypes = [vp, vp, vp, vp, i32, i32, i64, i32, i32, ctypes.c_uint64, vp, vp]
+        L.sro_pcfg_sample.restype = None
+        L.sro_infix_parse.argtypes = [vp, i64, i64, i32, i32, vp, vp]
+        L.sro_infix_parse.restype = None
         _lib = L
     return _lib
 
@@ -172,6 +177,30 @@ def node_fwd(op, a, b, c, x):
     out = np.empty(op.shape, np.float32)
     lib().sro_node_fwd_f32(op.size, _p(op), _p(a), _p(b), _p(c), _p(x), _p(out))
     return out
+
+
+def pcfg_sample(tables, start, B, max_len, max_tries, seed):
+    """Restatement of the grammar sampler (src/pcfg_cpu.cpp:10-119) with the
+    library's SplitMix64 stream.  tables = (nt_rule_ptr, cum_probs, rhs_ptr,
+    rhs_concat) as numpy arrays.  Returns (infix (B, max_len) int64, errors (B))."""
+    nt, cum, rp, rc = (_c(tables[0], np.int32), _c(tables[1], np.float32), _c(tables[2], np.int32),
+                       _c(tables[3], np.int32))
+    out = np.empty((B, max_len), np.int64)
+    err = np.empty(B, np.int64)
+    lib().sro_pcfg_sample(_p(nt), _p(cum), _p(rp), _p(rc), int(nt.size - 1), int(start), int(B), int(max_len),
+                          int(max_tries), int(seed) & 0xFFFFFFFFFFFFFFFF, _p(out), _p(err))
+    return out, err
+
+
+def infix_parse(infix, n_vars, prefix=False):
+    """Restatement of infix_to_postfix / infix_to_prefix (src/pcfg_cpu.cpp:121-448).
+    Returns (tokens (B, M) int64, errors (B))."""
+    x = _c(infix, np.int64)
+    B, M = x.shape
+    out = np.empty((B, M), np.int64)
+    err = np.empty(B, np.int64)
+    lib().sro_infix_parse(_p(x), B, M, int(n_vars), int(bool(prefix)), _p(out), _p(err))
+    return out, err
 
 
 def num_threads() -> int:

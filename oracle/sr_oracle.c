@@ -591,3 +591,164 @@ int sro_num_threads(void)
     return 1;
 #endif
 }
+
+/* ---- grammar sampling and infix parsing --------------------------------------------
+ * Restates the reference's sampler (src/pcfg_cpu.cpp:10-119, the same derivation as
+ * src/pcfg_cuda.cu:10-118) and shunting-yard parsers (src/pcfg_cpu.cpp:121-448).
+ * The random numbers are the library's own SplitMix64 stream per expression
+ * (Steele, Lea and Flood, OOPSLA 2014), restated here so that the device sampler is
+ * checked token for token; the reference draws from curand instead, so against the
+ * reference the sampler is checked by frequencies.
+ */
+#define SRO_HARD_MAX 128
+
+static uint64_t sro_mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static float sro_uniform(uint64_t *s)
+{
+    *s += 0x9E3779B97F4A7C15ull;
+    return (float)((sro_mix64(*s) >> 40) + 1ull) * (1.0f / 16777216.0f);
+}
+
+void sro_pcfg_sample(const int32_t *nt_ptr, const float *cum, const int32_t *rhs_ptr, const int32_t *rhs,
+                     int32_t n_symbols, int32_t start, int64_t B, int32_t max_len, int32_t max_tries,
+                     uint64_t seed, int64_t *out, int64_t *errors)
+{
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < B; ++b) {
+        uint64_t s = sro_mix64(seed ^ sro_mix64((uint64_t)b + 0x9E3779B97F4A7C15ull));
+        int32_t stack[SRO_HARD_MAX];
+        int64_t *row = out + b * max_len;
+        int err = 0, done = 0, len = 0;
+        for (int tr = 0; tr < max_tries && !done && !err; ++tr) {
+            int restart = 0, sp = 0;
+            len = 0;
+            stack[sp++] = start;
+            while (sp > 0) {
+                const int sym = stack[--sp];
+                const int r0 = sym < n_symbols ? nt_ptr[sym] : 0;
+                const int r1 = sym < n_symbols ? nt_ptr[sym + 1] : 0;
+                if (r0 != r1) {
+                    const float u = sro_uniform(&s);
+                    int chosen = -1;
+                    for (int r = r0; r < r1; ++r)
+                        if (u <= cum[r]) { chosen = r; break; }
+                    if (chosen < 0) { err = 304; break; }
+                    for (int i = rhs_ptr[chosen + 1] - 1; i >= rhs_ptr[chosen]; --i) {
+                        if (sp >= SRO_HARD_MAX) { restart = 1; break; }
+                        stack[sp++] = rhs[i];
+                    }
+                    if (restart) break;
+                } else {
+                    if (len >= max_len) { restart = 1; break; }
+                    row[len++] = sym;
+                }
+            }
+            if (!restart && !err && len > 0) done = 1;
+        }
+        if (!done && !err) err = 303;
+        if (!done) len = 0;
+        for (int i = len; i < max_len; ++i) row[i] = OP_NO_OP;
+        errors[b] = err;
+    }
+}
+
+static int sro_precedence(int64_t tok, int64_t lp, int64_t rp)
+{
+    if (tok == OP_ADD || tok == OP_SUB) return 1;
+    if (tok == OP_MUL || tok == OP_DIV) return 2;
+    if (tok == OP_POW) return 3;
+    if ((tok >= OP_SIN && tok <= OP_FIFTH) || tok == lp || tok == rp) return 4;
+    return 0;
+}
+
+static int sro_token_arity(int64_t tok)
+{
+    if (tok >= OP_SIN && tok <= OP_FIFTH) return 1;
+    if (tok >= OP_ADD && tok <= OP_POW) return 2;
+    return 0;
+}
+
+/* prefix = 0: infix -> postfix with the tree check; 1: infix -> prefix.  errors: 0,
+ * the reference's 401..408, or -1 / -2 for a token below 0 / at or above the
+ * terminal limit (the reference rejects those before parsing). */
+void sro_infix_parse(const int64_t *infix, int64_t B, int64_t M, int32_t n_vars, int32_t prefix, int64_t *outp,
+                     int64_t *errors)
+{
+    const int64_t lp = OP_VAR0 + n_vars, rp = lp + 1, limit = rp + 1;
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < B; ++b) {
+        const int64_t *in = infix + b * M;
+        int64_t *o = outp + b * M;
+        int64_t ops[SRO_HARD_MAX], queue[SRO_HARD_MAX];
+        int bad = 0, err = 0, len = 0, ended = 0, sp = 0, n_out = 0;
+        for (int64_t i = 0; i < M; ++i) {
+            if (in[i] < 0) bad = -1;
+            else if (in[i] >= limit && bad == 0) bad = -2;
+        }
+        for (int64_t i = 0; i < M && !err; ++i) {
+            if (in[i] == OP_NO_OP) ended = 1;
+            else if (ended) err = 408;
+            else ++len;
+        }
+        const int64_t open = prefix ? rp : lp, close = prefix ? lp : rp;
+        for (int step = 0; step < len && !err && !bad; ++step) {
+            const int64_t tok = in[prefix ? len - 1 - step : step];
+            const int pt = sro_precedence(tok, lp, rp);
+            if (pt == 0) {
+                if (n_out >= SRO_HARD_MAX) { err = 401; break; }
+                queue[n_out++] = tok;
+            } else if (tok == open) {
+                if (sp >= SRO_HARD_MAX) { err = 402; break; }
+                ops[sp++] = tok;
+            } else if (tok == close) {
+                while (sp > 0 && ops[sp - 1] != open) {
+                    if (n_out >= SRO_HARD_MAX) { err = 401; break; }
+                    queue[n_out++] = ops[--sp];
+                }
+                if (err) break;
+                if (sp == 0) { err = 403; break; }
+                --sp;
+            } else {
+                const int ra = tok == OP_POW || (tok >= OP_SIN && tok <= OP_FIFTH);
+                while (sp > 0 && ops[sp - 1] != open) {
+                    const int ptop = sro_precedence(ops[sp - 1], lp, rp);
+                    const int pop = prefix ? (ra ? ptop >= pt : ptop > pt) : (ra ? ptop > pt : ptop >= pt);
+                    if (!pop) break;
+                    if (n_out >= SRO_HARD_MAX) { err = 401; break; }
+                    queue[n_out++] = ops[--sp];
+                }
+                if (err) break;
+                if (sp >= SRO_HARD_MAX) { err = 402; break; }
+                ops[sp++] = tok;
+            }
+        }
+        while (!err && !bad && sp > 0) {
+            if (ops[sp - 1] == open) { err = 403; break; }
+            if (n_out >= SRO_HARD_MAX) { err = 401; break; }
+            queue[n_out++] = ops[--sp];
+        }
+        if (!prefix && !err && !bad && n_out > 0) {
+            int depth = 0;
+            for (int i = 0; i < n_out && !err; ++i) {
+                if (sro_precedence(queue[i], lp, rp) == 0) {
+                    ++depth;
+                } else {
+                    const int ar = sro_token_arity(queue[i]);
+                    if (depth < ar) err = ar == 1 ? 404 : 405;
+                    depth = depth - ar + 1;
+                }
+            }
+            if (!err && depth != 1) err = 407;
+        }
+        if (err || bad) n_out = 0;
+        for (int64_t i = 0; i < M; ++i)
+            o[i] = i < n_out ? queue[prefix ? n_out - 1 - i : i] : OP_NO_OP;
+        errors[b] = bad ? bad : err;
+    }
+}

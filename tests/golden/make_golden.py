@@ -22,6 +22,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, ROOT)
 
 import build_ref  # noqa: E402
+from grammars import BAD_GRAMMARS, NOTATION_GRAMMAR, README_GRAMMAR, SAMPLING_GRAMMAR  # noqa: E402
 
 from cudasymbolicregression_gb300 import tapes  # noqa: E402
 from cudasymbolicregression_gb300.operators import BINARY_OPS, UNARY_OPS, Operator  # noqa: E402
@@ -183,17 +184,6 @@ def case_optimize_linear(st):
                         ch=Ch.numpy(), C=C.numpy(), C_final=Cf.numpy(), Y_final=Yf.numpy())
 
 
-README_GRAMMAR = """E -> E + T [0.4]
-E -> T [0.6]
-T -> F * T [0.4]
-T -> F [0.6]
-F -> R ( V ) [0.3]
-F -> V [0.7]
-R -> sin [0.5]
-R -> cos [0.5]
-V -> X_0 [0.5]
-V -> C [0.5]
-"""
 
 
 def case_optimize_readme(st, B=128, max_iter=100):
@@ -260,30 +250,6 @@ def case_rosenbrock(st):
                         x_backtracking=res["backtracking"])
 
 
-NOTATION_GRAMMAR = """E -> E + F [0.2]
-E -> E - F [0.2]
-E -> F [0.6]
-F -> F * T [0.2]
-F -> F / T [0.2]
-F -> T [0.6]
-T -> ( E ) P [0.1]
-T -> R ( E ) [0.3]
-T -> V [0.4]
-T -> ( E ) [0.2]
-V -> X_0 [0.2]
-V -> X_1 [0.2]
-V -> C [0.3]
-V -> 5 [0.3]
-R -> sin [0.2]
-R -> cos [0.2]
-R -> exp [0.2]
-R -> sqrt [0.2]
-R -> log [0.2]
-P -> ^2 [0.25]
-P -> ^3 [0.25]
-P -> ^4 [0.25]
-P -> ^5 [0.25]
-"""
 
 
 def case_notation(st):
@@ -370,6 +336,120 @@ def case_multiple(st):
                         gC=Ct.grad.numpy().copy(), gX=Xt.grad.numpy().copy())
 
 
+
+
+
+def case_pcfg(st):
+    """Grammar object: symbol ids, arities, valid ops and operator names for some
+    grammars, the constructor's error messages, infix -> postfix / prefix of sampled
+    and hand-made rows (with the error reports), and sampling frequencies of the
+    reference's own sampler (src/pcfg.cpp, src/pcfg_cpu.cpp)."""
+    out = {}
+    names = sorted({n for n in ["NO_OP", "C", "1", "5", "pi", "PI", "e", "E", "sin", "Sin", "ln", "LN", "Ln", "log",
+                                "log10", "^2", "square", "u-", "minus", "^-1", "inv", "^5", "+", "-", "*", "/", "^",
+                                "X_0", "X_1", "X_2", "(", ")", "T", "F", "V", "R", "P", "asin", "atan", "floor"]})
+    out["names"] = np.array(names)
+    for tag, (g, start, nv) in {"readme": (README_GRAMMAR, "E", 1), "sampling": (SAMPLING_GRAMMAR, "E", 1),
+                                "notation": (NOTATION_GRAMMAR, "E", 2), "wide": ("S -> 1 [1.0]", "S", 5)}.items():
+        pcfg = st.ProbabilisticContextFreeGrammar(g, start, 32, nv, torch.device("cpu"))
+        ids = []
+        for n in names:
+            try:
+                ids.append(pcfg.get_symbol_id(n))
+            except RuntimeError:
+                ids.append(-999)
+        out[f"{tag}__ids"] = np.array(ids, np.int64)
+        out[f"{tag}__n_operators"] = np.array(pcfg.n_operators)
+        out[f"{tag}__arities"] = pcfg.get_arities().numpy()
+        out[f"{tag}__valid"] = pcfg.valid_ops().numpy()
+        out[f"{tag}__available"] = np.array(sorted(pcfg.available_operators()))
+    for tag, g in BAD_GRAMMARS.items():
+        try:
+            st.ProbabilisticContextFreeGrammar(g, "E", 16, 1, torch.device("cpu"))
+            out[f"bad_{tag}__msg"] = np.array("")
+        except (ValueError, RuntimeError) as e:
+            out[f"bad_{tag}__msg"] = np.array(str(e))
+    try:
+        st.ProbabilisticContextFreeGrammar("S -> 1 [1.0]", "S", 129, 0, torch.device("cpu"))
+        out["too_long__msg"] = np.array("")
+    except (ValueError, RuntimeError) as e:
+        out["too_long__msg"] = np.array(str(e))
+    # parsing: sampled rows of the notation grammar and hand-made ones
+    torch.manual_seed(17)
+    pcfg = st.ProbabilisticContextFreeGrammar(NOTATION_GRAMMAR, "E", 64, 2, torch.device("cpu"))
+    infix = pcfg.sample_infix(500)
+    out["parse_infix"] = infix.numpy()
+    out["parse_postfix"] = pcfg.infix_to_postfix(infix).numpy()
+    out["parse_prefix"] = pcfg.infix_to_prefix(infix).numpy()
+    V, LP, RP = 50, 52, 53
+    hand = {
+        "precedence": [2, 40, 2, 42, 2],
+        "paren": [LP, 2, 40, 2, RP, 42, 2],
+        "assoc_add": [2, 40, 2, 40, 2, 40, 2],
+        "assoc_pow": [2, 44, 2, 44, 2],
+        "assoc_sin": [10, 10, 10, 10, 2],
+        "mixed": [10, LP, 2, RP, 40, 2],
+        "all_ops": [10, LP, V, RP, 40, 2, 42, LP, 13, LP, V, RP, 41, 2, RP],
+        "sub_div": [V, 41, V + 1, 43, 2, 41, 3],
+        "unary_pow": [V, 44, 14, 44, 3],
+        "mismatch_close": [2, RP],
+        "mismatch_open": [LP, 2, 40, 2],
+        "after_end": [2, 0, 2],
+        "unary_missing": [10],
+        "binary_missing": [2, 40],
+        "too_many": [2, 2],
+        "empty": [0, 0],
+        "negative": [2, -4, 2],
+        "too_large": [2, 40, RP + 1],
+    }
+    for tag, row in hand.items():
+        x = torch.tensor([row + [0] * (16 - len(row))], dtype=torch.int64)
+        out[f"hand_{tag}__row"] = x.numpy()
+        for fn in ("postfix", "prefix"):
+            try:
+                r = getattr(pcfg, f"infix_to_{fn}")(x)
+                out[f"hand_{tag}__{fn}"] = r.numpy()
+                out[f"hand_{tag}__{fn}_msg"] = np.array("")
+            except (RuntimeError, ValueError) as e:
+                out[f"hand_{tag}__{fn}_msg"] = np.array(str(e))
+    # a batch with several errors, and the verbose report's first lines
+    batch = torch.tensor([[2, RP, 0, 0], [10, 0, 0, 0], [2, 40, 2, 0], [2, RP, 0, 0]], dtype=torch.int64)
+    for verbosity in (0, 1):
+        try:
+            pcfg.infix_to_postfix(batch, verbosity)
+        except RuntimeError as e:
+            out[f"batch_v{verbosity}_msg"] = np.array(str(e))
+    out["batch_rows"] = batch.numpy()
+    # generation failure and frequencies of the reference sampler
+    try:
+        st.ProbabilisticContextFreeGrammar("S -> 1 S [1.0]", "S", 5, 0, torch.device("cpu"), max_tries=10).sample_infix(3)
+    except RuntimeError as e:
+        out["max_tries_msg"] = np.array(str(e))
+    torch.manual_seed(23)
+    sp = st.ProbabilisticContextFreeGrammar(SAMPLING_GRAMMAR, "E", 128, 1, torch.device("cpu"))
+    strings = sp.to_string(sp.sample_infix(200000))
+    counts = {}
+    for s_ in strings:
+        counts[s_] = counts.get(s_, 0) + 1
+    top = sorted(counts.items(), key=lambda kv: -kv[1])[:40]
+    out["freq_strings"] = np.array([k for k, _ in top])
+    out["freq_counts"] = np.array([v for _, v in top], np.int64)
+    out["freq_total"] = np.array(len(strings))
+    lengths = np.array([len(s_.split()) for s_ in strings])
+    out["freq_length_hist"] = np.bincount(lengths, minlength=129)
+    torch.manual_seed(29)
+    rp = st.ProbabilisticContextFreeGrammar(README_GRAMMAR, "E", 32, 1, torch.device("cpu"))
+    rs = rp.to_string(rp.sample_infix(200000))
+    rc = {}
+    for s_ in rs:
+        rc[s_] = rc.get(s_, 0) + 1
+    rtop = sorted(rc.items(), key=lambda kv: -kv[1])[:40]
+    out["readme_strings"] = np.array([k for k, _ in rtop])
+    out["readme_counts"] = np.array([v for _, v in rtop], np.int64)
+    out["readme_length_hist"] = np.bincount(np.array([len(s_.split()) for s_ in rs]), minlength=129)
+    np.savez_compressed(os.path.join(OUT, "pcfg.npz"), **out)
+
+
 def main():
     st = build_ref.load_reference()
     torch.set_num_threads(1)
@@ -391,6 +471,7 @@ def main():
     case_rosenbrock(st)
     case_notation(st)
     case_multiple(st)
+    case_pcfg(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -1,0 +1,188 @@
+"""Grammar sampling and infix parsing on the GPU, through the C ABI, against the
+oracle (token for token) and the reference's own outputs (tests/golden/pcfg.npz)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "oracle"))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+import oracle  # noqa: E402
+from grammars import NOTATION_GRAMMAR, README_GRAMMAR, SAMPLING_GRAMMAR  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _pcfg(grammar, start, nv, length, **kw):
+    from cudasymbolicregression_gb300.pcfg import ProbabilisticContextFreeGrammar
+    return ProbabilisticContextFreeGrammar(grammar, start, length, nv, torch.device("cuda"), **kw)
+
+
+@pytest.fixture(scope="module")
+def g():
+    return np.load(os.path.join(HERE, "golden", "pcfg.npz"))
+
+
+def _seed_of(torch_seed):
+    """The 64-bit seed sample_infix draws after torch.manual_seed(torch_seed)."""
+    torch.manual_seed(torch_seed)
+    return int(torch.randint(0, 2 ** 63 - 1, (1,), dtype=torch.int64).item())
+
+
+@pytest.mark.parametrize("grammar,start,nv,length,B", [
+    (SAMPLING_GRAMMAR, "E", 1, 128, 20000), (README_GRAMMAR, "E", 1, 32, 50000),
+    (NOTATION_GRAMMAR, "E", 2, 64, 30000), (README_GRAMMAR, "E", 1, 7, 3000), (SAMPLING_GRAMMAR, "E", 1, 5, 1000)])
+def test_sampler_matches_oracle_token_for_token(grammar, start, nv, length, B):
+    p = _pcfg(grammar, start, nv, length, max_tries=64)
+    seed = _seed_of(11)
+    torch.manual_seed(11)
+    try:
+        got = p.sample_infix(B).cpu().numpy()
+        failed = None
+    except RuntimeError as e:
+        got, failed = None, str(e)
+    want, err = oracle.pcfg_sample(p._tables_np, p.get_symbol_id(start), B, length, 64, seed)
+    if err.any():
+        assert failed is not None and "max_tries" in failed
+    else:
+        assert failed is None
+        np.testing.assert_array_equal(got, want)
+
+
+def test_sampler_batch_edges():
+    """B = 1, a partial last CTA, and B = 0."""
+    p = _pcfg(README_GRAMMAR, "E", 1, 32)
+    for B in (1, 129, 0):
+        seed = _seed_of(3)
+        torch.manual_seed(3)
+        got = p.sample_infix(B).cpu().numpy()
+        want, _ = oracle.pcfg_sample(p._tables_np, p.get_symbol_id("E"), B, 32, 64, seed)
+        assert got.shape == (B, 32)
+        np.testing.assert_array_equal(got, want)
+
+
+def test_reference_sampling_patterns(g):
+    """tests/test_sampling.py of the reference: one-rule grammars, 50/50 rules, and
+    the max_tries error."""
+    for gram, nv, tok, text in (("S -> 1 [1.0]", 0, 2, "1"), ("S -> C [1.0]", 0, 1, "C"),
+                                ("S -> X_4 [1.0]", 10, 54, "X_4")):
+        p = _pcfg(gram, "S", nv, 1)
+        s = p.sample_infix(10)
+        assert s.shape == (10, 1) and (s == tok).all()
+        assert set(p.to_string(s)) == {text}
+    for op, code in (("exp", 12), ("sin", 10), ("cos", 11)):
+        p = _pcfg(f"S -> {op} ( 1 ) [0.5]\nS -> 1 [0.5]", "S", 0, 5)
+        s = p.sample_infix(1000)
+        assert (s == code).sum() > 400 and (s == 2).sum() > 400
+        assert all(op in t or t == "1" for t in p.to_string(s))
+    for sym, code in (("+", 40), ("-", 41), ("*", 42), ("/", 43), ("^", 44)):
+        p = _pcfg(f"S -> 1 {sym} 1 [0.5]\nS -> 1 [0.5]", "S", 0, 3)
+        s = p.sample_infix(1000)
+        assert torch.any(s == code, dim=1).sum() > 400 and (s == 2).sum() > 1400
+    p = _pcfg("S -> 1 S [1.0]", "S", 0, 5, max_tries=10)
+    with pytest.raises(RuntimeError) as e:
+        p.sample_infix(3)
+    assert str(e.value) == str(g["max_tries_msg"])
+
+
+def test_sampling_frequencies_match_reference(g):
+    """200000 device samples against the reference's own sampler: the 20 most
+    frequent expressions within 5 standard deviations, length histograms within
+    0.01 in total variation."""
+    p = _pcfg(SAMPLING_GRAMMAR, "E", 1, 128)
+    torch.manual_seed(41)
+    strings = p.to_string(p.sample_infix(200000))
+    n, n_ref = len(strings), int(g["freq_total"])
+    counts = {}
+    for s in strings:
+        counts[s] = counts.get(s, 0) + 1
+    for s, c in list(zip(g["freq_strings"], g["freq_counts"]))[:20]:
+        pr, po = c / n_ref, counts.get(str(s), 0) / n
+        assert abs(po - pr) < 5 * np.sqrt(pr * (1 - pr) * (1 / n + 1 / n_ref)), str(s)
+    ours = np.bincount(np.array([len(s.split()) for s in strings]), minlength=129)[:129] / n
+    ref = g["freq_length_hist"][:129] / g["freq_length_hist"].sum()
+    assert 0.5 * np.abs(ours - ref).sum() < 0.01
+
+
+def test_parser_matches_reference(g):
+    p = _pcfg(NOTATION_GRAMMAR, "E", 2, 64)
+    infix = torch.tensor(g["parse_infix"]).cuda()
+    np.testing.assert_array_equal(p.infix_to_postfix(infix).cpu().numpy(), g["parse_postfix"])
+    np.testing.assert_array_equal(p.infix_to_prefix(infix).cpu().numpy(), g["parse_prefix"])
+    tags = sorted({k.split("__")[0][5:] for k in g.files if k.startswith("hand_")})
+    for tag in tags:
+        row = torch.tensor(g[f"hand_{tag}__row"]).cuda()
+        for fn in ("postfix", "prefix"):
+            want = str(g[f"hand_{tag}__{fn}_msg"])
+            try:
+                out = getattr(p, f"infix_to_{fn}")(row)
+                assert want == "", (tag, fn)
+                np.testing.assert_array_equal(out.cpu().numpy(), g[f"hand_{tag}__{fn}"], err_msg=f"{tag} {fn}")
+            except RuntimeError as e:
+                assert str(e) == want, (tag, fn)
+    with pytest.raises(RuntimeError) as e:
+        p.infix_to_postfix(torch.tensor(g["batch_rows"]).cuda())
+    assert str(e.value) == str(g["batch_v0_msg"])
+    with pytest.raises(ValueError, match="HARD_MAX_LENGTH"):
+        p.infix_to_postfix(torch.zeros(2, 129, dtype=torch.int64, device="cuda"))
+
+
+def test_parser_matches_oracle_on_large_batches():
+    """Every sampled row of a large batch, both directions, plus rows damaged at
+    random positions (the error codes and NO_OP rows must agree too)."""
+    p = _pcfg(NOTATION_GRAMMAR, "E", 2, 64)
+    torch.manual_seed(5)
+    infix = p.sample_infix(40000)
+    rng = np.random.default_rng(0)
+    x = infix.cpu().numpy()
+    bad = rng.random(x.shape[0]) < 0.2
+    pos = rng.integers(0, 8, x.shape[0])
+    x[bad, pos[bad]] = rng.choice([10, 40, 52, 53, 0, 2], size=int(bad.sum()))
+    xd = torch.tensor(x).cuda()
+    lib = __import__("cudasymbolicregression_gb300._lib", fromlist=["lib"])
+    for prefix in (False, True):
+        out = torch.empty_like(xd)
+        err = torch.empty(x.shape[0], dtype=torch.int64, device="cuda")
+        fn = lib.lib().sr_infix_to_prefix if prefix else lib.lib().sr_infix_to_postfix
+        assert fn(lib.ptr(xd), x.shape[0], x.shape[1], 2, lib.ptr(out), lib.ptr(err), lib.stream_ptr(xd.device)) == 0
+        want, werr = oracle.infix_parse(x, 2, prefix=prefix)
+        np.testing.assert_array_equal(err.cpu().numpy(), werr)
+        np.testing.assert_array_equal(out.cpu().numpy(), want)
+        assert (werr != 0).any() and (werr == 0).any()
+
+
+def test_sample_pipeline_feeds_the_fit():
+    """sample(B): postfix Ops and the child table on the device, equal to the
+    separate steps; the batch then evaluates and fits."""
+    import cudasymbolicregression_gb300 as sr
+    p = _pcfg(README_GRAMMAR, "E", 1, 32)
+    torch.manual_seed(9)
+    ops, ch = p.sample(4096)
+    torch.manual_seed(9)
+    infix = p.sample_infix(4096)
+    post = p.infix_to_postfix(infix)
+    assert torch.equal(ops, post)
+    assert torch.equal(ch, p.get_postfix_children(post))
+    assert ops.device.type == "cuda" and ch.shape == (4096, 32, 2)
+    X = torch.linspace(-2, 2, 100, device="cuda").reshape(100, 1)
+    Y = (2.5 * torch.cos(X[:, 0]) - 1.5).expand(4096, 100).contiguous()
+    C0 = sr.create_constants(ops)
+    r = sr.optimize_ex(X, Y, ops, ch, C0, max_iter=50, raise_errors=False)
+    best = torch.nan_to_num(r.loss, nan=float("inf")).min()
+    assert float(best) < 1e-6  # the batch holds C * cos(X_0) + C-like forms
+
+
+def test_postfix_infix_round_trip():
+    """postfix -> infix (with the renderer's parentheses) -> postfix is the identity
+    (32-token expressions render to at most 96 tokens)."""
+    p = _pcfg(NOTATION_GRAMMAR, "E", 2, 32)
+    torch.manual_seed(13)
+    post, _ = p.sample(5000)
+    inf = p.postfix_to_infix(post, 128)
+    back = p.infix_to_postfix(inf)
+    assert torch.equal(back[:, :32], post)
+    assert (back[:, 32:] == 0).all()
