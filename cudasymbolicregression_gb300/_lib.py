@@ -91,6 +91,10 @@ _SIGS = {
     "sr_pcfg_sample_infix": ([vp, vp, vp, vp, i32, i32, i64, i32, i32, ctypes.c_uint64, vp, vp, vp], ctypes.c_int),
     "sr_infix_to_postfix": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
     "sr_infix_to_prefix": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
+    "sr_prefix_to_postfix": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
+    "sr_postfix_to_prefix": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
+    "sr_prefix_parent": ([vp, i64, i64, i32, vp, vp, vp], ctypes.c_int),
+    "sr_prefix_to_infix": ([vp, i64, i64, i32, vp, i64, vp, vp], ctypes.c_int),
     "sr_const_offsets": ([vp, i64, i64, i64, i64, vp, vp], ctypes.c_int),
     "sr_const_scatter": ([vp, i64, i64, i64, i64, vp, vp, vp, vp], ctypes.c_int),
     "sr_mlp_gemm": ([vp, i64, i64, i64, vp, i64, i64, ctypes.POINTER(MlpEpilogue), vp, vp], ctypes.c_int),

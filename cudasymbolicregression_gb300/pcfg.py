@@ -354,6 +354,39 @@ class ProbabilisticContextFreeGrammar:
         """(B, M) postfix -> (B, max_infix_len) infix token rows with parentheses."""
         return notation.postfix_to_infix(expressions, max_infix_len, self._n_variables)
 
+    def _convert(self, fn: str, expressions: torch.Tensor, context: str, check_kind: str, verbosity: int,
+                 width=None, fill=int(Operator.NO_OP)) -> torch.Tensor:
+        dev = _lib.require_cuda(expressions)
+        x = expressions.to(torch.int64).contiguous()
+        B, M = x.shape
+        out = torch.full((B, M if width is None else int(width)), fill, dtype=torch.int64, device=dev)
+        err = torch.zeros(B, dtype=torch.int64, device=dev)
+        args = [_lib.ptr(x), B, M, self._n_variables, _lib.ptr(out)]
+        if width is not None:
+            args.append(int(width))
+        _lib.check(getattr(_lib.lib(), fn)(*args, _lib.ptr(err), _lib.stream_ptr(dev)), fn)
+        self._parsing_error(err.cpu(), x, context, verbosity, check_kind)
+        return out
+
+    def prefix_to_infix(self, expressions: torch.Tensor, max_infix_len: int, verbosity: int = 0) -> torch.Tensor:
+        """(B, M) prefix -> (B, max_infix_len) infix token rows with parentheses."""
+        return self._convert("sr_prefix_to_infix", expressions, "prefix to infix conversion", "prefix_ops",
+                             verbosity, width=max_infix_len)
+
+    def prefix_to_postfix(self, expressions: torch.Tensor, verbosity: int = 0) -> torch.Tensor:
+        """(B, M) prefix -> (B, M) postfix."""
+        return self._convert("sr_prefix_to_postfix", expressions, "prefix to postfix parent conversion",
+                             "prefix_ops", verbosity)
+
+    def postfix_to_prefix(self, expressions: torch.Tensor, verbosity: int = 0) -> torch.Tensor:
+        """(B, M) postfix -> (B, M) prefix."""
+        return self._convert("sr_postfix_to_prefix", expressions, "postfix to prefix parent conversion",
+                             "postfix_ops", verbosity)
+
+    def get_prefix_parent(self, prefix_ops: torch.Tensor, verbosity: int = 0) -> torch.Tensor:
+        """(B, M) prefix -> (B, M) index of every node's parent (-1: root or padding)."""
+        return self._convert("sr_prefix_parent", prefix_ops, "get prefix parent", "prefix_ops", verbosity, fill=-1)
+
     def get_postfix_children(self, postfix_ops: torch.Tensor, verbosity: int = 0) -> torch.Tensor:
         """(B, M) postfix -> (B, M, 2) child table (NULL_CHILD = -1)."""
         return notation.get_postfix_children(postfix_ops, self._n_variables)

@@ -273,6 +273,24 @@ int sr_infix_to_postfix(const int64_t *infix_dev, int64_t B, int64_t M, int32_t 
 int sr_infix_to_prefix(const int64_t *infix_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *prefix_dev,
                        int64_t *err_dev, void *stream);
 
+/*
+ * Prefix rows: to postfix, from postfix, to infix (M_out tokens), and the parent of
+ * every node (-1 for the root and padding), all (B, M) int64, NO_OP padded; a row
+ * with an error is all NO_OP (all -1 for parents).  err (B) int64: 0, the
+ * reference's codes (404..408 for parents; 501..509 for the conversions), or -1 / -2
+ * for a symbol below 0 / at or above VAR_START_ID + n_vars.  Replace
+ * prefix_to_postfix, postfix_to_prefix, prefix_to_infix and get_prefix_parent
+ * (reference src/pcfg.cpp:827-955, src/pcfg_cpu.cpp:637-1064).
+ */
+int sr_prefix_to_postfix(const int64_t *prefix_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *postfix_dev,
+                         int64_t *err_dev, void *stream);
+int sr_postfix_to_prefix(const int64_t *postfix_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *prefix_dev,
+                         int64_t *err_dev, void *stream);
+int sr_prefix_to_infix(const int64_t *prefix_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *infix_dev,
+                       int64_t M_out, int64_t *err_dev, void *stream);
+int sr_prefix_parent(const int64_t *prefix_dev, int64_t B, int64_t M, int32_t n_vars, int64_t *parent_dev,
+                     int64_t *err_dev, void *stream);
+
 /* ---- Warm-start network ---------------------------------------------------------
  * No reference counterpart: the learned part of the fit.  A BF16 MLP with fp32
  * accumulation predicts starting constants from a tape (bag of tokens through a

@@ -450,6 +450,45 @@ def case_pcfg(st):
     np.savez_compressed(os.path.join(OUT, "pcfg.npz"), **out)
 
 
+def case_prefix(st):
+    """prefix_to_postfix, prefix_to_infix and get_prefix_parent of the reference
+    (src/pcfg_cpu.cpp:637-1064) on sampled expressions and on malformed rows, with the
+    error reports (postfix_to_prefix is not bound by the reference's module)."""
+    torch.manual_seed(19)
+    pcfg = st.ProbabilisticContextFreeGrammar(NOTATION_GRAMMAR, "E", 48, 2, torch.device("cpu"))
+    infix = pcfg.sample_infix(600)
+    post = pcfg.infix_to_postfix(infix)
+    pre = pcfg.infix_to_prefix(infix)
+    out = {"post": post.numpy(), "pre": pre.numpy(),
+           "pre_to_post": pcfg.prefix_to_postfix(pre).numpy(),
+           "pre_to_infix": pcfg.prefix_to_infix(pre, 160).numpy(),
+           "pre_parent": pcfg.get_prefix_parent(pre).numpy()}
+    V = int(Operator.VAR_START_ID)
+    rows = {
+        "binary_missing": [40, V, 0, 0],
+        "unary_missing": [10, 0, 0, 0],
+        "after_end": [40, V, V, 0, V],
+        "too_many": [40, V, V, V],
+        "two_leaves": [V, V, 0, 0],
+        "empty": [0, 0, 0, 0],
+        "negative": [40, -2, V, 0],
+        "too_large": [40, V, V + 2, 0],
+        "unary_chain": [10, 11, 14, V],
+        "nested": [42, 40, V, 2, 41, V + 1, 28],
+    }
+    for name, row in rows.items():
+        x = torch.tensor([row], dtype=torch.int64)
+        out[f"{name}__row"] = x.numpy()
+        for fn, call in (("to_post", lambda t: pcfg.prefix_to_postfix(t)), ("to_infix", lambda t: pcfg.prefix_to_infix(t, 12)),
+                         ("parent", lambda t: pcfg.get_prefix_parent(t))):
+            try:
+                out[f"{name}__{fn}"] = call(x).numpy()
+                out[f"{name}__{fn}_msg"] = np.array("")
+            except RuntimeError as e:
+                out[f"{name}__{fn}_msg"] = np.array(str(e))
+    np.savez_compressed(os.path.join(OUT, "prefix.npz"), **out)
+
+
 def main():
     st = build_ref.load_reference()
     torch.set_num_threads(1)
@@ -472,6 +511,7 @@ def main():
     case_notation(st)
     case_multiple(st)
     case_pcfg(st)
+    case_prefix(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

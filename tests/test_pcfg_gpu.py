@@ -186,3 +186,47 @@ def test_postfix_infix_round_trip():
     back = p.infix_to_postfix(inf)
     assert torch.equal(back[:, :32], post)
     assert (back[:, 32:] == 0).all()
+
+
+def test_prefix_conversions_match_reference():
+    """prefix_to_postfix, prefix_to_infix and get_prefix_parent against the
+    reference's outputs (tests/golden/prefix.npz), with its error reports;
+    postfix_to_prefix (not bound by the reference's module) must invert them."""
+    gp = np.load(os.path.join(HERE, "golden", "prefix.npz"))
+    p = _pcfg(NOTATION_GRAMMAR, "E", 2, 48)
+    pre = torch.tensor(gp["pre"]).cuda()
+    post = torch.tensor(gp["post"]).cuda()
+    np.testing.assert_array_equal(p.prefix_to_postfix(pre).cpu().numpy(), gp["pre_to_post"])
+    np.testing.assert_array_equal(p.prefix_to_infix(pre, 160).cpu().numpy(), gp["pre_to_infix"])
+    np.testing.assert_array_equal(p.get_prefix_parent(pre).cpu().numpy(), gp["pre_parent"])
+    np.testing.assert_array_equal(p.postfix_to_prefix(post).cpu().numpy(), gp["pre"])
+    calls = {"to_post": lambda t: p.prefix_to_postfix(t), "to_infix": lambda t: p.prefix_to_infix(t, 12),
+             "parent": lambda t: p.get_prefix_parent(t)}
+    tags = sorted({k.split("__")[0] for k in gp.files if k.endswith("__row")})
+    for tag in tags:
+        row = torch.tensor(gp[f"{tag}__row"]).cuda()
+        for fn, call in calls.items():
+            want = str(gp[f"{tag}__{fn}_msg"])
+            try:
+                out = call(row)
+                assert want == "", (tag, fn)
+                np.testing.assert_array_equal(out.cpu().numpy(), gp[f"{tag}__{fn}"], err_msg=f"{tag} {fn}")
+            except RuntimeError as e:
+                assert str(e) == want, (tag, fn)
+
+
+def test_prefix_round_trips_on_large_batches():
+    p = _pcfg(NOTATION_GRAMMAR, "E", 2, 64)
+    torch.manual_seed(21)
+    infix = p.sample_infix(30000)
+    post = p.infix_to_postfix(infix)
+    pre = p.infix_to_prefix(infix)
+    assert torch.equal(p.postfix_to_prefix(post), pre)
+    assert torch.equal(p.prefix_to_postfix(pre), post)
+    assert torch.equal(p.prefix_to_infix(pre, 200), p.postfix_to_infix(post, 200))
+    par = p.get_prefix_parent(pre)
+    # every non-root node's parent precedes it; exactly one root per expression
+    idx = torch.arange(pre.shape[1], device="cuda").expand_as(pre)
+    real = pre != 0
+    assert ((par < idx) | ~real).all()
+    assert (((par == -1) & real).sum(1) == 1).all()
