@@ -37,6 +37,9 @@ fits them (max_iter=100) to N=2048 points of one hidden seeded 5-operator target
 --rounds rounds; the plain arm starts from randn, the warm arm from the gated
 network, which is trained online on every finished round's fits.  Reported per arm:
 wall-clock to the first MSE < 1e-6 and expressions fitted/s over all rounds.
+--workload sample (the grammar object feeding a search): B=1048576 expressions drawn
+from a 17-rule grammar (infix padded to --N=64 tokens), parsed to postfix and linked
+(child table) on the device, one host synchronisation per step; value = expressions/s.
 --impl reference runs only the CPU port (the reference's own CPU path, restated).
 Multi-GPU: one process per GPU; every rank fits its own batch (independent seeds, no
 collective), value = all problems / max time over ranks.
@@ -64,7 +67,8 @@ M_DEFAULT = 64
 MAX_ITER = 200
 EVAL_METRIC = "evaluation forward+adjoint throughput (algorithmic HBM bytes)"
 DEFAULTS = {"warmstart": (65536, 512), "ragged": (16384, 512), "readme": (65536, 100), "eval": (65536, 1024),
-            "search": (262144, 2048)}
+            "search": (262144, 2048), "sample": (1048576, 64)}
+SAMPLE_METRIC = "expressions sampled from a grammar, parsed to postfix and linked (child table) per second"
 
 # DRAM bytes (read + write) of one launch of the dominant kernel on the default
 # workloads, from ncu captures of a 4x / 16x smaller batch scaled by the number of
@@ -178,10 +182,48 @@ def cpu_fit_workload(args, B, N):
     return workloads.ragged_fit_chunks(B=B, N=N, M=M_DEFAULT, seed=args.seed, n_chunks=1, root_eval=roots)
 
 
+def cpu_sample_run(n, L, seed):
+    """The oracle's sampler, parser and child table (OpenMP) on n expressions of the
+    sampling workload: (expressions/s, seconds, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the checker / CPU baseline only
+    oracle.build()
+    from cudasymbolicregression_gb300.pcfg import ProbabilisticContextFreeGrammar
+    from cudasymbolicregression_gb300.workloads import SEARCH_GRAMMAR
+    p = ProbabilisticContextFreeGrammar(SEARCH_GRAMMAR, "E", L, 3, torch.device("cpu"))
+    t0 = time.perf_counter()
+    rows, e1 = oracle.pcfg_sample(p._tables_np, p.get_symbol_id("E"), n, L, 64, seed)
+    post, e2 = oracle.infix_parse(rows, 3)
+    _, e3 = oracle.postfix_children(post)
+    dt = time.perf_counter() - t0
+    assert not (e1.any() or e2.any() or e3.any())
+    return n / dt, dt, oracle.num_threads()
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
     B, N = args.B, args.N
+    if args.workload == "sample":
+        n = min(B, args.cpu_sample_expr)
+        vals = []
+        threads = 1
+        for i in range(args.warmup + args.steps):
+            v, dt, threads = cpu_sample_run(n, N, args.seed + i)
+            if i >= args.warmup:
+                vals.append(v)
+        value = statistics.median(vals)
+        line = {"metric": SAMPLE_METRIC, "value": value, "unit": "expressions/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * n / value,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": f"grammar sampling: {n} expressions, infix padded to {N} (CPU sample)"},
+                "cpu_baseline": {"value": value, "unit": "expressions/s", "cores": threads, "kind": "port",
+                                 "sample": f"{n} expressions per step: sample, postfix, child table"},
+                "e2e": {"value": value, "unit": "expressions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "host_cores": os.cpu_count()}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload == "eval":
         from cudasymbolicregression_gb300 import tapes
         rng = np.random.default_rng(args.seed)
@@ -743,6 +785,118 @@ def run_search(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_sample(args, rank, world, local):
+    """The grammar object feeding a search: sample(B) = sampler -> infix to postfix ->
+    child table on the device, one host synchronisation (the error check) per step."""
+    from cudasymbolicregression_gb300 import _lib
+    from cudasymbolicregression_gb300.pcfg import ProbabilisticContextFreeGrammar
+    from cudasymbolicregression_gb300.workloads import SEARCH_GRAMMAR
+
+    dev = torch.device("cuda", local)
+    B, L = args.B, args.N
+    pcfg = ProbabilisticContextFreeGrammar(SEARCH_GRAMMAR, "E", L, 3, dev)
+    torch.manual_seed(args.seed + 1000 * rank)
+    for _ in range(args.warmup):
+        ops, ch = pcfg.sample(B)
+    torch.cuda.synchronize()
+    evs = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            ops, ch = pcfg.sample(B)
+            e1.record()
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+    barrier(world)
+    t_step = max_over_ranks(statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in evs), world, dev)
+    value = B * world / t_step
+    ok = int((ops != 0).any(dim=1).sum())
+    mean_len = float((ops != 0).sum(dim=1).float().mean())
+
+    # the three kernels alone, through the C ABI, on the launching stream
+    lib, st = _lib.lib(), _lib.stream_ptr(dev)
+    nt, cum, rp, rc = pcfg._tables
+    infix = torch.empty((B, L), dtype=torch.int64, device=dev)
+    post = torch.empty((B, L), dtype=torch.int64, device=dev)
+    chk = torch.empty((B, L, 2), dtype=torch.int64, device=dev)
+    err = torch.empty((3, B), dtype=torch.int64, device=dev)
+    start = pcfg.get_symbol_id("E")
+    calls = {
+        "sample_infix_kernel": lambda: lib.sr_pcfg_sample_infix(_lib.ptr(nt), _lib.ptr(cum), _lib.ptr(rp), _lib.ptr(rc),
+                                                                int(nt.numel() - 1), start, B, L, 64, 12345,
+                                                                _lib.ptr(infix), _lib.ptr(err[0]), st),
+        "infix_parse_kernel<postfix>": lambda: lib.sr_infix_to_postfix(_lib.ptr(infix), B, L, 3, _lib.ptr(post),
+                                                                       _lib.ptr(err[1]), st),
+        "postfix_children_kernel": lambda: lib.sr_postfix_children(_lib.ptr(post), B, L, 3, _lib.ptr(chk),
+                                                                   _lib.ptr(err[2]), st),
+    }
+    algo = {"sample_infix_kernel": B * (L * 8 + 8), "infix_parse_kernel<postfix>": B * (2 * L * 8 + 8),
+            "postfix_children_kernel": B * (L * 8 + 2 * L * 8 + 8)}
+    ktimes = {}
+    for name, fn in calls.items():
+        for _ in range(3):
+            _lib.check(fn(), name)
+        ts = []
+        for _ in range(max(3, args.steps)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.check(fn(), name)
+            e1.record()
+            ts.append((e0, e1))
+        torch.cuda.synchronize()
+        ktimes[name] = statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in ts)
+    assert int((err != 0).sum()) == 0
+
+    e2e = None
+    if not args.no_e2e:
+        h_ops = torch.empty((B, L), dtype=torch.int64).pin_memory()
+        h_ch = torch.empty((B, L, 2), dtype=torch.int64).pin_memory()
+        ts = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            o, c = pcfg.sample(B)
+            h_ops.copy_(o, non_blocking=True)
+            h_ch.copy_(c, non_blocking=True)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        e2e = {"value": B * world / statistics.median(ts), "unit": "expressions/s", "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": int(B * L * 8 * 3),
+               "path": "ProbabilisticContextFreeGrammar.sample(B), then Ops and Ch copied to pinned host memory"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        n = min(B, args.cpu_sample_expr)
+        v, dt, threads = cpu_sample_run(n, L, args.seed)
+        cpu = {"value": v, "unit": "expressions/s", "cores": threads, "kind": "port",
+               "sample": f"{n} expressions: sample, postfix, child table ({dt:.2f} s)"}
+
+    if rank == 0:
+        pk, pk_kind = peaks()
+        hbm = float(pk["hbm_gbs"])
+        dom = max(ktimes, key=ktimes.get)
+        ach = algo[dom] / ktimes[dom] / 1e9
+        line = {"metric": SAMPLE_METRIC, "value": value, "unit": "expressions/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+                "config": {"workload": f"grammar sampling: B={B} expressions of a 17-rule grammar (+ - * / sin cos exp "
+                                       f"log over X_0..X_2 and C), infix padded to {L} tokens, then postfix and the "
+                                       "child table", "B": B, "L": L, "mean_postfix_length": mean_len,
+                           "nonempty": ok, "l2": f"outputs larger than L2 ({B * L * 32 / 1e9:.1f} GB per step)"},
+                "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                             "traffic": None, "kernel": dom, "peak_kind": pk_kind},
+                "kernels": {k: {"ms": v * 1000.0, "GB/s": algo[k] / v / 1e9} for k, v in ktimes.items()},
+                "gpu_launches": 3 * args.steps, "clocks": clk.summary()}
+        if e2e:
+            line["e2e"] = e2e
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -758,6 +912,7 @@ def main():
     ap.add_argument("--rounds", type=int, default=10)
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--cpu-eval-sample", type=int, default=4096)
+    ap.add_argument("--cpu-sample-expr", type=int, default=1048576)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -778,6 +933,8 @@ def main():
             run_eval(args, rank, world, local)
         elif args.workload == "search":
             run_search(args, rank, world, local)
+        elif args.workload == "sample":
+            run_sample(args, rank, world, local)
         else:
             run_fit(args, rank, world, local)
     if world > 1:

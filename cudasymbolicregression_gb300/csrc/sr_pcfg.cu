@@ -149,10 +149,14 @@ __global__ void __launch_bounds__(kThreads) infix_parse_kernel(const int64_t* __
                                                                int64_t M, int32_t n_vars,
                                                                int64_t* __restrict__ outp,
                                                                int64_t* __restrict__ errors) {
+  // An M-token row never holds more than M operators on the stack or M tokens in the
+  // queue, so both are sized by M (the reference's 128-entry limits cannot be reached
+  // for M <= 128; their checks stay).
   extern __shared__ int16_t sm[];
-  int16_t* row = sm;                         // [M][kThreads]: the input, then the output
-  int16_t* ops = sm + M * kThreads;          // [kHardMax][kThreads] operator stack
-  int16_t* queue = ops + kHardMax * kThreads;  // [kHardMax][kThreads] output queue
+  const int cap = (int)M;
+  int16_t* row = sm;                    // [M][kThreads]: the input, then the output
+  int16_t* ops = sm + M * kThreads;     // [M][kThreads] operator stack
+  int16_t* queue = ops + M * kThreads;  // [M][kThreads] output queue
   const int t = threadIdx.x;
   const int64_t b0 = (int64_t)blockIdx.x * kThreads;
   const int64_t rows = B - b0 < kThreads ? B - b0 : kThreads;
@@ -194,14 +198,14 @@ __global__ void __launch_bounds__(kThreads) infix_parse_kernel(const int64_t* __
       const int open = (int)(kPrefix ? rp : lp), close = (int)(kPrefix ? lp : rp);
       const int pt = precedence(tok, lp, rp);
       if (pt == 0) {
-        if (n_out >= kHardMax) { err = PARSE_QUEUE_OVERFLOW; break; }
+        if (n_out >= cap) { err = PARSE_QUEUE_OVERFLOW; break; }
         queue[(n_out++) * kThreads + t] = (int16_t)tok;
       } else if (tok == open) {
-        if (sp >= kHardMax) { err = PARSE_STACK_OVERFLOW; break; }
+        if (sp >= cap) { err = PARSE_STACK_OVERFLOW; break; }
         ops[(sp++) * kThreads + t] = (int16_t)tok;
       } else if (tok == close) {
         while (sp > 0 && ops[(sp - 1) * kThreads + t] != open) {
-          if (n_out >= kHardMax) { err = PARSE_QUEUE_OVERFLOW; break; }
+          if (n_out >= cap) { err = PARSE_QUEUE_OVERFLOW; break; }
           queue[(n_out++) * kThreads + t] = ops[(--sp) * kThreads + t];
         }
         if (err) break;
@@ -217,19 +221,19 @@ __global__ void __launch_bounds__(kThreads) infix_parse_kernel(const int64_t* __
           // more tightly (right-assoc); to prefix the two conditions swap
           const bool pop = kPrefix ? (ra ? ptop >= pt : ptop > pt) : (ra ? ptop > pt : ptop >= pt);
           if (!pop) break;
-          if (n_out >= kHardMax) { err = PARSE_QUEUE_OVERFLOW; break; }
+          if (n_out >= cap) { err = PARSE_QUEUE_OVERFLOW; break; }
           queue[(n_out++) * kThreads + t] = (int16_t)top;
           --sp;
         }
         if (err) break;
-        if (sp >= kHardMax) { err = PARSE_STACK_OVERFLOW; break; }
+        if (sp >= cap) { err = PARSE_STACK_OVERFLOW; break; }
         ops[(sp++) * kThreads + t] = (int16_t)tok;
       }
     }
     while (!err && !bad && sp > 0) {
       const int top = ops[(sp - 1) * kThreads + t];
       if (top == (int)(kPrefix ? rp : lp)) { err = PARSE_PAREN; break; }
-      if (n_out >= kHardMax) { err = PARSE_QUEUE_OVERFLOW; break; }
+      if (n_out >= cap) { err = PARSE_QUEUE_OVERFLOW; break; }
       queue[(n_out++) * kThreads + t] = (int16_t)top;
       --sp;
     }
@@ -283,7 +287,7 @@ static int launch_parse(const int64_t* infix, int64_t B, int64_t M, int32_t n_va
   if (n_vars < 0 || n_vars > SR_MAX_VARS) { set_error("n_vars out of range (%d)", n_vars); return SR_ERR_UNSUPPORTED; }
   if (B == 0) return SR_OK;
   if (!errors || (M > 0 && (!infix || !outp))) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
-  const size_t smem = (size_t)(M + 2 * kHardMax) * kThreads * sizeof(int16_t);
+  const size_t smem = (size_t)(3 * M > 0 ? 3 * M : 1) * kThreads * sizeof(int16_t);
   auto kern = infix_parse_kernel<kPrefix>;
   int rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem");
   if (rc) return rc;

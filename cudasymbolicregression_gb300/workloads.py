@@ -211,6 +211,28 @@ def _readme_expression(rng: np.random.Generator, max_infix: int):
     return (post, n) if n <= max_infix else None
 
 
+# Candidate grammar of the sampling workload: +, -, *, /, sin, cos, exp, log over
+# X_0..X_2 and learnable constants (about 12 infix tokens on average).
+SEARCH_GRAMMAR = """E -> E + T [0.2]
+E -> E - T [0.15]
+E -> T [0.65]
+T -> T * F [0.2]
+T -> T / F [0.1]
+T -> F [0.7]
+F -> ( E ) [0.1]
+F -> U ( E ) [0.2]
+F -> V [0.7]
+U -> sin [0.3]
+U -> cos [0.3]
+U -> exp [0.2]
+U -> log [0.2]
+V -> X_0 [0.25]
+V -> X_1 [0.25]
+V -> X_2 [0.2]
+V -> C [0.3]
+"""
+
+
 def readme_fit(B: int = 1024, N: int = 100, M: int = 32, seed: int = 0) -> FitWorkload:
     """The README problem: expressions from the grammar above (infix capped at M
     tokens), X = 2 randn(N, 1), every target row 2.5 cos(X_0) - 1.5, C ~ N(0, 1)."""

@@ -67,6 +67,8 @@ def lib() -> ctypes.CDLL:
         L.sro_pcfg_sample.restype = None
         L.sro_infix_parse.argtypes = [vp, i64, i64, i32, i32, vp, vp]
         L.sro_infix_parse.restype = None
+        L.sro_postfix_children.argtypes = [vp, i64, i64, vp, vp]
+        L.sro_postfix_children.restype = None
         _lib = L
     return _lib
 
@@ -201,6 +203,17 @@ def infix_parse(infix, n_vars, prefix=False):
     err = np.empty(B, np.int64)
     lib().sro_infix_parse(_p(x), B, M, int(n_vars), int(bool(prefix)), _p(out), _p(err))
     return out, err
+
+
+def postfix_children(post):
+    """Restatement of get_postfix_children (src/pcfg_cpu.cpp:1066-1142).
+    Returns (ch (B, M, 2) int64, errors (B))."""
+    x = _c(post, np.int64)
+    B, M = x.shape
+    ch = np.empty((B, M, 2), np.int64)
+    err = np.empty(B, np.int64)
+    lib().sro_postfix_children(_p(x), B, M, _p(ch), _p(err))
+    return ch, err
 
 
 def num_threads() -> int:

@@ -752,3 +752,36 @@ void sro_infix_parse(const int64_t *infix, int64_t B, int64_t M, int32_t n_vars,
         errors[b] = bad ? bad : err;
     }
 }
+
+/* Child table of postfix rows (src/pcfg_cpu.cpp:1066-1142): ch (B, M, 2), -1 where a
+ * node has no such child; errors 0 or 404..408. */
+void sro_postfix_children(const int64_t *post, int64_t B, int64_t M, int64_t *ch, int64_t *errors)
+{
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < B; ++b) {
+        const int64_t *row = post + b * M;
+        int64_t *c = ch + b * M * 2;
+        int32_t st[SRO_HARD_MAX];
+        int sp = 0, ended = 0, len = 0, err = 0;
+        for (int64_t i = 0; i < 2 * M; ++i) c[i] = -1;
+        for (int64_t i = 0; i < M && !err; ++i) {
+            const int64_t t = row[i];
+            if (t == OP_NO_OP) { ended = 1; continue; }
+            ++len;
+            if (ended) { err = 408; break; }
+            const int ar = sro_token_arity(t);
+            if (ar == 1) {
+                if (sp < 1) { err = 404; break; }
+                c[2 * i] = st[--sp];
+            } else if (ar == 2) {
+                if (sp < 2) { err = 405; break; }
+                c[2 * i + 1] = st[--sp];
+                c[2 * i] = st[--sp];
+            }
+            if (sp >= SRO_HARD_MAX) { err = 406; break; }
+            st[sp++] = (int32_t)i;
+        }
+        if (!err && len > 0 && sp != 1) err = 407;
+        errors[b] = err;
+    }
+}

@@ -171,3 +171,13 @@ def test_gpu_entry_points_have_no_cpu_path():
         p.sample_infix(4)
     with pytest.raises(RuntimeError):
         p.infix_to_postfix(torch.zeros(2, 3, dtype=torch.int64))
+
+
+def test_oracle_postfix_children_matches_reference():
+    """The oracle's child table (the CPU baseline of the sampling workload) against the
+    reference's get_postfix_children on its own fixtures."""
+    gn = np.load(os.path.join(HERE, "golden", "notation.npz"))
+    for key_in, key_out in (("post", "ch"), ("ops_all", "ch_all")):
+        ch, err = oracle.postfix_children(gn[key_in])
+        assert not err.any()
+        np.testing.assert_array_equal(ch, gn[key_out])
