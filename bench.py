@@ -182,7 +182,7 @@ def cpu_fit_workload(args, B, N):
     return workloads.ragged_fit_chunks(B=B, N=N, M=M_DEFAULT, seed=args.seed, n_chunks=1, root_eval=roots)
 
 
-def cpu_sample_run(n, L, seed):
+def cpu_grammar_run(n, L, seed):
     """The oracle's sampler, parser and child table (OpenMP) on n expressions of the
     sampling workload: (expressions/s, seconds, threads)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -209,7 +209,7 @@ def run_reference(args, rank):
         vals = []
         threads = 1
         for i in range(args.warmup + args.steps):
-            v, dt, threads = cpu_sample_run(n, N, args.seed + i)
+            v, dt, threads = cpu_grammar_run(n, N, args.seed + i)
             if i >= args.warmup:
                 vals.append(v)
         value = statistics.median(vals)
@@ -870,7 +870,7 @@ def run_sample(args, rank, world, local):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         n = min(B, args.cpu_sample_expr)
-        v, dt, threads = cpu_sample_run(n, L, args.seed)
+        v, dt, threads = cpu_grammar_run(n, L, args.seed)
         cpu = {"value": v, "unit": "expressions/s", "cores": threads, "kind": "port",
                "sample": f"{n} expressions: sample, postfix, child table ({dt:.2f} s)"}
 

@@ -1,0 +1,37 @@
+"""bench.py's contract on the host: no top-level name defined twice (a later
+definition silently replaces an earlier one), and the reference arm of every
+workload prints one JSON line with the keys the contract asks for."""
+import ast
+import collections
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..")
+
+
+def test_no_top_level_name_defined_twice():
+    tree = ast.parse(open(os.path.join(ROOT, "bench.py")).read())
+    names = [n.name for n in tree.body if isinstance(n, (ast.FunctionDef, ast.ClassDef))]
+    dup = [k for k, v in collections.Counter(names).items() if v > 1]
+    assert not dup, dup
+
+
+@pytest.mark.parametrize("workload,extra", [("warmstart", ["--cpu-sample", "8"]), ("eval", ["--cpu-eval-sample", "64"]),
+                                            ("sample", ["--cpu-sample-expr", "4096"])])
+def test_reference_arm_prints_contract_line(workload, extra):
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", workload,
+           "--steps", "1", "--warmup", "1"] + extra
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "impl", "cpu_baseline",
+                "e2e", "config"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["value"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
