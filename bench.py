@@ -34,7 +34,8 @@ step time).
 --workload search (the full search round): every round samples B=262144 new
 expressions (tapes over {+,-,*,/,sin,cos,exp,log}, 3 variables, padded length 64) and
 fits them (max_iter=100) to N=2048 points of one hidden seeded 5-operator target, for
---rounds rounds; the plain arm starts from randn, the warm arm from the gated
+--rounds rounds (candidates from the grammar object on the device, --candidates pcfg,
+or the host generator, --candidates tapes); the plain arm starts from randn, the warm arm from the gated
 network, which is trained online on every finished round's fits.  Reported per arm:
 wall-clock to the first MSE < 1e-6 and expressions fitted/s over all rounds.
 --workload sample (the grammar object feeding a search): B=1048576 expressions drawn
@@ -719,15 +720,26 @@ def run_search(args, rank, world, local):
     torch.cuda.synchronize()
     n_train = min(B, 16384)
     n_pts = min(N, 256)
+    grammar = None
+    if args.candidates == "pcfg":
+        from cudasymbolicregression_gb300.pcfg import ProbabilisticContextFreeGrammar
+        grammar = ProbabilisticContextFreeGrammar(workloads.SEARCH_GRAMMAR, "E", M_DEFAULT, n_vars, dev)
+        grammar.sample(1024)  # first launch (kernel attributes) off the clock
     with ClockSampler(local) as clk:
         for r in range(args.rounds):
             t0 = time.perf_counter()
-            C0 = rng.standard_normal((B, M_DEFAULT)).astype(np.float32)
-            tb = tapes.generate(B, M_DEFAULT, seed=args.seed * 100 + r, mean_length=8.0, n_vars=n_vars,
-                                p_const_leaf=0.3, X_screen=Xs, C_screen=C0,
-                                screen_fn=lambda o, c, Xs_, Cs_: workloads._gpu_zero_denominators(Xs_, o, c, Cs_,
-                                                                                                   str(dev)))
-            O, Ch, C = (torch.tensor(a, device=dev) for a in (tb.ops, tb.ch, C0))
+            if args.candidates == "pcfg":
+                # the grammar object on the device: sample -> postfix -> child table, randn constants
+                torch.manual_seed(args.seed * 100 + r)
+                O, Ch = grammar.sample(B)
+                C = sr.create_constants(O)
+            else:
+                C0 = rng.standard_normal((B, M_DEFAULT)).astype(np.float32)
+                tb = tapes.generate(B, M_DEFAULT, seed=args.seed * 100 + r, mean_length=8.0, n_vars=n_vars,
+                                    p_const_leaf=0.3, X_screen=Xs, C_screen=C0,
+                                    screen_fn=lambda o, c, Xs_, Cs_: workloads._gpu_zero_denominators(
+                                        Xs_, o, c, Cs_, str(dev)))
+                O, Ch, C = (torch.tensor(a, device=dev) for a in (tb.ops, tb.ch, C0))
             torch.cuda.synchronize()
             gen_s += time.perf_counter() - t0
             for name in ("plain", "warm"):
@@ -776,10 +788,13 @@ def run_search(args, rank, world, local):
         line = {"metric": METRIC, "value": out["warm"]["expressions_per_s"], "unit": UNIT, "n_gpus": world,
                 "steps": args.rounds, "warmup": 0, "ms_per_step": 1000.0 * arms["warm"]["t"] / args.rounds,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": f"full search round: {args.rounds} rounds of B={B} new expressions (mean length 8, "
-                                       f"padded 64, +-*/ sin cos exp log, 3 variables) fitted to N={N} points of one "
-                                       "hidden 5-operator target, max_iter=100; warm arm trained online after every round",
-                           "B": B, "N": N, "target_ops": [int(v) for v in t_ops[t_ops != 0]]},
+                "config": {"workload": f"full search round: {args.rounds} rounds of B={B} new expressions ("
+                                       + ("drawn on the device from a 17-rule grammar, mean postfix length 6.7"
+                                          if args.candidates == "pcfg" else "host generator, mean length 8")
+                                       + f", padded 64, +-*/ sin cos exp log, 3 variables) fitted to N={N} points of "
+                                       "one hidden 5-operator target, max_iter=100; warm arm trained online after "
+                                       "every round", "B": B, "N": N, "candidates": args.candidates,
+                           "target_ops": [int(v) for v in t_ops[t_ops != 0]]},
                 "arms": out, "warm_vs_plain": out["warm"]["expressions_per_s"] / out["plain"]["expressions_per_s"],
                 "generation_s": gen_s, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
@@ -913,6 +928,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--cpu-eval-sample", type=int, default=4096)
     ap.add_argument("--cpu-sample-expr", type=int, default=1048576)
+    ap.add_argument("--candidates", default="pcfg", choices=["pcfg", "tapes"],
+                    help="search workload: candidates from the device grammar sampler or the host generator")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
