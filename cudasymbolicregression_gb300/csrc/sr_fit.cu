@@ -1095,10 +1095,12 @@ static void* pick_kernel(int V, int SPL) {
 // Launch shape.  A CTA of W warps works on one problem, each warp on every W-th
 // chunk of 32V points, so an expensive problem (many closures) finishes W times
 // sooner and the tail of the persistent grid shrinks.  Unless the caller fixes
-// them, W keeps about 64 points per warp (1..8 warps) and V is the one of 1 and 2
-// that keeps more work resident per SM (resident warps, with a warp of two points
-// per lane counted as 1.6 warps: its independent chains hide latency).  The warp
-// tables hold a row per distinct variable of a tape: VR = min(n_x, Lmax) rows.
+// them: V = 1 (two or four points per lane were slower on every workload timed on a
+// GB300: README problem 115 ms at V = 2 against 79 ms at V = 1), W the smallest
+// power of two that leaves at most 64 points to a warp (1..8), doubled while the
+// batch alone would leave the GPU short of 16 warps per SM and a warp still gets more
+// than 32 points (1024 README problems: 6.2 ms at W = 4 against 15.7 ms at W = 1).
+// The warp tables hold a row per distinct variable of a tape: VR = min(n_x, Lmax) rows.
 static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
   const int Imax = (o.max_operators > 0 && o.max_operators < Lmax) ? o.max_operators : Lmax;
   sh.Imax = Imax;
@@ -1115,7 +1117,9 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
   int W = o.warps_per_block;
   if (W <= 0) {
     W = 1;
-    while (W < 8 && (int64_t)W * 2 * 64 <= N) W *= 2;
+    while (W < 8 && (int64_t)W * 64 < N) W *= 2;
+    const int64_t want_warps = (int64_t)(sms > 0 ? sms : 148) * 16;
+    while (W < 8 && (int64_t)W * 32 < N && B * W < want_warps) W *= 2;
   }
   if (W > 8) W = 8;  // __launch_bounds__(256)
   const int vc[3] = {1, 2, 4};
@@ -1124,7 +1128,7 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
   for (int w = W; w >= 1 && best < 0; w >>= 1) {
     for (int vi = 0; vi < 3; ++vi) {
       const int V = vc[vi];
-      if (o.points_per_lane ? V != o.points_per_lane : V == 4) continue;
+      if (o.points_per_lane ? V != o.points_per_lane : V != 1) continue;
       void* k = pick_kernel(V, sh.SPL);
       if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
         set_error("fit kernel shared memory attribute failed");
@@ -1135,7 +1139,7 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
       int per_sm = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, w * 32, cb) != cudaSuccess || per_sm < 1)
         continue;
-      const double score = per_sm * w * (V == 1 ? 1.0 : V == 2 ? 1.6 : 2.4);
+      const double score = (double)per_sm * w;
       if (score > best) {
         best = score;
         bestV = V;
