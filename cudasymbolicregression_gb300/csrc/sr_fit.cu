@@ -65,7 +65,7 @@ struct FitArgs {
   int Imax;         // rows of the per-warp node tables: largest count of operator nodes
   int VR;           // rows of the per-warp table for variables (distinct variables of a tape)
   float* ws_vec;    // per warp: 2 * hist * SPL*32 floats (s and y rings)
-  double* ws_scal;  // per warp: 2 * hist doubles (alpha, rho)
+  double* ws_scal;  // per CTA: 2 * hist 8-byte words (alpha, rho of each pair, float pairs)
   int* counter;
   int32_t* status;
 };
@@ -193,6 +193,34 @@ __device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
 // The total of a float pair (see F2).
 __device__ __forceinline__ float f2_val(F2 a) { return isfinite(a.hi) ? __fadd_rn(a.hi, a.lo) : a.hi; }
 
+// Normalised float pairs for the two-loop recursion (Dekker's double-float
+// arithmetic on the FP32 pipe, about 44 significant bits): hi is the rounded value,
+// lo the remainder.  f2_norm turns a cascaded sum (see F2) into one (TwoSum of its
+// parts); products use FMA for the exact product of the high parts.
+__device__ __forceinline__ F2 f2_norm(F2 a) {
+  if (!isfinite(a.hi)) return F2{a.hi, 0.f};
+  const float s = __fadd_rn(a.hi, a.lo);
+  const float bv = __fsub_rn(s, a.hi);
+  return F2{s, __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bv)), __fsub_rn(a.lo, bv))};
+}
+
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  if (!isfinite(p)) return F2{p, 0.f};
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const float s = __fadd_rn(p, e);
+  return F2{s, __fsub_rn(e, __fsub_rn(s, p))};
+}
+
+__device__ __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_norm(f2_add(a, F2{-b.hi, -b.lo})); }
+
+__device__ __forceinline__ F2 f2_of_double(double d) {
+  const float hi = __double2float_rn(d);
+  return F2{hi, isfinite(hi) ? __double2float_rn(__dsub_rn(d, (double)hi)) : 0.f};
+}
+
 __device__ __forceinline__ F2 warp_sum_f2(float v) {
   F2 a{v, 0.f};
 #pragma unroll
@@ -241,6 +269,35 @@ __device__ __forceinline__ double dot(const Problem<SPL>& P, const Slots<SPL>& a
     return __shfl_sync(0xffffffffu, acc, 0);
   }
   return wsum_d(acc);
+}
+
+// Dot product of two slot vectors as a normalised float pair (TwoProduct by FMA,
+// cascaded pair sums, the same lane butterflies as dot()); every lane gets it.
+template <int SPL>
+__device__ __forceinline__ F2 dot_pair(const Problem<SPL>& P, const Slots<SPL>& a, const Slots<SPL>& b) {
+  F2 acc{0.f, 0.f};
+#pragma unroll
+  for (int s = 0; s < SPL; ++s) {
+    if (P.active(s)) {
+      const float pr = __fmul_rn(a.v[s], b.v[s]);
+      acc = f2_add(acc, F2{pr, __fmaf_rn(a.v[s], b.v[s], -pr)});
+    }
+  }
+  if (SPL == 1 && P.nslots <= 16) {
+    const int width = P.nslots <= 4 ? 4 : (P.nslots <= 8 ? 8 : 16);
+    for (int o = width >> 1; o > 0; o >>= 1) {
+      const F2 t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
+      acc = f2_add(acc, t);
+    }
+    acc = F2{__shfl_sync(0xffffffffu, acc.hi, 0), __shfl_sync(0xffffffffu, acc.lo, 0)};
+  } else {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const F2 t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
+      acc = f2_add(acc, t);
+    }
+  }
+  return f2_norm(acc);
 }
 
 // Dot product of two slot vectors with float-pair accumulation (TwoProduct by
@@ -606,8 +663,10 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
   // history rings and two-loop scalars of this CTA (used by warp 0)
   float* ringS = A.ws_vec + (int64_t)blockIdx.x * 2 * A.hist * SPL * 32;
   float* ringY = ringS + (int64_t)A.hist * SPL * 32;
-  double* alph = A.ws_scal + (int64_t)blockIdx.x * 2 * A.hist;
-  double* rhos = alph + A.hist;
+  // per history pair: alpha of the current direction and rho = 1 / (s.y + eps), each a
+  // normalised float pair in one 8-byte word
+  float2* alph = reinterpret_cast<float2*>(A.ws_scal + (int64_t)blockIdx.x * 2 * A.hist);
+  float2* rhos = alph + A.hist;
   const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
 
   while (true) {
@@ -903,7 +962,10 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
           // curvature of the new pair, computed once: rho of its slot, and s.y, y.y for gamma
           last_sy = dot(P, yv, sv);
           last_yy = dot(P, yv, yv);
-          if (lane == 0) rhos[slot] = 1.0 / __dadd_rn(last_sy, A.eps);
+          if (lane == 0) {
+            const F2 r = f2_of_double(1.0 / __dadd_rn(last_sy, A.eps));
+            rhos[slot] = make_float2(r.hi, r.lo);
+          }
         }
         __syncwarp();
         x = xn;
@@ -940,16 +1002,19 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
                 si.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
                 yi.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
               }
-              const double a = __dmul_rn(rhos[sl], dot(P, si, q));
+              // alpha = rho (s.q) and q -= alpha y: float pairs on the FP32 pipe (GB300's
+              // FP64 pipe runs a warp instruction at a small fraction of the FP32 rate)
+              const float2 r2 = rhos[sl];
+              const F2 a = f2_mul(F2{r2.x, r2.y}, dot_pair(P, si, q));
 #pragma unroll
-              for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dsub_rn((double)q.v[s], __dmul_rn(a, (double)yi.v[s]));
-              if (lane == 0) alph[i] = a;
+              for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(-a.lo, yi.v[s], __fmaf_rn(-a.hi, yi.v[s], q.v[s]));
+              if (lane == 0) alph[i] = make_float2(a.hi, a.lo);
             }
             __syncwarp();
             {
-              const double gam = last_sy / __dadd_rn(last_yy, A.eps);
+              const F2 gam = f2_of_double(last_sy / __dadd_rn(last_yy, A.eps));
 #pragma unroll
-              for (int s = 0; s < SPL; ++s) q.v[s] = (float)(gam * (double)q.v[s]);
+              for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(q.v[s], gam.lo, __fmul_rn(q.v[s], gam.hi));
             }
             for (int i = 0; i < h; ++i) {
               const int sl = (head + i) % A.hist;
@@ -959,10 +1024,12 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
                 si.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
                 yi.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
               }
-              const double be = __dmul_rn(rhos[sl], dot(P, yi, q));
-              const double coef = __dsub_rn(alph[i], be);
+              const float2 r2 = rhos[sl];
+              const F2 be = f2_mul(F2{r2.x, r2.y}, dot_pair(P, yi, q));
+              const float2 al = alph[i];
+              const F2 coef = f2_sub(F2{al.x, al.y}, be);
 #pragma unroll
-              for (int s = 0; s < SPL; ++s) q.v[s] = (float)__dadd_rn((double)q.v[s], __dmul_rn((double)si.v[s], coef));
+              for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(coef.lo, si.v[s], __fmaf_rn(coef.hi, si.v[s], q.v[s]));
             }
           }
           if (warp == 0) {

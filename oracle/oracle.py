@@ -146,8 +146,9 @@ def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_gra
              line_search_fn="strong_wolfe", line_search_max_iter=10, dot_mode=1):
     """Per-problem restatement of ``symbolic_torch.optimize``.
 
-    dot_mode=0 follows the reference's float32 arithmetic; dot_mode=1 follows the
-    fused kernel's (double dots and two-loop scalars).
+    dot_mode=0 follows the reference's float32 arithmetic; dot_mode=1 approximates
+    the fused kernel's (double dots and two-loop scalars, where the kernel uses
+    float pairs).
     Returns dict(C, Y, iters, evals, loss, err); iters[b] = -code for a problem
     whose closures raised an error.  Y=None selects the raw
     objective (mean of the root value) used by the Rosenbrock test.
