@@ -216,6 +216,20 @@ __device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
 
 __device__ __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_norm(f2_add(a, F2{-b.hi, -b.lo})); }
 
+// a / b for normalised pairs (one float division, the remainder by FMA, a second
+// division for the correction).
+__device__ __forceinline__ F2 f2_div(F2 a, F2 b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  if (!isfinite(q1)) return F2{q1, 0.f};
+  const float ph = __fmul_rn(q1, b.hi);
+  const float pl = __fmaf_rn(q1, b.hi, -ph);
+  float r = __fsub_rn(__fsub_rn(a.hi, ph), pl);
+  r = __fmaf_rn(-q1, b.lo, __fadd_rn(r, a.lo));
+  const float q2 = __fdiv_rn(r, b.hi);
+  const float sum = __fadd_rn(q1, q2);
+  return F2{sum, __fsub_rn(q2, __fsub_rn(sum, q1))};
+}
+
 __device__ __forceinline__ F2 f2_of_double(double d) {
   const float hi = __double2float_rn(d);
   return F2{hi, isfinite(hi) ? __double2float_rn(__dsub_rn(d, (double)hi)) : 0.f};
@@ -229,12 +243,6 @@ __device__ __forceinline__ F2 warp_sum_f2(float v) {
     a = f2_add(a, b);
   }
   return a;
-}
-
-__device__ __forceinline__ double wsum_d(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
 }
 
 // Parameter-slot vectors: slot j lives in lane j % 32, register j / 32.
@@ -255,24 +263,10 @@ struct Problem {
   __device__ __forceinline__ bool real(int s) const { return s * 32 + lane < K; }
 };
 
-template <int SPL>
-__device__ __forceinline__ double dot(const Problem<SPL>& P, const Slots<SPL>& a, const Slots<SPL>& b) {
-  double acc = 0.0;
-#pragma unroll
-  for (int s = 0; s < SPL; ++s)
-    if (P.active(s)) acc += (double)a.v[s] * (double)b.v[s];
-  if (SPL == 1 && P.nslots <= 16) {
-    // only lanes below 2^k hold terms: the butterfly steps above 2^(k-1) would add
-    // exact zeros, so lane 0 ends with the same sum after the lower steps alone
-    const int width = P.nslots <= 4 ? 4 : (P.nslots <= 8 ? 8 : 16);
-    for (int o = width >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    return __shfl_sync(0xffffffffu, acc, 0);
-  }
-  return wsum_d(acc);
-}
-
 // Dot product of two slot vectors as a normalised float pair (TwoProduct by FMA,
-// cascaded pair sums, the same lane butterflies as dot()); every lane gets it.
+// cascaded pair sums); every lane gets it.  With one slot per lane and at most 16
+// slots, only the lanes below the next power of two hold terms, so the butterfly
+// stops there and lane 0's total is broadcast.
 template <int SPL>
 __device__ __forceinline__ F2 dot_pair(const Problem<SPL>& P, const Slots<SPL>& a, const Slots<SPL>& b) {
   F2 acc{0.f, 0.f};
@@ -657,6 +651,10 @@ enum Phase : int { PH_INIT = 0, PH_BRACKET, PH_ZOOM_LO, PH_ZOOM, PH_BACKTRACK, P
 
 template <int V, int SPL>
 __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
+  // L-BFGS constants in the iteration's arithmetic: eps as a float pair, the gradient
+  // tolerance in float32 (the reference compares a float32 norm with it)
+  const F2 eps2 = f2_of_double(A.eps);
+  const float tolf = __double2float_rn(A.tol);
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, A.VR, warp);
@@ -773,7 +771,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
     float f = 0.f;
     bool poison = false;
     int h = 0, head = 0, it = 0;
-    double last_sy = 0.0, last_yy = 0.0;  // warp 0: s.y and y.y of the newest history pair
+    F2 last_sy{0.f, 0.f}, last_yy{0.f, 0.f};  // warp 0: s.y and y.y of the newest history pair
     // line-search state
     int phase = PH_INIT;
     int lsi = 0, zj = 0;
@@ -960,10 +958,10 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
             ringY[slot * SPL * 32 + s * 32 + lane] = yv.v[s];
           }
           // curvature of the new pair, computed once: rho of its slot, and s.y, y.y for gamma
-          last_sy = dot(P, yv, sv);
-          last_yy = dot(P, yv, yv);
+          last_sy = dot_pair(P, yv, sv);
+          last_yy = dot_pair(P, yv, yv);
           if (lane == 0) {
-            const F2 r = f2_of_double(1.0 / __dadd_rn(last_sy, A.eps));
+            const F2 r = f2_div(F2{1.f, 0.f}, f2_norm(f2_add(last_sy, eps2)));
             rhos[slot] = make_float2(r.hi, r.lo);
           }
         }
@@ -988,7 +986,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
 
       // ---- start of an outer iteration: convergence test, direction, line search ----
       if (begin_iter) {
-        if (it >= A.max_iter || sqrt((double)dot_f2(P, g, g)) < A.tol) {
+        if (it >= A.max_iter || __fsqrt_rn(dot_f2(P, g, g)) < tolf) {
           phase = PH_DONE;
         } else {
           // two-loop recursion (lbfgs_batch.py:65-103), by warp 0 for the CTA
@@ -1012,7 +1010,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
             }
             __syncwarp();
             {
-              const F2 gam = f2_of_double(last_sy / __dadd_rn(last_yy, A.eps));
+              const F2 gam = f2_div(last_sy, f2_norm(f2_add(last_yy, eps2)));
 #pragma unroll
               for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(q.v[s], gam.lo, __fmul_rn(q.v[s], gam.hi));
             }
