@@ -281,9 +281,10 @@ void sro_node_fwd_f32(int64_t n, const int64_t *op, const float *a, const float 
  * dot_mode 1 approximates the fused kernel's arithmetic: dots and two-loop scalars
  * in double (s.y, y.y, the alphas, beta, gamma, rho), vector updates rounded once
  * to float, line-search scalars in float, and the per-constant gradient summed
- * over the points in double.  The kernel carries the two-loop's dots, alphas and
- * betas as float pairs (about 44 significant bits) and its sums as cascaded float
- * pairs, so the two agree to far below a float ulp on well-conditioned problems.
+ * over the points in double.  The kernel carries all of these as float pairs
+ * (about 44 significant bits; no FP64 in its iteration) and its sums as cascaded
+ * float pairs, so the two agree to far below a float ulp on well-conditioned
+ * problems.
  */
 typedef struct {
     const float *X; int64_t N, nx;
