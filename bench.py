@@ -75,10 +75,10 @@ SAMPLE_METRIC = "expressions sampled from a grammar, parsed to postfix and linke
 # workloads, from ncu captures of a 4x / 16x smaller batch scaled by the number of
 # problems (profiles/fit_lbfgs_ragged_B16384_N512.txt,
 # profiles/eval_forward_B4096_N1024.txt).
-FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10780928 + 20224)}
+FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10720000 + 16384)}
 # Issue utilisation of the fit kernel from the same capture (smsp__issue_active, percent):
 # the binding resource of an interpreter whose instructions are mostly integer/control work.
-FIT_ISSUE_ACTIVE_PCT = 46.9
+FIT_ISSUE_ACTIVE_PCT = 49.5
 EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000)}
 
 
