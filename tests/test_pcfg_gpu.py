@@ -230,3 +230,21 @@ def test_prefix_round_trips_on_large_batches():
     real = pre != 0
     assert ((par < idx) | ~real).all()
     assert (((par == -1) & real).sum(1) == 1).all()
+
+
+def test_infix_rendering_length_limits():
+    """The reference's length cases (tests/test_to_infix.py:258-340): nested logs
+    rendered exactly at the output length in both notations, one token short raising
+    501, and 30 nested logs from the 128-token grammar."""
+    p = _pcfg(NOTATION_GRAMMAR, "E", 2, 64)
+    X0, LOG, LP, RP = 50, 13, 52, 53
+    for depth, width in ((3, 10), (5, 16)):
+        want = [LOG, LP] * depth + [X0] + [RP] * depth
+        for fn, row in (("postfix_to_infix", [X0] + [LOG] * depth), ("prefix_to_infix", [LOG] * depth + [X0])):
+            x = torch.tensor([row], device="cuda")
+            assert getattr(p, fn)(x, width)[0].tolist() == want, fn
+            with pytest.raises(RuntimeError, match="longer than the maximum allowed length"):
+                getattr(p, fn)(x, width - 1)
+    p128 = _pcfg(NOTATION_GRAMMAR, "E", 2, 128)
+    out = p128.postfix_to_infix(torch.tensor([[X0] + [LOG] * 30], device="cuda"), 91)
+    assert out[0].tolist() == [LOG, LP] * 30 + [X0] + [RP] * 30
