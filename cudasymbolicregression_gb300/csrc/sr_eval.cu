@@ -124,15 +124,16 @@ __global__ void __launch_bounds__(256) tape_compile_kernel(const int64_t* __rest
 // ------------------------------------------------------------------------------------
 constexpr int kSlice = 256;
 
-// Fill count values at p with NaN, 16-byte vector stores in the aligned middle.
+// Fill count values at p with NaN, 16-byte vector stores in the aligned middle;
+// threads tid = 0 .. nthreads - 1 share the range.
 template <typename T>
-__device__ __forceinline__ void warp_fill_nan(T* p, size_t count, int lane) {
+__device__ __forceinline__ void fill_nan(T* p, size_t count, int tid, int nthreads) {
   const T qnan = M_<T>::nan();
   constexpr int kVec = 16 / sizeof(T);
   size_t head = (size_t)((16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15) / sizeof(T);
   if (reinterpret_cast<uintptr_t>(p) % sizeof(T)) head = count;  // unaligned element type: scalar path
   if (head > count) head = count;
-  for (size_t i = lane; i < head; i += 32) __stcs(p + i, qnan);
+  for (size_t i = tid; i < head; i += nthreads) __stcs(p + i, qnan);
   const size_t nvec = (count - head) / kVec;
   float4 v4;
   if (sizeof(T) == 4) {
@@ -143,8 +144,21 @@ __device__ __forceinline__ void warp_fill_nan(T* p, size_t count, int lane) {
     v4 = make_float4(lo, hi, lo, hi);
   }
   float4* q = reinterpret_cast<float4*>(p + head);
-  for (size_t i = lane; i < nvec; i += 32) __stcs(q + i, v4);
-  for (size_t i = head + nvec * kVec + lane; i < count; i += 32) __stcs(p + i, qnan);
+  for (size_t i = tid; i < nvec; i += nthreads) __stcs(q + i, v4);
+  for (size_t i = head + nvec * kVec + tid; i < count; i += nthreads) __stcs(p + i, qnan);
+}
+
+// Rows L..M-1 of every tape's cache block are NaN.  They form one contiguous range per
+// tape, streamed by one CTA per tape (grid-stride) on a side stream, concurrently with
+// the forward kernel, which writes only the real rows: the forward is bound by
+// instruction latency and leaves most of the HBM write bandwidth to this kernel.
+template <typename T>
+__global__ void __launch_bounds__(256) pad_fill_kernel(const int32_t* __restrict__ meta, int64_t B, int64_t M,
+                                                       int64_t NK, T* __restrict__ cache) {
+  for (int64_t b = blockIdx.x; b < B; b += gridDim.x) {
+    const int64_t L = meta[b * 4];
+    fill_nan(cache + (size_t)b * M * NK + (size_t)L * NK, (size_t)(M - L) * NK, (int)threadIdx.x, (int)blockDim.x);
+  }
 }
 
 // Shared-memory layout of one warp of the forward kernel: the tape words, the
@@ -289,12 +303,7 @@ __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__
         }
       }
     }
-    // rows after the last real node: NaN (one contiguous block when the unit spans all points)
-    if (nslices == 1) {
-      warp_fill_nan(out + (size_t)L * N * K, (size_t)(M - L) * N * K, lane);
-    } else {
-      for (int64_t k = L; k < M; ++k) warp_fill_nan(out + ((size_t)k * N + n0) * K, (size_t)(n1 - n0) * K, lane);
-    }
+    // rows after the last real node are filled with NaN by pad_fill_kernel
     __syncwarp();
   }
 }
@@ -801,9 +810,28 @@ static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* de
     set_error("tape of %d nodes does not fit in shared memory", Lmax);
     return SR_ERR_UNSUPPORTED;
   }
-  kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, as_stream(stream)>>>(X, N, n_x, desc, meta, order, B, M, Lmax,
-                                                                          C, c_sb, c_sm, c_sk, K, cache);
-  return launch_check("eval_forward_kernel");
+  cudaStream_t st = as_stream(stream);
+  Aux* aux = aux_for_current_device();
+  if (!aux) return SR_ERR_CUDA;
+  std::lock_guard<std::mutex> hold(aux->mu);
+  rc = cuda_check(cudaEventRecord(aux->fork, st), "fork event");
+  if (!rc) rc = cuda_check(cudaStreamWaitEvent(aux->stream, aux->fork, 0), "fork wait");
+  if (rc) return rc;
+  kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, Lmax, C, c_sb, c_sm,
+                                                           c_sk, K, cache);
+  rc = launch_check("eval_forward_kernel");
+  if (!rc) {
+    // enqueued after the forward grid, whose CTAs are placed first (see launch_backward);
+    // eight CTAs per SM: at two the fill streamed too slowly to hide (3.75 against 3.65 ms
+    // for the forward of 65536 tapes, N = 1024)
+    int64_t fblocks = (int64_t)device_sm_count() * 8;
+    if (fblocks > B) fblocks = B;
+    pad_fill_kernel<T><<<(unsigned)fblocks, 256, 0, aux->stream>>>(meta, B, M, N * K, cache);
+    rc = launch_check("pad_fill_kernel");
+  }
+  const int rj = cuda_check(cudaEventRecord(aux->join, aux->stream), "join event");
+  const int rw = rj ? rj : cuda_check(cudaStreamWaitEvent(st, aux->join, 0), "join wait");
+  return rc ? rc : rw;
 }
 
 template <typename T, bool kMulti, int V>
