@@ -654,9 +654,9 @@ def run_eval(args, rank, world, local):
                                 "GB/s": (bwd_bytes if k == "eval_backward_kernel" else fwd_bytes) / v / 1e9}
                             for k, v in ktimes.items()},
                 "expressions_per_s": B * world / t_step,
-                # per step: tape compile, forward, padding fill, padding check, one adjoint
-                # grid per length class (<= 16, <= 32, longer) that the batch reaches
-                "gpu_launches": (4 + (tapes.max_len > 16) + (tapes.max_len > 32)) * args.steps,
+                # per step: tape compile, padding fill, padding check, and one forward and
+                # one adjoint grid per length class (<= 16, <= 32, longer) the batch reaches
+                "gpu_launches": (3 + 2 * (1 + (tapes.max_len > 16) + (tapes.max_len > 32))) * args.steps,
                 "clocks": clk.summary()}
         if e2e:
             line["e2e"] = e2e

@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__
                                                            const uint32_t* __restrict__ desc,
                                                            const int32_t* __restrict__ meta,
                                                            const int32_t* __restrict__ order, int64_t B,
-                                                           int64_t M, int Lmax, const T* __restrict__ C,
+                                                           int64_t M, int Llo, int Lhi, const T* __restrict__ C,
                                                            int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K_,
                                                            T* __restrict__ cache) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   constexpr uint32_t RB = 32u * (uint32_t)sizeof(T);
   constexpr uint32_t kRowStride = (uint32_t)sizeof(T) << 24;
-  const FwdLayout ly = forward_layout<T>(Lmax);
+  const FwdLayout ly = forward_layout<T>(Lhi);
   unsigned char* wb = smem + (size_t)warp * ly.bytes;
   uint32_t* tape = reinterpret_cast<uint32_t*>(wb);
   uint32_t* pw = reinterpret_cast<uint32_t*>(wb + ly.pw);
@@ -229,6 +229,7 @@ __global__ void __launch_bounds__(256) eval_forward_kernel(const T* __restrict__
     const int64_t ti = u / nslices, sl = u - ti * nslices;
     const int64_t b = order ? (int64_t)order[ti] : ti;
     const int L = meta[b * 4];
+    if (L <= Llo || L > Lhi) continue;  // another class's grid takes it (warp-uniform)
     for (int k = lane; k < L; k += 32) tape[k] = desc[b * M + k];
     if (lane == 0) bc[0] = T(0);
     __syncwarp();
@@ -802,14 +803,8 @@ static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* de
   if (!X && n_x > 0) { set_error("null X"); return SR_ERR_INVALID_ARGUMENT; }
   if (!desc || !meta || !C || !cache) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
-  const size_t per_warp = forward_layout<T>(Lmax).bytes;
-  Shape sh;
   auto kern = K == 1 ? eval_forward_kernel<T, false> : eval_forward_kernel<T, true>;
   const int64_t units = B * ((N + kSlice - 1) / kSlice);
-  if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, units, sh)) {
-    set_error("tape of %d nodes does not fit in shared memory", Lmax);
-    return SR_ERR_UNSUPPORTED;
-  }
   cudaStream_t st = as_stream(stream);
   Aux* aux = aux_for_current_device();
   if (!aux) return SR_ERR_CUDA;
@@ -817,17 +812,30 @@ static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* de
   rc = cuda_check(cudaEventRecord(aux->fork, st), "fork event");
   if (!rc) rc = cuda_check(cudaStreamWaitEvent(aux->stream, aux->fork, 0), "fork wait");
   if (rc) return rc;
-  kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, Lmax, C, c_sb, c_sm,
-                                                           c_sk, K, cache);
-  rc = launch_check("eval_forward_kernel");
-  if (!rc) {
-    // enqueued after the forward grid, whose CTAs are placed first (see launch_backward);
-    // eight CTAs per SM: at two the fill streamed too slowly to hide (3.75 against 3.65 ms
-    // for the forward of 65536 tapes, N = 1024)
-    int64_t fblocks = (int64_t)device_sm_count() * 8;
-    if (fblocks > B) fblocks = B;
-    pad_fill_kernel<T><<<(unsigned)fblocks, 256, 0, aux->stream>>>(meta, B, M, N * K, cache);
-    rc = launch_check("pad_fill_kernel");
+  // one persistent grid per class of tape lengths, as in launch_backward
+  int cls[3][2], nc = 0;
+  if (Lmax > 32) { cls[nc][0] = 32; cls[nc][1] = Lmax; ++nc; }
+  if (Lmax > 16) { cls[nc][0] = 16; cls[nc][1] = Lmax < 32 ? Lmax : 32; ++nc; }
+  cls[nc][0] = -1; cls[nc][1] = Lmax < 16 ? Lmax : 16; ++nc;
+  for (int ci = 0; ci < nc && !rc; ++ci) {
+    Shape sh;
+    if (!pick_shape(reinterpret_cast<const void*>(kern), forward_layout<T>(cls[ci][1]).bytes, units, sh)) {
+      set_error("tape of %d nodes does not fit in shared memory", cls[ci][1]);
+      rc = SR_ERR_UNSUPPORTED;
+      break;
+    }
+    kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, cls[ci][0],
+                                                             cls[ci][1], C, c_sb, c_sm, c_sk, K, cache);
+    rc = launch_check("eval_forward_kernel");
+    if (!rc && ci == 0) {
+      // enqueued after the first forward grid, whose CTAs are placed first (see
+      // launch_backward); eight CTAs per SM: at two the fill streamed too slowly to hide
+      // (3.75 against 3.65 ms for the forward of 65536 tapes, N = 1024)
+      int64_t fblocks = (int64_t)device_sm_count() * 8;
+      if (fblocks > B) fblocks = B;
+      pad_fill_kernel<T><<<(unsigned)fblocks, 256, 0, aux->stream>>>(meta, B, M, N * K, cache);
+      rc = launch_check("pad_fill_kernel");
+    }
   }
   const int rj = cuda_check(cudaEventRecord(aux->join, aux->stream), "join event");
   const int rw = rj ? rj : cuda_check(cudaStreamWaitEvent(st, aux->join, 0), "join wait");

@@ -64,7 +64,8 @@ def check_local(X, ops, ch, C, cache):
     return {"nodes": int(got.size), "max_ulp": int(d.max(initial=0))}
 
 
-def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999, gross=1e3, max_outliers=None):
+def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999, gross=1e3, max_outliers=None,
+                   abs_scale=None):
     """Device float32 result vs the reference float32 result and the FP64 oracle.
 
     * at least ``min_frac_tight`` of the entries within rtol of the reference result;
@@ -77,6 +78,11 @@ def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999
       difference upstream of a discontinuous operation (floor, ceil, a comparison
       in a domain check, tan near a pole) can move one value far although every
       node is exact given its inputs, which check_local verifies separately.
+
+    abs_scale (the sum of the absolute values of the terms an entry adds up) makes the
+    percentile test measure errors relative to max(|ref64|, abs_scale): for sums whose
+    order is not fixed (atomic accumulation, in the reference too) the rounding error
+    scales with the terms, not with a cancelled total.
     """
     got = np.asarray(got, np.float64)
     ref32 = np.asarray(ref32, np.float64)
@@ -98,6 +104,8 @@ def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999
     stats = {"frac_tight": frac}
     if fin.any():
         scale = np.maximum(np.abs(ref64[fin]), 1e-30)
+        if abs_scale is not None:
+            scale = np.maximum(scale, np.asarray(abs_scale, np.float64)[fin])
         rg = err_g[fin] / scale
         rr = err_r[fin] / scale
         for q in (50.0, 99.9):

@@ -78,7 +78,10 @@ def test_backward_vs_reference_golden(golden, name):
     out.backward(cuda(g["gout"]))
     gC64, gX64, err = oracle.eval_bwd(g["X"], g["ops"], g["ch"], g["C"], g["gout"], dtype=np.float64)
     check_accuracy(C.grad.cpu().numpy(), g["gC"], gC64, rtol=1e-5, atol=1e-5, min_frac_tight=0.99)
-    check_accuracy(X.grad.cpu().numpy(), g["gX"], gX64, rtol=1e-4, atol=1e-4, min_frac_tight=0.9)
+    # gX is an atomic sum over the tapes (in the reference too): where the fixture holds
+    # the per-tape contributions, errors are measured against their absolute sum
+    scale = np.abs(g["gX_rows"]).sum(0) if "gX_rows" in g.files else None
+    check_accuracy(X.grad.cpu().numpy(), g["gX"], gX64, rtol=1e-4, atol=1e-4, min_frac_tight=0.9, abs_scale=scale)
     if name == "single_ops":
         assert_close_nan(C.grad.cpu().numpy(), g["gC"], rtol=1e-5, atol_scale=1e-5)
 
