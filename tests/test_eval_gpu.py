@@ -465,3 +465,56 @@ def test_gradients_match_central_finite_differences_fp64():
             agree += int((np.abs(rich - ad) <= tol)[ok].sum())
     assert checked > 200
     assert agree / checked >= 0.99, (agree, checked)
+
+
+def test_forward_and_adjoint_replay_in_a_cuda_graph():
+    """The forward (length-class grids + the padding fill on the side stream) and the
+    adjoint (the padding check on the side stream + length-class grids), called through
+    the C ABI inside a CUDA graph capture: the fork/join of the side stream is recorded,
+    and a replay gives the direct calls' results bit for bit."""
+    sr = _sr()
+    from cudasymbolicregression_gb300 import _lib, tapes as tg
+    from cudasymbolicregression_gb300.tape import compile_tapes
+    rng = np.random.default_rng(31)
+    B, M, N, nx = 3000, 64, 256, 3
+    # no division: a zero denominator would make both runs report 204, which is not the point here
+    tb = tg.generate(B, M, seed=32, mean_length=20.0, n_vars=nx, p_const_leaf=0.3, binary=(40, 41, 42))
+    X = cuda(rng.uniform(-2, 2, (N, nx)).astype(np.float32))
+    C = cuda(rng.standard_normal((B, M)).astype(np.float32))
+    ops, ch = cuda(tb.ops), cuda(tb.ch)
+    tp = compile_tapes(ops, ch, nx)
+    L = _lib.lib()
+    gout = torch.zeros((B, M, N), device="cuda")
+    root = torch.tensor(np.maximum((tb.ops != 0).sum(1) - 1, 0), device="cuda")
+    gout[torch.arange(B, device="cuda"), root] = 1.0
+
+    def run(cache, gC, status):
+        st = _lib.stream_ptr(X.device)
+        _lib.check(L.sr_eval_forward_f32(_lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), _lib.ptr(tp.order),
+                                         B, M, tp.max_len, _lib.ptr(C), M, 1, _lib.ptr(cache), st), "forward")
+        _lib.check(L.sr_eval_backward_f32(_lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), _lib.ptr(tp.order),
+                                          B, M, tp.max_len, _lib.ptr(C), M, 1, _lib.ptr(gout), _lib.ptr(gC), None,
+                                          _lib.ptr(status), st), "backward")
+
+    ref = (torch.empty((B, M, N), device="cuda"), torch.empty((B, M), device="cuda"),
+           torch.zeros(1, dtype=torch.int32, device="cuda"))
+    run(*ref)
+    torch.cuda.synchronize()
+    assert int(ref[2].item()) == 0
+    out = (torch.full((B, M, N), 7.0, device="cuda"), torch.full((B, M), 7.0, device="cuda"),
+           torch.zeros(1, dtype=torch.int32, device="cuda"))
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        run(*out)  # warm-up on the capture stream
+    torch.cuda.current_stream().wait_stream(s)
+    out[0].fill_(7.0)
+    out[1].fill_(7.0)
+    with torch.cuda.graph(g):
+        run(*out)
+    g.replay()
+    torch.cuda.synchronize()
+    assert int(out[2].item()) == 0
+    assert torch.equal(torch.nan_to_num(out[0], nan=-9.0), torch.nan_to_num(ref[0], nan=-9.0))
+    assert torch.equal(torch.nan_to_num(out[1], nan=-9.0), torch.nan_to_num(ref[1], nan=-9.0))
