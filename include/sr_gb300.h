@@ -77,11 +77,14 @@ int sr_tape_compile(const int64_t *ops_dev, const int64_t *ch_dev, int64_t B, in
  * and the padding after the last real node are NaN.  Replaces the reference's
  * host loop of M launches of evaluation_forward_step_k
  * (reference src/symbolic_evaluation.cpp:39-92, src/evaluation_kernels_cuda.cu:51-216,
- * 634-652).  One warp interprets one tape, lanes over data points.
+ * 634-652).  One warp interprets one tape, lanes over data points, one grid per
+ * class of tape lengths; the NaN padding rows are written by a kernel on a
+ * library-owned side stream, forked from `stream` and joined back into it before the
+ * call returns (a CUDA graph capture of `stream` records both).
  * max_len: largest meta[0] of the batch (stats[1] of sr_tape_compile), or 0 for M;
- * it sizes the per-warp shared-memory node table.  order_dev (B) int32, or NULL:
- * the order in which the persistent warps take the tapes (longest first balances
- * the work).
+ * every tape's meta[0] must be at most max_len (it sizes the per-warp shared-memory
+ * node tables).  order_dev (B) int32, or NULL: the order in which the persistent warps
+ * take the tapes (longest first balances the work).
  */
 int sr_eval_forward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                         const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
@@ -98,9 +101,11 @@ int sr_eval_forward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint3
  * grad_C (B, M) (zero at non-constant nodes) and, when grad_X_dev is not NULL,
  * accumulates into grad_X (N, n_x), which the caller zeroes first.  status_dev
  * is zeroed and then receives 201 (nonzero gradient on a NO_OP node) or 204
- * (a/b with b = 0 and a nonzero gradient).  Replaces SymbolicEvaluation::backward
- * and evaluation_backward_step_k (reference src/symbolic_evaluation.cpp:94-168,
- * src/evaluation_kernels_cuda.cu:218-632, 654-673).
+ * (a/b with b = 0 and a nonzero gradient; 201 is kept over 204).  Replaces
+ * SymbolicEvaluation::backward and evaluation_backward_step_k (reference
+ * src/symbolic_evaluation.cpp:94-168, src/evaluation_kernels_cuda.cu:218-632, 654-673).
+ * order_dev, max_len and the side stream (here the padding-row check) as for the
+ * forward.
  */
 int sr_eval_backward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                          const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
