@@ -859,32 +859,20 @@ static int launch_backward_v(const T* X, int64_t N, int64_t n_x, const uint32_t*
   return launch_check("eval_backward_kernel");
 }
 
-// Points per lane of the adjoint for tapes of up to Lhi nodes.  One: two points per
-// lane (one dispatch for both, their chains interleaved in registers) run at half the
-// resident warps, and the adjoint took 1.4x as long on a GB300 (10.3 ms against 7.1 ms
-// for 65536 tapes of mean length 20, N = 1024).
-template <typename T>
-static int backward_points_per_lane(int64_t N, int Lhi) {
-  (void)N;
-  (void)Lhi;
-  return 1;
-}
-
+// One point per lane: two points per lane (one dispatch for both, their chains
+// interleaved in registers) ran at half the resident warps, and the adjoint took 1.4x as
+// long on a GB300 (10.3 ms against 7.1 ms for 65536 tapes of mean length 20, N = 1024),
+// so only the one-point kernels are instantiated.
 template <typename T>
 static int launch_backward_class(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                                  const int32_t* order, int64_t B, int64_t M, int Llo, int Lhi, const T* C,
                                  int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const T* gout, T* gC, T* gX,
                                  int32_t* status, bool vec16, cudaStream_t st) {
-  const int V = backward_points_per_lane<T>(N, Lhi);
   if (K == 1)
-    return V == 2 ? launch_backward_v<T, false, 2>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk,
-                                                   K, gout, gC, gX, status, vec16, st)
-                  : launch_backward_v<T, false, 1>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk,
-                                                   K, gout, gC, gX, status, vec16, st);
-  return V == 2 ? launch_backward_v<T, true, 2>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K,
-                                                gout, gC, gX, status, vec16, st)
-                : launch_backward_v<T, true, 1>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K,
-                                                gout, gC, gX, status, vec16, st);
+    return launch_backward_v<T, false, 1>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K, gout,
+                                          gC, gX, status, vec16, st);
+  return launch_backward_v<T, true, 1>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K, gout, gC,
+                                       gX, status, vec16, st);
 }
 
 template <typename T>
