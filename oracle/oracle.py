@@ -69,6 +69,13 @@ def lib() -> ctypes.CDLL:
         L.sro_infix_parse.restype = None
         L.sro_postfix_children.argtypes = [vp, i64, i64, vp, vp]
         L.sro_postfix_children.restype = None
+        for name in ("sro_postfix_to_infix", "sro_prefix_to_infix"):
+            getattr(L, name).argtypes = [vp, i64, i64, i32, vp, i64, vp]
+            getattr(L, name).restype = None
+        L.sro_prefix_reorder.argtypes = [vp, i64, i64, i32, i32, vp, vp]
+        L.sro_prefix_reorder.restype = None
+        L.sro_prefix_parent.argtypes = [vp, i64, i64, i32, vp, vp]
+        L.sro_prefix_parent.restype = None
         _lib = L
     return _lib
 
@@ -215,6 +222,40 @@ def postfix_children(post):
     err = np.empty(B, np.int64)
     lib().sro_postfix_children(_p(x), B, M, _p(ch), _p(err))
     return ch, err
+
+
+def to_infix(rows, n_vars, max_infix_len, prefix=False):
+    """Restatement of postfix_to_infix / prefix_to_infix (src/pcfg_cpu.cpp:449-811).
+    Returns (infix (B, max_infix_len) int64, errors (B))."""
+    x = _c(rows, np.int64)
+    B, M = x.shape
+    out = np.empty((B, int(max_infix_len)), np.int64)
+    err = np.empty(B, np.int64)
+    fn = lib().sro_prefix_to_infix if prefix else lib().sro_postfix_to_infix
+    fn(_p(x), B, M, int(n_vars), _p(out), int(max_infix_len), _p(err))
+    return out, err
+
+
+def reorder(rows, n_vars, from_prefix):
+    """Restatement of prefix_to_postfix (from_prefix) and postfix_to_prefix
+    (src/pcfg_cpu.cpp:812-993).  Returns (tokens (B, M) int64, errors (B))."""
+    x = _c(rows, np.int64)
+    B, M = x.shape
+    out = np.empty((B, M), np.int64)
+    err = np.empty(B, np.int64)
+    lib().sro_prefix_reorder(_p(x), B, M, int(n_vars), int(bool(from_prefix)), _p(out), _p(err))
+    return out, err
+
+
+def prefix_parent(rows, n_vars):
+    """Restatement of get_prefix_parent (src/pcfg_cpu.cpp:995-1064).
+    Returns (parents (B, M) int64, -1 for roots and padding; errors (B))."""
+    x = _c(rows, np.int64)
+    B, M = x.shape
+    out = np.empty((B, M), np.int64)
+    err = np.empty(B, np.int64)
+    lib().sro_prefix_parent(_p(x), B, M, int(n_vars), _p(out), _p(err))
+    return out, err
 
 
 def num_threads() -> int:

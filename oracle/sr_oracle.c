@@ -18,6 +18,10 @@
  *   - autograd host loops              src/symbolic_evaluation.cpp:39-168
  *   - optimize() closure               symbolic_torch/optimization.py:51-112
  *   - LBFGS_batch                      symbolic_torch/lbfgs_batch.py:61-326
+ *   - grammar sampler (own stream)     src/pcfg_cpu.cpp:10-119
+ *   - infix -> postfix / prefix        src/pcfg_cpu.cpp:121-448
+ *   - notation conversions             src/pcfg_cpu.cpp:449-1142 (postfix/prefix ->
+ *                                      infix, prefix <-> postfix, parents, children)
  *
  * Floating-point contraction must be off (-ffp-contract=off) so that x86 and
  * aarch64 hosts give the same bits.
@@ -785,6 +789,259 @@ void sro_postfix_children(const int64_t *post, int64_t B, int64_t M, int64_t *ch
             st[sp++] = (int32_t)i;
         }
         if (!err && len > 0 && sp != 1) err = 407;
+        errors[b] = err;
+    }
+}
+
+/* ---- the remaining notation conversions ------------------------------------------
+ * postfix -> infix (src/pcfg_cpu.cpp:449-635), prefix -> infix (637-811), prefix <->
+ * postfix (812-993) and the parent table of prefix rows (995-1064).  Symbols are
+ * checked first as the reference's wrappers do (src/pcfg.cpp:644-657): -1 for a symbol
+ * below 0, -2 for one at or above VAR_START_ID + n_vars.  A row with an error is left
+ * all NO_OP (parents: all -1); the reference raises for the batch instead. */
+static int sro_functional(int64_t op)
+{
+    return (op >= OP_SIN && op <= OP_LOG) || (op >= OP_SQRT && op <= OP_NEG);
+}
+
+static int sro_symbols(const int64_t *row, int64_t M, int64_t n_ops)
+{
+    int flag = 0;
+    for (int64_t i = 0; i < M; ++i) {
+        if (row[i] < 0) return -1;
+        if (row[i] >= n_ops) flag = -2;
+    }
+    return flag;
+}
+
+/* Shape of a row read from the right (postfix) or from the left (prefix): its length,
+ * 509 for a token after the padding, 508 for several roots. */
+static int sro_shape(const int64_t *row, int64_t M, int from_right, int *len)
+{
+    int started = 0, ended = 0, balance = 0, roots = 0;
+    *len = 0;
+    for (int64_t s = 0; s < M; ++s) {
+        const int64_t t = row[from_right ? M - 1 - s : s];
+        if (t == OP_NO_OP) {
+            if (from_right) { if (started) return 509; }
+            else ended = 1;
+            continue;
+        }
+        if (!from_right && ended) return 509;
+        started = 1;
+        ++*len;
+        balance += sro_token_arity(t) - 1;
+        if (balance == -1) ++roots;
+    }
+    return roots > 1 ? 508 : 0;
+}
+
+void sro_postfix_to_infix(const int64_t *post, int64_t B, int64_t M, int32_t n_vars, int64_t *infix, int64_t M_out,
+                          int64_t *errors)
+{
+    const int64_t lp = OP_VAR0 + n_vars, rp = lp + 1;
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < B; ++b) {
+        const int64_t *row = post + b * M;
+        int64_t *o = infix + b * M_out;
+        int64_t buf[3 * SRO_HARD_MAX];
+        int32_t ops[SRO_HARD_MAX];
+        int waiting_left[SRO_HARD_MAX];
+        int top = 3 * SRO_HARD_MAX - 1, sp = 0, len = 0, err;
+        for (int64_t i = 0; i < M_out; ++i) o[i] = OP_NO_OP;
+        err = sro_symbols(row, M, OP_VAR0 + n_vars);
+        if (!err) err = sro_shape(row, M, 1, &len);
+        for (int k = len - 1; k >= 0 && !err; --k) {   /* the rendering is built from its end */
+            const int64_t t = row[k];
+            if (sro_token_arity(t) == 0) {
+                if (top < 0) { err = 504; break; }
+                buf[top--] = t;
+                int done = 1;
+                while (done && sp > 0 && !err) {
+                    const int32_t parent = ops[sp - 1];
+                    if (sro_token_arity(parent) == 1) {
+                        if (sro_functional(parent)) {
+                            if (top - 1 < 0) { err = 504; break; }
+                            buf[top--] = lp;
+                            buf[top--] = parent;
+                        } else {
+                            if (top < 0) { err = 504; break; }
+                            buf[top--] = lp;
+                        }
+                        --sp;
+                    } else if (!waiting_left[sp - 1]) {
+                        if (top < 0) { err = 504; break; }
+                        buf[top--] = parent;
+                        waiting_left[sp - 1] = 1;
+                        done = 0;
+                    } else {
+                        if (top < 0) { err = 504; break; }
+                        buf[top--] = lp;
+                        --sp;
+                    }
+                }
+            } else {
+                if (sp >= SRO_HARD_MAX) { err = 504; break; }
+                ops[sp] = (int32_t)t;
+                waiting_left[sp] = 0;
+                if (sro_token_arity(t) == 1 && !sro_functional(t)) {
+                    if (top < 0) { err = 504; break; }
+                    buf[top--] = t;
+                }
+                if (top < 0) { err = 504; break; }
+                buf[top--] = rp;
+                ++sp;
+            }
+        }
+        if (!err && sp > 0) err = sro_token_arity(ops[sp - 1]) == 1 ? 505 : 506;
+        if (!err && len > 0) {
+            const int n = 3 * SRO_HARD_MAX - 1 - top;
+            if (n > M_out) err = 501;
+            else for (int i = 0; i < n; ++i) o[i] = buf[top + 1 + i];
+        }
+        errors[b] = err;
+    }
+}
+
+void sro_prefix_to_infix(const int64_t *pre, int64_t B, int64_t M, int32_t n_vars, int64_t *infix, int64_t M_out,
+                         int64_t *errors)
+{
+    const int64_t lp = OP_VAR0 + n_vars, rp = lp + 1;
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < B; ++b) {
+        const int64_t *row = pre + b * M;
+        int64_t *o = infix + b * M_out;
+        int32_t ops[SRO_HARD_MAX];
+        int waiting_right[SRO_HARD_MAX];
+        int64_t n = 0;
+        int sp = 0, len = 0, err;
+        for (int64_t i = 0; i < M_out; ++i) o[i] = OP_NO_OP;
+        err = sro_symbols(row, M, OP_VAR0 + n_vars);
+        if (!err) err = sro_shape(row, M, 0, &len);
+        for (int k = 0; k < len && !err; ++k) {       /* left to right */
+            const int64_t t = row[k];
+            const int ar = sro_token_arity(t);
+            if (ar == 0) {
+                if (n >= M_out) { err = 501; break; }
+                o[n++] = t;
+                int done = 1;
+                while (done && sp > 0 && !err) {
+                    const int32_t parent = ops[sp - 1];
+                    if (sro_token_arity(parent) == 1) {
+                        if (n >= M_out) { err = 501; break; }
+                        o[n++] = rp;
+                        if (!sro_functional(parent)) {
+                            if (n >= M_out) { err = 501; break; }
+                            o[n++] = parent;
+                        }
+                        --sp;
+                    } else if (!waiting_right[sp - 1]) {
+                        if (n >= M_out) { err = 501; break; }
+                        o[n++] = parent;
+                        waiting_right[sp - 1] = 1;
+                        done = 0;
+                    } else {
+                        if (n >= M_out) { err = 501; break; }
+                        o[n++] = rp;
+                        --sp;
+                    }
+                }
+            } else {
+                if (sp >= SRO_HARD_MAX) { err = 504; break; }
+                ops[sp] = (int32_t)t;
+                waiting_right[sp] = 0;
+                if (ar == 1 && sro_functional(t)) {
+                    if (n + 2 > M_out) { err = 501; break; }
+                    o[n++] = t;
+                    o[n++] = lp;
+                } else {
+                    if (n >= M_out) { err = 501; break; }
+                    o[n++] = lp;
+                }
+                ++sp;
+            }
+        }
+        if (!err && sp > 0) err = sro_token_arity(ops[sp - 1]) == 1 ? 505 : 506;
+        if (err) for (int64_t i = 0; i < M_out; ++i) o[i] = OP_NO_OP;
+        errors[b] = err;
+    }
+}
+
+/* from_prefix = 1: prefix -> postfix; 0: postfix -> prefix. */
+void sro_prefix_reorder(const int64_t *in, int64_t B, int64_t M, int32_t n_vars, int32_t from_prefix, int64_t *out,
+                        int64_t *errors)
+{
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < B; ++b) {
+        const int64_t *row = in + b * M;
+        int64_t *o = out + b * M;
+        int32_t node[SRO_HARD_MAX], missing[SRO_HARD_MAX];
+        int sp = 0, n = 0, balance = 0, roots = 0, seen = 0, err;
+        for (int64_t i = 0; i < M; ++i) o[i] = OP_NO_OP;
+        err = sro_symbols(row, M, OP_VAR0 + n_vars);
+        for (int64_t s = 0; s < M && !err; ++s) {
+            const int64_t i = from_prefix ? s : M - 1 - s;
+            const int64_t t = row[i];
+            if (t == OP_NO_OP) {
+                if (from_prefix) seen = 1;
+                else if (seen) err = 509;
+                continue;
+            }
+            if (from_prefix && seen) { err = 509; break; }
+            if (!from_prefix) seen = 1;
+            const int ar = sro_token_arity(t);
+            balance += ar - 1;
+            if (balance == -1) ++roots;
+            if (sp >= SRO_HARD_MAX) { err = 504; break; }
+            node[sp] = (int32_t)i;
+            missing[sp++] = ar;
+            while (sp > 0 && missing[sp - 1] == 0) {
+                --sp;
+                if (n >= M) { err = from_prefix ? 502 : 503; break; }
+                o[n++] = row[node[sp]];
+                if (sp > 0) --missing[sp - 1];
+            }
+        }
+        if (!err && sp != 0) err = sro_token_arity(row[node[sp - 1]]) == 1 ? 505 : 506;
+        if (!err && roots != 1 && n > 0) err = 508;
+        if (!err && !from_prefix)
+            for (int i = 0, j = n - 1; i < j; ++i, --j) { const int64_t x = o[i]; o[i] = o[j]; o[j] = x; }
+        if (err) for (int64_t i = 0; i < M; ++i) o[i] = OP_NO_OP;
+        errors[b] = err;
+    }
+}
+
+void sro_prefix_parent(const int64_t *pre, int64_t B, int64_t M, int32_t n_vars, int64_t *parent, int64_t *errors)
+{
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < B; ++b) {
+        const int64_t *row = pre + b * M;
+        int64_t *par = parent + b * M;
+        int32_t st[SRO_HARD_MAX];
+        int sp = 0, started = 0, err;
+        for (int64_t i = 0; i < M; ++i) par[i] = -1;
+        err = sro_symbols(row, M, OP_VAR0 + n_vars);
+        for (int64_t i = M - 1; i >= 0 && !err; --i) {   /* from the right */
+            const int64_t t = row[i];
+            if (t == OP_NO_OP) {
+                if (started) err = 408;
+                continue;
+            }
+            started = 1;
+            const int ar = sro_token_arity(t);
+            if (ar == 1) {
+                if (sp < 1) { err = 404; break; }
+                par[st[--sp]] = i;
+            } else if (ar == 2) {
+                if (sp < 2) { err = 405; break; }
+                par[st[--sp]] = i;
+                par[st[--sp]] = i;
+            }
+            if (sp >= SRO_HARD_MAX) { err = 406; break; }
+            st[sp++] = (int32_t)i;
+        }
+        if (!err && started && sp != 1) err = 407;
+        if (err) for (int64_t i = 0; i < M; ++i) par[i] = -1;
         errors[b] = err;
     }
 }
