@@ -355,7 +355,7 @@ def fit_objective(X, Y, ops, ch, C_base, pred, clip_grad: float = 10.0):
 
 
 def gated_warm_start(net: WarmStartMLP, X, Y, ops, ch, C_plain, clip: float = 10.0) -> torch.Tensor:
-    """The plain initialisation as fallback and judge: per problem, the start (warm
+    """The plain initialisation as fallback and arbiter: per problem, the start (warm
     or plain) with the lower initial MSE, measured by one closure of the fused fit
     kernel (max_iter=0) for each; a non-finite loss counts as +inf and ties keep the
     plain start."""
