@@ -1,5 +1,6 @@
 """Host-side checks that need no GPU: the C-ABI library loads and exports every
-entry point include/sr_gb300.h declares, the argument checks raise the
+entry point include/sr_gb300.h declares, the ctypes signatures and struct mirrors
+match the header's declarations, the argument checks raise the
 reference's messages, and the tape generator emits valid postfix tapes."""
 import os
 import re
@@ -109,3 +110,58 @@ def test_tape_generator_screens_zero_denominators():
         for k in range(16):
             if tb.ops[b, k] == 43:
                 assert not (cache[b, tb.ch[b, k, 1]] == 0).any()
+
+
+def _c_kind(decl: str) -> str:
+    """Kind of one C parameter or field declaration: pointer, integer width or float width."""
+    d = re.sub(r"\b(const|struct)\b", " ", decl).strip()
+    if "*" in d:
+        return "p"
+    return {"int64_t": "i64", "int32_t": "i32", "int": "i32", "uint64_t": "u64", "double": "f64",
+            "float": "f32"}[d.split()[0]]
+
+
+def _ctypes_kind(t) -> str:
+    import ctypes
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or isinstance(getattr(t, "_type_", None), type):
+        return "p"  # untyped pointers, strings and ctypes.POINTER(...)
+    return {ctypes.c_int64: "i64", ctypes.c_int32: "i32", ctypes.c_uint64: "u64", ctypes.c_double: "f64",
+            ctypes.c_float: "f32"}[t]
+
+
+def _header_text():
+    txt = open(os.path.join(ROOT, "include", "sr_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return re.sub(r"//[^\n]*", "", txt)
+
+
+def test_ctypes_signatures_match_header():
+    """Every prototype of include/sr_gb300.h against the ctypes table the package binds
+    with: parameter count, and for each parameter and the result its kind (pointer,
+    int32, int64, uint64, float, double), so that no argument is passed at the wrong
+    width."""
+    from cudasymbolicregression_gb300 import _lib
+    protos = re.findall(r"([A-Za-z_][A-Za-z0-9_ ]*?[\s*]+)(sr_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", _header_text())
+    assert {name for _, name, _ in protos} == set(_lib._SIGS)
+    for ret, name, params in protos:
+        args, res = _lib._SIGS[name]
+        kinds = [] if params.strip() in ("", "void") else [_c_kind(p) for p in params.split(",")]
+        assert kinds == [_ctypes_kind(a) for a in args], name
+        assert _c_kind(ret) == _ctypes_kind(res), name
+
+
+def test_ctypes_structs_match_header():
+    """sr_fit_options and sr_mlp_epilogue: field names (the header's device pointers
+    carry a ``_dev`` suffix), order and kinds of the ctypes mirrors equal the header's."""
+    from cudasymbolicregression_gb300 import _lib
+    txt = _header_text()
+    for cname, mirror in (("sr_fit_options", _lib.FitOptions), ("sr_mlp_epilogue", _lib.MlpEpilogue)):
+        body = re.search(r"typedef struct[^{]*\{([^}]*)\}\s*" + cname + r"\s*;", txt).group(1)
+        fields = []
+        for decl in filter(None, (d.strip() for d in body.split(";"))):
+            # a base type, then declarators whose own stars make them pointers
+            m = re.match(r"((?:const\s+)?[A-Za-z_][A-Za-z0-9_]*)\s*(.*)$", decl)
+            for d in (x.strip() for x in m.group(2).split(",")):
+                kind = "p" if d.startswith("*") else _c_kind(m.group(1))
+                fields.append((re.sub(r"_dev$", "", d.lstrip("* ")), kind))
+        assert fields == [(n, _ctypes_kind(t)) for n, t in mirror._fields_], cname
