@@ -108,3 +108,48 @@ def test_optimize_first_iteration_bit_exact(golden):
     g = golden("optimize_ragged")
     r1 = oracle.optimize(g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=0, dot_mode=0)
     assert np.array_equal(r1["C"], g["C"])
+
+
+def _rosenbrock_tape():
+    """f = (1 - c0)^2 + 100 (c1 - c0^2)^2 as a postfix tape over two constants (slots 1, 4)."""
+    ops = [2, 1, 41, 14, 1, 14, 41, 14, 6, 6, 42, 5, 42, 42, 40]
+    ch = [(-1, -1), (-1, -1), (0, 1), (2, -1), (-1, -1), (1, -1), (4, 5), (6, -1), (-1, -1), (-1, -1), (8, 9),
+          (-1, -1), (10, 11), (12, 7), (3, 13)]
+    return np.array(ops, np.int64), np.array(ch, np.int64)
+
+
+@pytest.mark.parametrize("ls,key", [("strong_wolfe", "x_wolfe"), ("backtracking", "x_backtracking")])
+def test_optimize_rosenbrock_known_answer(golden, ls, key):
+    """reference tests/test_lbfgs_batch.py:38-75: LBFGS_batch from ten starts reaches
+    (1, 1); the oracle, in the reference's float32 arithmetic, reaches the reference's
+    own end points (tests/golden/rosenbrock.npz)."""
+    g = golden("rosenbrock")
+    x0 = g["x0"]
+    B = x0.shape[1]
+    ops1, ch1 = _rosenbrock_tape()
+    ops, ch = np.tile(ops1, (B, 1)), np.tile(ch1, (B, 1, 1))
+    C = np.zeros((B, ops1.shape[0]), np.float32)
+    C[:, 1], C[:, 4] = x0[0], x0[1]
+    o = oracle.optimize(np.zeros((1, 1), np.float32), None, ops, ch, C, max_iter=250, history_size=15,
+                        line_search_fn=ls, dot_mode=0)
+    np.testing.assert_allclose(o["C"][:, [1, 4]], 1.0, atol=1e-3)
+    np.testing.assert_allclose(o["C"][:, [1, 4]], g[key].T, atol=1e-3)
+
+
+def test_evaluation_known_answers():
+    """reference tests/test_symbolic_evaluation.py:435-478 (C = 3.14 gives 1 + C = 4.14
+    and sin(3.14)) and :192-217 (a NO_OP row evaluates to NaN and passes zero
+    gradients), on the oracle."""
+    X = np.random.default_rng(0).standard_normal((4, 1)).astype(np.float32)
+    C = np.array([[3.14, 0, 0]], np.float32)
+    ch = np.array([[[-1, -1], [-1, -1], [0, 1]]], np.int64)
+    cache = oracle.eval_fwd(X, np.array([[1, 2, 40]], np.int64), ch, C)
+    np.testing.assert_allclose(cache[0, 2], np.float32(3.14) + np.float32(1), atol=1e-6)
+    ch = np.array([[[-1, -1], [0, -1]]], np.int64)
+    cache = oracle.eval_fwd(X, np.array([[1, 10]], np.int64), ch, C[:, :2])
+    np.testing.assert_allclose(cache[0, 1], np.sin(np.float32(3.14)), atol=1e-6)
+    ops, ch, C0 = np.zeros((1, 1), np.int64), -np.ones((1, 1, 2), np.int64), np.zeros((1, 1), np.float32)
+    X2 = np.random.default_rng(1).standard_normal((10, 2)).astype(np.float32)
+    assert np.isnan(oracle.eval_fwd(X2, ops, ch, C0)).all()
+    gC, gX, err = oracle.eval_bwd(X2, ops, ch, C0, np.zeros((1, 1, 10), np.float32))
+    assert err == 0 and not gC.any() and not gX.any()
