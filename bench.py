@@ -74,12 +74,18 @@ SAMPLE_METRIC = "expressions sampled from a grammar, parsed to postfix and linke
 # DRAM bytes (read + write) of one launch of the dominant kernel on the default
 # workloads, from ncu captures of a 4x / 16x smaller batch scaled by the number of
 # problems (profiles/fit_lbfgs_ragged_B16384_N512.txt,
-# profiles/eval_forward_B4096_N1024.txt).
-FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10720000 + 16384)}
+# profiles/eval_forward_B4096_N1024.txt, profiles/eval_backward_B4096_N1024.txt).
+# The fit kernel's traffic per problem is set by N, M and the history, not by the
+# operator set, so the warm-start line's held-out problems (same lengths, M and N)
+# scale the same B=4096 ragged capture.
+FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10720000 + 16384),
+                     ("warmstart", 65536, 512): 16 * (10720000 + 16384)}
 # Issue utilisation of the fit kernel from the same capture (smsp__issue_active, percent):
 # the binding resource of an interpreter whose instructions are mostly integer/control work.
 FIT_ISSUE_ACTIVE_PCT = 49.5
-EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000)}
+# The adjoint call: its three length-class grids and the concurrent padding check.
+EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000),
+                      ("eval_backward_kernel", 65536, 1024): 16 * (1075467264 + 10125312)}
 
 
 def peaks():
