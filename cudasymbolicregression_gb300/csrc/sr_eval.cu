@@ -722,12 +722,21 @@ static Aux* aux_for_current_device() {
   std::lock_guard<std::mutex> hold(create_mu);
   Aux& a = aux[dev];
   if (!a.stream) {
-    if (cuda_check(cudaStreamCreateWithFlags(&a.stream, cudaStreamNonBlocking), "side stream") ||
-        cuda_check(cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming), "fork event") ||
-        cuda_check(cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming), "join event")) {
-      a.stream = nullptr;
+    // created into locals and published together, so a failure leaves nothing behind
+    cudaStream_t s = nullptr;
+    cudaEvent_t f = nullptr, j = nullptr;
+    int rc = cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "side stream");
+    if (!rc) rc = cuda_check(cudaEventCreateWithFlags(&f, cudaEventDisableTiming), "fork event");
+    if (!rc) rc = cuda_check(cudaEventCreateWithFlags(&j, cudaEventDisableTiming), "join event");
+    if (rc) {
+      if (j) cudaEventDestroy(j);
+      if (f) cudaEventDestroy(f);
+      if (s) cudaStreamDestroy(s);
       return nullptr;
     }
+    a.fork = f;
+    a.join = j;
+    a.stream = s;
   }
   return &a;
 }

@@ -1176,9 +1176,10 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
     return SR_ERR_UNSUPPORTED;
   }
   int dev = 0, sms = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (cuda_check(cudaGetDevice(&dev), "cudaGetDevice") ||
+      cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count") ||
+      cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "shared memory limit"))
+    return SR_ERR_CUDA;
   int W = o.warps_per_block;
   if (W <= 0) {
     W = 1;
