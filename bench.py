@@ -159,11 +159,20 @@ def dist_env():
     return rank, world, local
 
 
+def load_oracle():
+    """The oracle (the checker and CPU baseline only), built, with every host thread
+    this process may use (a launcher such as torch.distributed.run sets
+    OMP_NUM_THREADS=1 for its ranks)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    oracle.set_num_threads(len(os.sched_getaffinity(0)))
+    return oracle
+
+
 def cpu_sample_run(wl, n_sample: int, max_iter: int = MAX_ITER):
     """The CPU oracle port of optimize() (plain start) on the first n_sample problems."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the checker / CPU baseline only
-    oracle.build()
+    oracle = load_oracle()
     idx = np.arange(min(n_sample, wl.ops.shape[0]))
     t0 = time.perf_counter()
     r = oracle.optimize(wl.X, wl.Y[idx], wl.ops[idx], wl.ch[idx], wl.C[idx], max_iter=max_iter, dot_mode=0)
@@ -192,9 +201,7 @@ def cpu_fit_workload(args, B, N):
 def cpu_grammar_run(n, L, seed):
     """The oracle's sampler, parser and child table (OpenMP) on n expressions of the
     sampling workload: (expressions/s, seconds, threads)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the checker / CPU baseline only
-    oracle.build()
+    oracle = load_oracle()
     from cudasymbolicregression_gb300.pcfg import ProbabilisticContextFreeGrammar
     from cudasymbolicregression_gb300.workloads import SEARCH_GRAMMAR
     p = ProbabilisticContextFreeGrammar(SEARCH_GRAMMAR, "E", L, 3, torch.device("cpu"))
@@ -506,9 +513,7 @@ def cpu_eval_sample(wl, chunk: int, seconds: float = 10.0):
     """The CPU oracle port of the reference's forward + adjoint over consecutive
     chunks of the workload's tapes (wrapping around) until `seconds` have passed;
     returns algorithmic GB/s, seconds and tapes processed."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the checker / CPU baseline only
-    oracle.build()
+    oracle = load_oracle()
     B, M = wl.ops.shape
     N = wl.X.shape[0]
     chunk = min(chunk, B)
@@ -944,22 +949,24 @@ def main():
     args.N = dN if args.N is None else args.N
 
     rank, world, local = dist_env()
+    if args.impl == "reference":
+        # the CPU port on rank 0 alone: no GPU and no process group; the other ranks
+        # exit without work
+        run_reference(args, rank)
+        return
     if world > 1:
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    if args.impl == "reference":
-        run_reference(args, rank)
+    torch.cuda.set_device(local)
+    if args.workload == "eval":
+        run_eval(args, rank, world, local)
+    elif args.workload == "search":
+        run_search(args, rank, world, local)
+    elif args.workload == "sample":
+        run_sample(args, rank, world, local)
     else:
-        torch.cuda.set_device(local)
-        if args.workload == "eval":
-            run_eval(args, rank, world, local)
-        elif args.workload == "search":
-            run_search(args, rank, world, local)
-        elif args.workload == "sample":
-            run_sample(args, rank, world, local)
-        else:
-            run_fit(args, rank, world, local)
+        run_fit(args, rank, world, local)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

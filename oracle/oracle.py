@@ -60,6 +60,8 @@ def lib() -> ctypes.CDLL:
                                        dbl, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
         L.sro_optimize_f32.restype = ctypes.c_int
         L.sro_num_threads.restype = ctypes.c_int
+        L.sro_set_num_threads.argtypes = [ctypes.c_int]
+        L.sro_set_num_threads.restype = ctypes.c_int
         L.sro_node_fwd_f32.argtypes = [i64, vp, vp, vp, vp, vp, vp]
         L.sro_node_fwd_f32.restype = None
         i32 = ctypes.c_int32
@@ -260,3 +262,8 @@ def prefix_parent(rows, n_vars):
 
 def num_threads() -> int:
     return lib().sro_num_threads()
+
+
+def set_num_threads(n: int) -> int:
+    """OpenMP threads of the oracle's parallel loops; returns the count in effect."""
+    return lib().sro_set_num_threads(int(n))

@@ -599,6 +599,18 @@ int sro_num_threads(void)
 #endif
 }
 
+/* Threads of the parallel loops from now on (a launcher may have set OMP_NUM_THREADS=1
+ * before the OpenMP runtime was loaded); returns the count now in effect. */
+int sro_set_num_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+    return sro_num_threads();
+}
+
 /* ---- grammar sampling and infix parsing --------------------------------------------
  * Restates the reference's sampler (src/pcfg_cpu.cpp:10-119, the same derivation as
  * src/pcfg_cuda.cu:10-118) and shunting-yard parsers (src/pcfg_cpu.cpp:121-448).
