@@ -457,7 +457,7 @@ def run_fit(args, rank, world, local):
                "d2h_bytes_per_step": int(d2h), "arm": "warm" if warm else "plain"}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the CPU baseline is an N=1 figure
         v, dt, threads, _ = cpu_sample_run(wl, args.cpu_sample, max_iter=max_iter)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"first {args.cpu_sample} problems, plain start, full max_iter={max_iter} ({dt:.1f} s)"}
@@ -642,7 +642,7 @@ def run_eval(args, rank, world, local):
                "path": "evaluate() + loss=sum of root outputs + loss.backward() from pinned host buffers"}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the CPU baseline is an N=1 figure
         v, dt, ntapes, threads = cpu_eval_sample(wl, args.cpu_eval_sample)
         cpu = {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"{ntapes} tapes in chunks of {args.cpu_eval_sample}, forward + adjoint ({dt:.1f} s)"}
@@ -894,7 +894,7 @@ def run_sample(args, rank, world, local):
                "path": "ProbabilisticContextFreeGrammar.sample(B), then Ops and Ch copied to pinned host memory"}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the CPU baseline is an N=1 figure
         n = min(B, args.cpu_sample_expr)
         v, dt, threads = cpu_grammar_run(n, L, args.seed)
         cpu = {"value": v, "unit": "expressions/s", "cores": threads, "kind": "port",
