@@ -160,7 +160,7 @@ def dist_env():
 
 
 def load_oracle():
-    """The oracle (the checker and CPU baseline only), built, with every host thread
+    """The oracle (the CPU baseline only), built, with every host thread
     this process may use (a launcher such as torch.distributed.run sets
     OMP_NUM_THREADS=1 for its ranks)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))

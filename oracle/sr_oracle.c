@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this file:
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
- * and only as the checker (or as the timed stand-in for the reference's CPU
+ * and only to check results (or as the timed stand-in for the reference's CPU
  * path).  Parity is pinned against outputs of the reference itself, run in the
  * development container and committed as fixtures under tests/golden/.
  *
