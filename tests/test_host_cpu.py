@@ -165,3 +165,25 @@ def test_ctypes_structs_match_header():
                 kind = "p" if d.startswith("*") else _c_kind(m.group(1))
                 fields.append((re.sub(r"_dev$", "", d.lstrip("* ")), kind))
         assert fields == [(n, _ctypes_kind(t)) for n, t in mirror._fields_], cname
+
+
+def test_ragged_chunks_prefix_property():
+    """The first chunks of a large ragged batch are the same problems as a smaller batch
+    (what lets a bounded CPU sample stand for the benchmark's batch problem by problem),
+    and the batch has the documented shapes: lengths 3..64, at most 8 constants."""
+    from cudasymbolicregression_gb300 import workloads
+
+    def roots(X, ops, ch, C):
+        cache = oracle.eval_fwd(X, ops, ch, C)
+        root = np.maximum((ops != 0).sum(1) - 1, 0)
+        return cache[np.arange(ops.shape[0]), root]
+    big = workloads.ragged_fit_chunks(B=1024, N=64, chunk=512, seed=3, root_eval=roots)
+    small = workloads.ragged_fit_chunks(B=512, N=64, chunk=512, seed=3, root_eval=roots)
+    for k in ("ops", "ch", "C", "Y"):
+        np.testing.assert_array_equal(getattr(big, k)[:512], getattr(small, k), err_msg=k)
+    np.testing.assert_array_equal(big.X, small.X)
+    L = (big.ops != 0).sum(1)
+    assert L.min() >= 3 and L.max() <= 64
+    assert ((big.ops == 1).sum(1) <= 8).all()
+    assert oracle.validate(big.ops, big.ch) == 0
+    assert np.isfinite(big.Y).all()
