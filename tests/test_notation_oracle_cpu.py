@@ -124,3 +124,38 @@ def test_round_trips_on_random_tapes():
     real = pre != 0
     assert (((par == -1) & real).sum(1) == 1).all()
     assert ((par < np.arange(pre.shape[1])) | ~real).all()
+
+
+@pytest.mark.parametrize("M,n_vars", [(1, 1), (2, 1), (7, 3), (64, 1), (128, 2)])
+def test_round_trips_at_edge_sizes(M, n_vars):
+    """Tapes of every length 1..M (single leaves, full-width rows) over every operator:
+    the child table equals the generator's, postfix -> prefix -> postfix is the
+    identity, both infix renderings agree and fit in 3M tokens (each operator adds at
+    most two parentheses), and every prefix node but the root has an earlier parent."""
+    from cudasymbolicregression_gb300 import tapes
+    from cudasymbolicregression_gb300.operators import BINARY_OPS, UNARY_OPS
+    B = 400
+    lengths = np.arange(B) % M + 1
+    tb = tapes.generate(B, M, seed=M, lengths=lengths, n_vars=n_vars, unary=UNARY_OPS, binary=BINARY_OPS,
+                        p_const_leaf=0.3)
+    ch, e0 = oracle.postfix_children(tb.ops)
+    assert not e0.any()
+    np.testing.assert_array_equal(ch, tb.ch)
+    pre, e1 = oracle.reorder(tb.ops, n_vars, False)
+    back, e2 = oracle.reorder(pre, n_vars, True)
+    assert not e1.any() and not e2.any()
+    np.testing.assert_array_equal(back, tb.ops)
+    np.testing.assert_array_equal((pre != 0).sum(1), lengths)
+    inf_post, e3 = oracle.to_infix(tb.ops, n_vars, 3 * M)
+    inf_pre, e4 = oracle.to_infix(pre, n_vars, 3 * M, prefix=True)
+    assert not e3.any() and not e4.any()
+    np.testing.assert_array_equal(inf_post, inf_pre)
+    # one token short of a rendering is reported (501, too long), not truncated
+    lens = (inf_post != 0).sum(1)
+    _, e5 = oracle.to_infix(tb.ops, n_vars, int(lens.max()) - 1)
+    np.testing.assert_array_equal(e5, np.where(lens == lens.max(), 501, 0))
+    par, e6 = oracle.prefix_parent(pre, n_vars)
+    assert not e6.any()
+    real = pre != 0
+    assert (((par == -1) & real).sum(1) == 1).all()
+    assert ((par < np.arange(M)) | ~real).all()
