@@ -134,3 +134,21 @@ def test_gemm_shape_checks(L):
     # split-K bookkeeping: the pieces the kernel actually uses for k and a requested split count
     assert [L.sr_mlp_gemm_splits_used(k, s) for k, s in ((256, 1), (256, 4), (256, 3), (256, 9), (0, 2))] == \
         [1, 4, 2, 4, 0]
+
+
+def test_last_error_is_per_thread(L):
+    """sr_last_error() holds the last failure of the calling host thread only."""
+    import threading
+    off = ctypes.byref(ctypes.c_int64())
+    _rejected(L, L.sr_const_offsets(None, -1, 4, 4, 1, off, None), SR_ERR_INVALID_ARGUMENT, "invalid arguments")
+    seen = {}
+
+    def other():
+        seen["fresh"] = L.sr_last_error()
+        seen["rc"] = L.sr_pcfg_sample_infix(None, None, None, None, 4, 0, 8, 0, 8, 1, None, None, None)
+        seen["own"] = L.sr_last_error()
+    t = threading.Thread(target=other)
+    t.start()
+    t.join()
+    assert seen["fresh"] == b"" and seen["rc"] == SR_ERR_INVALID_ARGUMENT and b"max_length=0" in seen["own"]
+    assert b"invalid arguments" in L.sr_last_error()
