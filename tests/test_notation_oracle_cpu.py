@@ -159,3 +159,10 @@ def test_round_trips_at_edge_sizes(M, n_vars):
     real = pre != 0
     assert (((par == -1) & real).sum(1) == 1).all()
     assert ((par < np.arange(M)) | ~real).all()
+
+
+def test_to_string_matches_reference(gn):
+    """notation.to_string (host code) renders the reference's infix rows as the
+    reference's own to_string does (tests/golden/notation.npz)."""
+    for key_inf, key_str in (("infix", "strings"), ("infix_all", "strings_all")):
+        assert notation.to_string(torch.tensor(gn[key_inf]), 2) == [str(s) for s in gn[key_str]]
