@@ -85,6 +85,21 @@ def build(ref_root: str | None = None, verbose: bool = False) -> str | None:
     return _built_so()
 
 
+def build_error_messages(ref_root: str | None = None) -> str | None:
+    """Compile ``oracle/ref_error_messages.cpp`` against the reference's
+    ``include/error_codes.h`` (where it lies) into ``oracle/_ref/``; return the
+    binary's path, or None without the reference checkout."""
+    import subprocess
+    ref_root = ref_root or reference_root()
+    if ref_root is None:
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    exe = os.path.join(OUT, "ref_error_messages")
+    src = os.path.join(HERE, "ref_error_messages.cpp")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ref_root, "include"), src, "-o", exe], check=True)
+    return exe
+
+
 def load_reference(ref_root: str | None = None) -> types.ModuleType:
     """Import the reference package ``symbolic_torch`` (Python files from the
     reference checkout, ``_C`` from ``oracle/_ref``)."""

@@ -489,6 +489,18 @@ def case_prefix(st):
     np.savez_compressed(os.path.join(OUT, "prefix.npz"), **out)
 
 
+def case_error_messages(st=None):
+    """getErrorMessage of the reference (include/error_codes.h) for every code of its
+    enum, the gaps between them and out-of-range values, with and without a context,
+    printed by a helper compiled against the reference's header."""
+    import subprocess
+    exe = build_ref.build_error_messages()
+    rows = [ln.split("\t") for ln in subprocess.run([exe], check=True, capture_output=True,
+                                                      text=True).stdout.splitlines()]
+    np.savez_compressed(os.path.join(OUT, "error_messages.npz"), code=np.array([int(r[0]) for r in rows]),
+                        context=np.array([r[1] for r in rows]), message=np.array([r[2] for r in rows]))
+
+
 def main():
     st = build_ref.load_reference()
     torch.set_num_threads(1)
@@ -512,6 +524,7 @@ def main():
     case_multiple(st)
     case_pcfg(st)
     case_prefix(st)
+    case_error_messages(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -187,3 +187,15 @@ def test_ragged_chunks_prefix_property():
     assert ((big.ops == 1).sum(1) <= 8).all()
     assert oracle.validate(big.ops, big.ch) == 0
     assert np.isfinite(big.Y).all()
+
+
+def test_error_messages_match_reference_table():
+    """operators.error_message for every code of the reference's ErrorCode enum, the
+    gaps between them and out-of-range values, with and without a context, against
+    the reference's own getErrorMessage (tests/golden/error_messages.npz, printed by a
+    helper compiled against include/error_codes.h)."""
+    from cudasymbolicregression_gb300.operators import error_message
+    g = np.load(os.path.join(ROOT, "tests", "golden", "error_messages.npz"))
+    assert len(g["code"]) > 150
+    for code, ctx, msg in zip(g["code"], g["context"], g["message"]):
+        assert error_message(int(code), str(ctx)) == str(msg), (int(code), str(ctx))
