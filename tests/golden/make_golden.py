@@ -489,6 +489,19 @@ def case_prefix(st):
     np.savez_compressed(os.path.join(OUT, "prefix.npz"), **out)
 
 
+def case_operators(st):
+    """get_arity and is_valid_op of the reference for ids -3..199 and 0..5 variables,
+    and the Operator enum's names and values."""
+    C = sys.modules["symbolic_torch._C"]
+    ids = np.arange(-3, 200)
+    arity = np.array([C.get_arity(int(o)) for o in ids])
+    valid = np.array([[bool(C.is_valid_op(int(o), nv)) for nv in range(6)] for o in ids])
+    names = sorted(n for n, v in C.Operator.__members__.items())
+    values = np.array([int(C.Operator.__members__[n]) for n in names])
+    np.savez_compressed(os.path.join(OUT, "operators.npz"), ids=ids, arity=arity, valid=valid,
+                        names=np.array(names), values=values)
+
+
 def case_error_messages(st=None):
     """getErrorMessage of the reference (include/error_codes.h) for every code of its
     enum, the gaps between them and out-of-range values, with and without a context,
@@ -525,6 +538,7 @@ def main():
     case_pcfg(st)
     case_prefix(st)
     case_error_messages(st)
+    case_operators(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

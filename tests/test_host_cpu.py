@@ -199,3 +199,15 @@ def test_error_messages_match_reference_table():
     assert len(g["code"]) > 150
     for code, ctx, msg in zip(g["code"], g["context"], g["message"]):
         assert error_message(int(code), str(ctx)) == str(msg), (int(code), str(ctx))
+
+
+def test_operator_table_matches_reference_fixture():
+    """get_arity and is_valid_op for ids -3..199 with 0..5 variables, and every name
+    and value of the Operator enum, against the reference's own functions
+    (tests/golden/operators.npz)."""
+    import cudasymbolicregression_gb300 as sr
+    g = np.load(os.path.join(ROOT, "tests", "golden", "operators.npz"))
+    np.testing.assert_array_equal([sr.get_arity(int(o)) for o in g["ids"]], g["arity"])
+    np.testing.assert_array_equal([[sr.is_valid_op(int(o), nv) for nv in range(6)] for o in g["ids"]], g["valid"])
+    for name, value in zip(g["names"], g["values"]):
+        assert int(getattr(sr.Operator, str(name))) == int(value), name
