@@ -180,6 +180,9 @@ class ProbabilisticContextFreeGrammar:
         return self._symbol_to_id[name]
 
     def _describe(self) -> None:
+        """The constructor's verbose report (src/pcfg.cpp:473-499).  Numbers print as a
+        C++ stream prints a float (six significant digits); the symbol lines come in id
+        order, where the reference lists its hash map in that map's own order."""
         lhs, rhs, prob = self._rules
         print(f"ProbabilisticContextFreeGrammar initialized with {len(lhs)} rules.")
         print(f"\tStart symbol: {self._start_symbol}, ID: {self._symbol_to_id.get(self._start_symbol)}")
@@ -187,11 +190,13 @@ class ProbabilisticContextFreeGrammar:
         print(f"\tNumber of variables: {self._n_variables}")
         print(f"\tDevice: {self._device}")
         print(f"\tMax tries: {self._max_tries}")
-        print(f"\tTolerance: {self._tolerance}")
+        print(f"\tTolerance: {self._tolerance:g}")
+        for name, i in sorted(self._symbol_to_id.items(), key=lambda kv: (kv[1], kv[0])):
+            print(f"\tSymbol: {name}, ID: {i}")
         print("Processed grammar rules:")
         for k in range(len(lhs)):
-            body = " ".join(self._id_to_symbol[t] for t in rhs[k])
-            print(f"\tRule {k + 1}: {self._id_to_symbol[lhs[k]]} -> {body} [{prob[k]}]")
+            body = "".join(self._id_to_symbol[t] + " " for t in rhs[k])
+            print(f"\tRule {k + 1}: {self._id_to_symbol[lhs[k]]} -> {body}[{prob[k]:g}]")
 
     # ---- read-only attributes (include/pcfg.h; bound read-only in src/pcfg.cpp:1045-1057)
     device = property(lambda self: self._device)

@@ -502,6 +502,25 @@ def case_operators(st):
                         names=np.array(names), values=values)
 
 
+def case_pcfg_verbose(st):
+    """The grammar constructor's verbose report (std::cout, so captured from a child
+    process) for the fixture grammars; max_tries 7, tolerance 1e-5 and lengths 32/48."""
+    import subprocess
+    out = {}
+    for tag, (gram, nv, length) in {"readme": (README_GRAMMAR, 1, 32), "sampling": (SAMPLING_GRAMMAR, 1, 48),
+                                    "notation": (NOTATION_GRAMMAR, 2, 32)}.items():
+        code = ("import sys, torch\n"
+                f"sys.path.insert(0, {os.path.join(ROOT, 'oracle')!r})\n"
+                "import build_ref\n"
+                "st = build_ref.load_reference()\n"
+                f"st.ProbabilisticContextFreeGrammar({gram!r}, 'E', {length}, {nv}, torch.device('cpu'), "
+                "max_tries=7, tolerance=1e-5, verbose=True)\n")
+        lines = subprocess.run([sys.executable, "-c", code], check=True, capture_output=True,
+                               text=True).stdout.splitlines()
+        out[tag] = np.array(lines)
+    np.savez_compressed(os.path.join(OUT, "pcfg_verbose.npz"), **out)
+
+
 def case_error_messages(st=None):
     """getErrorMessage of the reference (include/error_codes.h) for every code of its
     enum, the gaps between them and out-of-range values, with and without a context,
@@ -539,6 +558,7 @@ def main():
     case_prefix(st)
     case_error_messages(st)
     case_operators(st)
+    case_pcfg_verbose(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -181,3 +181,33 @@ def test_oracle_postfix_children_matches_reference():
         ch, err = oracle.postfix_children(gn[key_in])
         assert not err.any()
         np.testing.assert_array_equal(ch, gn[key_out])
+
+
+@pytest.mark.parametrize("tag,length", [("readme", 32), ("sampling", 48), ("notation", 32)])
+def test_verbose_report_matches_reference(tag, length, capsys):
+    """The constructor's verbose report against the reference's own output
+    (tests/golden/pcfg_verbose.npz): the same header lines in the same order; the same
+    symbol lines, which the reference lists in its hash map's order and this class by
+    id; the same rules under each left-hand side, in the same order where the grammar
+    has at most 16 rules (beyond that the reference's unstable sort may reorder rules
+    with equal left-hand sides, and this class keeps the grammar's order)."""
+    want = [str(s) for s in np.load(os.path.join(HERE, "golden", "pcfg_verbose.npz"))[tag]]
+    gram, start, nv = GRAMMARS[tag]
+    ProbabilisticContextFreeGrammar(gram, start, length, nv, torch.device("cpu"), max_tries=7, tolerance=1e-5,
+                                    verbose=True)
+    got = capsys.readouterr().out.splitlines()
+
+    def split(lines):
+        sym = [ln for ln in lines if ln.startswith("\tSymbol: ")]
+        rules = [ln.split(": ", 1)[1] for ln in lines if ln.startswith("\tRule ")]
+        rest = [ln for ln in lines if not ln.startswith(("\tSymbol: ", "\tRule "))]
+        return rest, sym, rules
+    (g_rest, g_sym, g_rules), (w_rest, w_sym, w_rules) = split(got), split(want)
+    assert g_rest == w_rest
+    assert sorted(g_sym) == sorted(w_sym)
+    ids = [int(ln.rsplit("ID: ", 1)[1]) for ln in g_sym]
+    assert ids == sorted(ids)
+    assert [r.split(" -> ")[0] for r in g_rules] == [r.split(" -> ")[0] for r in w_rules]
+    assert sorted(g_rules) == sorted(w_rules)
+    if len(w_rules) <= 16:
+        assert g_rules == w_rules
