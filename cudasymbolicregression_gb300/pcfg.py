@@ -35,6 +35,26 @@ from .operators import Operator, error_message, get_arity, is_valid_op
 HARD_MAX_LENGTH = 128  # include/pcfg_kernels.h:4
 DEFAULT_TOLERANCE = 1e-6  # include/pcfg.h:25
 
+# torch's names of its scalar types, as its "expected scalar type" errors print them
+_SCALAR_NAMES = {torch.float32: "Float", torch.float64: "Double", torch.float16: "Half", torch.bfloat16: "BFloat16",
+                 torch.int32: "Int", torch.int16: "Short", torch.int8: "Char", torch.uint8: "Byte",
+                 torch.bool: "Bool", torch.complex64: "ComplexFloat", torch.complex128: "ComplexDouble"}
+
+
+def _check_token_rows(x: torch.Tensor, accessor_only: bool = False) -> None:
+    """The reference's checks of a (B, M) int64 token tensor, in its order and with its
+    exceptions: the methods read ``size(0)`` and ``size(1)`` first (IndexError below two
+    dimensions), then take a two-dimensional int64 accessor; ``to_string`` takes the
+    accessor only (src/pcfg.cpp:660-986)."""
+    if not accessor_only and x.dim() == 0:
+        raise IndexError("Dimension specified as 0 but tensor has no dimensions")
+    if not accessor_only and x.dim() == 1:
+        raise IndexError("Dimension out of range (expected to be in range of [-1, 0], but got 1)")
+    if x.dim() != 2:
+        raise RuntimeError(f"TensorAccessor expected 2 dims but tensor has {x.dim()}")
+    if x.dtype != torch.int64:
+        raise RuntimeError(f"expected scalar type Long but found {_SCALAR_NAMES.get(x.dtype, str(x.dtype))}")
+
 
 def _terminal_symbols(n_variables: int):
     """(name, id) pairs in the order the reference registers them
@@ -230,6 +250,7 @@ class ProbabilisticContextFreeGrammar:
     def to_string(self, expressions: torch.Tensor) -> list[str]:
         """Token rows -> text, space separated, up to the first NO_OP; ids without a
         name are skipped (src/pcfg.cpp:760-788)."""
+        _check_token_rows(expressions, accessor_only=True)
         out = []
         for row in expressions.cpu().tolist():
             toks = []
@@ -334,6 +355,7 @@ class ProbabilisticContextFreeGrammar:
         raise RuntimeError(msg)
 
     def _parse(self, expressions: torch.Tensor, prefix: bool, verbosity: int) -> torch.Tensor:
+        _check_token_rows(expressions)
         dev = _lib.require_cuda(expressions)
         x = expressions.to(torch.int64).contiguous()
         B, M = x.shape
@@ -357,10 +379,12 @@ class ProbabilisticContextFreeGrammar:
 
     def postfix_to_infix(self, expressions: torch.Tensor, max_infix_len: int, verbosity: int = 0) -> torch.Tensor:
         """(B, M) postfix -> (B, max_infix_len) infix token rows with parentheses."""
+        _check_token_rows(expressions)
         return notation.postfix_to_infix(expressions, max_infix_len, self._n_variables)
 
     def _convert(self, fn: str, expressions: torch.Tensor, context: str, check_kind: str, verbosity: int,
                  width=None, fill=int(Operator.NO_OP)) -> torch.Tensor:
+        _check_token_rows(expressions)
         dev = _lib.require_cuda(expressions)
         x = expressions.to(torch.int64).contiguous()
         B, M = x.shape
@@ -394,4 +418,5 @@ class ProbabilisticContextFreeGrammar:
 
     def get_postfix_children(self, postfix_ops: torch.Tensor, verbosity: int = 0) -> torch.Tensor:
         """(B, M) postfix -> (B, M, 2) child table (NULL_CHILD = -1)."""
+        _check_token_rows(postfix_ops)
         return notation.get_postfix_children(postfix_ops, self._n_variables)

@@ -521,6 +521,29 @@ def case_pcfg_verbose(st):
     np.savez_compressed(os.path.join(OUT, "pcfg_verbose.npz"), **out)
 
 
+def case_pcfg_input_errors(st):
+    """Exception type and first message line of every token-row method of the grammar
+    object for inputs of the wrong rank or dtype."""
+    g = st.ProbabilisticContextFreeGrammar(README_GRAMMAR, "E", 32, 1, torch.device("cpu"))
+    inputs = {"0d": torch.tensor(8), "1d": torch.tensor([8, 40, 8]), "3d": torch.tensor([[[8, 40, 8]]]),
+              "float": torch.tensor([[8.0, 40.0, 8.0]]), "int32": torch.tensor([[8, 40, 8]], dtype=torch.int32),
+              "bool": torch.tensor([[True, False]]), "1d_float": torch.tensor([8.0, 40.0])}
+    calls = {"to_string": lambda x: g.to_string(x), "infix_to_postfix": lambda x: g.infix_to_postfix(x),
+             "infix_to_prefix": lambda x: g.infix_to_prefix(x), "postfix_to_infix": lambda x: g.postfix_to_infix(x, 10),
+             "prefix_to_infix": lambda x: g.prefix_to_infix(x, 10), "prefix_to_postfix": lambda x: g.prefix_to_postfix(x),
+             "get_prefix_parent": lambda x: g.get_prefix_parent(x),
+             "get_postfix_children": lambda x: g.get_postfix_children(x)}
+    rows = []
+    for m, f in calls.items():
+        for k, x in inputs.items():
+            try:
+                f(x)
+                rows.append((m, k, "ok", ""))
+            except Exception as e:  # the exception is the fixture
+                rows.append((m, k, type(e).__name__, str(e).splitlines()[0]))
+    np.savez_compressed(os.path.join(OUT, "pcfg_input_errors.npz"), rows=np.array(rows))
+
+
 def case_error_messages(st=None):
     """getErrorMessage of the reference (include/error_codes.h) for every code of its
     enum, the gaps between them and out-of-range values, with and without a context,
@@ -559,6 +582,7 @@ def main():
     case_error_messages(st)
     case_operators(st)
     case_pcfg_verbose(st)
+    case_pcfg_input_errors(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

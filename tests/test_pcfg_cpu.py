@@ -211,3 +211,25 @@ def test_verbose_report_matches_reference(tag, length, capsys):
     assert sorted(g_rules) == sorted(w_rules)
     if len(w_rules) <= 16:
         assert g_rules == w_rules
+
+
+def test_token_row_input_errors_match_reference():
+    """Every token-row method rejects inputs of the wrong rank or dtype with the
+    reference's exception type and message (tests/golden/pcfg_input_errors.npz), before
+    any device work, so the check runs here on CPU tensors."""
+    rows = np.load(os.path.join(HERE, "golden", "pcfg_input_errors.npz"))["rows"]
+    g = ProbabilisticContextFreeGrammar(README_GRAMMAR, "E", 32, 1, torch.device("cpu"))
+    inputs = {"0d": torch.tensor(8), "1d": torch.tensor([8, 40, 8]), "3d": torch.tensor([[[8, 40, 8]]]),
+              "float": torch.tensor([[8.0, 40.0, 8.0]]), "int32": torch.tensor([[8, 40, 8]], dtype=torch.int32),
+              "bool": torch.tensor([[True, False]]), "1d_float": torch.tensor([8.0, 40.0])}
+    calls = {"to_string": lambda x: g.to_string(x), "infix_to_postfix": lambda x: g.infix_to_postfix(x),
+             "infix_to_prefix": lambda x: g.infix_to_prefix(x), "postfix_to_infix": lambda x: g.postfix_to_infix(x, 10),
+             "prefix_to_infix": lambda x: g.prefix_to_infix(x, 10), "prefix_to_postfix": lambda x: g.prefix_to_postfix(x),
+             "get_prefix_parent": lambda x: g.get_prefix_parent(x),
+             "get_postfix_children": lambda x: g.get_postfix_children(x)}
+    assert len(rows) == len(calls) * len(inputs)
+    for method, kind, etype, msg in rows:
+        assert etype != "ok", (method, kind)
+        with pytest.raises(Exception) as e:
+            calls[str(method)](inputs[str(kind)])
+        assert (type(e.value).__name__, str(e.value)) == (str(etype), str(msg)), (str(method), str(kind))
