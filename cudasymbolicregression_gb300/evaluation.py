@@ -22,8 +22,17 @@ from __future__ import annotations
 import torch
 
 from . import _lib
-from .operators import error_message
+from .operators import error_message, scalar_type_name
 from .tape import CompiledTapes, compile_tapes
+
+
+def _check_dispatch(X, C):
+    """The reference's evaluation reads X through a two-dimensional accessor and C as
+    X's scalar type (its type dispatch): torch's messages for either mismatch."""
+    if X.dim() != 2:
+        raise RuntimeError(f"TensorAccessor expected 2 dims but tensor has {X.dim()}")
+    if C.dtype != X.dtype:
+        raise RuntimeError(f"expected scalar type {scalar_type_name(X.dtype)} but found {scalar_type_name(C.dtype)}")
 
 
 def _check_backend_inputs(X, Ops, Ch, C):
@@ -32,6 +41,8 @@ def _check_backend_inputs(X, Ops, Ch, C):
     dev = X.device
     if Ops.device != dev or Ch.device != dev or C.device != dev:
         raise RuntimeError("All input tensors must be on the same device.")
+    X.size(1)  # the reference reads n_x and M here: torch's IndexError below their ranks
+    Ops.size(0)
     if Ops.dim() != 2:
         raise RuntimeError("Ops must be a 2D tensor")
     if Ch.dim() != 3:
@@ -54,10 +65,7 @@ def _check_backend_inputs(X, Ops, Ch, C):
         raise RuntimeError("Ops must be a Long tensor")
     if Ch.dtype != torch.int64:
         raise RuntimeError("Ch must be a Long tensor")
-    if X.dim() != 2:
-        raise RuntimeError("X must be a 2D tensor (N, n_x)")
-    if C.dtype != X.dtype:
-        raise RuntimeError(f"C must have the same dtype as X (got {C.dtype} and {X.dtype})")
+    _check_dispatch(X, C)
     _lib.require_cuda(X, Ops, Ch, C)
 
 
@@ -129,10 +137,8 @@ def evaluate(X: torch.Tensor, Ops: torch.Tensor, Ch: torch.Tensor, C: torch.Tens
     Returns:
         (B, M, N) values of every node at every point; NO_OP nodes are NaN.
     """
-    # same checks as the reference, which permutes to M-first before checking
-    _check_backend_inputs(X, Ops.permute(1, 0) if Ops.dim() == 2 else Ops,
-                          Ch.permute(1, 0, 2) if Ch.dim() == 3 else Ch,
-                          C.permute(1, 0) if C.dim() == 2 else C)
+    # the reference permutes to M-first (torch's own error for a wrong rank), then checks
+    _check_backend_inputs(X, Ops.permute(1, 0), Ch.permute(1, 0, 2), C.permute(1, 0))
     return _evaluate_bmn(X, Ops, Ch, C)
 
 
@@ -144,6 +150,7 @@ def _check_multiple_inputs(X, Ops, Ch, C):
     dev = X.device
     if Ops.device != dev or Ch.device != dev or C.device != dev:
         raise RuntimeError("All input tensors must be on the same device.")
+    X.size(1)  # the reference reads n_x here: torch's IndexError below two dimensions
     if Ops.dim() != 2:
         raise RuntimeError("Ops must be a 2D tensor")
     if Ch.dim() != 3:
@@ -164,10 +171,7 @@ def _check_multiple_inputs(X, Ops, Ch, C):
         raise RuntimeError("Ops must be a Long tensor")
     if Ch.dtype != torch.int64:
         raise RuntimeError("Ch must be a Long tensor")
-    if X.dim() != 2:
-        raise RuntimeError("X must be a 2D tensor (N, n_x)")
-    if C.dtype != X.dtype:
-        raise RuntimeError(f"C must have the same dtype as X (got {C.dtype} and {X.dtype})")
+    _check_dispatch(X, C)
     _lib.require_cuda(X, Ops, Ch, C)
 
 
@@ -238,8 +242,6 @@ def evaluate_multiple(X: torch.Tensor, Ops: torch.Tensor, Ch: torch.Tensor, C: t
         (B, M, N, K) values of every node at every point for every set; NO_OP nodes
         are NaN.  Differentiable w.r.t. X (summed over the sets) and C.
     """
-    _check_multiple_inputs(X, Ops.permute(1, 0) if Ops.dim() == 2 else Ops,
-                           Ch.permute(1, 0, 2) if Ch.dim() == 3 else Ch,
-                           C.permute(1, 0, 2) if C.dim() == 3 else C)
+    _check_multiple_inputs(X, Ops.permute(1, 0), Ch.permute(1, 0, 2), C.permute(1, 0, 2))
     tapes = compile_tapes(Ops, Ch, X.shape[1])
     return _EvaluateMultiple.apply(X, C, tapes)

@@ -137,6 +137,18 @@ _MESSAGES = {
 }
 
 
+# torch's names of its scalar types, as its "expected scalar type" errors print them
+_SCALAR_NAMES = {"torch.float32": "Float", "torch.float64": "Double", "torch.float16": "Half",
+                 "torch.bfloat16": "BFloat16", "torch.int64": "Long", "torch.int32": "Int", "torch.int16": "Short",
+                 "torch.int8": "Char", "torch.uint8": "Byte", "torch.bool": "Bool",
+                 "torch.complex64": "ComplexFloat", "torch.complex128": "ComplexDouble"}
+
+
+def scalar_type_name(dtype) -> str:
+    """The name torch's C++ type checks print for a torch dtype ("Float", "Long", ...)."""
+    return _SCALAR_NAMES.get(str(dtype), str(dtype))
+
+
 def error_message(code: int, context: str = "") -> str:
     """Human-readable text for a status code, optionally prefixed with
     ``"Error during <context>: "`` as the reference's getErrorMessage does."""

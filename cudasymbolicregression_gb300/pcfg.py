@@ -30,15 +30,10 @@ import numpy as np
 import torch
 
 from . import _lib, notation
-from .operators import Operator, error_message, get_arity, is_valid_op
+from .operators import Operator, error_message, get_arity, is_valid_op, scalar_type_name
 
 HARD_MAX_LENGTH = 128  # include/pcfg_kernels.h:4
 DEFAULT_TOLERANCE = 1e-6  # include/pcfg.h:25
-
-# torch's names of its scalar types, as its "expected scalar type" errors print them
-_SCALAR_NAMES = {torch.float32: "Float", torch.float64: "Double", torch.float16: "Half", torch.bfloat16: "BFloat16",
-                 torch.int32: "Int", torch.int16: "Short", torch.int8: "Char", torch.uint8: "Byte",
-                 torch.bool: "Bool", torch.complex64: "ComplexFloat", torch.complex128: "ComplexDouble"}
 
 
 def _check_token_rows(x: torch.Tensor, accessor_only: bool = False) -> None:
@@ -53,7 +48,7 @@ def _check_token_rows(x: torch.Tensor, accessor_only: bool = False) -> None:
     if x.dim() != 2:
         raise RuntimeError(f"TensorAccessor expected 2 dims but tensor has {x.dim()}")
     if x.dtype != torch.int64:
-        raise RuntimeError(f"expected scalar type Long but found {_SCALAR_NAMES.get(x.dtype, str(x.dtype))}")
+        raise RuntimeError(f"expected scalar type Long but found {scalar_type_name(x.dtype)}")
 
 
 def _terminal_symbols(n_variables: int):

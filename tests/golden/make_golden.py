@@ -23,6 +23,7 @@ sys.path.insert(0, ROOT)
 
 import build_ref  # noqa: E402
 from grammars import BAD_GRAMMARS, NOTATION_GRAMMAR, README_GRAMMAR, SAMPLING_GRAMMAR  # noqa: E402
+from inputs import EVAL_INPUT_CASES, MULTI_INPUT_CASES, eval_input_case  # noqa: E402
 
 from cudasymbolicregression_gb300 import tapes  # noqa: E402
 from cudasymbolicregression_gb300.operators import BINARY_OPS, UNARY_OPS, Operator  # noqa: E402
@@ -544,6 +545,21 @@ def case_pcfg_input_errors(st):
     np.savez_compressed(os.path.join(OUT, "pcfg_input_errors.npz"), rows=np.array(rows))
 
 
+def case_eval_input_errors(st):
+    """Exception type and first message line of evaluate and evaluate_multiple for
+    malformed inputs (wrong ranks, shapes and dtypes)."""
+    rows = []
+    for fn, names, multiple in ((st.evaluation.evaluate, EVAL_INPUT_CASES, False),
+                                (st.evaluation.evaluate_multiple, MULTI_INPUT_CASES, True)):
+        for name in names:
+            try:
+                fn(*eval_input_case(name, multiple))
+                rows.append((str(multiple), name, "ok", ""))
+            except Exception as e:  # the exception is the fixture
+                rows.append((str(multiple), name, type(e).__name__, str(e).splitlines()[0]))
+    np.savez_compressed(os.path.join(OUT, "eval_input_errors.npz"), rows=np.array(rows))
+
+
 def case_error_messages(st=None):
     """getErrorMessage of the reference (include/error_codes.h) for every code of its
     enum, the gaps between them and out-of-range values, with and without a context,
@@ -583,6 +599,7 @@ def main():
     case_operators(st)
     case_pcfg_verbose(st)
     case_pcfg_input_errors(st)
+    case_eval_input_errors(st)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -384,7 +384,8 @@ def test_multiple_backend_layout_and_errors(golden):
     direct = sr.evaluation.evaluate_multiple(X, ops, ch, C)
     assert torch.equal(torch.nan_to_num(out.permute(2, 0, 1, 3), nan=3.0), torch.nan_to_num(direct, nan=3.0))
     with pytest.raises(RuntimeError, match="C must be a 3D tensor for multiple constant evaluation"):
-        sr.evaluation.evaluate_multiple(X, ops, ch, C[:, :, 0])
+        sr.evaluation.evaluate_multiple_constant_backend(X, ops.permute(1, 0), ch.permute(1, 0, 2),
+                                                         C[:, :, 0].permute(1, 0))
     with pytest.raises(RuntimeError, match="must have the same batch size"):
         sr.evaluation.evaluate_multiple(X, ops, ch, C[:-1])
     e = golden("errors")

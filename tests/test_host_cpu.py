@@ -211,3 +211,22 @@ def test_operator_table_matches_reference_fixture():
     np.testing.assert_array_equal([[sr.is_valid_op(int(o), nv) for nv in range(6)] for o in g["ids"]], g["valid"])
     for name, value in zip(g["names"], g["values"]):
         assert int(getattr(sr.Operator, str(name))) == int(value), name
+
+
+def test_evaluation_input_errors_match_reference():
+    """evaluate and evaluate_multiple reject malformed inputs (wrong ranks, shapes,
+    dtypes, mixed float types) with the reference's exception type and message
+    (tests/golden/eval_input_errors.npz), before any device work."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from inputs import eval_input_case
+    import cudasymbolicregression_gb300 as sr
+    rows = np.load(os.path.join(ROOT, "tests", "golden", "eval_input_errors.npz"))["rows"]
+    assert len(rows) > 20
+    for multiple, name, etype, msg in rows:
+        multiple = str(multiple) == "True"
+        fn = sr.evaluation.evaluate_multiple if multiple else sr.evaluation.evaluate
+        assert str(etype) != "ok"
+        with pytest.raises(Exception) as e:
+            fn(*eval_input_case(str(name), multiple))
+        assert (type(e.value).__name__, str(e.value).splitlines()[0]) == (str(etype), str(msg)), (multiple, str(name))
