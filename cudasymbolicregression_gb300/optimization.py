@@ -70,28 +70,41 @@ def _autotune(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, lin
     return _TUNED[key]
 
 
+def _targets(Y: torch.Tensor, B: int, N: int, dev: torch.device) -> torch.Tensor:
+    """(B, N) float32 contiguous targets.  The reference's loss broadcasts Y against
+    the (B, N) predictions (nn.MSELoss(reduction='none'), symbolic_torch/optimization.py:
+    69, 87), so one target row of shape (N,) or (1, N), a column (B, 1) or a scalar
+    serves every expression; a Y that does not broadcast to (B, N) is an error."""
+    if Y.device != dev:
+        raise RuntimeError("All input tensors must be on the same device.")
+    try:
+        shape = tuple(torch.broadcast_shapes(tuple(Y.shape), (B, N)))
+    except RuntimeError:
+        shape = None
+    if shape != (B, N):
+        raise RuntimeError(f"Y must broadcast to (B, N) = ({B}, {N}), got {tuple(Y.shape)}")
+    return Y.to(torch.float32).expand(B, N).contiguous()
+
+
 def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_search_fn, *,
          objective: int = 0, line_search_max_iter: int = 10, eps: float = 1e-10,
          warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
          order: Optional[torch.Tensor] = None, want_y: bool = True, raise_errors: bool = True,
          class_width: int = 0, kernel_events=None, autotune: bool = False) -> FitResult:
+    # the reference's order: unpack Ops' shape (ValueError for another rank), permute C_init
+    # and Ops (torch's error for a wrong rank), build the optimizer (line search name),
+    # then the evaluation's own checks
+    B, M = Ops.shape
+    C_init.permute(1, 0)
     if line_search_fn not in ("strong_wolfe", "backtracking"):
         raise ValueError(f"Invalid line_search_fn: {line_search_fn}. Choose 'strong_wolfe' or 'backtracking'.")
-    if Ops.dim() != 2:
-        raise RuntimeError("Ops must be a 2D tensor")
-    _check_backend_inputs(X, Ops.permute(1, 0), Ch.permute(1, 0, 2) if Ch.dim() == 3 else Ch,
-                          C_init.permute(1, 0) if C_init.dim() == 2 else C_init)
+    _check_backend_inputs(X, Ops.permute(1, 0), Ch.permute(1, 0, 2), C_init.permute(1, 0))
     if X.dtype != torch.float32:
         raise RuntimeError("optimize runs in float32: X and C_init must be float32")
     dev = X.device
-    B, M = Ops.shape
     N, nx = X.shape
     if Y is not None:
-        if Y.shape != (B, N):
-            raise RuntimeError(f"Y must have shape (B, N) = ({B}, {N}), got {tuple(Y.shape)}")
-        if Y.device != dev:
-            raise RuntimeError("All input tensors must be on the same device.")
-        Y = Y.to(torch.float32).contiguous()
+        Y = _targets(Y, B, N, dev)
     tapes = compile_tapes(Ops, Ch, nx)
     Xc = X.contiguous()
     if autotune and warps_per_block == 0 and points_per_lane == 0:
@@ -236,7 +249,7 @@ class FitPlan:
         N, nx = X.shape
         self.B, self.M, self.N, self.nx = B, M, N, nx
         self.X = X.contiguous()
-        self.Y = None if Y is None else Y.to(torch.float32).contiguous()
+        self.Y = None if Y is None else _targets(Y, B, N, dev)
         self.tapes = compile_tapes(Ops, Ch, nx)
         self.order = torch.argsort(self.tapes.meta[:, 1] + 1, descending=True, stable=True).to(torch.int32)
         self.opts = _lib.FitOptions(max_iter=int(max_iter), history_size=int(history_size),

@@ -230,3 +230,41 @@ def test_evaluation_input_errors_match_reference():
         with pytest.raises(Exception) as e:
             fn(*eval_input_case(str(name), multiple))
         assert (type(e.value).__name__, str(e.value).splitlines()[0]) == (str(etype), str(msg)), (multiple, str(name))
+
+
+def test_fit_targets_broadcast_like_the_reference():
+    """optimize's targets: the reference's loss broadcasts Y against the (B, N)
+    predictions, so a row (N,) or (1, N), a column (B, 1) and a scalar serve every
+    expression; shapes that do not broadcast to (B, N) are rejected before any kernel
+    (the fit kernel reads B x N targets)."""
+    from cudasymbolicregression_gb300.optimization import _targets
+    B, N = 3, 5
+    full = torch.arange(B * N, dtype=torch.float64).reshape(B, N)
+    for Y in (full, full[:1], full[0], full[:, :1], torch.tensor(2.0)):
+        got = _targets(Y, B, N, torch.device("cpu"))
+        assert got.shape == (B, N) and got.dtype == torch.float32 and got.is_contiguous()
+        torch.testing.assert_close(got, torch.broadcast_to(Y, (B, N)).float())
+    for Y in (full[:2], torch.zeros(N + 1), torch.zeros(B, N, 1), torch.zeros(B + 1, 1)):
+        with pytest.raises(RuntimeError, match="Y must broadcast to"):
+            _targets(Y, B, N, torch.device("cpu"))
+
+
+def test_optimize_argument_errors_in_reference_order():
+    """optimize's errors before any kernel, as the reference raises them: Ops' shape is
+    unpacked first, C_init is permuted, then the line search name and the evaluation's
+    checks (reference symbolic_torch/optimization.py:44-63)."""
+    import cudasymbolicregression_gb300 as sr
+    X, Y = torch.randn(10, 1), torch.randn(1, 10)
+    ops = torch.tensor([[50, 1, 40]])
+    ch = torch.tensor([[[-1, -1], [-1, -1], [0, 1]]])
+    C = torch.zeros(1, 3)
+    with pytest.raises(ValueError, match="not enough values to unpack"):
+        sr.optimize(X, Y, ops[0], ch, C, line_search_fn="nope")
+    with pytest.raises(RuntimeError, match="permute"):
+        sr.optimize(X, Y, ops, ch, C[0], line_search_fn="nope")
+    with pytest.raises(ValueError, match="Invalid line_search_fn"):
+        sr.optimize(X, Y, ops, ch[0], C, line_search_fn="nope")
+    with pytest.raises(RuntimeError, match="permute"):
+        sr.optimize(X, Y, ops, ch[0], C)
+    with pytest.raises(RuntimeError, match="expected scalar type Float but found Double"):
+        sr.optimize(X, Y, ops, ch, C.double())
