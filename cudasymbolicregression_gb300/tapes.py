@@ -87,7 +87,8 @@ def _children(ar: np.ndarray) -> np.ndarray:
 
 def _screen_eval(ops: np.ndarray, ch: np.ndarray, X: np.ndarray, C: np.ndarray) -> np.ndarray:
     """Mask of tapes with a DIV whose denominator is exactly 0 at some row of X
-    (float32, vectorised over B; only the default operator sets are modelled)."""
+    (float32, vectorised over B; the default operator sets plus SQUARE and NEG are
+    modelled)."""
     B, M = ops.shape
     N = X.shape[0]
     vals = np.zeros((M, B, N), np.float32)
@@ -108,6 +109,7 @@ def _screen_eval(ops: np.ndarray, ch: np.ndarray, X: np.ndarray, C: np.ndarray) 
                              (Operator.DIV, lambda a, b: np.where(b == 0, np.nan, a / b)),
                              (Operator.SIN, lambda a, b: np.sin(a)), (Operator.COS, lambda a, b: np.cos(a)),
                              (Operator.EXP, lambda a, b: np.exp(a)),
+                             (Operator.SQUARE, lambda a, b: a * a), (Operator.NEG, lambda a, b: -a),
                              (Operator.LOG, lambda a, b: np.where(a <= 0, np.nan, np.log(np.abs(a))))):
                 m = op == int(code)
                 if m.any():

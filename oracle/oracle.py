@@ -59,6 +59,10 @@ def lib() -> ctypes.CDLL:
         L.sro_optimize_f32.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, i64, ctypes.c_int, ctypes.c_int,
                                        dbl, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
         L.sro_optimize_f32.restype = ctypes.c_int
+        L.sro_optimize_shape_f32.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, i64, ctypes.c_int, ctypes.c_int,
+                                             dbl, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
+        L.sro_optimize_shape_f32.restype = ctypes.c_int
         L.sro_num_threads.restype = ctypes.c_int
         L.sro_set_num_threads.argtypes = [ctypes.c_int]
         L.sro_set_num_threads.restype = ctypes.c_int
@@ -151,13 +155,30 @@ def eval_bwd_multi(X, ops, ch, C3, gout4, dtype=np.float32, want_gx=True):
     return np.stack(gCs, axis=2), gX, err
 
 
+def kernel_slot_registers(ops, M=None):
+    """Slot registers per lane of the fused fit kernel for a batch: 1, 2 or 4 (one
+    register holds 32 slots: the largest count of constants up to the root, plus the
+    virtual slot)."""
+    ops = np.asarray(ops)
+    nz = (ops != 0).sum(1)
+    root = np.maximum(nz - 1, 0)
+    pos = np.arange(ops.shape[1])[None, :]
+    kmax = int(((ops == 1) & (pos <= root[:, None])).sum(1).max()) if ops.size else 0
+    return 1 if kmax + 1 <= 32 else (2 if kmax + 1 <= 64 else 4)
+
+
 def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_grad=1e-7,
-             line_search_fn="strong_wolfe", line_search_max_iter=10, dot_mode=1):
+             line_search_fn="strong_wolfe", line_search_max_iter=10, dot_mode=1, warps=1,
+             points_per_lane=1, slot_registers=None):
     """Per-problem restatement of ``symbolic_torch.optimize``.
 
     dot_mode=0 follows the reference's float32 arithmetic; dot_mode=1 approximates
     the fused kernel's (double dots and two-loop scalars, where the kernel uses
-    float pairs).
+    float pairs); dot_mode=2 is the fused kernel's arithmetic exactly for a launch
+    shape of `warps` warps per problem and `points_per_lane` points per lane (its
+    per-lane sums, lane and warp reduction order, float-pair dots and two-loop
+    scalars, slot vectors and closure count; slot_registers defaults to the batch's
+    own, as the kernel derives it).
     Returns dict(C, Y, iters, evals, loss, err); iters[b] = -code for a problem
     whose closures raised an error.  Y=None selects the raw
     objective (mean of the root value) used by the Rosenbrock test.
@@ -166,7 +187,7 @@ def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_gra
     ops = _c(ops, np.int64)
     ch = _c(ch, np.int64)
     C_init = _c(C_init, np.float32)
-    Yc = None if Y is None else _c(Y, np.float32)
+    Yc = None if Y is None else _c(np.broadcast_to(Y, (ops.shape[0], X.shape[0])), np.float32)
     N, nx = X.shape
     B, M = ops.shape
     C = np.empty((B, M), np.float32)
@@ -175,10 +196,11 @@ def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_gra
     evals = np.empty(B, np.int64)
     loss = np.empty(B, np.float32)
     ls = {"strong_wolfe": 0, "backtracking": 1}[line_search_fn]
-    err = lib().sro_optimize_f32(_p(X), N, nx, _p(Yc), _p(ops), _p(ch), _p(C_init), B, M,
-                                 int(max_iter), int(history_size), float(tolerance_grad), ls,
-                                 int(line_search_max_iter), int(dot_mode),
-                                 _p(C), _p(Yo), _p(iters), _p(evals), _p(loss))
+    spl = kernel_slot_registers(ops) if slot_registers is None else int(slot_registers)
+    err = lib().sro_optimize_shape_f32(_p(X), N, nx, _p(Yc), _p(ops), _p(ch), _p(C_init), B, M,
+                                       int(max_iter), int(history_size), float(tolerance_grad), ls,
+                                       int(line_search_max_iter), int(dot_mode), int(warps), int(points_per_lane),
+                                       spl, _p(C), _p(Yo), _p(iters), _p(evals), _p(loss))
     return dict(C=C, Y=Yo, iters=iters, evals=evals, loss=loss, err=err)
 
 

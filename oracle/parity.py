@@ -114,3 +114,20 @@ def check_accuracy(got, ref32, ref64, rtol=1e-5, atol=1e-6, min_frac_tight=0.999
             stats[f"p{q}_rel_err_device"] = float(pg)
             stats[f"p{q}_rel_err_reference"] = float(pr)
     return stats
+
+
+def first_divergence(run_a, run_b, idx, max_iter, rtol=1e-4):
+    """For the problems idx, the first iteration count k (0..max_iter) at which the
+    constants of run_a(k, idx) and run_b(k, idx) part by more than rtol relative or
+    in NaN placement; max_iter + 1 where they never do.  Problems are independent of
+    the rest of their batch, so each run fits only the problems asked about."""
+    idx = np.asarray(idx)
+    first = np.full(idx.size, max_iter + 1)
+    for k in range(max_iter + 1):
+        a = np.asarray(run_a(k, idx), np.float64)
+        b = np.asarray(run_b(k, idx), np.float64)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-30)
+        d = ((np.isnan(a) != np.isnan(b)) | (np.nan_to_num(rel, nan=0.0) > rtol)).any(1)
+        first = np.where((first > max_iter) & d, k, first)
+    return first

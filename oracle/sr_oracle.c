@@ -278,17 +278,21 @@ void sro_node_fwd_f32(int64_t n, const int64_t *op, const float *a, const float 
  * all reductions are per column and the batch-wide tests (done.all(), all(done)
  * in the line searches) only stop loops early for columns whose state no longer
  * changes.  So this restatement runs one problem at a time, with the reference's
- * D = M parameter slots (non-constant slots get zero gradient, optimization.py:95-97).
+ * control flow (strong_wolfe, zoom, backtracking and the outer loop below follow
+ * lbfgs_batch.py:105-326 line by line) and one of three arithmetics:
  *
- * dot_mode 0 follows the reference arithmetic: float32 vectors, float32 dots
- * summed in slot order, float32 scalars.
- * dot_mode 1 approximates the fused kernel's arithmetic: dots and two-loop scalars
- * in double (s.y, y.y, the alphas, beta, gamma, rho), vector updates rounded once
- * to float, line-search scalars in float, and the per-constant gradient summed
- * over the points in double.  The kernel carries all of these as float pairs
- * (about 44 significant bits; no FP64 in its iteration) and its sums as cascaded
- * float pairs, so the two agree to far below a float ulp on well-conditioned
- * problems.
+ * dot_mode 0 follows the reference arithmetic: float32 vectors over the D = M
+ * parameter slots, float32 dots summed in slot order, float32 scalars.
+ * dot_mode 1 approximates the fused kernel's arithmetic with double dots and
+ * two-loop scalars and per-constant gradients summed over the points in double.
+ * dot_mode 2 is the fused kernel's arithmetic exactly (see "the fused kernel's
+ * arithmetic" below): its slot vectors (the real constants and one virtual slot
+ * for all other slots), its per-lane point sums and lane/warp reduction order for a
+ * given launch shape, its float-pair (Sum2/Dot2, Dekker) dots and two-loop scalars,
+ * and the closures it evaluates (it reuses points the reference evaluates twice).
+ * On tapes whose operators are IEEE-exact (+ - * /, square, neg, inv, cube,
+ * fourth, fifth) this mode and the kernel give the same bits; with transcendental
+ * operators the two differ by the ulps of the two math libraries.
  */
 typedef struct {
     const float *X; int64_t N, nx;
@@ -355,11 +359,410 @@ static float closure_f32(problem_t *P, const float *x, float *g)
     return (float)(acc / (double)N);
 }
 
-typedef struct { int mode; double eps; } lb_cfg_t;
+/* ---- the fused kernel's arithmetic (dot_mode 2) ------------------------------------
+ *
+ * Float pairs.  f2_add is Knuth's TwoSum of the high parts with the low parts summed
+ * (Ogita, Rump and Oishi's cascaded Sum2); f2_val is hi + lo for a finite hi and hi
+ * otherwise; f2_norm renormalises a cascaded pair; f2_mul / f2_div are Dekker's
+ * double-float product and quotient with FMA.  Every operation is a single IEEE
+ * float32 operation (the file is compiled with -ffp-contract=off; fmaf is the
+ * correctly rounded fused multiply-add). */
+typedef struct { float hi, lo; } f2_t;
 
-static double dotv(const lb_cfg_t *cf, const float *a, const float *b, int64_t D)
+static f2_t f2_mk(float hi, float lo) { f2_t r; r.hi = hi; r.lo = lo; return r; }
+
+static f2_t f2_add(f2_t a, f2_t b)
 {
-    if (cf->mode == 0) {
+    float s = a.hi + b.hi;
+    float bv = s - a.hi;
+    float e = (a.hi - (s - bv)) + (b.hi - bv);
+    return f2_mk(s, (a.lo + b.lo) + e);
+}
+
+static float f2_val(f2_t a) { return isfinite(a.hi) ? a.hi + a.lo : a.hi; }
+
+static f2_t f2_norm(f2_t a)
+{
+    if (!isfinite(a.hi)) return f2_mk(a.hi, 0.0f);
+    float s = a.hi + a.lo;
+    float bv = s - a.hi;
+    return f2_mk(s, (a.hi - (s - bv)) + (a.lo - bv));
+}
+
+static f2_t f2_mul(f2_t a, f2_t b)
+{
+    float p = a.hi * b.hi;
+    if (!isfinite(p)) return f2_mk(p, 0.0f);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    float s = p + e;
+    return f2_mk(s, e - (s - p));
+}
+
+static f2_t f2_sub(f2_t a, f2_t b) { return f2_norm(f2_add(a, f2_mk(-b.hi, -b.lo))); }
+
+static f2_t f2_div(f2_t a, f2_t b)
+{
+    float q1 = a.hi / b.hi;
+    if (!isfinite(q1)) return f2_mk(q1, 0.0f);
+    float ph = q1 * b.hi;
+    float pl = fmaf(q1, b.hi, -ph);
+    float r = (a.hi - ph) - pl;
+    r = fmaf(-q1, b.lo, r + a.lo);
+    float q2 = r / b.hi;
+    float sum = q1 + q2;
+    return f2_mk(sum, q2 - (sum - q1));
+}
+
+static f2_t f2_of_double(double d)
+{
+    float hi = (float)d;
+    return f2_mk(hi, isfinite(hi) ? (float)(d - (double)hi) : 0.0f);
+}
+
+/* Local adjoint of one operator node at one point, as (add0, o0, add1, o1): the
+ * same rules as bwd_f32 (evaluation_kernels_cuda.cu:218-632), in the form in which
+ * the fused kernel adds them to their destinations. */
+static int ladj_f32(int64_t op, float g, float a, float b, float v, int *add0, float *o0, int *add1, float *o1)
+{
+    const float qnan = (float)NAN;
+    const int zero = g == 0.0f;
+    *add0 = *add1 = 0;
+    *o0 = *o1 = 0.0f;
+    switch (op) {
+    case OP_NO_OP: return zero ? 0 : ERR_GRAD_NO_OP;
+    case OP_SIN: if (zero) return 0; *o0 = g * cosf(a); *add0 = 1; return 0;
+    case OP_COS: if (zero) return 0; *o0 = g * -sinf(a); *add0 = 1; return 0;
+    case OP_EXP: if (zero) return 0; *o0 = g * v; *add0 = 1; return 0;
+    case OP_LOG: case OP_LN: if (zero) return 0; *o0 = div_f32(g, a); *add0 = 1; return 0;
+    case OP_SQUARE: if (zero) return 0; *o0 = g * 2.0f * a; *add0 = 1; return 0;
+    case OP_SQRT:
+        *add0 = 1;
+        if (a < 0.0f) *o0 = qnan;
+        else if (zero) *o0 = 0.0f;
+        else *o0 = div_f32(g * 0.5f, sqrtf(a));
+        return 0;
+    case OP_TAN: { if (zero) return 0; float cv = cosf(a); *o0 = div_f32(g, cv * cv); *add0 = 1; return 0; }
+    case OP_ARCSIN: case OP_ARCCOS: {
+        if (zero) return 0;
+        *add0 = 1;
+        if (a < -1.0f || a > 1.0f) { *o0 = qnan; return 0; }
+        float r = 1.0f - a * a;
+        float den = r < 0.0f ? qnan : sqrtf(r);
+        *o0 = div_f32(g, den);
+        if (op == OP_ARCCOS) *o0 = -*o0;
+        return 0; }
+    case OP_ARCTAN: if (zero) return 0; *o0 = div_f32(g, 1.0f + a * a); *add0 = 1; return 0;
+    case OP_SINH: if (zero) return 0; *o0 = g * coshf(a); *add0 = 1; return 0;
+    case OP_COSH: if (zero) return 0; *o0 = g * sinhf(a); *add0 = 1; return 0;
+    case OP_TANH: { if (zero) return 0; float t = tanhf(a); *o0 = g * (1.0f - t * t); *add0 = 1; return 0; }
+    case OP_LOG10: if (zero) return 0; *o0 = div_f32(g, a * logf(10.0f)); *add0 = 1; return 0;
+    case OP_NEG: if (zero) return 0; *o0 = -g; *add0 = 1; return 0;
+    case OP_INV: if (zero) return 0; *o0 = (a == 0.0f) ? qnan : -div_f32(g, a * a); *add0 = 1; return 0;
+    case OP_CUBE: if (zero) return 0; *o0 = g * 3.0f * (a * a); *add0 = 1; return 0;
+    case OP_FOURTH: if (zero) return 0; *o0 = g * 4.0f * (a * a * a); *add0 = 1; return 0;
+    case OP_FIFTH: { if (zero) return 0; float s = a * a; *o0 = g * 5.0f * (s * s); *add0 = 1; return 0; }
+    case OP_ADD: if (zero) return 0; *o0 = g; *o1 = g; *add0 = *add1 = 1; return 0;
+    case OP_SUB: if (zero) return 0; *o0 = g; *o1 = -g; *add0 = *add1 = 1; return 0;
+    case OP_MUL: if (zero) return 0; *o0 = g * b; *o1 = g * a; *add0 = *add1 = 1; return 0;
+    case OP_DIV:
+        if (zero) return 0;
+        *add0 = *add1 = 1;
+        if (b == 0.0f) return ERR_DIV_ZERO;
+        *o0 = div_f32(g, b);
+        *o1 = -div_f32(g * a, b * b);
+        return 0;
+    case OP_POW:
+        if (a < 0.0f) { *o0 = qnan; *o1 = qnan; *add0 = *add1 = 1; return 0; }
+        if (zero) return 0;
+        {
+            float pm1 = powf(a, b - 1.0f), pw = powf(a, b), lg = a <= 0.0f ? qnan : logf(a);
+            *o0 = g * (pm1 * b);
+            *o1 = g * (lg * pw);
+        }
+        *add0 = *add1 = 1;
+        return 0;
+    default: return 0;  /* FLOOR, CEIL */
+    }
+}
+
+static int is_operator_node(int64_t op) { return op == OP_NO_OP || arity_of(op) >= 1; }
+
+/* State of one problem in the fused kernel's arithmetic (one CTA of W warps, V
+ * points per lane).  Slot vectors hold D = 32 spl entries: the K learnable
+ * constants up to the root in tape order, then, when M > K, one virtual slot that
+ * stands for all other slots (its gradient is always 0; it only carries the NaN
+ * that 0 * NaN spreads into them); the rest are inactive zeros. */
+typedef struct {
+    int W, V, spl, D;
+    int K, nslots, has_virtual;
+    int objective;
+    int *slot_of;                   /* (M) slot of a learnable node up to the root, else -1 */
+    int64_t *slot_node;             /* (K) */
+    float *vals, *adjs;             /* (V, 32, M) node values / adjoints of one chunk */
+    float *gl;                      /* (K, 32 V) per-point-row gradient partials of one warp */
+    f2_t *red_g, *red_l;            /* (W, K), (W) */
+    int *lane_err;                  /* (32 W) first error each thread met, over the whole fit */
+    int hist, h, head;
+    float *ringS, *ringY;           /* (hist, D) */
+    f2_t *rho, *alph;               /* (hist) rho per ring slot, alpha per position */
+    f2_t last_sy, last_yy, eps2;
+    int poison;
+} kern_t;
+
+/* Sum over the 32 lanes of a warp of x[lane][0..KP) (per-slot partials, the loss
+ * partial at K) by recursive halving (the kernel's reduce_slots): at each step a lane
+ * keeps half of its values and adds its partner's partial sums of that half; the
+ * lowest lane of each group then holds one slot's total. */
+static void reduce_lanes(int KP, int K, f2_t x[32][32], f2_t *out_g, f2_t *out_l)
+{
+    int slot[32] = { 0 };
+    int n = KP;
+    f2_t t[32][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        if (n > 1) {
+            int h = n >> 1;
+            for (int l = 0; l < 32; ++l) {
+                int p = l ^ o, up = (l & o) != 0;
+                for (int q = 0; q < h; ++q) {
+                    f2_t keep = up ? x[l][q + h] : x[l][q];
+                    f2_t recv = up ? x[p][q + h] : x[p][q];  /* the half the partner gives away */
+                    t[l][q] = f2_add(keep, recv);
+                }
+                slot[l] = slot[l] * 2 + up;
+            }
+            for (int l = 0; l < 32; ++l) for (int q = 0; q < h; ++q) x[l][q] = t[l][q];
+            n = h;
+        } else {
+            for (int l = 0; l < 32; ++l) t[l][0] = f2_add(x[l][0], x[l ^ o][0]);
+            for (int l = 0; l < 32; ++l) x[l][0] = t[l][0];
+        }
+    }
+    int group = 32 / KP;
+    for (int l = 0; l < 32; ++l) {
+        if (l & (group - 1)) continue;
+        if (slot[l] < K) out_g[slot[l]] = x[l][0];
+        else if (slot[l] == K) *out_l = x[l][0];
+    }
+}
+
+/* xor butterfly over groups of `width` lanes: every lane ends with its group's total. */
+static void lane_butterfly(f2_t acc[32], int width)
+{
+    f2_t t[32];
+    for (int o = width >> 1; o > 0; o >>= 1) {
+        for (int l = 0; l < 32; ++l) t[l] = f2_add(acc[l], acc[l ^ o]);
+        memcpy(acc, t, sizeof(t));
+    }
+}
+
+/* The fused kernel's closure (sr_fit.cu tape_pass + reduce_slots + closure): warp w
+ * takes the chunks of 32 V points starting at w 32 V, W 32 V apart; lane l of a chunk
+ * holds points base + v 32 + l.  Per thread: the loss is a float sum over its points,
+ * each constant's gradient a float sum per point row, the contributions of a point
+ * added in the order of the reverse sweep (parents last to first, child 0 first). */
+static float kclosure(problem_t *P, kern_t *k, const float *xt, float *g)
+{
+    const int64_t N = P->N, M = P->M, root = P->root;
+    const int W = k->W, V = k->V, RW = 32 * k->V, K = k->K;
+    const float invN = 1.0f / (float)N;
+    for (int w = 0; w < W; ++w) {
+        float lpart[32];
+        for (int l = 0; l < 32; ++l) lpart[l] = 0.0f;
+        for (int64_t i = 0; i < (int64_t)K * RW; ++i) k->gl[i] = 0.0f;
+        for (int64_t base = (int64_t)w * RW; base < N; base += (int64_t)W * RW) {
+            /* forward and residuals, point by point */
+            for (int v = 0; v < V; ++v)
+                for (int l = 0; l < 32; ++l) {
+                    int64_t n = base + v * 32 + l;
+                    if (n >= N) continue;
+                    float *val = k->vals + ((int64_t)v * 32 + l) * M, *adj = k->adjs + ((int64_t)v * 32 + l) * M;
+                    for (int64_t kk = 0; kk <= root; ++kk) {
+                        int64_t op = P->ops[kk];
+                        int ar = arity_of(op);
+                        float a = 0, bb = 0;
+                        if (op != OP_NO_OP) {
+                            if (ar >= 1) a = val[P->ch[kk * 2]];
+                            if (ar == 2) bb = val[P->ch[kk * 2 + 1]];
+                        }
+                        float cval = k->slot_of[kk] >= 0 ? xt[k->slot_of[kk]] : 0.0f;
+                        val[kk] = fwd_f32(op, a, bb, cval, P->X + n * P->nx, P->nx);
+                        adj[kk] = 0.0f;
+                    }
+                    float f = val[root], groot;
+                    if (k->objective == 0) {
+                        float rr = f - P->Y[n];
+                        lpart[l] = lpart[l] + rr * rr;
+                        groot = (rr * 2.0f) * invN;
+                    } else {
+                        lpart[l] = lpart[l] + f;
+                        groot = invN;
+                    }
+                    if (is_operator_node(P->ops[root])) adj[root] = groot;
+                    else if (groot != 0.0f && k->slot_of[root] >= 0) {
+                        float *d = k->gl + (int64_t)k->slot_of[root] * RW + v * 32 + l;
+                        *d = *d + groot;
+                    }
+                }
+            /* reverse sweep: node by node, the points of a node in row order */
+            for (int64_t kk = root; kk >= 0; --kk) {
+                int64_t op = P->ops[kk];
+                if (!is_operator_node(op)) continue;
+                int64_t c0 = P->ch[kk * 2], c1 = P->ch[kk * 2 + 1];
+                for (int v = 0; v < V; ++v)
+                    for (int l = 0; l < 32; ++l) {
+                        int64_t n = base + v * 32 + l;
+                        if (n >= N) continue;
+                        float *val = k->vals + ((int64_t)v * 32 + l) * M, *adj = k->adjs + ((int64_t)v * 32 + l) * M;
+                        int ar = arity_of(op), a0, a1;
+                        float o0, o1;
+                        float a = ar >= 1 ? val[c0] : 0.0f, bb = ar == 2 ? val[c1] : 0.0f;
+                        int e = ladj_f32(op, adj[kk], a, bb, val[kk], &a0, &o0, &a1, &o1);
+                        int *te = k->lane_err + w * 32 + l;
+                        if (e && !*te) *te = e;
+                        for (int side = 0; side < 2; ++side) {
+                            if (!(side ? a1 : a0)) continue;
+                            int64_t c = side ? c1 : c0;
+                            float o = side ? o1 : o0;
+                            float *d = NULL;
+                            if (is_operator_node(P->ops[c])) d = adj + c;
+                            else if (k->slot_of[c] >= 0) d = k->gl + (int64_t)k->slot_of[c] * RW + v * 32 + l;
+                            if (d) *d = *d + o;
+                        }
+                    }
+            }
+        }
+        /* lanes, then warps */
+        if (K < 32) {
+            int KP = K < 1 ? 1 : K < 2 ? 2 : K < 4 ? 4 : K < 8 ? 8 : K < 16 ? 16 : 32;
+            f2_t x[32][32];
+            for (int l = 0; l < 32; ++l)
+                for (int j = 0; j < KP; ++j) {
+                    float part = 0.0f;
+                    if (j < K) {
+                        part = k->gl[(int64_t)j * RW + l];
+                        for (int v = 1; v < V; ++v) part = part + k->gl[(int64_t)j * RW + v * 32 + l];
+                    } else if (j == K) {
+                        part = lpart[l];
+                    }
+                    x[l][j] = f2_mk(part, 0.0f);
+                }
+            reduce_lanes(KP, K, x, k->red_g + (int64_t)w * K, k->red_l + w);
+        } else {
+            f2_t acc[32];
+            for (int l = 0; l < 32; ++l) acc[l] = f2_mk(lpart[l], 0.0f);
+            lane_butterfly(acc, 32);
+            k->red_l[w] = acc[0];
+            for (int j = 0; j < K; ++j) {
+                for (int l = 0; l < 32; ++l) {
+                    float part = k->gl[(int64_t)j * RW + l];
+                    for (int v = 1; v < V; ++v) part = part + k->gl[(int64_t)j * RW + v * 32 + l];
+                    acc[l] = f2_mk(part, 0.0f);
+                }
+                lane_butterfly(acc, 32);
+                k->red_g[(int64_t)w * K + j] = acc[0];
+            }
+        }
+    }
+    for (int j = 0; j < k->D; ++j) {
+        f2_t acc = f2_mk(0.0f, 0.0f);
+        if (j < K)
+            for (int w = 0; w < W; ++w) acc = f2_add(acc, k->red_g[(int64_t)w * K + j]);
+        g[j] = f2_val(acc);
+    }
+    f2_t lt = f2_mk(0.0f, 0.0f);
+    for (int w = 0; w < W; ++w) lt = f2_add(lt, k->red_l[w]);
+    P->n_evals++;
+    return f2_val(lt) / (float)N;
+}
+
+/* Per-lane float-pair terms of a slot-vector dot (TwoProduct by FMA). */
+static void lane_terms(const kern_t *k, const float *a, const float *b, f2_t acc[32])
+{
+    for (int l = 0; l < 32; ++l) {
+        acc[l] = f2_mk(0.0f, 0.0f);
+        for (int s = 0; s < k->spl; ++s) {
+            int j = s * 32 + l;
+            if (j >= k->nslots) continue;
+            float pr = a[j] * b[j];
+            acc[l] = f2_add(acc[l], f2_mk(pr, fmaf(a[j], b[j], -pr)));
+        }
+    }
+}
+
+/* Line-search slopes and the gradient norm (the kernel's dot_f2, Dot2 rounded to float). */
+static float kdot_f2(const kern_t *k, const float *a, const float *b)
+{
+    f2_t acc[32];
+    lane_terms(k, a, b, acc);
+    lane_butterfly(acc, 32);
+    return f2_val(acc[0]);
+}
+
+/* Curvature dots of the two-loop recursion (the kernel's dot_pair, a normalised pair). */
+static f2_t kdot_pair(const kern_t *k, const float *a, const float *b)
+{
+    f2_t acc[32];
+    lane_terms(k, a, b, acc);
+    if (k->spl == 1 && k->nslots <= 16)
+        lane_butterfly(acc, k->nslots <= 4 ? 4 : (k->nslots <= 8 ? 8 : 16));
+    else
+        lane_butterfly(acc, 32);
+    return f2_norm(acc[0]);
+}
+
+/* The kernel's two-loop recursion over its history ring (oldest pair at `head`). */
+static void kdirection(kern_t *k, const float *g, float *q, float *p)
+{
+    const int D = k->D;
+    for (int j = 0; j < D; ++j) q[j] = g[j];
+    if (k->h > 0) {
+        for (int i = k->h - 1; i >= 0; --i) {
+            int sl = (k->head + i) % k->hist;
+            const float *si = k->ringS + (int64_t)sl * D, *yi = k->ringY + (int64_t)sl * D;
+            f2_t a = f2_mul(k->rho[sl], kdot_pair(k, si, q));
+            for (int j = 0; j < D; ++j) q[j] = fmaf(-a.lo, yi[j], fmaf(-a.hi, yi[j], q[j]));
+            k->alph[i] = a;
+        }
+        f2_t gam = f2_div(k->last_sy, f2_norm(f2_add(k->last_yy, k->eps2)));
+        for (int j = 0; j < D; ++j) q[j] = fmaf(q[j], gam.lo, q[j] * gam.hi);
+        for (int i = 0; i < k->h; ++i) {
+            int sl = (k->head + i) % k->hist;
+            const float *si = k->ringS + (int64_t)sl * D, *yi = k->ringY + (int64_t)sl * D;
+            f2_t be = f2_mul(k->rho[sl], kdot_pair(k, yi, q));
+            f2_t coef = f2_sub(k->alph[i], be);
+            for (int j = 0; j < D; ++j) q[j] = fmaf(coef.lo, si[j], fmaf(coef.hi, si[j], q[j]));
+        }
+    }
+    for (int j = 0; j < D; ++j) p[j] = j < k->nslots ? -q[j] : 0.0f;
+}
+
+/* One problem's fit: the closure and dots of the chosen arithmetic behind the
+ * reference's control flow.  kevals counts the closures the fused kernel
+ * evaluates: it reuses phi(0), phi(alpha_lo) and the accepted trial point, which
+ * the reference evaluates again (bit-identical, both being deterministic). */
+typedef struct {
+    problem_t *P;
+    kern_t *k;          /* dot_mode 2 */
+    int mode;
+    double eps;
+    int64_t D;          /* vector length */
+    long kevals;
+} fit_t;
+
+static float fit_closure(fit_t *F, const float *x, float *g, int counted)
+{
+    if (F->mode == 2) {
+        if (counted) F->kevals++;
+        return kclosure(F->P, F->k, x, g);
+    }
+    return closure_f32(F->P, x, g);
+}
+
+static double dotv(const fit_t *F, const float *a, const float *b, int64_t D)
+{
+    if (F->mode == 0) {
         float s = 0.0f;
         for (int64_t j = 0; j < D; ++j) s += a[j] * b[j];
         return (double)s;
@@ -369,50 +772,51 @@ static double dotv(const lb_cfg_t *cf, const float *a, const float *b, int64_t D
     return s;
 }
 
-/* Two-loop recursion (lbfgs_batch.py:65-103); writes p = -z. */
-static void direction(const lb_cfg_t *cf, const float *g, float *const *S, float *const *Yh, int h,
+static float dotf(const fit_t *F, const float *a, const float *b)
+{
+    if (F->mode == 2) return kdot_f2(F->k, a, b);
+    return (float)dotv(F, a, b, F->D);
+}
+
+/* Two-loop recursion (lbfgs_batch.py:65-103) in dot_mode 0 / 1; writes p = -z. */
+static void direction(const fit_t *F, const float *g, float *const *S, float *const *Yh, int h,
                       int64_t D, float *q, float *p, double *alph)
 {
     for (int64_t j = 0; j < D; ++j) q[j] = g[j];
     if (h == 0) { for (int64_t j = 0; j < D; ++j) p[j] = -q[j]; return; }
-    if (cf->mode == 0) {
-        float eps = (float)cf->eps;
+    if (F->mode == 0) {
+        float eps = (float)F->eps;
         for (int i = h - 1; i >= 0; --i) {
-            float rho = 1.0f / ((float)dotv(cf, Yh[i], S[i], D) + eps);
-            float al = rho * (float)dotv(cf, S[i], q, D);
+            float rho = 1.0f / ((float)dotv(F, Yh[i], S[i], D) + eps);
+            float al = rho * (float)dotv(F, S[i], q, D);
             for (int64_t j = 0; j < D; ++j) q[j] = q[j] - al * Yh[i][j];
             alph[i] = al;
         }
-        float gam = (float)dotv(cf, S[h - 1], Yh[h - 1], D) / ((float)dotv(cf, Yh[h - 1], Yh[h - 1], D) + eps);
+        float gam = (float)dotv(F, S[h - 1], Yh[h - 1], D) / ((float)dotv(F, Yh[h - 1], Yh[h - 1], D) + eps);
         for (int64_t j = 0; j < D; ++j) q[j] = gam * q[j];
         for (int i = 0; i < h; ++i) {
-            float rho = 1.0f / ((float)dotv(cf, Yh[i], S[i], D) + eps);
-            float be = rho * (float)dotv(cf, Yh[i], q, D);
+            float rho = 1.0f / ((float)dotv(F, Yh[i], S[i], D) + eps);
+            float be = rho * (float)dotv(F, Yh[i], q, D);
             float coef = (float)alph[i] - be;
             for (int64_t j = 0; j < D; ++j) q[j] = q[j] + S[i][j] * coef;
         }
     } else {
-        double eps = cf->eps;
+        double eps = F->eps;
         for (int i = h - 1; i >= 0; --i) {
-            double rho = 1.0 / (dotv(cf, Yh[i], S[i], D) + eps);
-            double al = rho * dotv(cf, S[i], q, D);
+            double rho = 1.0 / (dotv(F, Yh[i], S[i], D) + eps);
+            double al = rho * dotv(F, S[i], q, D);
             for (int64_t j = 0; j < D; ++j) q[j] = (float)((double)q[j] - al * (double)Yh[i][j]);
             alph[i] = al;
         }
-        double gam = dotv(cf, S[h - 1], Yh[h - 1], D) / (dotv(cf, Yh[h - 1], Yh[h - 1], D) + eps);
+        double gam = dotv(F, S[h - 1], Yh[h - 1], D) / (dotv(F, Yh[h - 1], Yh[h - 1], D) + eps);
         for (int64_t j = 0; j < D; ++j) q[j] = (float)(gam * (double)q[j]);
         for (int i = 0; i < h; ++i) {
-            double rho = 1.0 / (dotv(cf, Yh[i], S[i], D) + eps);
-            double be = rho * dotv(cf, Yh[i], q, D);
+            double rho = 1.0 / (dotv(F, Yh[i], S[i], D) + eps);
+            double be = rho * dotv(F, Yh[i], q, D);
             for (int64_t j = 0; j < D; ++j) q[j] = (float)((double)q[j] + (double)S[i][j] * (alph[i] - be));
         }
     }
     for (int64_t j = 0; j < D; ++j) p[j] = -q[j];
-}
-
-static float dotf(const lb_cfg_t *cf, const float *a, const float *b, int64_t D)
-{
-    return (float)dotv(cf, a, b, D);
 }
 
 static void trial_point(const float *x, const float *p, float al, float *xt, int64_t D)
@@ -421,21 +825,24 @@ static void trial_point(const float *x, const float *p, float al, float *xt, int
 }
 
 /* Zoom (lbfgs_batch.py:204-264) for one problem.  phi0/dphi0 are re-evaluated
- * by the reference at x; they equal the bracket phase's values. */
-static float zoom(problem_t *P, const lb_cfg_t *cf, const float *x, const float *p, float lo, float hi,
-                  float phi0, float dphi0, float *xt, float *gt, int64_t D)
+ * by the reference at x; they equal the bracket phase's values.  lo_counted: the
+ * fused kernel evaluates phi(alpha_lo) itself (alpha_lo = 0 and x + 0 p differs
+ * from x in its bits); otherwise it holds that point already. */
+static float zoom(fit_t *F, const float *x, const float *p, float lo, float hi,
+                  float phi0, float dphi0, float *xt, float *gt, int lo_counted)
 {
     const float c1 = 1e-4f, c2 = 0.9f;
+    const int64_t D = F->D;
     trial_point(x, p, lo, xt, D);
-    float phi_lo = closure_f32(P, xt, gt);
+    float phi_lo = fit_closure(F, xt, gt, lo_counted);
     float alpha = 0.0f;
     int zdone = 0;
     for (int it = 0; it < 10; ++it) {
         if (zdone) break;
         float aj = (lo + hi) / 2.0f;
         trial_point(x, p, aj, xt, D);
-        float phij = closure_f32(P, xt, gt);
-        float dphij = dotf(cf, gt, p, D);
+        float phij = fit_closure(F, xt, gt, 1);
+        float dphij = dotf(F, gt, p);
         int bad = (phij > phi0 + (c1 * aj) * dphi0) || (phij >= phi_lo);
         int good = fabsf(dphij) <= c2 * fabsf(dphi0);
         if (good) { alpha = aj; zdone = 1; }
@@ -451,25 +858,35 @@ static float zoom(problem_t *P, const lb_cfg_t *cf, const float *x, const float 
     return alpha;
 }
 
-/* Strong-Wolfe bracketing (lbfgs_batch.py:138-202) for one problem. */
-static float strong_wolfe(problem_t *P, const lb_cfg_t *cf, const float *x, const float *p, float phi0,
-                          float dphi0, int ls_max, float *xt, float *gt, int64_t D)
+/* Strong-Wolfe bracketing (lbfgs_batch.py:138-202) for one problem.  *known: the
+ * returned step was evaluated (found by the bracket or the zoom), not the next
+ * extrapolated step of an unfinished bracket. */
+static float strong_wolfe(fit_t *F, const float *x, const float *p, float phi0,
+                          float dphi0, int ls_max, float *xt, float *gt, int *known)
 {
     const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
+    const int64_t D = F->D;
     float a_prev = 0.0f, phi_prev = phi0, a_i = 1.0f, fin = 0.0f;
     int done = 0;
     for (int i = 0; i < ls_max; ++i) {
         if (done) break;
         trial_point(x, p, a_i, xt, D);
-        float phii = closure_f32(P, xt, gt);
-        float dphii = dotf(cf, gt, p, D);
+        float phii = fit_closure(F, xt, gt, 1);
+        float dphii = dotf(F, gt, p);
         int bad = (phii > phi0 + (c1 * a_i) * dphi0) || (i > 0 && phii >= phi_prev);
         int good = fabsf(dphii) <= c2 * fabsf(dphi0);
         int passed = dphii >= 0.0f;
         if (good) { fin = a_i; done = 1; }
         else if (bad || passed) {
             float lo = bad ? a_prev : a_i, hi = bad ? a_i : a_prev;
-            fin = zoom(P, cf, x, p, lo, hi, phi0, dphi0, xt, gt, D);
+            int lo_counted = 0;
+            if (F->mode == 2 && bad && i == 0) {  /* alpha_lo = 0: is x + 0 p bit-identical to x? */
+                for (int j = 0; j < F->k->K; ++j) {
+                    float z = x[j] + 0.0f * p[j];
+                    if (memcmp(&z, &x[j], sizeof(float)) != 0) lo_counted = 1;
+                }
+            }
+            fin = zoom(F, x, p, lo, hi, phi0, dphi0, xt, gt, lo_counted);
             done = 1;
         }
         if (!done) {
@@ -477,37 +894,161 @@ static float strong_wolfe(problem_t *P, const lb_cfg_t *cf, const float *x, cons
             a_i = a_i + (amax - a_i) * 0.8f;
         }
     }
+    *known = done;
     return done ? fin : a_i;
 }
 
 /* Armijo backtracking (lbfgs_batch.py:105-136) for one problem: alpha halves
  * after every failed try, including the last. */
-static float backtracking(problem_t *P, const lb_cfg_t *cf, const float *x, const float *p, float fk,
-                          const float *gk, int ls_max, float *xt, float *gt, int64_t D)
+static float backtracking(fit_t *F, const float *x, const float *p, float fk,
+                          const float *gk, int ls_max, float *xt, float *gt, int *known)
 {
-    float gfp = dotf(cf, gk, p, D);
+    float gfp = dotf(F, gk, p);
     float al = 1.0f;
     for (int t = 0; t < ls_max; ++t) {
-        trial_point(x, p, al, xt, D);
-        float ft = closure_f32(P, xt, gt);
-        if (ft <= fk + (1e-4f * al) * gfp) return al;
+        trial_point(x, p, al, xt, F->D);
+        float ft = fit_closure(F, xt, gt, 1);
+        if (ft <= fk + (1e-4f * al) * gfp) { *known = 1; return al; }
         al = al * 0.5f;
     }
+    *known = 0;
     return al;
+}
+
+static void final_forward(const float *X, int64_t N, int64_t nx, problem_t *P, const float *cvals, float *Yrow)
+{
+    for (int64_t n = 0; n < N; ++n) {
+        for (int64_t k = 0; k < P->M; ++k) {
+            int64_t op = P->ops[k];
+            int ar = arity_of(op);
+            float a = 0, bb = 0;
+            if (op != OP_NO_OP) {
+                if (ar >= 1) a = P->val[P->ch[k * 2]];
+                if (ar == 2) bb = P->val[P->ch[k * 2 + 1]];
+            }
+            P->val[k] = fwd_f32(op, a, bb, cvals[k], X + n * nx, nx);
+        }
+        Yrow[n] = P->val[P->root];
+    }
+}
+
+/* One problem in dot_mode 0 / 1 (reference slot vectors, D = M). */
+static void fit_problem_ref(problem_t *P, fit_t *F, const float *C_init, int max_iter, int history, double tol,
+                            int ls_kind, int ls_max, float *C_out, int *iters_out, float *loss_out)
+{
+    const int64_t D = P->M;
+    const int dot_mode = F->mode;
+    size_t vb = sizeof(float) * (size_t)D;
+    float *x = malloc(vb), *g = malloc(vb), *p = malloc(vb), *q = malloc(vb), *xt = malloc(vb),
+          *gt = malloc(vb), *gn = malloc(vb);
+    float **S = malloc(sizeof(float *) * (size_t)(history + 1)), **Yh = malloc(sizeof(float *) * (size_t)(history + 1));
+    double *alph = malloc(sizeof(double) * (size_t)(history + 1));
+    for (int i = 0; i <= history; ++i) { S[i] = malloc(vb); Yh[i] = malloc(vb); }
+    int h = 0, it = 0, known = 0;
+    memcpy(x, C_init, vb);
+    float f = fit_closure(F, x, g, 1);
+    for (it = 0; it < max_iter; ++it) {
+        double gn2 = 0.0;
+        if (dot_mode == 0) { float s = 0.0f; for (int64_t j = 0; j < D; ++j) s += g[j] * g[j]; gn2 = (double)s; }
+        else for (int64_t j = 0; j < D; ++j) gn2 += (double)g[j] * (double)g[j];
+        double gnorm = dot_mode == 0 ? (double)sqrtf((float)gn2) : sqrt(gn2);
+        if (gnorm < (dot_mode == 0 ? (double)(float)tol : tol)) break;
+        direction(F, g, S, Yh, h, D, q, p, alph);
+        float al;
+        if (ls_kind == 0) {
+            float dphi0 = dotf(F, g, p);
+            al = strong_wolfe(F, x, p, f, dphi0, ls_max, xt, gt, &known);
+        } else {
+            al = backtracking(F, x, p, f, g, ls_max, xt, gt, &known);
+        }
+        /* s = alpha p ; x += s ; closure at the new x (lbfgs_batch.py:305-312) */
+        float *s_new = S[h], *y_new = Yh[h];
+        for (int64_t j = 0; j < D; ++j) { s_new[j] = al * p[j]; x[j] = x[j] + s_new[j]; }
+        float fn = fit_closure(F, x, gn, 1);
+        for (int64_t j = 0; j < D; ++j) y_new[j] = gn[j] - g[j];
+        if (h < history) h++;
+        else {  /* drop the oldest pair; the slot just written becomes the newest */
+            float *s0 = S[0], *y0 = Yh[0];
+            for (int i = 0; i < history; ++i) { S[i] = S[i + 1]; Yh[i] = Yh[i + 1]; }
+            S[history] = s0; Yh[history] = y0;
+        }
+        memcpy(g, gn, vb);
+        f = fn;
+    }
+    memcpy(C_out, x, vb);
+    *iters_out = it;
+    *loss_out = f;
+    for (int i = 0; i <= history; ++i) { free(S[i]); free(Yh[i]); }
+    free(S); free(Yh); free(alph);
+    free(x); free(g); free(p); free(q); free(xt); free(gt); free(gn);
+}
+
+/* One problem in dot_mode 2 (the fused kernel's slot vectors, history ring and
+ * end-of-fit rules).  C_out gets the fitted constants in their tape slots and
+ * C_init in the others (NaN everywhere when the virtual slot was poisoned). */
+static void fit_problem_kernel(problem_t *P, fit_t *F, const float *C_init, int max_iter, double tol,
+                               int ls_kind, int ls_max, float *C_out, int *iters_out, float *loss_out)
+{
+    kern_t *k = F->k;
+    const int D = k->D;
+    size_t vb = sizeof(float) * (size_t)D;
+    float *x = calloc((size_t)D, sizeof(float)), *g = malloc(vb), *p = malloc(vb), *q = malloc(vb),
+          *xt = malloc(vb), *gt = malloc(vb), *gn = malloc(vb), *sv = malloc(vb), *yv = malloc(vb);
+    const float tolf = (float)tol;
+    int it = 0, known = 0;
+    for (int j = 0; j < k->K; ++j) x[j] = C_init[k->slot_node[j]];
+    float f = fit_closure(F, x, g, 1);
+    for (it = 0; it < max_iter;) {
+        if (sqrtf(kdot_f2(k, g, g)) < tolf) break;
+        kdirection(k, g, q, p);
+        float al;
+        if (ls_kind == 0) al = strong_wolfe(F, x, p, f, kdot_f2(k, g, p), ls_max, xt, gt, &known);
+        else al = backtracking(F, x, p, f, g, ls_max, xt, gt, &known);
+        for (int j = 0; j < D; ++j) {
+            sv[j] = j < k->nslots ? al * p[j] : 0.0f;
+            x[j] = x[j] + sv[j];
+        }
+        float fn = fit_closure(F, x, gn, !known);
+        if (k->has_virtual && isnan(sv[k->K])) k->poison = 1;
+        int slot;
+        if (k->h < k->hist) { slot = (k->head + k->h) % k->hist; k->h++; }
+        else { slot = k->head; k->head = (k->head + 1) % k->hist; }
+        for (int j = 0; j < D; ++j) yv[j] = j < k->nslots ? gn[j] - g[j] : 0.0f;
+        memcpy(k->ringS + (int64_t)slot * D, sv, vb);
+        memcpy(k->ringY + (int64_t)slot * D, yv, vb);
+        k->last_sy = kdot_pair(k, yv, sv);
+        k->last_yy = kdot_pair(k, yv, yv);
+        k->rho[slot] = f2_div(f2_mk(1.0f, 0.0f), f2_norm(f2_add(k->last_sy, k->eps2)));
+        memcpy(g, gn, vb);
+        f = fn;
+        ++it;
+        /* every real slot NaN and the others poisoned: nothing changes any more */
+        int allnan = 1;
+        for (int j = 0; j < k->K; ++j) if (!isnan(x[j])) allnan = 0;
+        if (k->K > 0 && allnan && (k->poison || !k->has_virtual)) { it = max_iter; break; }
+    }
+    for (int64_t m = 0; m < P->M; ++m) C_out[m] = k->poison ? (float)NAN : C_init[m];
+    for (int j = 0; j < k->K; ++j) C_out[k->slot_node[j]] = x[j];
+    *iters_out = it;
+    *loss_out = f;
+    free(x); free(g); free(p); free(q); free(xt); free(gt); free(gn); free(sv); free(yv);
 }
 
 /* Runs optimize() for problems [0, B).  Layouts: X (N,nx), Y (B,N) or NULL,
  * ops (B,M), ch (B,M,2), C_init/C_out (B,M), Y_out (B,N) or NULL.
  * iters_out/evals_out/loss_out (B) may be NULL; iters_out[b] = -code for a
- * problem whose closures raised an error.  Returns 0 or an error code. */
-int sro_optimize_f32(const float *X, int64_t N, int64_t nx, const float *Y, const int64_t *ops,
-                     const int64_t *ch, const float *C_init, int64_t B, int64_t M, int max_iter,
-                     int history, double tol, int ls_kind, int ls_max, int dot_mode,
-                     float *C_out, float *Y_out, int *iters_out, long *evals_out, float *loss_out)
+ * problem whose closures raised an error.  dot_mode 2 takes the fused kernel's
+ * launch shape (warps W, points per lane V) and slot registers per lane (spl:
+ * 1, 2 or 4, from the batch's largest constant count); its evals are the kernel's
+ * closure count.  Returns 0 or an error code. */
+int sro_optimize_shape_f32(const float *X, int64_t N, int64_t nx, const float *Y, const int64_t *ops,
+                           const int64_t *ch, const float *C_init, int64_t B, int64_t M, int max_iter,
+                           int history, double tol, int ls_kind, int ls_max, int dot_mode, int warps,
+                           int points_per_lane, int spl, float *C_out, float *Y_out, int *iters_out,
+                           long *evals_out, float *loss_out)
 {
     int err_all = 0;
-    lb_cfg_t cf = { dot_mode, 1e-10 };
-    const int64_t D = M;
+    if (dot_mode == 2 && (warps < 1 || points_per_lane < 1 || spl < 1 || history < 1)) return -1;
     _Pragma("omp parallel for schedule(dynamic, 1)")
     for (int64_t b = 0; b < B; ++b) {
         problem_t P;
@@ -520,74 +1061,71 @@ int sro_optimize_f32(const float *X, int64_t N, int64_t nx, const float *Y, cons
         P.val = (float *)malloc(sizeof(float) * (size_t)M);
         P.adj = (float *)malloc(sizeof(float) * (size_t)M);
         P.gacc = (double *)malloc(sizeof(double) * (size_t)M);
-        P.dmode = dot_mode;
-        size_t vb = sizeof(float) * (size_t)D;
-        float *x = malloc(vb), *g = malloc(vb), *p = malloc(vb), *q = malloc(vb), *xt = malloc(vb),
-              *gt = malloc(vb), *gn = malloc(vb);
-        float **S = malloc(sizeof(float *) * (size_t)(history + 1)), **Yh = malloc(sizeof(float *) * (size_t)(history + 1));
-        double *alph = malloc(sizeof(double) * (size_t)(history + 1));
-        for (int i = 0; i <= history; ++i) { S[i] = malloc(vb); Yh[i] = malloc(vb); }
-        int h = 0, it = 0;
-        memcpy(x, C_init + b * M, vb);
-        float f = closure_f32(&P, x, g);
-        for (it = 0; it < max_iter; ++it) {
-            double gn2 = 0.0;
-            if (dot_mode == 0) { float s = 0.0f; for (int64_t j = 0; j < D; ++j) s += g[j] * g[j]; gn2 = (double)s; }
-            else for (int64_t j = 0; j < D; ++j) gn2 += (double)g[j] * (double)g[j];
-            double gnorm = dot_mode == 0 ? (double)sqrtf((float)gn2) : sqrt(gn2);
-            if (gnorm < (dot_mode == 0 ? (double)(float)tol : tol)) break;
-            direction(&cf, g, S, Yh, h, D, q, p, alph);
-            float al;
-            if (ls_kind == 0) {
-                float dphi0 = dotf(&cf, g, p, D);
-                al = strong_wolfe(&P, &cf, x, p, f, dphi0, ls_max, xt, gt, D);
-            } else {
-                al = backtracking(&P, &cf, x, p, f, g, ls_max, xt, gt, D);
+        P.dmode = dot_mode == 1;
+        fit_t F;
+        memset(&F, 0, sizeof(F));
+        F.P = &P; F.mode = dot_mode; F.eps = 1e-10; F.D = M;
+        int it = 0;
+        float f = 0.0f;
+        float *cout = C_out + b * M;
+        if (dot_mode == 2) {
+            kern_t K;
+            memset(&K, 0, sizeof(K));
+            K.W = warps; K.V = points_per_lane; K.spl = spl; K.D = 32 * spl;
+            K.objective = Y ? 0 : 1;
+            K.slot_of = malloc(sizeof(int) * (size_t)M);
+            K.slot_node = malloc(sizeof(int64_t) * (size_t)M);
+            for (int64_t k = 0; k < M; ++k) {
+                K.slot_of[k] = -1;
+                if (k <= P.root && P.ops[k] == OP_LEARNABLE) { K.slot_node[K.K] = k; K.slot_of[k] = K.K++; }
             }
-            /* s = alpha p ; x += s ; closure at the new x (lbfgs_batch.py:305-312) */
-            float *s_new = S[h], *y_new = Yh[h];
-            for (int64_t j = 0; j < D; ++j) { s_new[j] = al * p[j]; x[j] = x[j] + s_new[j]; }
-            float fn = closure_f32(&P, x, gn);
-            for (int64_t j = 0; j < D; ++j) y_new[j] = gn[j] - g[j];
-            if (h < history) h++;
-            else {  /* drop the oldest pair; the slot just written becomes the newest */
-                float *s0 = S[0], *y0 = Yh[0];
-                for (int i = 0; i < history; ++i) { S[i] = S[i + 1]; Yh[i] = Yh[i + 1]; }
-                S[history] = s0; Yh[history] = y0;
-            }
-            memcpy(g, gn, vb);
-            f = fn;
+            K.has_virtual = M > K.K;
+            K.nslots = K.K + K.has_virtual;
+            int RW = 32 * K.V;
+            K.vals = malloc(sizeof(float) * (size_t)RW * (size_t)M);
+            K.adjs = malloc(sizeof(float) * (size_t)RW * (size_t)M);
+            K.gl = malloc(sizeof(float) * (size_t)RW * (size_t)(K.K > 0 ? K.K : 1));
+            K.red_g = malloc(sizeof(f2_t) * (size_t)K.W * (size_t)(K.K > 0 ? K.K : 1));
+            K.red_l = malloc(sizeof(f2_t) * (size_t)K.W);
+            K.lane_err = calloc((size_t)32 * K.W, sizeof(int));
+            K.hist = history;
+            K.ringS = calloc((size_t)history * K.D, sizeof(float));
+            K.ringY = calloc((size_t)history * K.D, sizeof(float));
+            K.rho = calloc((size_t)history, sizeof(f2_t));
+            K.alph = calloc((size_t)history, sizeof(f2_t));
+            K.eps2 = f2_of_double(F.eps);
+            F.k = &K; F.D = K.D;
+            if (K.nslots <= K.D)
+                fit_problem_kernel(&P, &F, C_init + b * M, max_iter, tol, ls_kind, ls_max, cout, &it, &f);
+            else
+                P.err = -1;
+            for (int t = 0; t < 32 * K.W; ++t) if (K.lane_err[t] > P.err) P.err = K.lane_err[t];
+            free(K.slot_of); free(K.slot_node); free(K.vals); free(K.adjs); free(K.gl); free(K.red_g);
+            free(K.red_l); free(K.lane_err); free(K.ringS); free(K.ringY); free(K.rho); free(K.alph);
+        } else {
+            fit_problem_ref(&P, &F, C_init + b * M, max_iter, history, tol, ls_kind, ls_max, cout, &it, &f);
         }
-        memcpy(C_out + b * M, x, vb);
         if (iters_out) iters_out[b] = it;
-        if (Y_out) {  /* final forward pass at the optimized constants */
-            for (int64_t n = 0; n < N; ++n) {
-                for (int64_t k = 0; k < M; ++k) {
-                    int64_t op = P.ops[k];
-                    int ar = arity_of(op);
-                    float a = 0, bb = 0;
-                    if (op != OP_NO_OP) {
-                        if (ar >= 1) a = P.val[P.ch[k * 2]];
-                        if (ar == 2) bb = P.val[P.ch[k * 2 + 1]];
-                    }
-                    P.val[k] = fwd_f32(op, a, bb, x[k], X + n * nx, nx);
-                }
-                Y_out[b * N + n] = P.val[P.root];
-            }
-        }
+        if (Y_out) final_forward(X, N, nx, &P, cout, Y_out + b * N);
         if (loss_out) loss_out[b] = f;
-        if (evals_out) evals_out[b] = P.n_evals;
+        if (evals_out) evals_out[b] = dot_mode == 2 ? F.kevals : P.n_evals;
         if (P.err && iters_out) iters_out[b] = -P.err;
         if (P.err) {
             _Pragma("omp critical")
             { if (!err_all) err_all = P.err; }
         }
-        for (int i = 0; i <= history; ++i) { free(S[i]); free(Yh[i]); }
-        free(S); free(Yh); free(alph);
-        free(x); free(g); free(p); free(q); free(xt); free(gt); free(gn);
         free(P.val); free(P.adj); free(P.gacc);
     }
     return err_all;
+}
+
+int sro_optimize_f32(const float *X, int64_t N, int64_t nx, const float *Y, const int64_t *ops,
+                     const int64_t *ch, const float *C_init, int64_t B, int64_t M, int max_iter,
+                     int history, double tol, int ls_kind, int ls_max, int dot_mode,
+                     float *C_out, float *Y_out, int *iters_out, long *evals_out, float *loss_out)
+{
+    return sro_optimize_shape_f32(X, N, nx, Y, ops, ch, C_init, B, M, max_iter, history, tol, ls_kind, ls_max,
+                                  dot_mode, 1, 1, 1, C_out, Y_out, iters_out, evals_out, loss_out);
 }
 
 int sro_num_threads(void)
