@@ -1252,6 +1252,24 @@ int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len,
   return sr::ws_bytes_for(sh, o.history_size);
 }
 
+int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t max_len, int32_t max_consts,
+                        const sr_fit_options* opt, int32_t* shape) {
+  sr_fit_options o;
+  int rc = sr::fit_defaults(opt, o);
+  if (rc) return rc;
+  if (!shape) { sr::set_error("null shape"); return SR_ERR_INVALID_ARGUMENT; }
+  if (B < 0 || M < 0 || N < 0 || n_x < 0 || max_consts < 0) { sr::set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (M > sr::kMaxNodes) { sr::set_error("tapes longer than %d nodes are not supported", sr::kMaxNodes); return SR_ERR_UNSUPPORTED; }
+  sr::FitShape sh;
+  const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)(M < 1 ? 1 : M);
+  rc = sr::fit_shape(B, N, n_x, Lmax, max_consts, o, sh);
+  if (rc) return rc;
+  shape[0] = sh.V;
+  shape[1] = sh.warps;
+  shape[2] = sh.blocks;
+  return SR_OK;
+}
+
 int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const uint32_t* desc, const int32_t* meta,
                  int64_t B, int64_t M, const float* C_init, float* C_out, int64_t c_sb, int64_t c_sm, float* Y_final,
                  int32_t* iters_out, float* loss_out, int32_t* evals_out, const int32_t* order, int32_t max_len,

@@ -21,6 +21,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "sr_fmath.h"
+
 namespace sr {
 
 enum Op : int {
@@ -59,10 +61,12 @@ __device__ __forceinline__ int child1(uint32_t d) { return int(d >> 20); }
 template <typename T> struct M_;
 template <> struct M_<float> {
   static __device__ __forceinline__ float nan() { return __int_as_float(0x7fffffff); }
-  static __device__ __forceinline__ float sin(float x) { return ::sinf(x); }
-  static __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
-  static __device__ __forceinline__ float exp(float x) { return ::expf(x); }
-  static __device__ __forceinline__ float log(float x) { return ::logf(x); }
+  // sin, cos, exp and log: the library's own functions (sr_fmath.h), which the
+  // oracle reproduces bit for bit; the other functions are CUDA's
+  static __device__ __forceinline__ float sin(float x) { return sr_sinf(x); }
+  static __device__ __forceinline__ float cos(float x) { return sr_cosf(x); }
+  static __device__ __forceinline__ float exp(float x) { return sr_expf(x); }
+  static __device__ __forceinline__ float log(float x) { return sr_logf(x); }
   static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
   static __device__ __forceinline__ float tan(float x) { return ::tanf(x); }
   static __device__ __forceinline__ float asin(float x) { return ::asinf(x); }

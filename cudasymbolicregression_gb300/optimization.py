@@ -28,6 +28,10 @@ class FitResult:
     iters: torch.Tensor    # (B,) int32 L-BFGS iterations run (-code for a problem that hit an error)
     loss: torch.Tensor     # (B,) float32 final mean squared error
     evals: torch.Tensor    # (B,) int32 closures (forward + adjoint passes) evaluated
+    # per kernel launch: (problems, points per lane, warps per problem); the launch
+    # shape fixes the order of the sums over the points, so a host restatement of a
+    # fit needs it to reproduce the bits
+    shapes: Optional[list] = None
 
 
 # Launch shapes (points per lane V, warps per CTA W) the autotuner tries, and its
@@ -135,6 +139,7 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
         order = order.to(device=dev, dtype=torch.int32).contiguous()
         classes = [(0, B, max(tapes.max_root, 1))]
     status = torch.zeros(max(len(classes), 1), dtype=torch.int32, device=dev)
+    shapes = []
     if kernel_events is not None:
         kernel_events[0].record()
     for ci, (start, count, max_len) in enumerate(classes):
@@ -147,6 +152,7 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
         if wsb < 0:
             _lib.check(-1, "sr_fit_workspace_bytes")
         ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)
+        shapes.append((order[start:start + count], *_launch_shape(L, count, N, nx, M, max_len, tapes.max_consts, opts)))
         optr = ctypes.c_void_p(order.data_ptr() + 4 * start)
         rc = L.sr_fit_lbfgs(_lib.ptr(Xc), N, nx, _lib.ptr(Y), _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), count, M,
                             _lib.ptr(Cin), _lib.ptr(C_out), M, 1, _lib.ptr(Y_out), _lib.ptr(iters), _lib.ptr(loss),
@@ -160,7 +166,15 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
     if code and raise_errors:
         ctx = "input validation" if code in (101, 102) else "symbolic evaluation backward pass"
         raise RuntimeError(error_message(code, ctx))
-    return FitResult(C=C_out, Y=Y_out, iters=iters, loss=loss, evals=evals)
+    return FitResult(C=C_out, Y=Y_out, iters=iters, loss=loss, evals=evals, shapes=shapes)
+
+
+def _launch_shape(L, B, N, nx, M, max_len, max_consts, opts):
+    """(points per lane, warps per problem) that sr_fit_lbfgs picks for a launch."""
+    shape = (ctypes.c_int32 * 3)()
+    _lib.check(L.sr_fit_launch_shape(B, N, nx, M, max_len, max_consts, opts, ctypes.cast(shape, ctypes.c_void_p)),
+               "sr_fit_launch_shape")
+    return int(shape[0]), int(shape[1])
 
 
 def _length_classes(lens: torch.Tensor, order: torch.Tensor, width: int):

@@ -169,6 +169,15 @@ int sr_eval_backward_multi_f64(const double *X_dev, int64_t N, int64_t n_x, cons
 int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len, int32_t max_consts,
                                const sr_fit_options *opt);
 
+/* Launch shape sr_fit_lbfgs picks on the current device for these arguments (as
+ * passed to it): shape[0] points per lane, shape[1] warps per problem, shape[2]
+ * persistent CTAs (before any shrinking to fit a workspace).  The warps and points
+ * per lane fix the order in which a fit sums over its points, so they are what a
+ * bit-exact host restatement of a fit needs.  No counterpart in the reference.
+ * Returns 0 or an error code. */
+int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t max_len, int32_t max_consts,
+                        const sr_fit_options *opt, int32_t *shape);
+
 /*
  * Fused batched L-BFGS fit of the learnable constants of every tape: one
  * persistent kernel in which each CTA owns one problem at a time (its warps split

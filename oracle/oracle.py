@@ -18,6 +18,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "sr_oracle.c")
+# the kernels' own float math, compiled into the kernel-arithmetic mode
+FMATH = os.path.join(os.path.dirname(HERE), "cudasymbolicregression_gb300", "csrc", "sr_fmath.h")
 LIB = os.path.join(HERE, "libsr_oracle.so")
 
 ERR_MESSAGES = {
@@ -32,7 +34,8 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle shared library (no-op when it is up to date)."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC),
+                                                                         os.path.getmtime(FMATH)):
         return LIB
     cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
            "-std=gnu11", SRC, "-o", LIB + ".tmp", "-lm"]
@@ -68,6 +71,12 @@ def lib() -> ctypes.CDLL:
         L.sro_set_num_threads.restype = ctypes.c_int
         L.sro_node_fwd_f32.argtypes = [i64, vp, vp, vp, vp, vp, vp]
         L.sro_node_fwd_f32.restype = None
+        L.sro_node_fwd_kf32.argtypes = [i64, vp, vp, vp, vp, vp, vp]
+        L.sro_node_fwd_kf32.restype = None
+        L.sro_fmath_f32.argtypes = [ctypes.c_int, i64, vp, vp]
+        L.sro_fmath_f32.restype = None
+        L.sro_fmath_error.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp]
+        L.sro_fmath_error.restype = None
         i32 = ctypes.c_int32
         L.sro_pcfg_sample.argtypes = [vp, vp, vp, vp, i32, i32, i64, i32, i32, ctypes.c_uint64, vp, vp]
         L.sro_pcfg_sample.restype = None
@@ -204,13 +213,35 @@ def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_gra
     return dict(C=C, Y=Yo, iters=iters, evals=evals, loss=loss, err=err)
 
 
-def node_fwd(op, a, b, c, x):
-    """Elementwise single-node forward (float32) of flat arrays."""
+def node_fwd(op, a, b, c, x, kernel_math=False):
+    """Elementwise single-node forward (float32) of flat arrays; kernel_math takes sin,
+    cos, exp and log from the kernels' own functions (sr_fmath.h) instead of libm."""
     op = _c(op, np.int64)
     a, b, c, x = (_c(v, np.float32) for v in (a, b, c, x))
     out = np.empty(op.shape, np.float32)
-    lib().sro_node_fwd_f32(op.size, _p(op), _p(a), _p(b), _p(c), _p(x), _p(out))
+    fn = lib().sro_node_fwd_kf32 if kernel_math else lib().sro_node_fwd_f32
+    fn(op.size, _p(op), _p(a), _p(b), _p(c), _p(x), _p(out))
     return out
+
+
+FMATH_FN = {"sin": 0, "cos": 1, "exp": 2, "log": 3}
+
+
+def fmath(name, x):
+    """The kernels' own float32 sin, cos, exp or log (sr_fmath.h) on the host."""
+    x = _c(x, np.float32)
+    y = np.empty_like(x)
+    lib().sro_fmath_f32(FMATH_FN[name], x.size, _p(x), _p(y))
+    return y
+
+
+def fmath_error(name, lo_bits, hi_bits, step=1):
+    """Largest error in ulps of the kernels' float32 function over the inputs whose bit
+    patterns run from lo_bits to hi_bits in steps of `step`, against the double
+    function: (max ulp, input at the max, special-value mismatches, inputs checked)."""
+    out = np.zeros(4)
+    lib().sro_fmath_error(FMATH_FN[name], int(lo_bits), int(hi_bits), int(step), _p(out))
+    return float(out[0]), float(out[1]), int(out[2]), int(out[3])
 
 
 def pcfg_sample(tables, start, B, max_len, max_tries, seed):

@@ -7,8 +7,9 @@ are used instead:
 
 * local: every node value of the device cache is recomputed by the oracle from
   the device's own child values; IEEE-exact operations (+ - * /, sqrt, inv,
-  neg, square, floor, ceil, leaves) must agree bit for bit, transcendental ones
-  within a few ulps, and NaN placement exactly.
+  neg, square, floor, ceil, leaves) and the library's own sin, cos, exp and log
+  must agree bit for bit, CUDA's other transcendental functions within a few
+  ulps, and NaN placement exactly.
 * accuracy: against the FP64 oracle, the device's float32 result must be within
   1e-5 relative, or no less accurate than the reference float32 result (the
   reference's own CPU output, or the float32 oracle) up to a factor of 4.
@@ -18,6 +19,8 @@ import numpy as np
 import oracle
 
 EXACT = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 14, 15, 23, 24, 27, 28, 40, 41, 42, 43}
+# sin, cos, exp, log, ln: the kernels' own functions (sr_fmath.h), reproduced bit for bit
+KERNEL_MATH = {10, 11, 12, 13, 25}
 ULP_TRANSC = 8
 ULP_POW = 16
 
@@ -48,12 +51,15 @@ def check_local(X, ops, ch, C, cache):
     xv = X[:, var].T                        # (B*M, N)
     opn = np.repeat(op[:, None], N, 1)
     ref = oracle.node_fwd(opn.ravel(), a.ravel(), b.ravel(), cv.ravel(), xv.ravel()).reshape(a.shape)
+    km = np.isin(opn, list(KERNEL_MATH))
+    if km.any():  # the same function on both sides: the same bits
+        ref[km] = oracle.node_fwd(opn[km], a[km], b[km], cv[km], xv[km], kernel_math=True)
     got = cache[bb, kk]
     nan_r, nan_g = np.isnan(ref), np.isnan(got)
     assert np.array_equal(nan_r, nan_g), f"local NaN placement differs for ops {np.unique(opn[nan_r != nan_g])}"
     both = ~nan_r
     d = ulp_dist(got[both], ref[both])
-    tol = np.where(np.isin(opn[both], list(EXACT)), 0, np.where(opn[both] == 44, ULP_POW, ULP_TRANSC))
+    tol = np.where(np.isin(opn[both], list(EXACT | KERNEL_MATH)), 0, np.where(opn[both] == 44, ULP_POW, ULP_TRANSC))
     with np.errstate(invalid="ignore"):
         tiny = (np.abs(got[both].astype(np.float64) - ref[both]) <= 1e-37) | (got[both] == ref[both])
     bad = (d > tol) & ~tiny
@@ -131,3 +137,42 @@ def first_divergence(run_a, run_b, idx, max_iter, rtol=1e-4):
         d = ((np.isnan(a) != np.isnan(b)) | (np.nan_to_num(rel, nan=0.0) > rtol)).any(1)
         first = np.where((first > max_iter) & d, k, first)
     return first
+
+
+def oracle_fit_like(r, X, Y, ops, ch, C, **kw):
+    """The oracle's kernel-arithmetic fit (dot_mode 2) of the problems of a device fit
+    r (a FitResult), each with the launch shape its kernel launch used (r.shapes);
+    kw are the fit's options (max_iter, line_search_fn, ...).  Returns the oracle's
+    outputs in batch order, as oracle.optimize does."""
+    ops = np.asarray(ops)
+    B, M = ops.shape
+    N = np.asarray(X).shape[0]
+    spl = oracle.kernel_slot_registers(ops)
+    out = dict(C=np.empty((B, M), np.float32), Y=np.empty((B, N), np.float32), iters=np.empty(B, np.int32),
+               evals=np.empty(B, np.int64), loss=np.empty(B, np.float32), err=0)
+    Yb = None if Y is None else np.broadcast_to(np.asarray(Y, np.float32), (B, N))
+    for idx, V, W in r.shapes:
+        idx = idx.cpu().numpy().astype(np.int64) if hasattr(idx, "cpu") else np.asarray(idx, np.int64)
+        o = oracle.optimize(X, None if Yb is None else Yb[idx], ops[idx], np.asarray(ch)[idx], np.asarray(C)[idx],
+                            dot_mode=2, warps=W, points_per_lane=V, slot_registers=spl, **kw)
+        for k in ("C", "Y", "iters", "evals", "loss"):
+            out[k][idx] = o[k]
+        out["err"] = out["err"] or o["err"]
+    return out
+
+
+def fit_bits_differ(r, o):
+    """Per problem: does the device fit r differ from the oracle's o in any bit of its
+    constants, root values or loss, or in its iteration or closure count (NaN
+    compares as NaN)."""
+    def bits(a, b):
+        a = np.ascontiguousarray(a, np.float32)
+        b = np.ascontiguousarray(b, np.float32)
+        na, nb = np.isnan(a), np.isnan(b)
+        d = (na != nb) | (~na & ~nb & (a.view(np.uint32) != b.view(np.uint32)))
+        return d.reshape(d.shape[0], -1).any(1)
+    bad = (r.iters.cpu().numpy() != o["iters"]) | (r.evals.cpu().numpy() != o["evals"])
+    bad |= bits(r.C.cpu().numpy(), o["C"]) | bits(r.loss.cpu().numpy(), o["loss"])
+    if r.Y is not None:
+        bad |= bits(r.Y.cpu().numpy(), o["Y"])
+    return bad

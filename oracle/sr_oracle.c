@@ -34,6 +34,10 @@
 #include <omp.h>
 #endif
 
+/* The library's own float sin, cos, exp and log (used by the kernel-arithmetic mode
+ * below): the same source the kernels compile, a fixed sequence of IEEE operations. */
+#include "../cudasymbolicregression_gb300/csrc/sr_fmath.h"
+
 enum {
     OP_NO_OP = 0, OP_LEARNABLE = 1, OP_C1 = 2, OP_C2 = 3, OP_C3 = 4, OP_C4 = 5, OP_C5 = 6,
     OP_PI = 7, OP_E = 8,
@@ -184,6 +188,9 @@ DEFINE_SCALAR_OPS(float, f32, sinf, cosf, expf, logf, sqrtf, tanf, asinf, acosf,
                   floorf, ceilf, log10f, powf)
 DEFINE_SCALAR_OPS(double, f64, sin, cos, exp, log, sqrt, tan, asin, acos, atan, sinh, cosh, tanh,
                   floor, ceil, log10, pow)
+/* The fused kernels' float operators: sin, cos, exp and log from sr_fmath.h. */
+DEFINE_SCALAR_OPS(float, kf32, sr_sinf, sr_cosf, sr_expf, sr_logf, sqrtf, tanf, asinf, acosf, atanf, sinhf, coshf,
+                  tanhf, floorf, ceilf, log10f, powf)
 
 /* ---- forward / backward over a batch ------------------------------------------
  * Layouts (user-facing, B first): X (N,nx), ops (B,M), ch (B,M,2), C (B,M),
@@ -272,6 +279,16 @@ void sro_node_fwd_f32(int64_t n, const int64_t *op, const float *a, const float 
     }
 }
 
+/* The same with the kernels' own sin, cos, exp and log (sr_fmath.h). */
+void sro_node_fwd_kf32(int64_t n, const int64_t *op, const float *a, const float *b, const float *c,
+                       const float *x, float *out)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t o = op[i] >= OP_VAR0 ? OP_VAR0 : op[i];
+        out[i] = fwd_kf32(o, a[i], b[i], c[i], x + i, 1);
+    }
+}
+
 /* ---- optimize(): per-problem batched L-BFGS --------------------------------------
  *
  * Every problem (column) of the reference's LBFGS_batch evolves independently:
@@ -290,9 +307,10 @@ void sro_node_fwd_f32(int64_t n, const int64_t *op, const float *a, const float 
  * for all other slots), its per-lane point sums and lane/warp reduction order for a
  * given launch shape, its float-pair (Sum2/Dot2, Dekker) dots and two-loop scalars,
  * and the closures it evaluates (it reuses points the reference evaluates twice).
- * On tapes whose operators are IEEE-exact (+ - * /, square, neg, inv, cube,
- * fourth, fifth) this mode and the kernel give the same bits; with transcendental
- * operators the two differ by the ulps of the two math libraries.
+ * Its sin, cos, exp and log are the kernels' own (sr_fmath.h), so on tapes over
+ * the IEEE-exact operators (+ - * /, square, sqrt, neg, inv, cube, fourth, fifth)
+ * and sin, cos, exp, log this mode and the kernel give the same bits; the other
+ * transcendental operators are CUDA's on the device and the host's here.
  */
 typedef struct {
     const float *X; int64_t N, nx;
@@ -423,7 +441,7 @@ static f2_t f2_of_double(double d)
 
 /* Local adjoint of one operator node at one point, as (add0, o0, add1, o1): the
  * same rules as bwd_f32 (evaluation_kernels_cuda.cu:218-632), in the form in which
- * the fused kernel adds them to their destinations. */
+ * the fused kernel adds them to their destinations, with its sin, cos and log. */
 static int ladj_f32(int64_t op, float g, float a, float b, float v, int *add0, float *o0, int *add1, float *o1)
 {
     const float qnan = (float)NAN;
@@ -432,8 +450,8 @@ static int ladj_f32(int64_t op, float g, float a, float b, float v, int *add0, f
     *o0 = *o1 = 0.0f;
     switch (op) {
     case OP_NO_OP: return zero ? 0 : ERR_GRAD_NO_OP;
-    case OP_SIN: if (zero) return 0; *o0 = g * cosf(a); *add0 = 1; return 0;
-    case OP_COS: if (zero) return 0; *o0 = g * -sinf(a); *add0 = 1; return 0;
+    case OP_SIN: if (zero) return 0; *o0 = g * sr_cosf(a); *add0 = 1; return 0;
+    case OP_COS: if (zero) return 0; *o0 = g * -sr_sinf(a); *add0 = 1; return 0;
     case OP_EXP: if (zero) return 0; *o0 = g * v; *add0 = 1; return 0;
     case OP_LOG: case OP_LN: if (zero) return 0; *o0 = div_f32(g, a); *add0 = 1; return 0;
     case OP_SQUARE: if (zero) return 0; *o0 = g * 2.0f * a; *add0 = 1; return 0;
@@ -443,7 +461,7 @@ static int ladj_f32(int64_t op, float g, float a, float b, float v, int *add0, f
         else if (zero) *o0 = 0.0f;
         else *o0 = div_f32(g * 0.5f, sqrtf(a));
         return 0;
-    case OP_TAN: { if (zero) return 0; float cv = cosf(a); *o0 = div_f32(g, cv * cv); *add0 = 1; return 0; }
+    case OP_TAN: { if (zero) return 0; float cv = sr_cosf(a); *o0 = div_f32(g, cv * cv); *add0 = 1; return 0; }
     case OP_ARCSIN: case OP_ARCCOS: {
         if (zero) return 0;
         *add0 = 1;
@@ -457,7 +475,7 @@ static int ladj_f32(int64_t op, float g, float a, float b, float v, int *add0, f
     case OP_SINH: if (zero) return 0; *o0 = g * coshf(a); *add0 = 1; return 0;
     case OP_COSH: if (zero) return 0; *o0 = g * sinhf(a); *add0 = 1; return 0;
     case OP_TANH: { if (zero) return 0; float t = tanhf(a); *o0 = g * (1.0f - t * t); *add0 = 1; return 0; }
-    case OP_LOG10: if (zero) return 0; *o0 = div_f32(g, a * logf(10.0f)); *add0 = 1; return 0;
+    case OP_LOG10: if (zero) return 0; *o0 = div_f32(g, a * sr_logf(10.0f)); *add0 = 1; return 0;
     case OP_NEG: if (zero) return 0; *o0 = -g; *add0 = 1; return 0;
     case OP_INV: if (zero) return 0; *o0 = (a == 0.0f) ? qnan : -div_f32(g, a * a); *add0 = 1; return 0;
     case OP_CUBE: if (zero) return 0; *o0 = g * 3.0f * (a * a); *add0 = 1; return 0;
@@ -477,7 +495,7 @@ static int ladj_f32(int64_t op, float g, float a, float b, float v, int *add0, f
         if (a < 0.0f) { *o0 = qnan; *o1 = qnan; *add0 = *add1 = 1; return 0; }
         if (zero) return 0;
         {
-            float pm1 = powf(a, b - 1.0f), pw = powf(a, b), lg = a <= 0.0f ? qnan : logf(a);
+            float pm1 = powf(a, b - 1.0f), pw = powf(a, b), lg = a <= 0.0f ? qnan : sr_logf(a);
             *o0 = g * (pm1 * b);
             *o1 = g * (lg * pw);
         }
@@ -587,7 +605,7 @@ static float kclosure(problem_t *P, kern_t *k, const float *xt, float *g)
                             if (ar == 2) bb = val[P->ch[kk * 2 + 1]];
                         }
                         float cval = k->slot_of[kk] >= 0 ? xt[k->slot_of[kk]] : 0.0f;
-                        val[kk] = fwd_f32(op, a, bb, cval, P->X + n * P->nx, P->nx);
+                        val[kk] = fwd_kf32(op, a, bb, cval, P->X + n * P->nx, P->nx);
                         adj[kk] = 0.0f;
                     }
                     float f = val[root], groot;
@@ -915,7 +933,8 @@ static float backtracking(fit_t *F, const float *x, const float *p, float fk,
     return al;
 }
 
-static void final_forward(const float *X, int64_t N, int64_t nx, problem_t *P, const float *cvals, float *Yrow)
+static void final_forward(const float *X, int64_t N, int64_t nx, problem_t *P, const float *cvals, float *Yrow,
+                          int kernel_math)
 {
     for (int64_t n = 0; n < N; ++n) {
         for (int64_t k = 0; k < P->M; ++k) {
@@ -926,7 +945,8 @@ static void final_forward(const float *X, int64_t N, int64_t nx, problem_t *P, c
                 if (ar >= 1) a = P->val[P->ch[k * 2]];
                 if (ar == 2) bb = P->val[P->ch[k * 2 + 1]];
             }
-            P->val[k] = fwd_f32(op, a, bb, cvals[k], X + n * nx, nx);
+            P->val[k] = kernel_math ? fwd_kf32(op, a, bb, cvals[k], X + n * nx, nx)
+                                    : fwd_f32(op, a, bb, cvals[k], X + n * nx, nx);
         }
         Yrow[n] = P->val[P->root];
     }
@@ -1106,7 +1126,7 @@ int sro_optimize_shape_f32(const float *X, int64_t N, int64_t nx, const float *Y
             fit_problem_ref(&P, &F, C_init + b * M, max_iter, history, tol, ls_kind, ls_max, cout, &it, &f);
         }
         if (iters_out) iters_out[b] = it;
-        if (Y_out) final_forward(X, N, nx, &P, cout, Y_out + b * N);
+        if (Y_out) final_forward(X, N, nx, &P, cout, Y_out + b * N, dot_mode == 2);
         if (loss_out) loss_out[b] = f;
         if (evals_out) evals_out[b] = dot_mode == 2 ? F.kevals : P.n_evals;
         if (P.err && iters_out) iters_out[b] = -P.err;
@@ -1594,4 +1614,80 @@ void sro_prefix_parent(const int64_t *pre, int64_t B, int64_t M, int32_t n_vars,
         if (err) for (int64_t i = 0; i < M; ++i) par[i] = -1;
         errors[b] = err;
     }
+}
+
+/* ---- the library's float math (sr_fmath.h) -----------------------------------------
+ * fn: 0 sin, 1 cos, 2 exp, 3 log. */
+static float fmath_eval(int fn, float x)
+{
+    switch (fn) {
+    case 0: return sr_sinf(x);
+    case 1: return sr_cosf(x);
+    case 2: return sr_expf(x);
+    default: return sr_logf(x);
+    }
+}
+
+static double fmath_ref(int fn, double x)
+{
+    switch (fn) {
+    case 0: return sin(x);
+    case 1: return cos(x);
+    case 2: return exp(x);
+    default: return log(x);
+    }
+}
+
+void sro_fmath_f32(int fn, int64_t n, const float *x, float *y)
+{
+    _Pragma("omp parallel for schedule(static)")
+    for (int64_t i = 0; i < n; ++i) y[i] = fmath_eval(fn, x[i]);
+}
+
+/* Error of fn over the float inputs whose bit patterns are lo, lo + step, ... <= hi,
+ * against the double-precision function: out[0] = largest error in units of the last
+ * place of the float result (the spacing of floats at the exact value), out[1] = the
+ * input where it occurs, out[2] = inputs whose special-value class (NaN, +-inf, +-0)
+ * differs from the correctly rounded result, out[3] = inputs checked. */
+void sro_fmath_error(int fn, uint32_t lo, uint32_t hi, uint32_t step, double *out)
+{
+    double worst = 0.0, worst_x = 0.0, bad = 0.0, count = 0.0;
+    int64_t n = ((int64_t)hi - (int64_t)lo) / (int64_t)step + 1;
+    _Pragma("omp parallel")
+    {
+        double w = 0.0, wx = 0.0, b = 0.0, c = 0.0;
+        _Pragma("omp for schedule(static)")
+        for (int64_t i = 0; i < n; ++i) {
+            uint32_t bits = lo + (uint32_t)(i * (int64_t)step);
+            float x = srm_i2f((int32_t)bits);
+            if (x != x) continue;
+            float y = fmath_eval(fn, x);
+            double v = fmath_ref(fn, (double)x);
+            float vf = (float)v;
+            c += 1.0;
+            int cy = (y != y) ? 1 : isinf(y) ? 2 + (y < 0) : (y == 0.0f) ? 4 : 0;
+            int cv = (vf != vf) ? 1 : isinf(vf) ? 2 + (vf < 0) : (vf == 0.0f) ? 4 : 0;
+            if (cy != cv) {
+                /* a result at the overflow or underflow edge may round either way */
+                double ulp0 = ldexp(1.0, -149);
+                if (!(cy == 4 && fabs(v) <= ulp0) && !(cv == 4 && fabs((double)y) <= ulp0) &&
+                    !(cy >= 2 && cy <= 3 && fabs(v) >= 3.4028234e38) && !(cv >= 2 && cv <= 3 && fabs((double)y) >= 3.4028234e38))
+                    b += 1.0;
+                continue;
+            }
+            if (cy) continue;
+            int e;
+            frexp(v, &e);                               /* |v| in [2^(e-1), 2^e) */
+            double ulp = ldexp(1.0, (e - 1 - 23) < -149 ? -149 : e - 1 - 23);
+            double err = fabs((double)y - v) / ulp;
+            if (err > w) { w = err; wx = (double)x; }
+        }
+        _Pragma("omp critical")
+        {
+            if (w > worst) { worst = w; worst_x = wx; }
+            bad += b;
+            count += c;
+        }
+    }
+    out[0] = worst; out[1] = worst_x; out[2] = bad; out[3] = count;
 }

@@ -1,10 +1,17 @@
 """GPU parity of optimize() (the fused batched L-BFGS kernel).
 
-References: the reference's own optimize() outputs (tests/golden) and the CPU
-oracle's per-problem restatement.  Tolerances, as stated for the fitted MSE:
-within 1e-4 relative at equal iteration counts.  Trajectories of ill-conditioned
-problems diverge from ulp-level differences (different libm, different summation
-order), so agreement is asserted on the fraction of problems and on the median.
+Two references.  The oracle's kernel-arithmetic mode (oracle/sr_oracle.c, dot_mode 2)
+runs the reference's control flow with the kernel's arithmetic, and the kernel must
+equal it bit for bit (here and in tests/test_fit_exact_gpu.py).  The reference's own
+fits (tests/golden, written by the reference's CPU path on one thread) are matched
+statistically: the reference's float32 sums differ from the kernel's float-pair
+sums, and L-BFGS amplifies such rounding on ill-conditioned problems.  The reference
+itself is not reproducible run to run: its CPU path sums gradients with OpenMP
+atomics (its CUDA path with atomicAdd), and rerun on 2, 4 or 8 threads it matches its
+own single-thread fixture within 1e-4 on 97.7-99.2% of the README problems and
+95.8-97.9% of the backtracking set (medians 10.24-11.07 against 10.56), and on the
+strong-Wolfe ragged set every multi-thread rerun aborts with error 204.  The bars
+below sit at or under those figures.
 """
 import numpy as np
 import pytest
@@ -52,14 +59,16 @@ def test_linear_known_answer(golden):
     np.testing.assert_allclose(Cf, g["C_final"], rtol=1e-4, atol=1e-5)
 
 
-@pytest.mark.parametrize("name,ls,min_frac,median_tol", [("optimize_readme", "strong_wolfe", 0.9, 1.05),
-                                                         ("optimize_ragged", "strong_wolfe", 0.7, 1.05),
-                                                         ("optimize_ragged_bt", "backtracking", 0.8, 1.10)])
-def test_matches_reference_golden(golden, name, ls, min_frac, median_tol):
-    """Final MSE against the reference's own fits.  The backtracking set has about 22
-    finite fits, and its median sits between two of them whose ill-conditioned
-    trajectories depend on rounding: the oracle with double dots already lands 4.8%
-    above the reference's float32 median there, hence the wider bound."""
+@pytest.mark.parametrize("name,ls,min_frac", [("optimize_readme", "strong_wolfe", 0.97),
+                                              ("optimize_ragged", "strong_wolfe", 0.8),
+                                              ("optimize_ragged_bt", "backtracking", 0.95)])
+def test_matches_reference_golden(golden, name, ls, min_frac):
+    """Final MSE against the reference's own fits: within 1e-4 relative on at least
+    min_frac of the problems (the reference's own reruns reach 0.977 and 0.958 on the
+    first and last set and cannot run the second).  Quality, paired: among the
+    problems finite in both whose MSE differs by more than 1e-4, the geometric mean of
+    the ratio device / reference is at most 1.1 (no systematic loss), and the device
+    leaves at most 2 more problems non-finite than the reference."""
     sr = _sr()
     g = golden(name)
     r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]),
@@ -68,8 +77,13 @@ def test_matches_reference_golden(golden, name, ls, min_frac, median_tol):
     assert ok.mean() >= 0.95
     m_gpu = mse(r.Y.cpu().numpy(), g["Y"])
     m_ref = mse(g["Y_final"], g["Y"])
-    assert rel_close(m_gpu, m_ref, 1e-4)[ok].mean() >= min_frac
-    assert np.nanmedian(m_gpu[ok]) <= np.nanmedian(m_ref[ok]) * median_tol + 1e-6
+    close = rel_close(m_gpu, m_ref, 1e-4)
+    assert close[ok].mean() >= min_frac
+    fin = ok & np.isfinite(m_gpu) & np.isfinite(m_ref)
+    diff = fin & ~close
+    if diff.any():
+        assert np.exp(np.mean(np.log(np.maximum(m_gpu[diff], 1e-30) / np.maximum(m_ref[diff], 1e-30)))) <= 1.1
+    assert (ok & ~np.isfinite(m_gpu) & np.isfinite(m_ref)).sum() <= (ok & np.isfinite(m_gpu) & ~np.isfinite(m_ref)).sum() + 2
     # NaN placement of the constants: NaN expressions end with every slot NaN
     nan_ref = np.isnan(g["C_final"]).all(1)
     nan_gpu = np.isnan(r.C.cpu().numpy()).all(1)
@@ -78,35 +92,34 @@ def test_matches_reference_golden(golden, name, ls, min_frac, median_tol):
 
 @pytest.mark.parametrize("ls", ["strong_wolfe", "backtracking"])
 def test_matches_oracle_kernel_arithmetic(golden, ls):
-    """The oracle in the kernel's arithmetic (double dots): equal iteration counts
-    and final MSE within 1e-4 for the large majority of problems."""
+    """The oracle in the kernel's arithmetic, with the launch shape the library picks:
+    every problem bit-identical at 25 iterations (constants, root values, loss,
+    iterations, closures), and the reported loss is the MSE of the reported Y."""
+    from parity import fit_bits_differ, oracle_fit_like
     sr = _sr()
     g = golden("optimize_ragged")
     mi = 25
     r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=mi,
                        line_search_fn=ls, raise_errors=False)
-    o = oracle.optimize(g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=mi, dot_mode=1, line_search_fn=ls)
+    o = oracle_fit_like(r, g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=mi, line_search_fn=ls)
+    assert not fit_bits_differ(r, o).any()
     it_gpu = r.iters.cpu().numpy()
-    same_it = (it_gpu == o["iters"]) & (it_gpu >= 0)
-    assert same_it.mean() >= 0.75
-    close = rel_close(mse(r.Y.cpu().numpy(), g["Y"]), mse(o["Y"], g["Y"]), 1e-4)
-    assert close[same_it].mean() >= 0.8
-    # the kernel's reported loss is the MSE of its own Y_final
     m = mse(r.Y.cpu().numpy(), g["Y"])
     fin = np.isfinite(m) & (it_gpu >= 0)
     np.testing.assert_allclose(r.loss.cpu().numpy()[fin], m[fin], rtol=1e-5, atol=1e-6)
 
 
 def test_initial_closure_matches_oracle(golden):
-    """max_iter=0: only the first closure runs; C is returned unchanged."""
+    """max_iter=0: only the first closure runs; C is returned unchanged and the loss is
+    the oracle's in the kernel's arithmetic, bit for bit."""
+    from parity import oracle_fit_like
     sr = _sr()
     g = golden("optimize_ragged")
     r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]), max_iter=0,
                        raise_errors=False)
-    o = oracle.optimize(g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=0, dot_mode=1)
+    o = oracle_fit_like(r, g["X"], g["Y"], g["ops"], g["ch"], g["C"], max_iter=0)
     np.testing.assert_array_equal(r.C.cpu().numpy(), g["C"])
-    a, b = r.loss.cpu().numpy(), o["loss"]
-    assert rel_close(a, b, 1e-5).all()
+    np.testing.assert_array_equal(r.loss.cpu().numpy(), o["loss"])
     assert (r.iters.cpu().numpy() == 0).all()
 
 
