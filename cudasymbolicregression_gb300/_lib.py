@@ -83,6 +83,8 @@ _SIGS = {
                                     vp], ctypes.c_int),
     "sr_fit_workspace_bytes": ([i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions)], i64),
     "sr_fit_launch_shape": ([i64, i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions), vp], ctypes.c_int),
+    "sr_fit_screen": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, i64, i64, i64, i64, vp, i32, i32,
+                       ctypes.POINTER(FitOptions), vp], ctypes.c_int),
     "sr_fit_lbfgs": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, vp, vp, i32, i32,
                       ctypes.POINTER(FitOptions), vp, i64, vp, vp], ctypes.c_int),
     "sr_fit_lbfgs_static_scratch": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, vp, vp,

@@ -402,12 +402,15 @@ __device__ __forceinline__ float* row_ptr(unsigned char* wb, uint32_t off, int l
 
 // ---------------------------------------------------------------------------------
 // One pass over the problem's points at the constants in the warp's broadcast
-// entries.  kGrad: loss + gradient (forward, residual, reverse sweep); otherwise
-// forward only, writing the root values to Y_final.  Adjoint contributions are added
-// in the reference's order (parents from the last to the first, child 0 before
-// child 1).
+// entries.  kPassGrad: loss + gradient (forward, residual, reverse sweep);
+// kPassYFinal: forward only, writing the root values to Y_final; kPassLoss: forward
+// and residuals only (the loss of a candidate start).  Adjoint contributions are
+// added in the reference's order (parents from the last to the first, child 0
+// before child 1).
 // ---------------------------------------------------------------------------------
-template <int V, bool kGrad>
+enum PassMode : int { kPassGrad = 0, kPassYFinal = 1, kPassLoss = 2 };
+
+template <int V, int kMode>
 __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, int64_t b, int lane, int warp, int W,
                                             int& err) {
   const int64_t N = A.N;
@@ -458,16 +461,30 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
         const int li = v * 32 + lane;
         const float r = op_value<float>(code, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li));
         S.vals[i * RW + li] = r;
-        if (kGrad) S.adj[i * RW + li] = 0.f;
+        if (kMode == kPassGrad) S.adj[i * RW + li] = 0.f;
       }
     }
     float fval[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) fval[v] = lds_src<V>(wb, root_src, v * 32 + lane);
-    if constexpr (!kGrad) {
+    if constexpr (kMode == kPassYFinal) {
 #pragma unroll
       for (int v = 0; v < V; ++v)
         if (valid[v]) A.Y_final[b * N + nn[v]] = fval[v];
+      __syncwarp();
+      continue;
+    } else if constexpr (kMode == kPassLoss) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        if (valid[v]) {
+          if (A.objective == 0) {
+            const float rr = fval[v] - __ldg(Yrow + nn[v]);
+            loss_part = __fadd_rn(loss_part, __fmul_rn(rr, rr));
+          } else {
+            loss_part = __fadd_rn(loss_part, fval[v]);
+          }
+        }
+      }
       __syncwarp();
       continue;
     } else {
@@ -526,7 +543,7 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
       }
     }
     __syncwarp();
-    }  // kGrad
+    }  // kPassGrad
   }
   return loss_part;
 }
@@ -601,7 +618,7 @@ __device__ __forceinline__ float closure(const FitArgs& A, const WarpSmem& S, co
     for (int v = 0; v < V; ++v) S.gl[j * 32 * V + v * 32 + lane] = 0.f;
   }
   __syncthreads();  // also: every warp has read the previous closure's reduction buffers
-  const float lpart = tape_pass<V, true>(A, S, P.b, lane, warp, W, err);
+  const float lpart = tape_pass<V, kPassGrad>(A, S, P.b, lane, warp, W, err);
   F2* out_g = S.red_g + warp * P.K;
   if (P.K < 32) {
     if (P.K < 1) reduce_slots<1>(S.gl, V, P.K, lpart, lane, out_g, S.red_l + warp);
@@ -643,6 +660,88 @@ struct Point {
   Slots<SPL> g;
 };
 
+// Stages problem b (a tape of L = root + 1 nodes) for the CTA: the tape, the numbering
+// of its constant slots, operator nodes and variables, the operator-node program
+// (warp 0), then every warp's broadcast entries (0 and the fixed constants).  Ends
+// with the tables visible to the CTA.
+template <int V>
+__device__ __forceinline__ void stage_problem(const FitArgs& A, const WarpSmem& S, int64_t b, int L, int lane,
+                                              int warp) {
+  // stage the tape; number the constant slots, the operator nodes and the
+  // variables; write the operator-node program (warp 0), visible to the CTA
+  if (warp == 0) {
+    for (int k = lane; k < L; k += 32) S.tape[k] = A.desc[b * A.M + k];
+    __syncwarp();
+    int nslot = 0, nop = 0;
+    for (int k0 = 0; k0 < L; k0 += 32) {
+      const int k = k0 + lane;
+      const int code = k < L ? code_of(S.tape[k]) : -1;
+      const bool lc = code == LEARNABLE;
+      const bool opn = k < L && is_operator_node(code);
+      const unsigned mc = __ballot_sync(0xffffffffu, lc);
+      const unsigned mo = __ballot_sync(0xffffffffu, opn);
+      const unsigned below = (1u << lane) - 1u;
+      if (lc) {
+        const int slot = nslot + __popc(mc & below);
+        S.node_slot[k] = slot;
+        S.slot_node[slot] = k;
+      }
+      if (opn) S.node_slot[k] = nop + __popc(mo & below);
+      nslot += __popc(mc);
+      nop += __popc(mo);
+    }
+    if (lane == 0) {  // one row per distinct variable, in order of first use
+      int nvr = 0;
+      for (int k = 0; k < L; ++k) {
+        const uint32_t d = S.tape[k];
+        if (code_of(d) != VAR) continue;
+        const int var = child0(d);
+        int r = 0;
+        while (r < nvr && S.rowvar[r] != var) ++r;
+        if (r == nvr) S.rowvar[nvr++] = var;
+        S.node_slot[k] = r;
+      }
+      S.info[2] = nvr;
+    }
+    __syncwarp();
+    const WarpLayout WL = warp_layout(A.Lmax, A.Imax, A.Kmax, V, A.VR);
+    const uint32_t RWB = 32u * V * 4u;
+    for (int k = lane; k < L; k += 32) {
+      const uint32_t d = S.tape[k];
+      const int code = code_of(d);
+      if (!is_operator_node(code)) continue;
+      const int ar = arity_of(code);
+      uint32_t sa = 0u, sb = 0u, da = WL.sink, db = WL.sink;
+      if (ar >= 1) operand_words(S.tape, S.node_slot, child0(d), A.Kmax, A.Imax, WL, RWB, sa, da);
+      if (ar == 2) operand_words(S.tape, S.node_slot, child1(d), A.Kmax, A.Imax, WL, RWB, sb, db);
+      const int row = S.node_slot[k];
+      S.pcode[row] = (uint32_t)dense_op(code);
+      S.psa[row] = sa;
+      S.psb[row] = sb;
+      S.pda[row] = da;
+      S.pdb[row] = db;
+    }
+    if (lane == 0) {
+      const int R = (L - 1);
+      uint32_t rs, rdst;
+      operand_words(S.tape, S.node_slot, R, A.Kmax, A.Imax, WL, RWB, rs, rdst);
+      S.info[0] = nop;
+      S.info[1] = is_operator_node(code_of(S.tape[R])) ? S.node_slot[R] : -1;
+      S.info[3] = (int)rs;
+      S.info[4] = (int)rdst;
+      S.info[5] = (int)WL.sink;
+    }
+  }
+  __syncthreads();
+  // this warp's broadcast entries: 0 and the fixed constants of the tape
+  if (lane == 0) S.bc[0] = 0.f;
+  for (int k = lane; k < L; k += 32) {
+    const int code = code_of(S.tape[k]);
+    if (is_fixed_leaf(code)) S.bc[1 + A.Kmax + k] = node_value<float>(code, 0.f, 0.f, 0.f, 0.f);
+  }
+  __syncwarp();
+}
+
 // Line-search phases of the per-problem state machine.  Every loop turn of the
 // kernel evaluates exactly one closure (one call site, inlined), then advances the
 // state; the transitions follow LBFGS_batch.step / _strong_wolfe /
@@ -683,79 +782,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
     P.nslots = P.K + (P.has_virtual ? 1 : 0);
     const int L = P.root + 1;
 
-    // stage the tape; number the constant slots, the operator nodes and the
-    // variables; write the operator-node program (warp 0), visible to the CTA
-    if (warp == 0) {
-      for (int k = lane; k < L; k += 32) S.tape[k] = A.desc[P.b * A.M + k];
-      __syncwarp();
-      int nslot = 0, nop = 0;
-      for (int k0 = 0; k0 < L; k0 += 32) {
-        const int k = k0 + lane;
-        const int code = k < L ? code_of(S.tape[k]) : -1;
-        const bool lc = code == LEARNABLE;
-        const bool opn = k < L && is_operator_node(code);
-        const unsigned mc = __ballot_sync(0xffffffffu, lc);
-        const unsigned mo = __ballot_sync(0xffffffffu, opn);
-        const unsigned below = (1u << lane) - 1u;
-        if (lc) {
-          const int slot = nslot + __popc(mc & below);
-          S.node_slot[k] = slot;
-          S.slot_node[slot] = k;
-        }
-        if (opn) S.node_slot[k] = nop + __popc(mo & below);
-        nslot += __popc(mc);
-        nop += __popc(mo);
-      }
-      if (lane == 0) {  // one row per distinct variable, in order of first use
-        int nvr = 0;
-        for (int k = 0; k < L; ++k) {
-          const uint32_t d = S.tape[k];
-          if (code_of(d) != VAR) continue;
-          const int var = child0(d);
-          int r = 0;
-          while (r < nvr && S.rowvar[r] != var) ++r;
-          if (r == nvr) S.rowvar[nvr++] = var;
-          S.node_slot[k] = r;
-        }
-        S.info[2] = nvr;
-      }
-      __syncwarp();
-      const WarpLayout WL = warp_layout(A.Lmax, A.Imax, A.Kmax, V, A.VR);
-      const uint32_t RWB = 32u * V * 4u;
-      for (int k = lane; k < L; k += 32) {
-        const uint32_t d = S.tape[k];
-        const int code = code_of(d);
-        if (!is_operator_node(code)) continue;
-        const int ar = arity_of(code);
-        uint32_t sa = 0u, sb = 0u, da = WL.sink, db = WL.sink;
-        if (ar >= 1) operand_words(S.tape, S.node_slot, child0(d), A.Kmax, A.Imax, WL, RWB, sa, da);
-        if (ar == 2) operand_words(S.tape, S.node_slot, child1(d), A.Kmax, A.Imax, WL, RWB, sb, db);
-        const int row = S.node_slot[k];
-        S.pcode[row] = (uint32_t)dense_op(code);
-        S.psa[row] = sa;
-        S.psb[row] = sb;
-        S.pda[row] = da;
-        S.pdb[row] = db;
-      }
-      if (lane == 0) {
-        const int R = P.root;
-        uint32_t rs, rdst;
-        operand_words(S.tape, S.node_slot, R, A.Kmax, A.Imax, WL, RWB, rs, rdst);
-        S.info[0] = nop;
-        S.info[1] = is_operator_node(code_of(S.tape[R])) ? S.node_slot[R] : -1;
-        S.info[3] = (int)rs;
-        S.info[4] = (int)rdst;
-        S.info[5] = (int)WL.sink;
-      }
-    }
-    __syncthreads();
-    // this warp's broadcast entries: 0 and the fixed constants of the tape
-    if (lane == 0) S.bc[0] = 0.f;
-    for (int k = lane; k < L; k += 32) {
-      const int code = code_of(S.tape[k]);
-      if (is_fixed_leaf(code)) S.bc[1 + A.Kmax + k] = node_value<float>(code, 0.f, 0.f, 0.f, 0.f);
-    }
-    __syncwarp();
+    stage_problem<V>(A, S, P.b, L, lane, warp);
 
     const float* Cin = A.C_init + P.b * A.c_sb;
     Slots<SPL> x, g, p, xn;
@@ -1094,9 +1121,44 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
     __syncthreads();
     if (A.Y_final) {
       int dummy = 0;
-      tape_pass<V, false>(A, S, P.b, lane, warp, W, dummy);
+      tape_pass<V, kPassYFinal>(A, S, P.b, lane, warp, W, dummy);
     }
     __syncthreads();
+  }
+}
+
+// Loss of K candidate starts per problem (multi-start screening in one launch): the
+// problem's tape is staged once, then for each candidate its constants are published
+// and one forward pass over the points sums the squared residuals (float per lane,
+// float pairs over the lanes and then the warps in a fixed order), so
+// loss_out[b, k] is the mean squared error from candidate k, as the fit's first
+// closure measures it (to the last bit but for the order of the lane sum).
+// Candidate k of problem b: C_sets + k c_sk + b c_sb, slot m at + m c_sm.
+template <int V>
+__global__ void __launch_bounds__(256, 2) fit_screen_kernel(FitArgs A, const float* __restrict__ C_sets, int64_t c_sk,
+                                                            int64_t K, float* __restrict__ loss_out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+  const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, A.VR, warp);
+  for (int64_t b = blockIdx.x; b < A.B; b += gridDim.x) {
+    const int L = A.meta[b * 4 + 1] + 1;
+    const int Kc = A.meta[b * 4 + 2];
+    stage_problem<V>(A, S, b, L, lane, warp);
+    for (int64_t k = 0; k < K; ++k) {
+      const float* Cin = C_sets + k * c_sk + b * A.c_sb;
+      for (int j = lane; j < Kc; j += 32) S.bc[1 + j] = Cin[(int64_t)S.slot_node[j] * A.c_sm];
+      __syncthreads();  // also: thread 0 has read the previous candidate's warp sums
+      int dummy = 0;
+      const F2 lsum = warp_sum_f2(tape_pass<V, kPassLoss>(A, S, b, lane, warp, W, dummy));
+      if (lane == 0) S.red_l[warp] = lsum;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        F2 lt{0.f, 0.f};
+        for (int w = 0; w < W; ++w) lt = f2_add(lt, S.red_l[w]);
+        loss_out[b * K + k] = __fdiv_rn(f2_val(lt), (float)A.N);
+      }
+    }
+    __syncthreads();  // the next problem's staging overwrites the tables
   }
 }
 
@@ -1268,6 +1330,49 @@ int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t ma
   shape[1] = sh.warps;
   shape[2] = sh.blocks;
   return SR_OK;
+}
+
+int sr_fit_screen(const float* X, int64_t N, int64_t n_x, const float* Y, const uint32_t* desc, const int32_t* meta,
+                  int64_t B, int64_t M, const float* C_sets, int64_t c_sk, int64_t c_sb, int64_t c_sm, int64_t K,
+                  float* loss_out, int32_t max_len, int32_t max_consts, const sr_fit_options* opt, void* stream) {
+  using namespace sr;
+  sr_fit_options o;
+  int rc = fit_defaults(opt, o);
+  if (rc) return rc;
+  if (B < 0 || M < 0 || N < 0 || n_x < 0 || K < 0 || max_consts < 0) {
+    set_error("negative size");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
+  if (M > kMaxNodes) { set_error("tapes longer than %d nodes are not supported", kMaxNodes); return SR_ERR_UNSUPPORTED; }
+  if (B == 0 || M == 0 || K == 0) return SR_OK;
+  if (N == 0) { set_error("screening needs at least one data point"); return SR_ERR_INVALID_ARGUMENT; }
+  if (!desc || !meta || !C_sets || !loss_out || (o.objective == 0 && !Y) || (n_x > 0 && !X)) {
+    set_error("null pointer argument");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
+  FitShape sh;
+  const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
+  rc = fit_shape(B, N, n_x, Lmax, max_consts, o, sh);
+  if (rc) return rc;
+  FitArgs A{};
+  A.X = X; A.N = N; A.n_x = n_x; A.Y = o.objective == 0 ? Y : nullptr;
+  A.desc = desc; A.meta = meta; A.B = B; A.M = M;
+  A.c_sb = c_sb; A.c_sm = c_sm;
+  A.objective = o.objective;
+  A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.VR = sh.VR;
+  void* k = sh.V == 1 ? reinterpret_cast<void*>(fit_screen_kernel<1>)
+                      : (sh.V == 2 ? reinterpret_cast<void*>(fit_screen_kernel<2>) : reinterpret_cast<void*>(fit_screen_kernel<4>));
+  int dev = 0, optin = 0;
+  if (cuda_check(cudaGetDevice(&dev), "cudaGetDevice") ||
+      cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "shared memory limit") ||
+      cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin), "screen smem attribute"))
+    return SR_ERR_CUDA;
+  const float* Cs = C_sets;
+  int64_t csk = c_sk, kk = K;
+  float* lo = loss_out;
+  void* args[] = {&A, &Cs, &csk, &kk, &lo};
+  return cuda_check(cudaLaunchKernel(k, dim3(sh.blocks), dim3(sh.warps * 32), args, sh.smem, as_stream(stream)),
+                    "fit_screen_kernel");
 }
 
 int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const uint32_t* desc, const int32_t* meta,

@@ -169,6 +169,37 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
     return FitResult(C=C_out, Y=Y_out, iters=iters, loss=loss, evals=evals, shapes=shapes)
 
 
+def screen_starts(X, Y, Ops, Ch, C_sets, *, objective: int = 0, tapes=None) -> torch.Tensor:
+    """Multi-start screening: the loss of each of K candidate starting constant sets
+    for every problem, as the fit's first closure measures it, in one kernel launch
+    (``sr_fit_screen``; forward passes only).  C_sets is (K, B, M) float32; returns
+    (B, K) float32 (NaN where a candidate's loss is not finite).  No counterpart in
+    the reference, whose optimize starts from one C."""
+    B, M = Ops.shape
+    K = C_sets.shape[0]
+    if C_sets.dim() != 3 or tuple(C_sets.shape[1:]) != (B, M):
+        raise RuntimeError(f"C_sets must be (K, B, M) = (K, {B}, {M}), got {tuple(C_sets.shape)}")
+    _check_backend_inputs(X, Ops.permute(1, 0), Ch.permute(1, 0, 2), C_sets[0].permute(1, 0))
+    if X.dtype != torch.float32:
+        raise RuntimeError("optimize runs in float32: X and C_init must be float32")
+    dev = X.device
+    N, nx = X.shape
+    if Y is not None:
+        Y = _targets(Y, B, N, dev)
+    if tapes is None:
+        tapes = compile_tapes(Ops, Ch, nx)
+    opts = _lib.FitOptions(max_iter=0, history_size=1, tolerance_grad=0.0, line_search=0, line_search_max_iter=0,
+                           eps=0.0, objective=int(objective), max_operators=int(max(tapes.max_operators, 1)))
+    Cs = C_sets.to(torch.float32).contiguous()
+    out = torch.empty((B, K), dtype=torch.float32, device=dev)
+    L = _lib.lib()
+    rc = L.sr_fit_screen(_lib.ptr(X.contiguous()), N, nx, _lib.ptr(Y), _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), B,
+                         M, _lib.ptr(Cs), B * M, M, 1, K, _lib.ptr(out), min(max(tapes.max_root, 1), M),
+                         tapes.max_consts, opts, _lib.stream_ptr(dev))
+    _lib.check(rc, "sr_fit_screen")
+    return out
+
+
 def _launch_shape(L, B, N, nx, M, max_len, max_consts, opts):
     """(points per lane, warps per problem) that sr_fit_lbfgs picks for a launch."""
     shape = (ctypes.c_int32 * 3)()

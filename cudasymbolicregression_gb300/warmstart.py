@@ -354,19 +354,37 @@ def fit_objective(X, Y, ops, ch, C_base, pred, clip_grad: float = 10.0):
     return mse.detach(), g
 
 
+def candidate_starts(X, Y, ops, C_plain, net: WarmStartMLP | None = None, extra: int = 0, clip: float = 10.0,
+                     generator: torch.Generator | None = None) -> torch.Tensor:
+    """(K, B, M) candidate starting constants: the plain start C_plain first, then the
+    network's start (when net is given), then `extra` further standard-normal draws
+    in the learnable slots (as create_constants draws them)."""
+    cands = [C_plain]
+    if net is not None:
+        cands.append(warm_start_constants(net, X, Y, ops, C_plain, clip))
+    is_c = ops == 1
+    for _ in range(extra):
+        draw = torch.randn(C_plain.shape, device=C_plain.device, generator=generator)
+        cands.append(torch.where(is_c, draw, C_plain))
+    return torch.stack(cands)
+
+
+def screened_start(X, Y, ops, ch, C_sets: torch.Tensor) -> torch.Tensor:
+    """Per problem, the candidate start (C_sets (K, B, M)) with the lowest initial loss,
+    all candidates measured in one launch of the screening kernel; a non-finite loss
+    counts as +inf and ties keep the earlier candidate (the plain start first)."""
+    from .optimization import screen_starts
+    loss = screen_starts(X, Y, ops, ch, C_sets)
+    loss = torch.where(torch.isfinite(loss), loss, torch.full_like(loss, float("inf")))
+    best = torch.argmin(loss, dim=1)
+    return C_sets[best, torch.arange(ops.shape[0], device=ops.device)]
+
+
 def gated_warm_start(net: WarmStartMLP, X, Y, ops, ch, C_plain, clip: float = 10.0) -> torch.Tensor:
     """The plain initialisation as fallback and arbiter: per problem, the start (warm
-    or plain) with the lower initial MSE, measured by one closure of the fused fit
-    kernel (max_iter=0) for each; a non-finite loss counts as +inf and ties keep the
-    plain start."""
-    from .optimization import optimize_ex
-    Cw = warm_start_constants(net, X, Y, ops, C_plain, clip)
-    lw = optimize_ex(X, Y, ops, ch, Cw, max_iter=0, raise_errors=False, want_y=False).loss
-    lp = optimize_ex(X, Y, ops, ch, C_plain, max_iter=0, raise_errors=False, want_y=False).loss
-    inf = torch.tensor(float("inf"), device=lw.device)
-    lw = torch.where(torch.isfinite(lw), lw, inf)
-    lp = torch.where(torch.isfinite(lp), lp, inf)
-    return torch.where((lw < lp).unsqueeze(1), Cw, C_plain)
+    or plain) with the lower initial MSE; a non-finite loss counts as +inf and ties
+    keep the plain start."""
+    return screened_start(X, Y, ops, ch, candidate_starts(X, Y, ops, C_plain, net, 0, clip))
 
 
 def warm_start_constants(net: WarmStartMLP, X, Y, ops, C_plain, clip: float = 10.0) -> torch.Tensor:

@@ -169,6 +169,19 @@ int sr_eval_backward_multi_f64(const double *X_dev, int64_t N, int64_t n_x, cons
 int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len, int32_t max_consts,
                                const sr_fit_options *opt);
 
+/* Multi-start screening: the mean squared error (or, with opt->objective = 1, the
+ * mean root value) of K candidate constant sets per problem, each measured as the
+ * fit's first closure measures the loss, in one launch (the tape is staged once per
+ * problem; forward passes only).  Candidate k of problem b is C_sets_dev + k c_sk +
+ * b c_sb with slot m at + m c_sm; loss_dev is (B, K) row-major.  The other arguments
+ * are sr_fit_lbfgs's; opt's launch-shape fields apply, its iteration fields are
+ * ignored.  No counterpart in the reference (its optimize starts from one C).
+ * Returns 0 or an error code. */
+int sr_fit_screen(const float *X_dev, int64_t N, int64_t n_x, const float *Y_dev, const uint32_t *desc_dev,
+                  const int32_t *meta_dev, int64_t B, int64_t M, const float *C_sets_dev, int64_t c_sk, int64_t c_sb,
+                  int64_t c_sm, int64_t K, float *loss_dev, int32_t max_len, int32_t max_consts,
+                  const sr_fit_options *opt, void *stream);
+
 /* Launch shape sr_fit_lbfgs picks on the current device for these arguments (as
  * passed to it): shape[0] points per lane, shape[1] warps per problem, shape[2]
  * persistent CTAs (before any shrinking to fit a workspace).  The warps and points

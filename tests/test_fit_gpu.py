@@ -367,3 +367,27 @@ def test_large_noisy_fit_recovers_signal():
     init = ((_root_values(sr, X, ops, ch, C0)[ok] - Y_true[ok]) ** 2).mean()
     final = ((Yf[ok] - Y_true[ok]) ** 2).mean()
     assert final < 0.6 * init
+
+
+def test_screen_starts_match_the_first_closure(golden):
+    """Multi-start screening (one launch, forward passes only) reports for every
+    candidate start the loss the fit's first closure reports from it, NaN where it is
+    NaN; the screened start is the candidate with the lowest loss, the plain start on
+    ties."""
+    from cudasymbolicregression_gb300 import warmstart
+    from cudasymbolicregression_gb300.optimization import screen_starts
+    sr = _sr()
+    g = golden("optimize_ragged")
+    X, Y, O, Ch, C = cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"])
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    Cs = warmstart.candidate_starts(X, Y, O, C, None, 3, generator=gen)
+    loss = screen_starts(X, Y, O, Ch, Cs).cpu().numpy()
+    for k in range(Cs.shape[0]):
+        first = sr.optimize_ex(X, Y, O, Ch, Cs[k], max_iter=0, raise_errors=False, want_y=False).loss.cpu().numpy()
+        assert rel_close(loss[:, k], first, 1e-6).all()
+    pick = warmstart.screened_start(X, Y, O, Ch, Cs)
+    lf = np.where(np.isfinite(loss), loss, np.inf)
+    best = np.argmin(lf, axis=1)
+    np.testing.assert_array_equal(pick.cpu().numpy(), Cs.cpu().numpy()[best, np.arange(len(best))])
+    with pytest.raises(RuntimeError, match="C_sets must be"):
+        screen_starts(X, Y, O, Ch, Cs[:, :5])
