@@ -61,6 +61,7 @@ class MlpEpilogue(ctypes.Structure):
 MLP_EPI_RELU, MLP_EPI_LINEAR, MLP_EPI_F32, MLP_EPI_RELU_GRAD, MLP_EPI_SPLIT_F32 = 0, 1, 2, 3, 4
 MLP_VOCAB, MLP_EMB, MLP_FEATS, MLP_PROJ, MLP_IN = 64, 64, 32, 28, 128
 MLP_TIMEOUT = 601
+TAPE_EXCEEDS_LAUNCH = 602
 
 _SIGS = {
     "sr_last_error": ([], ctypes.c_char_p),
@@ -84,7 +85,7 @@ _SIGS = {
     "sr_fit_workspace_bytes": ([i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions)], i64),
     "sr_fit_launch_shape": ([i64, i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions), vp], ctypes.c_int),
     "sr_fit_screen": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, i64, i64, i64, i64, vp, i32, i32,
-                       ctypes.POINTER(FitOptions), vp], ctypes.c_int),
+                       ctypes.POINTER(FitOptions), vp, vp], ctypes.c_int),
     "sr_fit_lbfgs": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, vp, vp, i32, i32,
                       ctypes.POINTER(FitOptions), vp, i64, vp, vp], ctypes.c_int),
     "sr_fit_lbfgs_static_scratch": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, vp, vp,

@@ -152,11 +152,14 @@ __device__ __forceinline__ void fill_nan(T* p, size_t count, int tid, int nthrea
 // tape, streamed by one CTA per tape (grid-stride) on a side stream, concurrently with
 // the forward kernel, which writes only the real rows: the forward is bound by
 // instruction latency and leaves most of the HBM write bandwidth to this kernel.
+// A tape longer than the max_len the call was given is evaluated by no class grid: its
+// whole block is NaN, so no row keeps what the buffer held before.
 template <typename T>
 __global__ void __launch_bounds__(256) pad_fill_kernel(const int32_t* __restrict__ meta, int64_t B, int64_t M,
-                                                       int64_t NK, T* __restrict__ cache) {
+                                                       int64_t NK, int Lmax, T* __restrict__ cache) {
   for (int64_t b = blockIdx.x; b < B; b += gridDim.x) {
-    const int64_t L = meta[b * 4];
+    int64_t L = meta[b * 4];
+    if (L > Lmax) L = 0;
     fill_nan(cache + (size_t)b * M * NK + (size_t)L * NK, (size_t)(M - L) * NK, (int)threadIdx.x, (int)blockDim.x);
   }
 }
@@ -327,16 +330,23 @@ __device__ __forceinline__ void report_adjoint(int* status, int code) {
 // ---- padding rows: any nonzero output gradient on a NO_OP row is error 201 ----------
 // One CTA per tape (grid-stride): rows L..M-1 of its (M, N) gradient block are one
 // contiguous range, read with 16-byte streaming loads, four in flight per thread.
+// A tape longer than the max_len the call was given is adjoined by no class grid: it
+// is reported (status 602) instead of being skipped silently.
 template <typename T>
 __global__ void __launch_bounds__(256) padding_check_kernel(const T* __restrict__ gout,
                                                             const int32_t* __restrict__ meta, int64_t B,
-                                                            int64_t M, int64_t N, int32_t* __restrict__ status) {
+                                                            int64_t M, int64_t N, int Lmax,
+                                                            int32_t* __restrict__ status) {
   constexpr int kVec = 16 / sizeof(T);
   for (int64_t b = blockIdx.x; b < B; b += gridDim.x) {
     // the whole CTA stops once a 201 is recorded (uniform decision)
     if (__syncthreads_or(threadIdx.x == 0 && *reinterpret_cast<volatile int32_t*>(status) == ERR_GRAD_ON_NO_OP))
       return;
     const int64_t L = meta[b * 4];
+    if (L > Lmax) {
+      if (threadIdx.x == 0) report(status, SR_TAPE_EXCEEDS_LAUNCH);
+      continue;
+    }
     const T* p = gout + (size_t)b * M * N + (size_t)L * N;
     const size_t count = (size_t)(M - L) * N;
     size_t head = (size_t)((16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15) / sizeof(T);
@@ -842,7 +852,7 @@ static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* de
       // (3.75 against 3.65 ms for the forward of 65536 tapes, N = 1024)
       int64_t fblocks = (int64_t)device_sm_count() * 8;
       if (fblocks > B) fblocks = B;
-      pad_fill_kernel<T><<<(unsigned)fblocks, 256, 0, aux->stream>>>(meta, B, M, N * K, cache);
+      pad_fill_kernel<T><<<(unsigned)fblocks, 256, 0, aux->stream>>>(meta, B, M, N * K, Lmax, cache);
       rc = launch_check("pad_fill_kernel");
     }
   }
@@ -926,7 +936,7 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
       // the check's CTAs take the registers and warp slots they leave
       int64_t pblocks = (int64_t)device_sm_count() * 2;
       if (pblocks > B) pblocks = B;
-      padding_check_kernel<T><<<(unsigned)pblocks, 256, 0, aux->stream>>>(gout, meta, B, M, N * K, status);
+      padding_check_kernel<T><<<(unsigned)pblocks, 256, 0, aux->stream>>>(gout, meta, B, M, N * K, Lmax, status);
       rc = launch_check("padding_check_kernel");
       if (rc) break;
     }

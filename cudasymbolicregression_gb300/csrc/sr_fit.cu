@@ -12,8 +12,8 @@
 //               run and the same in every warp.
 //   direction   two-loop recursion over the last `history_size` (s, y) pairs held in
 //               warp 0's slice of the workspace, broadcast to the CTA through shared
-//               memory; dots, rho, alpha, beta, gamma in double, vectors in float
-//               (one slot per lane).
+//               memory; dots, rho, alpha, beta, gamma as normalised float pairs
+//               (Dekker), vectors in float (one slot per lane).
 //   line search strong Wolfe (bracket + bisection zoom) or Armijo backtracking, with
 //               the reference's acceptance rules and float32 scalar arithmetic.
 //
@@ -297,8 +297,8 @@ __device__ __forceinline__ F2 dot_pair(const Problem<SPL>& P, const Slots<SPL>& 
 // Dot product of two slot vectors with float-pair accumulation (TwoProduct by
 // FMA, then pair sums: Ogita, Rump and Oishi's Dot2), as accurate as a dot in twice
 // the precision on the FP32 pipe, rounded to float.  Used for the line-search slope
-// g.p and the gradient norm; the curvature dots of the two-loop recursion stay in
-// double.
+// g.p and the gradient norm; the curvature dots of the two-loop recursion are kept as
+// normalised pairs (dot_pair).
 template <int SPL>
 __device__ __forceinline__ float dot_f2(const Problem<SPL>& P, const Slots<SPL>& a, const Slots<SPL>& b) {
   F2 acc{0.f, 0.f};
@@ -660,6 +660,24 @@ struct Point {
   Slots<SPL> g;
 };
 
+// Status of a tape larger than the tables the launch was sized for (its root + 1
+// above max_len, its constants above max_consts or its operator nodes above
+// max_operators): the problem is skipped before it touches shared memory.
+constexpr int kStatusTapeExceedsLaunch = 602;
+
+// Whether problem b fits the launch's tables: counted by every warp from the node
+// words in global memory, so the answer is the same in every thread of the CTA.
+__device__ __forceinline__ bool problem_fits(const FitArgs& A, int64_t b, int L, int K, int lane) {
+  if (L < 1 || L > A.Lmax || K < 0 || K > (A.Kmax > 0 ? A.Kmax : 0)) return false;
+  int nop = 0;
+  for (int k0 = 0; k0 < L; k0 += 32) {
+    const int k = k0 + lane;
+    const bool opn = k < L && is_operator_node(code_of(A.desc[b * A.M + k]));
+    nop += __popc(__ballot_sync(0xffffffffu, opn));
+  }
+  return nop <= A.Imax;
+}
+
 // Stages problem b (a tape of L = root + 1 nodes) for the CTA: the tape, the numbering
 // of its constant slots, operator nodes and variables, the operator-node program
 // (warp 0), then every warp's broadcast entries (0 and the fixed constants).  Ends
@@ -781,6 +799,21 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
     P.has_virtual = A.M > P.K;
     P.nslots = P.K + (P.has_virtual ? 1 : 0);
     const int L = P.root + 1;
+    if (!problem_fits(A, P.b, L, P.K, lane)) {  // a caller's max_len / max_consts too small
+      if (warp == 0) {
+        const float qnan = __int_as_float(0x7fffffff);
+        for (int64_t k = lane; k < A.M; k += 32) A.C_out[P.b * A.c_sb + k * A.c_sm] = A.C_init[P.b * A.c_sb + k * A.c_sm];
+        if (A.Y_final)
+          for (int64_t n = lane; n < A.N; n += 32) A.Y_final[P.b * A.N + n] = qnan;
+        if (lane == 0) {
+          report(A.status, kStatusTapeExceedsLaunch);
+          if (A.iters_out) A.iters_out[P.b] = -kStatusTapeExceedsLaunch;
+          if (A.loss_out) A.loss_out[P.b] = qnan;
+          if (A.evals_out) A.evals_out[P.b] = 0;
+        }
+      }
+      continue;
+    }
 
     stage_problem<V>(A, S, P.b, L, lane, warp);
 
@@ -1143,6 +1176,13 @@ __global__ void __launch_bounds__(256, 2) fit_screen_kernel(FitArgs A, const flo
   for (int64_t b = blockIdx.x; b < A.B; b += gridDim.x) {
     const int L = A.meta[b * 4 + 1] + 1;
     const int Kc = A.meta[b * 4 + 2];
+    if (!problem_fits(A, b, L, Kc, lane)) {  // a caller's max_len / max_consts too small
+      if (threadIdx.x == 0) {
+        report(A.status, kStatusTapeExceedsLaunch);
+        for (int64_t k = 0; k < K; ++k) loss_out[b * K + k] = __int_as_float(0x7fffffff);
+      }
+      continue;
+    }
     stage_problem<V>(A, S, b, L, lane, warp);
     for (int64_t k = 0; k < K; ++k) {
       const float* Cin = C_sets + k * c_sk + b * A.c_sb;
@@ -1305,6 +1345,10 @@ int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len,
                                const sr_fit_options* opt) {
   sr_fit_options o;
   if (sr::fit_defaults(opt, o)) return -1;
+  if (max_len < 0 || max_consts < 0 || B < 0 || N < 0 || M < 0) {
+    sr::set_error("negative size");
+    return -1;
+  }
   sr::FitShape sh;
   // the same node-table size sr_fit_lbfgs uses; one variable row gives the smallest
   // tables, hence the most resident CTAs: an upper bound for any n_x (sr_fit_lbfgs
@@ -1320,7 +1364,10 @@ int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t ma
   int rc = sr::fit_defaults(opt, o);
   if (rc) return rc;
   if (!shape) { sr::set_error("null shape"); return SR_ERR_INVALID_ARGUMENT; }
-  if (B < 0 || M < 0 || N < 0 || n_x < 0 || max_consts < 0) { sr::set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (B < 0 || M < 0 || N < 0 || n_x < 0 || max_len < 0 || max_consts < 0) {
+    sr::set_error("negative size");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
   if (M > sr::kMaxNodes) { sr::set_error("tapes longer than %d nodes are not supported", sr::kMaxNodes); return SR_ERR_UNSUPPORTED; }
   sr::FitShape sh;
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)(M < 1 ? 1 : M);
@@ -1334,17 +1381,20 @@ int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t ma
 
 int sr_fit_screen(const float* X, int64_t N, int64_t n_x, const float* Y, const uint32_t* desc, const int32_t* meta,
                   int64_t B, int64_t M, const float* C_sets, int64_t c_sk, int64_t c_sb, int64_t c_sm, int64_t K,
-                  float* loss_out, int32_t max_len, int32_t max_consts, const sr_fit_options* opt, void* stream) {
+                  float* loss_out, int32_t max_len, int32_t max_consts, const sr_fit_options* opt, int32_t* status,
+                  void* stream) {
   using namespace sr;
   sr_fit_options o;
   int rc = fit_defaults(opt, o);
   if (rc) return rc;
-  if (B < 0 || M < 0 || N < 0 || n_x < 0 || K < 0 || max_consts < 0) {
+  if (B < 0 || M < 0 || N < 0 || n_x < 0 || K < 0 || max_len < 0 || max_consts < 0) {
     set_error("negative size");
     return SR_ERR_INVALID_ARGUMENT;
   }
   if (M > kMaxNodes) { set_error("tapes longer than %d nodes are not supported", kMaxNodes); return SR_ERR_UNSUPPORTED; }
-  if (B == 0 || M == 0 || K == 0) return SR_OK;
+  if (!status) { set_error("null status"); return SR_ERR_INVALID_ARGUMENT; }
+  rc = cuda_check(cudaMemsetAsync(status, 0, sizeof(int32_t), as_stream(stream)), "status reset");
+  if (rc || B == 0 || M == 0 || K == 0) return rc;
   if (N == 0) { set_error("screening needs at least one data point"); return SR_ERR_INVALID_ARGUMENT; }
   if (!desc || !meta || !C_sets || !loss_out || (o.objective == 0 && !Y) || (n_x > 0 && !X)) {
     set_error("null pointer argument");
@@ -1360,6 +1410,7 @@ int sr_fit_screen(const float* X, int64_t N, int64_t n_x, const float* Y, const 
   A.c_sb = c_sb; A.c_sm = c_sm;
   A.objective = o.objective;
   A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.VR = sh.VR;
+  A.status = status;
   void* k = sh.V == 1 ? reinterpret_cast<void*>(fit_screen_kernel<1>)
                       : (sh.V == 2 ? reinterpret_cast<void*>(fit_screen_kernel<2>) : reinterpret_cast<void*>(fit_screen_kernel<4>));
   int dev = 0, optin = 0;
@@ -1384,7 +1435,10 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   sr_fit_options o;
   int rc = fit_defaults(opt, o);
   if (rc) return rc;
-  if (B < 0 || M < 0 || N < 0 || n_x < 0 || max_consts < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (B < 0 || M < 0 || N < 0 || n_x < 0 || max_len < 0 || max_consts < 0) {
+    set_error("negative size");
+    return SR_ERR_INVALID_ARGUMENT;
+  }
   if (M > kMaxNodes) { set_error("tapes longer than %d nodes are not supported", kMaxNodes); return SR_ERR_UNSUPPORTED; }
   if (!status) { set_error("null status"); return SR_ERR_INVALID_ARGUMENT; }
   cudaStream_t st = as_stream(stream);
@@ -1442,33 +1496,20 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
 // For them the fit's scratch (work counter, per-warp L-BFGS history rings) lives in
 // a file-scope device array of fixed size instead of a caller buffer.
 // ---------------------------------------------------------------------------------
-#include <mutex>
-
 namespace sr {
 
 constexpr int64_t kStaticFitScratchBytes = 16LL << 20;  // 16 MiB, held on every device that loads the library
 static __device__ __align__(256) unsigned char g_fit_static_scratch[kStaticFitScratchBytes];
 
-// Device address of g_fit_static_scratch on the current device, looked up once per
-// device (the name is only a host-side stand-in in host code).
+// Device address of g_fit_static_scratch on the current device (the name is only a
+// host-side stand-in in host code).  Looked up on every call: the lookup allocates
+// nothing and does not synchronise, and an address kept from an earlier call would
+// dangle after a device reset.
 static int static_scratch_address(void** out) {
-  static std::mutex mu;
-  static void* addr[128] = {nullptr};
-  int dev = 0;
-  int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  void* p = nullptr;
+  const int rc = cuda_check(cudaGetSymbolAddress(&p, g_fit_static_scratch), "cudaGetSymbolAddress(static fit scratch)");
   if (rc) return rc;
-  if (dev < 0 || dev >= 128) {
-    set_error("device ordinal %d out of range", dev);
-    return SR_ERR_UNSUPPORTED;
-  }
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
-    void* p = nullptr;
-    rc = cuda_check(cudaGetSymbolAddress(&p, g_fit_static_scratch), "cudaGetSymbolAddress(static fit scratch)");
-    if (rc) return rc;
-    addr[dev] = p;
-  }
-  *out = addr[dev];
+  *out = p;
   return SR_OK;
 }
 
@@ -1484,7 +1525,7 @@ extern "C" int sr_fit_lbfgs_static_scratch(const float* X, int64_t N, int64_t n_
   sr_fit_options o;
   int rc = fit_defaults(opt, o);
   if (rc) return rc;
-  if (B < 0 || M < 0 || max_consts < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (B < 0 || M < 0 || max_len < 0 || max_consts < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
   if (B == 0 || M == 0) return sr_fit_lbfgs(X, N, n_x, Y, desc, meta, B, M, C_init, C_out, c_sb, c_sm, Y_final,
                                             iters_out, loss_out, evals_out, order, max_len, max_consts, &o, nullptr,
                                             0, status, stream);

@@ -163,6 +163,8 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
         kernel_events[1].record()
     codes = [c for c in status.tolist() if c]
     code = codes[0] if codes else 0
+    if code == _lib.TAPE_EXCEEDS_LAUNCH:  # the sizes above come from compile_tapes: cannot happen here
+        raise RuntimeError("a tape exceeds the table sizes the fit kernel was launched with")
     if code and raise_errors:
         ctx = "input validation" if code in (101, 102) else "symbolic evaluation backward pass"
         raise RuntimeError(error_message(code, ctx))
@@ -192,10 +194,11 @@ def screen_starts(X, Y, Ops, Ch, C_sets, *, objective: int = 0, tapes=None) -> t
                            eps=0.0, objective=int(objective), max_operators=int(max(tapes.max_operators, 1)))
     Cs = C_sets.to(torch.float32).contiguous()
     out = torch.empty((B, K), dtype=torch.float32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
     L = _lib.lib()
     rc = L.sr_fit_screen(_lib.ptr(X.contiguous()), N, nx, _lib.ptr(Y), _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), B,
                          M, _lib.ptr(Cs), B * M, M, 1, K, _lib.ptr(out), min(max(tapes.max_root, 1), M),
-                         tapes.max_consts, opts, _lib.stream_ptr(dev))
+                         tapes.max_consts, opts, _lib.ptr(status), _lib.stream_ptr(dev))
     _lib.check(rc, "sr_fit_screen")
     return out
 

@@ -37,6 +37,9 @@ extern "C" {
 
 /* Largest tape (M) and variable count the node encoding holds. */
 #define SR_MAX_NODES 4095
+/* device status of the fit, screening and adjoint kernels: a tape exceeds the table
+ * sizes the call was given (max_len, max_consts, max_operators) */
+#define SR_TAPE_EXCEEDS_LAUNCH 602
 #define SR_MAX_VARS 4095
 
 /* Text of the last API-level error on this host thread ("" if none). */
@@ -82,9 +85,10 @@ int sr_tape_compile(const int64_t *ops_dev, const int64_t *ch_dev, int64_t B, in
  * library-owned side stream, forked from `stream` and joined back into it before the
  * call returns (a CUDA graph capture of `stream` records both).
  * max_len: largest meta[0] of the batch (stats[1] of sr_tape_compile), or 0 for M;
- * every tape's meta[0] must be at most max_len (it sizes the per-warp shared-memory
- * node tables).  order_dev (B) int32, or NULL: the order in which the persistent warps
- * take the tapes (longest first balances the work).
+ * it sizes the per-warp shared-memory node tables, and a tape whose meta[0] exceeds
+ * it is not evaluated: its whole (M, N) block is NaN.  order_dev (B) int32, or NULL:
+ * the order in which the persistent warps take the tapes (longest first balances
+ * the work).
  */
 int sr_eval_forward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                         const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
@@ -105,7 +109,8 @@ int sr_eval_forward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint3
  * SymbolicEvaluation::backward and evaluation_backward_step_k (reference
  * src/symbolic_evaluation.cpp:94-168, src/evaluation_kernels_cuda.cu:218-632, 654-673).
  * order_dev, max_len and the side stream (here the padding-row check) as for the
- * forward.
+ * forward; a tape whose meta[0] exceeds max_len is not adjoined and status_dev
+ * receives SR_TAPE_EXCEEDS_LAUNCH (its grad_C row is left as it was).
  */
 int sr_eval_backward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                          const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
@@ -175,12 +180,13 @@ int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len,
  * problem; forward passes only).  Candidate k of problem b is C_sets_dev + k c_sk +
  * b c_sb with slot m at + m c_sm; loss_dev is (B, K) row-major.  The other arguments
  * are sr_fit_lbfgs's; opt's launch-shape fields apply, its iteration fields are
- * ignored.  No counterpart in the reference (its optimize starts from one C).
- * Returns 0 or an error code. */
+ * ignored.  status_dev is zeroed, then receives SR_TAPE_EXCEEDS_LAUNCH for a
+ * tape larger than max_len / max_consts (its losses are NaN).  No counterpart in
+ * the reference (its optimize starts from one C).  Returns 0 or an error code. */
 int sr_fit_screen(const float *X_dev, int64_t N, int64_t n_x, const float *Y_dev, const uint32_t *desc_dev,
                   const int32_t *meta_dev, int64_t B, int64_t M, const float *C_sets_dev, int64_t c_sk, int64_t c_sb,
                   int64_t c_sm, int64_t K, float *loss_dev, int32_t max_len, int32_t max_consts,
-                  const sr_fit_options *opt, void *stream);
+                  const sr_fit_options *opt, int32_t *status_dev, void *stream);
 
 /* Launch shape sr_fit_lbfgs picks on the current device for these arguments (as
  * passed to it): shape[0] points per lane, shape[1] warps per problem, shape[2]
@@ -201,7 +207,10 @@ int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t ma
  * C_init/C_out (B, M) use (c_sb, c_sm) strides; Y and Y_final (B, N) are
  * contiguous (Y_final may be NULL); iters_out/loss_out/evals_out (B) may be NULL.
  * iters_out[b] is the number of L-BFGS iterations run, or -code when a closure
- * of problem b hit error 201/204 (status_dev then holds the first such code).
+ * of problem b hit error 201/204 (status_dev then holds the first such code), or
+ * -SR_TAPE_EXCEEDS_LAUNCH when its tape is longer than max_len, has more
+ * constants than max_consts or more operator nodes than opt->max_operators: such a
+ * problem is not fitted (C_out = C_init, Y_final and loss NaN).
  * order_dev (B) int32 gives the processing order (NULL = 0..B-1).
  * max_len: largest root + 1 (stats[2] of sr_tape_compile; 0 = M); max_consts:
  * largest meta[2] (stats[3]).  workspace_dev must hold sr_fit_workspace_bytes(...)
@@ -223,9 +232,11 @@ int sr_fit_lbfgs(const float *X_dev, int64_t N, int64_t n_x, const float *Y_dev,
  * counter and L-BFGS history rings) is a fixed 16 MiB device array inside the
  * library, present on every device that loads it until the process exits.  The
  * persistent grid is shrunk until its history fits; when even one CTA does not fit
- * (very large history_size) the call fails with SR_ERR_WORKSPACE.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture.  Every call uses the same array and resets
+ * (very large history_size) the call fails with SR_ERR_WORKSPACE.  Every call looks
+ * up the array's device address on the current device (cudaGetSymbolAddress: no
+ * allocation, no synchronisation), so a device reset between calls leaves no stale
+ * address; the first call on a device may load the library's device code, so make
+ * it before any stream capture.  Every call uses the same array and resets
  * the work counter itself, so calls that overlap on the same GPU (for instance on
  * two streams) race on it and must be serialised by the caller; each device has
  * its own array.  Arguments and results are those of sr_fit_lbfgs; nothing is

@@ -114,13 +114,16 @@ def test_fit_option_checks(L):
     _rejected(L, L.sr_fit_lbfgs(None, 16, 1, None, None, None, 8, 32, None, None, 32, 1, None, None, None, None, None,
                                 4, 4, None, None, 0, None, None), SR_ERR_INVALID_ARGUMENT, "status")
     # screening: sizes and pointers are checked before any CUDA call; nothing to screen is fine
-    _rejected(L, L.sr_fit_screen(None, 16, 1, None, None, None, 8, 32, None, 256, 32, 1, -1, None, 4, 4, None, None),
-              SR_ERR_INVALID_ARGUMENT, "negative")
+    _rejected(L, L.sr_fit_screen(None, 16, 1, None, None, None, 8, 32, None, 256, 32, 1, -1, None, 4, 4, None,
+                                 ctypes.byref(st), None), SR_ERR_INVALID_ARGUMENT, "negative")
+    _rejected(L, L.sr_fit_screen(None, 16, 1, None, None, None, 8, 32, None, 256, 32, 1, 2, None, -1, 4, None,
+                                 ctypes.byref(st), None), SR_ERR_INVALID_ARGUMENT, "negative")
     _rejected(L, L.sr_fit_screen(None, 16, 1, None, None, None, 8, MAX_NODES + 1, None, 256, 32, 1, 2, None, 4, 4,
-                                 None, None), SR_ERR_UNSUPPORTED)
-    assert L.sr_fit_screen(None, 16, 1, None, None, None, 8, 32, None, 256, 32, 1, 0, None, 4, 4, None, None) == 0
-    _rejected(L, L.sr_fit_screen(None, 16, 1, None, None, None, 8, 32, None, 256, 32, 1, 2, None, 4, 4, None, None),
-              SR_ERR_INVALID_ARGUMENT, "null pointer")
+                                 None, ctypes.byref(st), None), SR_ERR_UNSUPPORTED)
+    _rejected(L, L.sr_fit_screen(None, 16, 1, None, None, None, 8, 32, None, 256, 32, 1, 2, None, 4, 4, None, None,
+                                 None), SR_ERR_INVALID_ARGUMENT, "status")
+    _rejected(L, L.sr_fit_lbfgs(None, 16, 1, None, None, None, 8, 32, None, None, 32, 1, None, None, None, None, None,
+                                -1, 4, None, None, 0, ctypes.byref(st), None), SR_ERR_INVALID_ARGUMENT, "negative")
     shape = (ctypes.c_int32 * 3)()
     _rejected(L, L.sr_fit_launch_shape(8, 16, 1, 32, 4, 4, None, None), SR_ERR_INVALID_ARGUMENT, "shape")
     _rejected(L, L.sr_fit_launch_shape(-8, 16, 1, 32, 4, 4, None, ctypes.cast(shape, ctypes.c_void_p)),

@@ -519,3 +519,41 @@ def test_forward_and_adjoint_replay_in_a_cuda_graph():
     assert int(out[2].item()) == 0
     assert torch.equal(torch.nan_to_num(out[0], nan=-9.0), torch.nan_to_num(ref[0], nan=-9.0))
     assert torch.equal(torch.nan_to_num(out[1], nan=-9.0), torch.nan_to_num(ref[1], nan=-9.0))
+
+
+def test_tape_longer_than_max_len_is_nan_and_reported():
+    """A C-ABI caller that passes a max_len below some tape's length: the forward leaves
+    no stale rows (that tape's whole block is NaN; the others are evaluated as usual)
+    and the adjoint reports status 602 instead of skipping the tape silently."""
+    from cudasymbolicregression_gb300 import _lib, tapes as tg
+    from cudasymbolicregression_gb300.tape import compile_tapes
+    rng = np.random.default_rng(41)
+    B, M, N, nx = 200, 48, 64, 2
+    tb = tg.generate(B, M, seed=42, lengths=rng.integers(2, M + 1, size=B), n_vars=nx, binary=(40, 41, 42))
+    X = cuda(rng.uniform(-2, 2, (N, nx)).astype(np.float32))
+    C = cuda(rng.standard_normal((B, M)).astype(np.float32))
+    tp = compile_tapes(cuda(tb.ops), cuda(tb.ch), nx)
+    L = _lib.lib()
+    st = _lib.stream_ptr(X.device)
+    max_len = 20
+    lens = tp.meta[:, 0].cpu().numpy()
+    over = lens > max_len
+    assert over.any() and (~over).any()
+    cache = torch.full((B, M, N), 7.0, device="cuda")
+    _lib.check(L.sr_eval_forward_f32(_lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), None, B, M, max_len,
+                                     _lib.ptr(C), M, 1, _lib.ptr(cache), st), "forward")
+    full = torch.empty((B, M, N), device="cuda")
+    _lib.check(L.sr_eval_forward_f32(_lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), None, B, M, tp.max_len,
+                                     _lib.ptr(C), M, 1, _lib.ptr(full), st), "forward")
+    torch.cuda.synchronize()
+    got, ref = cache.cpu().numpy(), full.cpu().numpy()
+    assert np.isnan(got[over]).all()
+    np.testing.assert_array_equal(np.nan_to_num(got[~over], nan=-9.0), np.nan_to_num(ref[~over], nan=-9.0))
+    gout = torch.zeros((B, M, N), device="cuda")
+    gC = torch.zeros((B, M), device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.check(L.sr_eval_backward_f32(_lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), None, B, M, max_len,
+                                      _lib.ptr(C), M, 1, _lib.ptr(gout), _lib.ptr(gC), None, _lib.ptr(status), st),
+               "backward")
+    torch.cuda.synchronize()
+    assert int(status.item()) == _lib.TAPE_EXCEEDS_LAUNCH

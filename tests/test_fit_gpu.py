@@ -391,3 +391,41 @@ def test_screen_starts_match_the_first_closure(golden):
     np.testing.assert_array_equal(pick.cpu().numpy(), Cs.cpu().numpy()[best, np.arange(len(best))])
     with pytest.raises(RuntimeError, match="C_sets must be"):
         screen_starts(X, Y, O, Ch, Cs[:, :5])
+
+
+def test_tape_longer_than_the_launch_is_reported_not_fitted(golden):
+    """A C-ABI caller that passes a max_len below a tape's root + 1 (or a max_consts
+    below its constants) gets that problem skipped with status 602 and iters -602,
+    its C_out = C_init and its loss NaN; the other problems are fitted as usual."""
+    import ctypes
+    from cudasymbolicregression_gb300 import _lib
+    from cudasymbolicregression_gb300.tape import compile_tapes
+    g = golden("optimize_ragged")
+    X, Y, O, Ch, C = cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"])
+    tp = compile_tapes(O, Ch, X.shape[1])
+    L = _lib.lib()
+    B, M = tp.B, tp.M
+    N, nx = X.shape
+    roots = tp.meta[:, 1].cpu().numpy() + 1
+    kc = tp.meta[:, 2].cpu().numpy()
+    for max_len, max_consts in ((tp.max_root - 1, tp.max_consts), (tp.max_root, max(tp.max_consts - 1, 0))):
+        opts = _lib.FitOptions(max_iter=10, history_size=10, tolerance_grad=1e-7, line_search=0,
+                               line_search_max_iter=10, eps=1e-10, max_operators=0)
+        wsb = L.sr_fit_workspace_bytes(B, N, M, tp.max_root, tp.max_consts, ctypes.byref(opts))
+        ws = torch.empty(int(wsb), dtype=torch.uint8, device="cuda")
+        Cout, Yf = torch.empty(B, M, device="cuda"), torch.empty(B, N, device="cuda")
+        it, loss = torch.empty(B, dtype=torch.int32, device="cuda"), torch.empty(B, device="cuda")
+        ev, st = torch.empty(B, dtype=torch.int32, device="cuda"), torch.zeros(1, dtype=torch.int32, device="cuda")
+        rc = L.sr_fit_lbfgs(_lib.ptr(X), N, nx, _lib.ptr(Y), _lib.ptr(tp.desc), _lib.ptr(tp.meta), B, M, _lib.ptr(C),
+                            _lib.ptr(Cout), M, 1, _lib.ptr(Yf), _lib.ptr(it), _lib.ptr(loss), _lib.ptr(ev), None,
+                            max_len, max_consts, ctypes.byref(opts), _lib.ptr(ws), ws.numel(), _lib.ptr(st),
+                            _lib.stream_ptr(X.device))
+        _lib.check(rc, "sr_fit_lbfgs")
+        torch.cuda.synchronize()
+        over = (roots > max_len) | (kc > max_consts)
+        assert over.any() and int(st.item()) == _lib.TAPE_EXCEEDS_LAUNCH
+        itn = it.cpu().numpy()
+        assert (itn[over] == -_lib.TAPE_EXCEEDS_LAUNCH).all() and (itn[~over] >= -204).all()
+        assert (itn[~over] != -_lib.TAPE_EXCEEDS_LAUNCH).all()
+        np.testing.assert_array_equal(Cout.cpu().numpy()[over], g["C"][over])
+        assert np.isnan(loss.cpu().numpy()[over]).all()

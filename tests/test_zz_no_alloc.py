@@ -59,10 +59,17 @@ def test_static_scratch_matches_workspace_entry_point_twice(history):
                         eps=1e-10, objective=0, warps_per_block=0, points_per_lane=0, grid_blocks=0)
     wsb = lib.sr_fit_workspace_bytes(tp.B, X.shape[0], tp.M, max(tp.max_root, 1), tp.max_consts,
                                      ctypes.byref(opts))
+    if history == 200:  # the full grid's rings would not fit the 16 MiB array: the shrinking path runs
+        assert wsb > 16 << 20
     ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)
     ref = _call(L, lib.sr_fit_lbfgs, X, Y, tp, C, _outputs(tp.B, tp.M, X.shape[0], dev), opts, ws)
-    for _ in range(2):  # the array keeps the previous call's contents; results must not depend on them
-        got = _call(L, lib.sr_fit_lbfgs_static_scratch, X, Y, tp, C, _outputs(tp.B, tp.M, X.shape[0], dev), opts)
+    outs = [_outputs(tp.B, tp.M, X.shape[0], dev) for _ in range(2)]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(dev)[0]
+    for i in range(2):  # the array keeps the previous call's contents; results must not depend on them
+        got = _call(L, lib.sr_fit_lbfgs_static_scratch, X, Y, tp, C, outs[i], opts)
+        # the entry point allocated no device memory (a change would show in the device's free memory)
+        assert torch.cuda.mem_get_info(dev)[0] == free0
         C_r, Y_r, it_r, loss_r, ev_r, st_r = ref
         C_g, Y_g, it_g, loss_g, ev_g, st_g = got
         assert st_g[0] == st_r[0]
