@@ -3,13 +3,14 @@
 Every expression is an independent problem, so a batch shards with no exchange on
 the data path: rank r fits a contiguous slice of the problems with the replicated X
 and Y (weak scaling when every rank gets its own batch).  The only collectives are
-bookkeeping: the slowest rank's step time (the job's time), and, in a search round,
-the best expression over all ranks, one (MSE, global index) pair per rank.
+the gather of the fitted constants and root values of one batch fitted in shards
+(``fit_sharded``), the slowest rank's step time (the job's time), and, in a search
+round, the best expression over all ranks, one (MSE, global index) pair per rank.
 Everything here works with any torch.distributed backend (gloo on CPU, nccl on GPU).
 """
 from __future__ import annotations
 
-from typing import Tuple
+from typing import Callable, Optional, Tuple
 
 import torch
 
@@ -58,3 +59,41 @@ def best_over_ranks(loss: torch.Tensor, offset: int, device=None) -> Tuple[float
     if not cands:
         return float("inf"), -1
     return min(cands, key=lambda c: (c[0], c[1]))
+
+
+def gather_rows(part: torch.Tensor, total: int) -> torch.Tensor:
+    """Every rank's contiguous share of the rows of a (total, ...) result, gathered on
+    every rank in batch order (rank r holds rows shard_range(total, r, world)).  The
+    shares may differ by one row: each is padded to the largest before the all_gather
+    and trimmed after."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return part
+    world = dist.get_world_size()
+    spans = [shard_range(total, r, world) for r in range(world)]
+    rows = max(b - a for a, b in spans)
+    pad = torch.zeros((rows,) + tuple(part.shape[1:]), dtype=part.dtype, device=part.device)
+    pad[: part.shape[0]] = part
+    out = [torch.empty_like(pad) for _ in range(world)]
+    dist.all_gather(out, pad)
+    return torch.cat([o[: b - a] for o, (a, b) in zip(out, spans)], dim=0)
+
+
+def fit_sharded(X, Y, Ops, Ch, C_init, fit: Optional[Callable] = None, **kw) -> Tuple[torch.Tensor, torch.Tensor]:
+    """``optimize`` of one batch on every rank of the process group: rank r fits the
+    contiguous share shard_range(B, r, world) of the problems with X (and a target row
+    that serves every problem) replicated, then C_final (B, M) and Y_final (B, N) are
+    gathered on every rank in batch order.  The only collective is that gather: the
+    problems are independent, so the result equals the unsharded fit's.  fit(X, Y, Ops,
+    Ch, C_init, **kw) -> (C_final, Y_final) defaults to this package's ``optimize``.
+    Without an initialised process group it is one plain fit."""
+    import torch.distributed as dist
+    if fit is None:
+        from .optimization import optimize as fit
+    B = Ops.shape[0]
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return fit(X, Y, Ops, Ch, C_init, **kw)
+    start, stop = shard_range(B, dist.get_rank(), dist.get_world_size())
+    Ys = Y[start:stop] if (Y is not None and Y.dim() == 2 and Y.shape[0] == B and B > 1) else Y
+    C_part, Y_part = fit(X, Ys, Ops[start:stop], Ch[start:stop], C_init[start:stop], **kw)
+    return gather_rows(C_part, B), gather_rows(Y_part, B)

@@ -72,3 +72,67 @@ def test_two_ranks_gloo():
     assert r0[2] == pytest.approx(0.2) and r1[2] == pytest.approx(0.2)  # the slowest rank's time on both
     assert r0[3] == r1[3] == (pytest.approx(0.25), 637)               # the global minimum and its index
     assert r0[4] == r1[4] == (float("inf"), -1)
+
+
+def _oracle_fit(X, Y, Ops, Ch, C_init, max_iter=30):
+    """The oracle's optimize (the reference's float32 arithmetic) as a fit function."""
+    import numpy as np
+    import oracle
+    o = oracle.optimize(X.numpy(), None if Y is None else Y.numpy(), Ops.numpy(), Ch.numpy(), C_init.numpy(),
+                        max_iter=max_iter, dot_mode=0)
+    return torch.from_numpy(np.ascontiguousarray(o["C"])), torch.from_numpy(np.ascontiguousarray(o["Y"]))
+
+
+def _fit_batch():
+    import numpy as np
+    from cudasymbolicregression_gb300 import tapes
+    rng = np.random.default_rng(5)
+    B, M, N = 37, 16, 24
+    X = rng.uniform(-2, 2, (N, 2)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    tb = tapes.generate(B, M, seed=6, lengths=rng.integers(3, M + 1, size=B), const_counts=rng.integers(0, 4, size=B),
+                        n_vars=2, X_screen=X, C_screen=C)
+    Y = (np.sin(X[:, 0]) + 0.5 * X[:, 1]).astype(np.float32)[None, :].repeat(B, 0)
+    return tuple(torch.from_numpy(a) for a in (X, Y, tb.ops, tb.ch, C))
+
+
+def _fit_worker(rank, world, port, results):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        X, Y, O, Ch, C = _fit_batch()
+        Cf, Yf = sharding.fit_sharded(X, Y, O, Ch, C, fit=_oracle_fit)
+        start, stop = sharding.shard_range(O.shape[0], rank, world)
+        results[rank] = (Cf.numpy(), Yf.numpy(), (start, stop))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_fit_equals_the_whole_batch_fit():
+    """fit_sharded on two gloo ranks (37 problems: shares of 19 and 18): each rank fits
+    its share with the oracle's optimize, and the gathered C_final and Y_final equal the
+    fit of the whole batch bit for bit, in batch order, on both ranks."""
+    import numpy as np
+    ctx = mp.get_context("spawn")
+    manager = ctx.Manager()
+    results = manager.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_fit_worker, args=(r, 2, port, results)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=180)
+        assert p.exitcode == 0
+    X, Y, O, Ch, C = _fit_batch()
+    Cw, Yw = _oracle_fit(X, Y, O, Ch, C)
+    for r in (0, 1):
+        Cf, Yf, span = results[r]
+        assert Cf.shape == tuple(Cw.shape) and Yf.shape == tuple(Yw.shape)
+        np.testing.assert_array_equal(np.nan_to_num(Cf, nan=7.0), np.nan_to_num(Cw.numpy(), nan=7.0))
+        np.testing.assert_array_equal(np.nan_to_num(Yf, nan=7.0), np.nan_to_num(Yw.numpy(), nan=7.0))
+    assert results[0][2] == (0, 19) and results[1][2] == (19, 37)
+    # without a process group it is one plain fit
+    Cs, Ys = sharding.fit_sharded(X, Y, O, Ch, C, fit=_oracle_fit)
+    assert torch.equal(torch.nan_to_num(Cs, nan=7.0), torch.nan_to_num(Cw, nan=7.0))
