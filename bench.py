@@ -88,11 +88,14 @@ SAMPLE_METRIC = "expressions sampled from a grammar, parsed to postfix and linke
 # The fit kernel's traffic per problem is set by N, M and the history, not by the
 # operator set, so the warm-start line's held-out problems (same lengths, M and N)
 # scale the same B=4096 ragged capture.
-FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10720000 + 16384),
-                     ("warmstart", 65536, 512): 16 * (10720000 + 16384)}
-# Issue utilisation of the fit kernel from the same capture (smsp__issue_active, percent):
-# the binding resource of an interpreter whose instructions are mostly integer/control work.
-FIT_ISSUE_ACTIVE_PCT = 49.5
+FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10579200 + 3840),
+                     ("warmstart", 65536, 512): 16 * (10579200 + 3840)}
+# Pipe and issue utilisation of the fit kernel (percent of peak, active cycles) from the
+# same capture, the kernel of commit 9a52c77 (profiles/fit_lbfgs_ragged_B16384_N512.txt):
+# an interpreter whose instructions are mostly integer and control work.
+FIT_PROFILE = {"commit": "9a52c77", "issue_active_pct": 50.1, "fp32_pipe_pct": 13.9, "xu_pipe_pct": 1.75,
+               "alu_pipe_pct": 43.9, "lsu_pipe_pct": 23.4, "fp64_pipe_pct": 1.71, "warps_active_pct": 23.3,
+               "capture": "ncu --set full, ragged B=4096, N=512"}
 # The adjoint call: its three length-class grids and the concurrent padding check.
 EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000),
                       ("eval_backward_kernel", 65536, 1024): 16 * (1075467264 + 10125312)}
@@ -529,7 +532,9 @@ def run_fit(args, rank, world, local):
                              "frac": achieved_tflops / fp32_peak,
                              "traffic": FIT_TRAFFIC_BYTES.get((args.workload, B, N)),
                              "kernel": "fit_lbfgs_kernel", "kernel_ms": head_tk * 1000.0,
-                             "issue_active_pct_ncu": FIT_ISSUE_ACTIVE_PCT,
+                             "issue_active_pct": FIT_PROFILE["issue_active_pct"],
+                             "fp32_pipe_pct": FIT_PROFILE["fp32_pipe_pct"], "xu_pipe_pct": FIT_PROFILE["xu_pipe_pct"],
+                             "ncu_profile": FIT_PROFILE,
                              "peak_kind": f"nominal: {sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz "
                                           f"({pk_kind} clock); no measured FP32 peak exists"},
                 "quality": q_head,
