@@ -64,8 +64,9 @@ struct FitArgs {
   int Lmax, Kmax;
   int Imax;         // rows of the per-warp node tables: largest count of operator nodes
   int VR;           // rows of the per-warp table for variables (distinct variables of a tape)
-  float* ws_vec;    // per warp: 2 * hist * SPL*32 floats (s and y rings)
-  double* ws_scal;  // per CTA: 2 * hist 8-byte words (alpha, rho of each pair, float pairs)
+  float* ws_vec;    // per CTA: 2 * hist * SPL*32 floats (s and y rings), when not in shared memory
+  double* ws_scal;  // per CTA: 2 * hist 8-byte words (alpha, rho of each pair, float pairs), likewise
+  int ring_off;     // > 0: the rings and scalars sit in shared memory at this byte offset
   int* counter;
   int32_t* status;
 };
@@ -776,11 +777,13 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, A.VR, warp);
   // history rings and two-loop scalars of this CTA (used by warp 0)
-  float* ringS = A.ws_vec + (int64_t)blockIdx.x * 2 * A.hist * SPL * 32;
+  float* ringS = A.ring_off ? reinterpret_cast<float*>(smem + A.ring_off)
+                            : A.ws_vec + (int64_t)blockIdx.x * 2 * A.hist * SPL * 32;
   float* ringY = ringS + (int64_t)A.hist * SPL * 32;
   // per history pair: alpha of the current direction and rho = 1 / (s.y + eps), each a
   // normalised float pair in one 8-byte word
-  float2* alph = reinterpret_cast<float2*>(A.ws_scal + (int64_t)blockIdx.x * 2 * A.hist);
+  float2* alph = A.ring_off ? reinterpret_cast<float2*>(ringY + (int64_t)A.hist * SPL * 32)
+                            : reinterpret_cast<float2*>(A.ws_scal + (int64_t)blockIdx.x * 2 * A.hist);
   float2* rhos = alph + A.hist;
   const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
 
@@ -1237,7 +1240,13 @@ static int spl_for(int Kmax) {
 struct FitShape {
   int V, SPL, warps, blocks, Imax, VR;
   size_t smem;
+  size_t ring_off;  // > 0: the history rings sit in shared memory from this byte offset
 };
+
+// Bytes of one CTA's history rings and two-loop scalars.
+static size_t ring_bytes(int hist, int SPL) {
+  return fit_align16((size_t)2 * hist * SPL * 32 * sizeof(float)) + fit_align16((size_t)2 * hist * sizeof(double));
+}
 
 template <int V, int SPL>
 static void* fit_kernel_ptr() {
@@ -1324,6 +1333,20 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
   sh.V = bestV;
   sh.warps = W;
   sh.smem = fit_cta_bytes(Lmax, Imax, Kmax, bestV, W, sh.VR);
+  // Warp 0's two-loop recursion reads the history at every step: keep it in shared
+  // memory when that costs no resident CTA, else in the workspace.
+  sh.ring_off = 0;
+  {
+    const size_t off = fit_align16(sh.smem), with = off + ring_bytes(o.history_size, sh.SPL);
+    int per_sm = 0;
+    if (with <= (size_t)optin &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_kernel(bestV, sh.SPL), W * 32, with) ==
+            cudaSuccess &&
+        per_sm >= bestPerSm) {
+      sh.ring_off = off;
+      sh.smem = with;
+    }
+  }
   int64_t blocks = o.grid_blocks > 0 ? o.grid_blocks : (int64_t)sms * bestPerSm;
   if (blocks > B) blocks = B;  // one problem per CTA at a time
   if (blocks < 1) blocks = 1;
@@ -1331,7 +1354,10 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
   return SR_OK;
 }
 
-static int64_t ws_bytes_for(const FitShape& sh, int hist) {
+// Workspace of a launch: the work counter, and the history rings unless they sit in
+// shared memory (rings_anyway: the size with the rings, an upper bound for any n_x).
+static int64_t ws_bytes_for(const FitShape& sh, int hist, bool rings_anyway = false) {
+  if (sh.ring_off && !rings_anyway) return 256;
   const int64_t vec = (int64_t)sh.blocks * 2LL * hist * sh.SPL * 32 * (int64_t)sizeof(float);
   const int64_t scal = (int64_t)sh.blocks * 2LL * hist * (int64_t)sizeof(double);
   return 256 + fit_align16((size_t)vec) + fit_align16((size_t)scal);
@@ -1355,7 +1381,7 @@ int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len,
   // shrinks its grid to the workspace it is given)
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)(M < 1 ? 1 : M);
   if (sr::fit_shape(B, N, 1, Lmax, max_consts, o, sh)) return -1;
-  return sr::ws_bytes_for(sh, o.history_size);
+  return sr::ws_bytes_for(sh, o.history_size, true);
 }
 
 int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t max_len, int32_t max_consts,
@@ -1473,8 +1499,9 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.VR = sh.VR;
   A.counter = reinterpret_cast<int*>(ws);
   const int64_t vec = (int64_t)sh.blocks * 2LL * o.history_size * sh.SPL * 32 * (int64_t)sizeof(float);
-  A.ws_vec = reinterpret_cast<float*>(ws + 256);
-  A.ws_scal = reinterpret_cast<double*>(ws + 256 + fit_align16((size_t)vec));
+  A.ws_vec = sh.ring_off ? nullptr : reinterpret_cast<float*>(ws + 256);
+  A.ws_scal = sh.ring_off ? nullptr : reinterpret_cast<double*>(ws + 256 + fit_align16((size_t)vec));
+  A.ring_off = (int)sh.ring_off;
   A.status = status;
   rc = cuda_check(cudaMemsetAsync(ws, 0, 256, st), "work counter reset");
   if (rc) return rc;
