@@ -59,6 +59,10 @@ def lib() -> ctypes.CDLL:
             g = getattr(L, "sro_eval_bwd_" + suf)
             g.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, vp]
             g.restype = ctypes.c_int
+        L.sro_eval_fwd_kf32.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp]
+        L.sro_eval_fwd_kf32.restype = None
+        L.sro_eval_bwd_gc_kernel_order_f32.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp, vp]
+        L.sro_eval_bwd_gc_kernel_order_f32.restype = ctypes.c_int
         L.sro_optimize_f32.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, i64, ctypes.c_int, ctypes.c_int,
                                        dbl, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
         L.sro_optimize_f32.restype = ctypes.c_int
@@ -110,8 +114,9 @@ def validate(ops, ch) -> int:
     return lib().sro_validate(_p(ops), _p(ch), B, M, M, 1, 2 * M, 2)
 
 
-def eval_fwd(X, ops, ch, C, dtype=np.float32):
-    """Node values (B,M,N) of every tape at every point."""
+def eval_fwd(X, ops, ch, C, dtype=np.float32, kernel_math=False):
+    """Node values (B,M,N) of every tape at every point; kernel_math (float32) takes
+    sin, cos, exp and log from the kernels' own functions (sr_fmath.h)."""
     X = _c(X, dtype)
     ops = _c(ops, np.int64)
     ch = _c(ch, np.int64)
@@ -120,8 +125,27 @@ def eval_fwd(X, ops, ch, C, dtype=np.float32):
     B, M = ops.shape
     out = np.empty((B, M, N), dtype=dtype)
     fn = lib().sro_eval_fwd_f32 if dtype == np.float32 else lib().sro_eval_fwd_f64
+    if kernel_math:
+        assert dtype == np.float32
+        fn = lib().sro_eval_fwd_kf32
     fn(_p(X), N, nx, _p(ops), _p(ch), _p(C), B, M, _p(out))
     return out
+
+
+def eval_gc_kernel_order(X, ops, ch, C, gout):
+    """grad_C (B, M) of the evaluation adjoint for a dense output gradient, with the
+    kernels' own sin/cos/exp/log and in the device kernel's summation order (per lane
+    over the points l, l + 32, ..., then a 32-lane xor butterfly); returns (gC, err)."""
+    X = _c(X, np.float32)
+    ops = _c(ops, np.int64)
+    ch = _c(ch, np.int64)
+    C = _c(C, np.float32)
+    gout = _c(gout, np.float32)
+    N, nx = X.shape
+    B, M = ops.shape
+    gC = np.zeros((B, M), np.float32)
+    err = lib().sro_eval_bwd_gc_kernel_order_f32(_p(X), N, nx, _p(ops), _p(ch), _p(C), B, M, _p(gout), _p(gC))
+    return gC, err
 
 
 def eval_bwd(X, ops, ch, C, gout, dtype=np.float32, want_gx=True):

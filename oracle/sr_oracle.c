@@ -266,6 +266,75 @@ int sro_eval_bwd_##SUF(const T *X, int64_t N, int64_t nx, const int64_t *ops, co
 
 DEFINE_BATCH(float, f32)
 DEFINE_BATCH(double, f64)
+/* The same loops with the kernels' sin, cos, exp and log (sr_fmath.h): forward values
+ * the device reproduces bit for bit on tapes whose other operators are IEEE-exact. */
+DEFINE_BATCH(float, kf32)
+
+static int ladj_f32(int64_t op, float g, float a, float b, float v, int *add0, float *o0, int *add1, float *o1);
+
+/* grad_C of the evaluation adjoint in the device kernel's summation order
+ * (csrc/sr_eval.cu eval_backward_kernel, one point per lane): per point the leaf
+ * adjoints as sro_eval_bwd_kf32 forms them; per constant node, lane l (0..31) sums
+ * its nonzero adjoints at the points l, l + 32, l + 64, ... in that order, then the 32
+ * lane sums are added by an xor butterfly (offsets 16, 8, 4, 2, 1).  gC (B, M) gets
+ * the constant nodes' sums and 0 elsewhere; returns the first error code. */
+int sro_eval_bwd_gc_kernel_order_f32(const float *X, int64_t N, int64_t nx, const int64_t *ops, const int64_t *ch,
+                                     const float *C, int64_t B, int64_t M, const float *gout, float *gC)
+{
+    int err = 0;
+    int *errs = (int *)calloc((size_t)(B > 0 ? B : 1), sizeof(int));
+    _Pragma("omp parallel for schedule(dynamic, 1)")
+    for (int64_t b = 0; b < B; ++b) {
+        float *val = (float *)malloc(sizeof(float) * (size_t)(M > 0 ? M : 1));
+        float *adj = (float *)malloc(sizeof(float) * (size_t)(M > 0 ? M : 1));
+        float *lanes = (float *)calloc((size_t)(M > 0 ? M : 1) * 32, sizeof(float));
+        const int64_t *o = ops + b * M, *c = ch + b * M * 2;
+        for (int64_t n = 0; n < N; ++n) {
+            for (int64_t k = 0; k < M; ++k) {
+                int64_t op = o[k];
+                int ar = arity_of(op);
+                float a = 0, bb = 0;
+                if (op != OP_NO_OP) {
+                    if (ar >= 1) a = val[c[k * 2]];
+                    if (ar == 2) bb = val[c[k * 2 + 1]];
+                }
+                val[k] = fwd_kf32(op, a, bb, C[b * M + k], X + n * nx, nx);
+                adj[k] = gout[(b * M + k) * N + n];
+            }
+            for (int64_t k = M - 1; k >= 0; --k) {
+                int64_t op = o[k];
+                if (op == OP_LEARNABLE) {
+                    float g = adj[k];
+                    float *d = lanes + k * 32 + (n & 31);
+                    if (g != 0.0f) *d = *d + g;
+                    continue;
+                }
+                if (op != OP_NO_OP && arity_of(op) == 0) continue;
+                int a0, a1;
+                float o0, o1;
+                int ar = arity_of(op);
+                float a = ar >= 1 ? val[c[k * 2]] : 0.0f, bb = ar == 2 ? val[c[k * 2 + 1]] : 0.0f;
+                int e = ladj_f32(op, adj[k], a, bb, val[k], &a0, &o0, &a1, &o1);
+                if (e && !errs[b]) errs[b] = e;
+                if (a0) adj[c[k * 2]] = adj[c[k * 2]] + o0;
+                if (a1) adj[c[k * 2 + 1]] = adj[c[k * 2 + 1]] + o1;
+            }
+        }
+        for (int64_t k = 0; k < M; ++k) {
+            float v[32], t[32];
+            for (int l = 0; l < 32; ++l) v[l] = lanes[k * 32 + l];
+            for (int off = 16; off > 0; off >>= 1) {
+                for (int l = 0; l < 32; ++l) t[l] = v[l] + v[l ^ off];
+                memcpy(v, t, sizeof(v));
+            }
+            gC[b * M + k] = o[k] == OP_LEARNABLE ? v[0] : 0.0f;
+        }
+        free(val); free(adj); free(lanes);
+    }
+    for (int64_t b = 0; b < B && !err; ++b) err = errs[b];
+    free(errs);
+    return err;
+}
 
 /* Elementwise forward of single nodes: out[i] = op[i](a[i], b[i]) with constant
  * c[i] and variable value x[i] (for VAR nodes pass op = OP_VAR0 and nx = 1).

@@ -1,0 +1,79 @@
+"""Exact parity of the evaluation kernels against the oracle in the kernels' arithmetic.
+
+A forward value depends only on per-point arithmetic, and sin, cos, exp and log are the
+library's own functions (csrc/sr_fmath.h), which the oracle compiles from the same
+source.  On tapes whose other operators are IEEE-exact (+ - * /, square, sqrt, neg, inv,
+cube, fourth, fifth, floor, ceil) the whole (B, M, N) cache must therefore equal the
+oracle's bit for bit, NaN placement included, along entire tapes and not just node by
+node.  The gradient of the constants is a sum over the points in a fixed order (per
+lane over the 32-point chunks, then a lane butterfly), which
+oracle.eval_gc_kernel_order restates: grad_C must equal it bit for bit as well.  (The
+X gradient is an atomic sum over the tapes, in the reference too, so its order is not
+fixed; tests/test_eval_gpu.py bounds its error.)
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+EXACT_UNARY = (10, 11, 12, 13, 14, 15, 23, 24, 25, 27, 28, 29, 30, 31)  # sin cos exp log square sqrt floor ceil ln neg inv cube fourth fifth
+EXACT_BINARY = (40, 41, 42, 43)
+
+
+def cuda(a):
+    return torch.as_tensor(np.ascontiguousarray(a)).cuda()
+
+
+def _bits_equal(a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(a.view(np.uint32)[~na], b.view(np.uint32)[~nb])
+
+
+def _batch(seed, B, M, N, nx):
+    from cudasymbolicregression_gb300 import tapes
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-3, 3, (N, nx)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    tb = tapes.generate(B, M, seed=seed, mean_length=M / 3, n_vars=nx, unary=EXACT_UNARY, binary=EXACT_BINARY,
+                        p_const_leaf=0.3, X_screen=X, C_screen=C)
+    return rng, X, C, tb.ops, tb.ch
+
+
+@pytest.mark.parametrize("seed,B,M,N,nx", [(1, 300, 40, 45, 3), (2, 64, 64, 1000, 4), (3, 7, 5, 1, 1),
+                                             (4, 33, 17, 129, 2), (5, 512, 64, 256, 4)])
+def test_cache_and_constant_gradient_bit_identical(seed, B, M, N, nx):
+    import cudasymbolicregression_gb300 as sr
+    rng, X, C, ops, ch = _batch(seed, B, M, N, nx)
+    Ct = cuda(C).requires_grad_(True)
+    out = sr.evaluation.evaluate(cuda(X), cuda(ops), cuda(ch), Ct)
+    got = out.detach().cpu().numpy()
+    want = oracle.eval_fwd(X, ops, ch, C, kernel_math=True)
+    assert _bits_equal(got, want), "forward cache differs from the oracle"
+    gout = rng.standard_normal(got.shape).astype(np.float32)
+    gout[np.isnan(got)] = 0.0
+    gc_want, err = oracle.eval_gc_kernel_order(X, ops, ch, C, gout)
+    if err:
+        pytest.skip("seeded tapes hit a zero denominator under a nonzero gradient")
+    out.backward(cuda(gout))
+    assert _bits_equal(Ct.grad.cpu().numpy(), gc_want), "grad_C differs from the oracle"
+
+
+def test_reference_fixture_cache_bit_identical(golden):
+    """The reference's own random tapes over +,-,*,/,sin,cos,exp,log (the evaluation
+    workload's operators): the device cache equals the kernel-arithmetic oracle's
+    everywhere, and the constant gradient of the fixture's dense output gradient too."""
+    import cudasymbolicregression_gb300 as sr
+    g = golden("random_default_ops")
+    assert np.isin(g["ops"], (0, 1, 2, 3, 4, 5, 6, 7, 8) + EXACT_UNARY + EXACT_BINARY + tuple(range(50, 60))).all()
+    Ct = cuda(g["C"]).requires_grad_(True)
+    out = sr.evaluation.evaluate(cuda(g["X"]), cuda(g["ops"]), cuda(g["ch"]), Ct)
+    assert _bits_equal(out.detach().cpu().numpy(), oracle.eval_fwd(g["X"], g["ops"], g["ch"], g["C"], kernel_math=True))
+    gc_want, err = oracle.eval_gc_kernel_order(g["X"], g["ops"], g["ch"], g["C"], g["gout"])
+    assert err == 0
+    out.backward(cuda(g["gout"]))
+    assert _bits_equal(Ct.grad.cpu().numpy(), gc_want)
