@@ -8,15 +8,17 @@
  * sin/cos, double operations, so a GPU and a CPU compute the same bits.  That makes a
  * whole fit over tapes with these operators reproducible on the host, bit for bit.
  *
- * Methods (textbook, the coefficients are the Taylor coefficients rounded to float):
+ * Methods (textbook; the coefficients of exp, sin and cos are the Taylor coefficients
+ * rounded to float, those of log fitted here):
  *   exp  x = j ln2 + r with j = round(x / ln2) and r by a two-part Cody-Waite
  *        reduction (FMA), e^r by its degree-7 Taylor polynomial (|r| <= ln2/2),
  *        then 2^j applied as two exact powers of two (one rounding, correct into
  *        the subnormal range).
- *   log  x = m 2^e with m in [sqrt(1/2), sqrt(2)), f = m - 1, s = f / (2 + f),
- *        log(1 + f) = f - f^2/2 + s (f^2/2 + R(s^2)) with R(z) = 2z/3 + 2z^2/5 +
- *        2z^3/7 + 2z^4/9 (the series of 2 atanh(s) rearranged), plus e ln2 with ln2
- *        split so that e ln2_hi is exact.
+ *   log  x = m 2^e with m in [sqrt(1/2), sqrt(2)), f = m - 1 (exact), log(1 + f) =
+ *        f - f^2/2 + f^3 h(f) with h a degree-8 polynomial fitted to the remainder
+ *        (weighted least squares on Chebyshev nodes, iteratively reweighted towards
+ *        the minimax error: sr_fmath_coefficients.py), plus e ln2 with ln2 split so
+ *        that e ln2_hi is exact.  No division.
  *   sin, cos  x = q pi/2 + r: below 2^19 by a three-part Cody-Waite reduction with
  *        FMA (its first step is exact); above, by Payne and Hanek's method, the
  *        product of x's 24-bit significand with a 96-bit window of the bits of 2/pi
@@ -123,14 +125,20 @@ SRM_FN float sr_logf(float x)
         e += 1;
     }
     float f = SRM_SUB(SRM_I2F(ix), 1.0f);           /* exact */
-    float s = SRM_DIV(f, SRM_ADD(2.0f, f));
-    float z = SRM_MUL(s, s);
-    float R = SRM_FMA(z, 0.222222223877907f, 0.285714298486710f);  /* 2/9, 2/7 */
-    R = SRM_FMA(z, R, 0.400000005960464f);                          /* 2/5 */
-    R = SRM_FMA(z, R, 0.666666686534882f);                          /* 2/3 */
-    R = SRM_MUL(z, R);
-    float hfsq = SRM_MUL(SRM_MUL(0.5f, f), f);
-    float lg = SRM_SUB(f, SRM_SUB(hfsq, SRM_MUL(s, SRM_ADD(hfsq, R))));
+    /* log(1 + f) = f - f^2/2 + f^3 h(f), h a degree-8 polynomial fitted to
+     * (log(1 + f) - f + f^2/2) / f^3 on [sqrt(1/2) - 1, sqrt(2) - 1]
+     * (sr_fmath_coefficients.py; its own error is 0.06 ulp of the result) */
+    float h = SRM_FMA(f, 0.054545700550079346f, -0.10845454782247543f);
+    h = SRM_FMA(f, h, 0.12036514282226562f);
+    h = SRM_FMA(f, h, -0.12560544908046722f);
+    h = SRM_FMA(f, h, 0.14218197762966156f);
+    h = SRM_FMA(f, h, -0.1665862649679184f);
+    h = SRM_FMA(f, h, 0.20001961290836334f);
+    h = SRM_FMA(f, h, -0.2500019073486328f);
+    h = SRM_FMA(f, h, 0.3333331048488617f);
+    float f2 = SRM_MUL(f, f);
+    float hfsq = SRM_MUL(0.5f, f2);
+    float lg = SRM_SUB(f, SRM_SUB(hfsq, SRM_MUL(SRM_MUL(f2, f), h)));
     const float ln2_hi = 0.693145751953125f;        /* ln 2 to 16 bits: e ln2_hi is exact */
     const float ln2_lo = 1.42860676533019e-06f;     /* ln 2 - ln2_hi */
     float fe = (float)e;
@@ -196,7 +204,6 @@ SRM_FN float srm_sincos(float x, int odd)
 {
     float ax = SRM_I2F(SRM_F2I(x) & 0x7fffffff);
     if (!(ax < SRM_I2F(0x7f800000))) return SRM_SUB(x, x);  /* NaN, +-inf */
-    if (!odd && ax < 2.44140625e-4f) return x;     /* |x| < 2^-12: sin x rounds to x (keeps -0) */
     float r;
     int q;
     if (ax < 524288.0f) {                           /* 2^19 */
@@ -212,22 +219,21 @@ SRM_FN float srm_sincos(float x, int odd)
         if (x < 0.0f) { r = -r; q = -q; }
     }
     q += odd;
+    /* both polynomials, then a select: lanes in different quadrants do not diverge */
     float w = SRM_MUL(r, r);
-    float res;
-    if (q & 1) {                                    /* cos r = 1 - w/2 + w^2 C(w) */
-        float c = SRM_FMA(w, -2.75573188446288e-07f, 2.48015876422869e-05f);  /* -1/10!, 1/8! */
-        c = SRM_FMA(w, c, -1.38888892251998e-03f);                          /* -1/6! */
-        c = SRM_FMA(w, c, 4.16666679084301e-02f);                           /* 1/4! */
-        float hw = SRM_MUL(0.5f, w);
-        float t = SRM_SUB(1.0f, hw);
-        res = SRM_ADD(t, SRM_FMA(SRM_MUL(w, w), c, SRM_SUB(SRM_SUB(1.0f, t), hw)));
-    } else {                                        /* sin r = r + r^3 S(w) */
-        float sp = SRM_FMA(w, 2.75573188446288e-06f, -1.98412701138295e-04f);  /* 1/9!, -1/7! */
-        sp = SRM_FMA(w, sp, 8.33333376795053e-03f);                            /* 1/5! */
-        sp = SRM_FMA(w, sp, -1.66666671633720e-01f);                           /* -1/3! */
-        res = SRM_FMA(SRM_MUL(r, w), sp, r);
-    }
-    return (q & 2) ? -res : res;
+    float c = SRM_FMA(w, -2.75573188446288e-07f, 2.48015876422869e-05f);  /* -1/10!, 1/8! */
+    c = SRM_FMA(w, c, -1.38888892251998e-03f);                          /* -1/6! */
+    c = SRM_FMA(w, c, 4.16666679084301e-02f);                           /* 1/4! */
+    float hw = SRM_MUL(0.5f, w);
+    float t = SRM_SUB(1.0f, hw);
+    float cosr = SRM_ADD(t, SRM_FMA(SRM_MUL(w, w), c, SRM_SUB(SRM_SUB(1.0f, t), hw)));  /* 1 - w/2 + w^2 C(w) */
+    float sp = SRM_FMA(w, 2.75573188446288e-06f, -1.98412701138295e-04f);  /* 1/9!, -1/7! */
+    sp = SRM_FMA(w, sp, 8.33333376795053e-03f);                            /* 1/5! */
+    sp = SRM_FMA(w, sp, -1.66666671633720e-01f);                           /* -1/3! */
+    float sinr = SRM_FMA(SRM_MUL(r, w), sp, r);                          /* r + r^3 S(w) */
+    float res = (q & 1) ? cosr : sinr;
+    res = (q & 2) ? -res : res;
+    return (!odd && ax < 2.44140625e-4f) ? x : res;  /* |x| < 2^-12: sin x rounds to x (keeps -0) */
 }
 
 SRM_FN float sr_sinf(float x) { return srm_sincos(x, 0); }

@@ -77,3 +77,26 @@ def test_reference_fixture_cache_bit_identical(golden):
     assert err == 0
     out.backward(cuda(g["gout"]))
     assert _bits_equal(Ct.grad.cpu().numpy(), gc_want)
+
+
+def test_multiple_sets_bit_identical():
+    """evaluate_multiple: every constant set's cache and grad_C equal the oracle's for
+    that set (the sets are evaluated one after the other inside one launch)."""
+    import cudasymbolicregression_gb300 as sr
+    rng, X, C, ops, ch = _batch(7, 96, 32, 200, 3)
+    K = 3
+    C3 = rng.standard_normal((C.shape[0], C.shape[1], K)).astype(np.float32)
+    Ct = cuda(C3).requires_grad_(True)
+    out = sr.evaluation.evaluate_multiple(cuda(X), cuda(ops), cuda(ch), Ct)
+    got = out.detach().cpu().numpy()
+    gout = rng.standard_normal(got.shape).astype(np.float32)
+    gout[np.isnan(got)] = 0.0
+    want_gc = []
+    for k in range(K):
+        assert _bits_equal(got[..., k], oracle.eval_fwd(X, ops, ch, C3[:, :, k], kernel_math=True)), f"set {k}"
+        gc, err = oracle.eval_gc_kernel_order(X, ops, ch, C3[:, :, k], gout[..., k])
+        if err:
+            pytest.skip("seeded tapes hit a zero denominator under a nonzero gradient")
+        want_gc.append(gc)
+    out.backward(cuda(gout))
+    assert _bits_equal(Ct.grad.cpu().numpy(), np.stack(want_gc, axis=2))

@@ -6,7 +6,7 @@ them is reproducible bit for bit (tests/test_fit_exact_gpu.py); this file checks
 functions themselves against the double-precision functions of the host's libm.
 
 Over every float32 input (2^32 of them, checked once with the same checker at step
-1) the largest errors are: sin 1.544 ulp, cos 1.540 ulp, exp 0.939 ulp, log 0.917
+1) the largest errors are: sin 1.544 ulp, cos 1.540 ulp, exp 0.939 ulp, log 0.876
 ulp, with every special value (NaN, +-inf, +-0, overflow to inf, underflow to 0)
 where the correctly rounded result has it.  CUDA's own float functions are
 documented at 2 ulp (sinf, cosf, expf) and 1 ulp (logf).  Here a strided sweep over
@@ -18,7 +18,7 @@ import pytest
 
 import oracle
 
-BOUND = {"sin": 1.55, "cos": 1.55, "exp": 0.94, "log": 0.92}
+BOUND = {"sin": 1.55, "cos": 1.55, "exp": 0.94, "log": 0.88}
 
 
 def f32_bits(x):
