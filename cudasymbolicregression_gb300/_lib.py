@@ -35,6 +35,7 @@ class FitOptions(ctypes.Structure):
         ("points_per_lane", i32),
         ("grid_blocks", i32),
         ("max_operators", i32),
+        ("max_live", i32),
     ]
 
 
@@ -83,6 +84,7 @@ _SIGS = {
     "sr_eval_backward_multi_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp, vp, vp,
                                     vp], ctypes.c_int),
     "sr_fit_workspace_bytes": ([i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions)], i64),
+    "sr_tape_live_rows": ([vp, vp, i64, i64, vp, vp], ctypes.c_int),
     "sr_fit_launch_shape": ([i64, i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions), vp], ctypes.c_int),
     "sr_fit_screen": ([vp, i64, i64, vp, vp, vp, i64, i64, vp, i64, i64, i64, i64, vp, i32, i32,
                        ctypes.POINTER(FitOptions), vp, vp], ctypes.c_int),

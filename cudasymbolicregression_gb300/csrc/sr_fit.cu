@@ -63,6 +63,7 @@ struct FitArgs {
   double tol, eps;
   int Lmax, Kmax;
   int Imax;         // rows of the per-warp node tables: largest count of operator nodes
+  int Amax;         // rows of the per-warp adjoint tables: most operator-node adjoints live at once
   int VR;           // rows of the per-warp table for variables (distinct variables of a tape)
   float* ws_vec;    // per CTA: 2 * hist * SPL*32 floats (s and y rings), when not in shared memory
   double* ws_scal;  // per CTA: 2 * hist 8-byte words (alpha, rho of each pair, float pairs), likewise
@@ -92,6 +93,8 @@ struct WarpSmem {
   uint32_t* psb;     // [Lmax] operand 1 source word                             (CTA)
   uint32_t* pda;     // [Lmax] operand 0 adjoint destination (byte offset)        (CTA)
   uint32_t* pdb;     // [Lmax] operand 1 adjoint destination                      (CTA)
+  int* arow;         // [Lmax] adjoint row of each operator node (by liveness)    (CTA)
+  int* frees;        // [Lmax] free adjoint rows while they are assigned          (CTA)
   int* rowvar;       // [VR] variable held in each variable row                  (CTA)
   int* info;         // [8] operator nodes, root row, variable rows, root source, root destination (CTA)
   int* node_slot;    // [Lmax] slot of a LEARNABLE node / row of an operator node / row of a variable (CTA)
@@ -104,7 +107,7 @@ struct WarpSmem {
   unsigned char* wb; // this warp's table base (warp):
   float* bc;         //   [1 + Kmax + Lmax] broadcast values: 0, constants, fixed constants
   float* vals;       //   [Imax + VR][32V] operator-node values, then variable values
-  float* adj;        //   [Imax + 1][32V] operator-node adjoints, then a sink row
+  float* adj;        //   [Amax + 1][32V] live operator-node adjoints, then a sink row
   float* gl;         //   [Kmax][32V] per-lane, per-point gradient partial sums
 };
 
@@ -114,13 +117,14 @@ struct WarpLayout {
   uint32_t vals, adj, sink, gl, bytes;
 };
 
-__host__ __device__ __forceinline__ WarpLayout warp_layout(int Lmax, int Imax, int Kmax, int V, int VR) {
+__host__ __device__ __forceinline__ WarpLayout warp_layout(int Lmax, int Imax, int Amax, int Kmax, int V, int VR) {
   const uint32_t K = (uint32_t)(Kmax > 0 ? Kmax : 1), I = (uint32_t)(Imax > 0 ? Imax : 1);
+  const uint32_t Ar = (uint32_t)(Amax > 0 ? Amax : 1);
   const uint32_t RW = 32u * (uint32_t)V * 4u;  // bytes per row
   WarpLayout w;
   w.vals = (uint32_t)((4u * (1u + K + (uint32_t)Lmax) + 127u) & ~127u);
   w.adj = w.vals + (I + (uint32_t)VR) * RW;
-  w.sink = w.adj + I * RW;
+  w.sink = w.adj + Ar * RW;
   w.gl = w.sink + RW;
   w.bytes = w.gl + K * RW;
   return w;
@@ -128,17 +132,18 @@ __host__ __device__ __forceinline__ WarpLayout warp_layout(int Lmax, int Imax, i
 
 __host__ __device__ __forceinline__ size_t fit_shared_bytes(int Lmax, int Kmax, int W, int VR) {
   const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
-  return fit_align16((size_t)Lmax * 4) * 8 + fit_align16(K * 4) + fit_align16((size_t)W * K * 8) +
+  return fit_align16((size_t)Lmax * 4) * 9 + fit_align16(K * 4) + fit_align16((size_t)W * K * 8) +
          fit_align16((size_t)W * 8) + fit_align16((size_t)W * 4) + fit_align16((size_t)VR * 4) + 32 + 16 + 512 +
          128;  // + alignment of the warp tables
 }
 
-__host__ __device__ __forceinline__ size_t fit_cta_bytes(int Lmax, int Imax, int Kmax, int V, int W, int VR) {
-  return fit_shared_bytes(Lmax, Kmax, W, VR) + (size_t)W * warp_layout(Lmax, Imax, Kmax, V, VR).bytes;
+__host__ __device__ __forceinline__ size_t fit_cta_bytes(int Lmax, int Imax, int Amax, int Kmax, int V, int W,
+                                                         int VR) {
+  return fit_shared_bytes(Lmax, Kmax, W, VR) + (size_t)W * warp_layout(Lmax, Imax, Amax, Kmax, V, VR).bytes;
 }
 
-__device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Imax, int Kmax, int V, int W, int VR,
-                                          int warp) {
+__device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Imax, int Amax, int Kmax, int V, int W,
+                                          int VR, int warp) {
   WarpSmem s;
   const size_t K = (size_t)(Kmax > 0 ? Kmax : 1);
   unsigned char* p = base;
@@ -168,11 +173,15 @@ __device__ __forceinline__ WarpSmem carve(unsigned char* base, int Lmax, int Ima
   p += fit_align16((size_t)Lmax * 4);
   s.pdb = reinterpret_cast<uint32_t*>(p);
   p += fit_align16((size_t)Lmax * 4);
+  s.arow = reinterpret_cast<int*>(p);
+  p += fit_align16((size_t)Lmax * 4);
+  s.frees = reinterpret_cast<int*>(p);
+  p += fit_align16((size_t)Lmax * 4);
   s.rowvar = reinterpret_cast<int*>(p);
   p += fit_align16((size_t)VR * 4);
   s.info = reinterpret_cast<int*>(p);
   p += 32;
-  const WarpLayout L = warp_layout(Lmax, Imax, Kmax, V, VR);
+  const WarpLayout L = warp_layout(Lmax, Imax, Amax, Kmax, V, VR);
   unsigned char* t = base + fit_shared_bytes(Lmax, Kmax, W, VR) - 128;
   t = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(t) + 127) & ~uintptr_t(127));
   s.wb = t + (size_t)warp * L.bytes;
@@ -371,12 +380,13 @@ __device__ __forceinline__ bool is_fixed_leaf(int code) { return code >= C1 && c
 
 // Source word and destination of operand node c (operator row / slot / variable row
 // numbers in node_slot).
-__device__ __forceinline__ void operand_words(const uint32_t* tape, const int* node_slot, int c, int Kmax, int Imax,
-                                              const WarpLayout& L, uint32_t RW, uint32_t& src, uint32_t& dst) {
+__device__ __forceinline__ void operand_words(const uint32_t* tape, const int* node_slot, const int* arow, int c,
+                                              int Kmax, int Imax, const WarpLayout& L, uint32_t RW, uint32_t& src,
+                                              uint32_t& dst) {
   const int code = code_of(tape[c]);
   if (is_operator_node(code)) {
     src = (L.vals + (uint32_t)node_slot[c] * RW) | (4u << 24);
-    dst = L.adj + (uint32_t)node_slot[c] * RW;
+    dst = L.adj + (uint32_t)arow[node_slot[c]] * RW;
   } else if (code == VAR) {
     src = (L.vals + (uint32_t)(Imax + node_slot[c]) * RW) | (4u << 24);
     dst = L.sink;
@@ -419,7 +429,7 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
   const float* __restrict__ Yrow = A.Y ? A.Y + b * N : nullptr;
   const bool xin = A.n_x <= kMaxRegVars;
   const int nI = S.info[0];              // operator nodes
-  const int root_row = S.info[1];        // the root's operator row, or -1 for a leaf root
+  const int root_row = S.info[1];        // the root's adjoint row, or -1 for a leaf root
   const int nvr = S.info[2];             // variable rows in use
   const uint32_t root_src = (uint32_t)S.info[3], root_dst = (uint32_t)S.info[4];
   const uint32_t sink = (uint32_t)S.info[5];  // adjoints of variables and fixed constants go nowhere
@@ -450,7 +460,7 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
     // ---- forward over the operator nodes ----
     uint32_t cn = nI > 0 ? S.pcode[0] : 0u, san = nI > 0 ? S.psa[0] : 0u, sbn = nI > 0 ? S.psb[0] : 0u;
     for (int i = 0; i < nI; ++i) {
-      const int code = (int)cn;
+      const int code = (int)(cn & 0xffu);
       const uint32_t sa = san, sb = sbn;
       if (i + 1 < nI) {
         cn = S.pcode[i + 1];
@@ -462,7 +472,6 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
         const int li = v * 32 + lane;
         const float r = op_value<float>(code, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li));
         S.vals[i * RW + li] = r;
-        if (kMode == kPassGrad) S.adj[i * RW + li] = 0.f;
       }
     }
     float fval[V];
@@ -505,7 +514,7 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
       }
       const int li = v * 32 + lane;
       if (root_row >= 0) {
-        S.adj[root_row * RW + li] = groot;  // the seed of the root (the forward wrote 0)
+        S.adj[root_row * RW + li] = groot;  // the seed of the root (its row holds 0)
       } else if (groot != 0.f) {
         float* d = row_ptr(wb, root_dst, li);  // a leaf root: its slot's row, or the sink
         *d = __fadd_rn(*d, groot);
@@ -517,7 +526,8 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
       cp = S.pcode[nI - 1]; sap = S.psa[nI - 1]; sbp = S.psb[nI - 1]; dap = S.pda[nI - 1]; dbp = S.pdb[nI - 1];
     }
     for (int i = nI - 1; i >= 0; --i) {
-      const int code = (int)cp;
+      const int code = (int)(cp & 0xffu);
+      const uint32_t arow = (cp >> 8) * RW;  // the node's adjoint row (float offset)
       const uint32_t sa = sap, sb = sbp, da = dap, db = dbp;
       if (i > 0) {
         cp = S.pcode[i - 1]; sap = S.psa[i - 1]; sbp = S.psb[i - 1]; dap = S.pda[i - 1]; dbp = S.pdb[i - 1];
@@ -525,7 +535,8 @@ __device__ __forceinline__ float tape_pass(const FitArgs& A, const WarpSmem& S, 
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         const int li = v * 32 + lane;
-        const float g = S.adj[i * RW + li];
+        const float g = S.adj[arow + li];
+        S.adj[arow + li] = 0.f;  // read once: the row is free for the nodes swept next
         bool a0, a1;
         float r0, r1;
         const int e = op_adjoint<float>(code, g, lds_src<V>(wb, sa, li), lds_src<V>(wb, sb, li), S.vals[i * RW + li],
@@ -680,11 +691,12 @@ __device__ __forceinline__ bool problem_fits(const FitArgs& A, int64_t b, int L,
 }
 
 // Stages problem b (a tape of L = root + 1 nodes) for the CTA: the tape, the numbering
-// of its constant slots, operator nodes and variables, the operator-node program
-// (warp 0), then every warp's broadcast entries (0 and the fixed constants).  Ends
-// with the tables visible to the CTA.
+// of its constant slots, operator nodes and variables, the adjoint rows by liveness,
+// the operator-node program (warp 0), then every warp's broadcast entries (0 and the
+// fixed constants) and zeroed adjoint rows.  Ends with the tables visible to the CTA;
+// false when the tape needs more live adjoint rows than the launch's max_live.
 template <int V>
-__device__ __forceinline__ void stage_problem(const FitArgs& A, const WarpSmem& S, int64_t b, int L, int lane,
+__device__ __forceinline__ bool stage_problem(const FitArgs& A, const WarpSmem& S, int64_t b, int L, int lane,
                                               int warp) {
   // stage the tape; number the constant slots, the operator nodes and the
   // variables; write the operator-node program (warp 0), visible to the CTA
@@ -721,9 +733,40 @@ __device__ __forceinline__ void stage_problem(const FitArgs& A, const WarpSmem& 
         S.node_slot[k] = r;
       }
       S.info[2] = nvr;
+      // adjoint rows by liveness: an operator node holds a row from the sweep of its
+      // first parent (the root from the start) to its own sweep, then frees it; rows
+      // are taken from a stack, so the assignment is the same in every run
+      int top = 0;
+      for (int r = A.Amax - 1; r >= 0; --r) S.frees[top++] = r;
+      for (int i = 0; i < nop; ++i) S.arow[i] = -1;
+      bool over = false;
+      const int R = L - 1;
+      if (is_operator_node(code_of(S.tape[R]))) {
+        if (top > 0) S.arow[S.node_slot[R]] = S.frees[--top];
+        else over = true;
+      }
+      for (int k = R; k >= 0 && !over; --k) {
+        const uint32_t d = S.tape[k];
+        const int code = code_of(d);
+        if (!is_operator_node(code)) continue;
+        const int i = S.node_slot[k];
+        if (S.arow[i] < 0) {  // no parent: a zero row for the length of its own sweep
+          if (top == 0) { over = true; break; }
+          S.arow[i] = S.frees[--top];
+        }
+        S.frees[top++] = S.arow[i];
+        const int ar = arity_of(code);
+        for (int j = 0; j < ar && !over; ++j) {
+          const int c = j == 0 ? child0(d) : child1(d);
+          if (!is_operator_node(code_of(S.tape[c])) || S.arow[S.node_slot[c]] >= 0) continue;
+          if (top == 0) { over = true; break; }
+          S.arow[S.node_slot[c]] = S.frees[--top];
+        }
+      }
+      S.info[6] = over ? 1 : 0;
     }
     __syncwarp();
-    const WarpLayout WL = warp_layout(A.Lmax, A.Imax, A.Kmax, V, A.VR);
+    const WarpLayout WL = warp_layout(A.Lmax, A.Imax, A.Amax, A.Kmax, V, A.VR);
     const uint32_t RWB = 32u * V * 4u;
     for (int k = lane; k < L; k += 32) {
       const uint32_t d = S.tape[k];
@@ -731,10 +774,10 @@ __device__ __forceinline__ void stage_problem(const FitArgs& A, const WarpSmem& 
       if (!is_operator_node(code)) continue;
       const int ar = arity_of(code);
       uint32_t sa = 0u, sb = 0u, da = WL.sink, db = WL.sink;
-      if (ar >= 1) operand_words(S.tape, S.node_slot, child0(d), A.Kmax, A.Imax, WL, RWB, sa, da);
-      if (ar == 2) operand_words(S.tape, S.node_slot, child1(d), A.Kmax, A.Imax, WL, RWB, sb, db);
+      if (ar >= 1) operand_words(S.tape, S.node_slot, S.arow, child0(d), A.Kmax, A.Imax, WL, RWB, sa, da);
+      if (ar == 2) operand_words(S.tape, S.node_slot, S.arow, child1(d), A.Kmax, A.Imax, WL, RWB, sb, db);
       const int row = S.node_slot[k];
-      S.pcode[row] = (uint32_t)dense_op(code);
+      S.pcode[row] = (uint32_t)dense_op(code) | ((uint32_t)S.arow[row] << 8);  // opcode | adjoint row
       S.psa[row] = sa;
       S.psb[row] = sb;
       S.pda[row] = da;
@@ -743,22 +786,28 @@ __device__ __forceinline__ void stage_problem(const FitArgs& A, const WarpSmem& 
     if (lane == 0) {
       const int R = (L - 1);
       uint32_t rs, rdst;
-      operand_words(S.tape, S.node_slot, R, A.Kmax, A.Imax, WL, RWB, rs, rdst);
+      operand_words(S.tape, S.node_slot, S.arow, R, A.Kmax, A.Imax, WL, RWB, rs, rdst);
       S.info[0] = nop;
-      S.info[1] = is_operator_node(code_of(S.tape[R])) ? S.node_slot[R] : -1;
+      S.info[1] = is_operator_node(code_of(S.tape[R])) ? S.arow[S.node_slot[R]] : -1;  // the root's adjoint row
       S.info[3] = (int)rs;
       S.info[4] = (int)rdst;
       S.info[5] = (int)WL.sink;
     }
   }
   __syncthreads();
+  const bool rows_suffice = S.info[6] == 0;  // written by warp 0 before the barrier
   // this warp's broadcast entries: 0 and the fixed constants of the tape
   if (lane == 0) S.bc[0] = 0.f;
   for (int k = lane; k < L; k += 32) {
     const int code = code_of(S.tape[k]);
     if (is_fixed_leaf(code)) S.bc[1 + A.Kmax + k] = node_value<float>(code, 0.f, 0.f, 0.f, 0.f);
   }
+  // this warp's adjoint rows start at zero; every sweep leaves them so (a node's row is
+  // reset when the node reads it)
+  for (int r = 0; r < A.Amax; ++r)
+    for (int v = 0; v < V; ++v) S.adj[r * 32 * V + v * 32 + lane] = 0.f;
   __syncwarp();
+  return rows_suffice;
 }
 
 // Line-search phases of the per-problem state machine.  Every loop turn of the
@@ -775,7 +824,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
   const float tolf = __double2float_rn(A.tol);
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
-  const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, A.VR, warp);
+  const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Amax, A.Kmax, V, W, A.VR, warp);
   // history rings and two-loop scalars of this CTA (used by warp 0)
   float* ringS = A.ring_off ? reinterpret_cast<float*>(smem + A.ring_off)
                             : A.ws_vec + (int64_t)blockIdx.x * 2 * A.hist * SPL * 32;
@@ -802,7 +851,8 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
     P.has_virtual = A.M > P.K;
     P.nslots = P.K + (P.has_virtual ? 1 : 0);
     const int L = P.root + 1;
-    if (!problem_fits(A, P.b, L, P.K, lane)) {  // a caller's max_len / max_consts too small
+    // a caller's max_len / max_consts / max_operators / max_live too small: not fitted
+    if (!problem_fits(A, P.b, L, P.K, lane) || !stage_problem<V>(A, S, P.b, L, lane, warp)) {
       if (warp == 0) {
         const float qnan = __int_as_float(0x7fffffff);
         for (int64_t k = lane; k < A.M; k += 32) A.C_out[P.b * A.c_sb + k * A.c_sm] = A.C_init[P.b * A.c_sb + k * A.c_sm];
@@ -817,8 +867,6 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
       }
       continue;
     }
-
-    stage_problem<V>(A, S, P.b, L, lane, warp);
 
     const float* Cin = A.C_init + P.b * A.c_sb;
     Slots<SPL> x, g, p, xn;
@@ -1175,18 +1223,19 @@ __global__ void __launch_bounds__(256, 2) fit_screen_kernel(FitArgs A, const flo
                                                             int64_t K, float* __restrict__ loss_out) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
-  const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Kmax, V, W, A.VR, warp);
+  const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Amax, A.Kmax, V, W, A.VR, warp);
   for (int64_t b = blockIdx.x; b < A.B; b += gridDim.x) {
     const int L = A.meta[b * 4 + 1] + 1;
     const int Kc = A.meta[b * 4 + 2];
-    if (!problem_fits(A, b, L, Kc, lane)) {  // a caller's max_len / max_consts too small
+    // a caller's max_len / max_consts / max_operators / max_live too small
+    if (!problem_fits(A, b, L, Kc, lane) || !stage_problem<V>(A, S, b, L, lane, warp)) {
       if (threadIdx.x == 0) {
         report(A.status, kStatusTapeExceedsLaunch);
         for (int64_t k = 0; k < K; ++k) loss_out[b * K + k] = __int_as_float(0x7fffffff);
       }
+      __syncthreads();  // the next problem's staging overwrites the tables
       continue;
     }
-    stage_problem<V>(A, S, b, L, lane, warp);
     for (int64_t k = 0; k < K; ++k) {
       const float* Cin = C_sets + k * c_sk + b * A.c_sb;
       for (int j = lane; j < Kc; j += 32) S.bc[1 + j] = Cin[(int64_t)S.slot_node[j] * A.c_sm];
@@ -1205,6 +1254,49 @@ __global__ void __launch_bounds__(256, 2) fit_screen_kernel(FitArgs A, const flo
   }
 }
 
+// Rows the fit's liveness assignment needs per tape (the same events as in
+// stage_problem: a row is taken at the first parent's sweep, or at the node's own
+// sweep when it has no parent, and freed after the node's sweep), the batch's largest
+// into stats[5].  One warp per tape, lane 0 walks the tape; tapes longer than 128
+// nodes to the root count all their operator nodes (a bound).
+__global__ void __launch_bounds__(256) tape_live_kernel(const uint32_t* __restrict__ desc,
+                                                        const int32_t* __restrict__ meta, int64_t B, int64_t M,
+                                                        int32_t* __restrict__ stats) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  int best = 0;
+  for (int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < B; b += warps) {
+    if (lane != 0) continue;
+    const int L = meta[b * 4 + 1] + 1;
+    const uint32_t* d = desc + b * M;
+    int live = 0;
+    if (L > 128) {
+      for (int k = 0; k < L; ++k) live += is_operator_node(code_of(d[k])) ? 1 : 0;
+    } else {
+      uint64_t held[2] = {0ull, 0ull};
+      auto has = [&](int k) { return (held[k >> 6] >> (k & 63)) & 1ull; };
+      auto take = [&](int k, int& cur) { held[k >> 6] |= 1ull << (k & 63); ++cur; live = cur > live ? cur : live; };
+      int cur = 0;
+      const int R = L - 1;
+      if (is_operator_node(code_of(d[R]))) take(R, cur);
+      for (int k = R; k >= 0; --k) {
+        const uint32_t w = d[k];
+        const int code = code_of(w);
+        if (!is_operator_node(code)) continue;
+        if (!has(k)) take(k, cur);
+        --cur;
+        const int ar = arity_of(code);
+        for (int j = 0; j < ar; ++j) {
+          const int c = j == 0 ? child0(w) : child1(w);
+          if (is_operator_node(code_of(d[c])) && !has(c)) take(c, cur);
+        }
+      }
+    }
+    best = live > best ? live : best;
+  }
+  if (lane == 0 && best > 0) atomicMax(stats + 5, best);
+}
+
 static int fit_defaults(const sr_fit_options* o, sr_fit_options& r) {
   r.max_iter = 100;
   r.history_size = 10;
@@ -1217,9 +1309,10 @@ static int fit_defaults(const sr_fit_options* o, sr_fit_options& r) {
   r.points_per_lane = 0;
   r.grid_blocks = 0;
   r.max_operators = 0;
+  r.max_live = 0;
   if (o) r = *o;
   if (r.max_iter < 0 || r.history_size < 1 || r.line_search < 0 || r.line_search > 1 || r.line_search_max_iter < 0 ||
-      r.objective < 0 || r.objective > 1) {
+      r.objective < 0 || r.objective > 1 || r.max_operators < 0 || r.max_live < 0) {
     set_error("invalid fit options");
     return SR_ERR_INVALID_ARGUMENT;
   }
@@ -1238,7 +1331,7 @@ static int spl_for(int Kmax) {
 }
 
 struct FitShape {
-  int V, SPL, warps, blocks, Imax, VR;
+  int V, SPL, warps, blocks, Imax, Amax, VR;
   size_t smem;
   size_t ring_off;  // > 0: the history rings sit in shared memory from this byte offset
 };
@@ -1280,6 +1373,10 @@ static void* pick_kernel(int V, int SPL) {
 static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, const sr_fit_options& o, FitShape& sh) {
   const int Imax = (o.max_operators > 0 && o.max_operators < Lmax) ? o.max_operators : Lmax;
   sh.Imax = Imax;
+  // adjoint rows: the most operator-node adjoints live at once (rows are assigned by
+  // liveness), at most one per operator node
+  const int Amax = (o.max_live > 0 && o.max_live < Imax) ? o.max_live : Imax;
+  sh.Amax = Amax;
   sh.VR = (int)(n_x < 1 ? 1 : (n_x < Lmax ? n_x : Lmax));
   sh.SPL = spl_for(Kmax);
   if (!sh.SPL) {
@@ -1311,7 +1408,7 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
         set_error("fit kernel shared memory attribute failed");
         return SR_ERR_CUDA;
       }
-      const size_t cb = fit_cta_bytes(Lmax, Imax, Kmax, V, w, sh.VR);
+      const size_t cb = fit_cta_bytes(Lmax, Imax, Amax, Kmax, V, w, sh.VR);
       if (cb > (size_t)optin) continue;
       int per_sm = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, w * 32, cb) != cudaSuccess || per_sm < 1)
@@ -1332,7 +1429,7 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
   }
   sh.V = bestV;
   sh.warps = W;
-  sh.smem = fit_cta_bytes(Lmax, Imax, Kmax, bestV, W, sh.VR);
+  sh.smem = fit_cta_bytes(Lmax, Imax, Amax, Kmax, bestV, W, sh.VR);
   // Warp 0's two-loop recursion reads the history at every step: keep it in shared
   // memory when that costs no resident CTA, else in the workspace.
   sh.ring_off = 0;
@@ -1382,6 +1479,17 @@ int64_t sr_fit_workspace_bytes(int64_t B, int64_t N, int64_t M, int32_t max_len,
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)(M < 1 ? 1 : M);
   if (sr::fit_shape(B, N, 1, Lmax, max_consts, o, sh)) return -1;
   return sr::ws_bytes_for(sh, o.history_size, true);
+}
+
+int sr_tape_live_rows(const uint32_t* desc, const int32_t* meta, int64_t B, int64_t M, int32_t* stats, void* stream) {
+  if (B < 0 || M < 0) { sr::set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
+  if (M > sr::kMaxNodes) { sr::set_error("tapes longer than %d nodes are not supported", sr::kMaxNodes); return SR_ERR_UNSUPPORTED; }
+  if (B == 0 || M == 0) return SR_OK;
+  if (!desc || !meta || !stats) { sr::set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
+  int64_t blocks = (B + 7) / 8;
+  if (blocks > 65535) blocks = 65535;
+  sr::tape_live_kernel<<<(unsigned)blocks, 256, 0, sr::as_stream(stream)>>>(desc, meta, B, M, stats);
+  return sr::launch_check("tape_live_kernel");
 }
 
 int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t max_len, int32_t max_consts,
@@ -1435,7 +1543,7 @@ int sr_fit_screen(const float* X, int64_t N, int64_t n_x, const float* Y, const 
   A.desc = desc; A.meta = meta; A.B = B; A.M = M;
   A.c_sb = c_sb; A.c_sm = c_sm;
   A.objective = o.objective;
-  A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.VR = sh.VR;
+  A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.Amax = sh.Amax; A.VR = sh.VR;
   A.status = status;
   void* k = sh.V == 1 ? reinterpret_cast<void*>(fit_screen_kernel<1>)
                       : (sh.V == 2 ? reinterpret_cast<void*>(fit_screen_kernel<2>) : reinterpret_cast<void*>(fit_screen_kernel<4>));
@@ -1496,7 +1604,7 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   A.order = order;
   A.max_iter = o.max_iter; A.hist = o.history_size; A.ls_kind = o.line_search; A.ls_max = o.line_search_max_iter;
   A.objective = o.objective; A.tol = o.tolerance_grad; A.eps = o.eps;
-  A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.VR = sh.VR;
+  A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.Amax = sh.Amax; A.VR = sh.VR;
   A.counter = reinterpret_cast<int*>(ws);
   const int64_t vec = (int64_t)sh.blocks * 2LL * o.history_size * sh.SPL * 32 * (int64_t)sizeof(float);
   A.ws_vec = sh.ring_off ? nullptr : reinterpret_cast<float*>(ws + 256);

@@ -109,7 +109,7 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
     N, nx = X.shape
     if Y is not None:
         Y = _targets(Y, B, N, dev)
-    tapes = compile_tapes(Ops, Ch, nx)
+    tapes = compile_tapes(Ops, Ch, nx, live=True)
     Xc = X.contiguous()
     if autotune and warps_per_block == 0 and points_per_lane == 0:
         key = (N, nx, tapes.max_root, tapes.max_consts, line_search_fn, objective)
@@ -122,7 +122,8 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
                            line_search_max_iter=int(line_search_max_iter), eps=float(eps),
                            objective=int(objective), warps_per_block=int(warps_per_block),
                            points_per_lane=int(points_per_lane), grid_blocks=int(grid_blocks),
-                           max_operators=int(max(tapes.max_operators, 1)))
+                           max_operators=int(max(tapes.max_operators, 1)),
+                           max_live=int(tapes.max_live))
     L = _lib.lib()
     C_out = torch.empty((B, M), dtype=torch.float32, device=dev)
     Y_out = torch.empty((B, N), dtype=torch.float32, device=dev) if want_y else None
@@ -189,9 +190,10 @@ def screen_starts(X, Y, Ops, Ch, C_sets, *, objective: int = 0, tapes=None) -> t
     if Y is not None:
         Y = _targets(Y, B, N, dev)
     if tapes is None:
-        tapes = compile_tapes(Ops, Ch, nx)
+        tapes = compile_tapes(Ops, Ch, nx, live=True)
     opts = _lib.FitOptions(max_iter=0, history_size=1, tolerance_grad=0.0, line_search=0, line_search_max_iter=0,
-                           eps=0.0, objective=int(objective), max_operators=int(max(tapes.max_operators, 1)))
+                           eps=0.0, objective=int(objective), max_operators=int(max(tapes.max_operators, 1)),
+                           max_live=int(tapes.max_live))
     Cs = C_sets.to(torch.float32).contiguous()
     out = torch.empty((B, K), dtype=torch.float32, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -298,7 +300,7 @@ class FitPlan:
         self.B, self.M, self.N, self.nx = B, M, N, nx
         self.X = X.contiguous()
         self.Y = None if Y is None else _targets(Y, B, N, dev)
-        self.tapes = compile_tapes(Ops, Ch, nx)
+        self.tapes = compile_tapes(Ops, Ch, nx, live=True)
         self.order = torch.argsort(self.tapes.meta[:, 1] + 1, descending=True, stable=True).to(torch.int32)
         self.opts = _lib.FitOptions(max_iter=int(max_iter), history_size=int(history_size),
                                     tolerance_grad=float(tolerance_grad),
@@ -306,7 +308,8 @@ class FitPlan:
                                     line_search_max_iter=int(line_search_max_iter), eps=float(eps),
                                     objective=int(objective), warps_per_block=int(warps_per_block),
                                     points_per_lane=int(points_per_lane), grid_blocks=int(grid_blocks),
-                                    max_operators=int(max(self.tapes.max_operators, 1)))
+                                    max_operators=int(max(self.tapes.max_operators, 1)),
+                                    max_live=int(self.tapes.max_live))
         L = _lib.lib()
         self.max_len = min(max(self.tapes.max_root, 1), M)
         wsb = L.sr_fit_workspace_bytes(B, N, M, self.max_len, self.tapes.max_consts, self.opts)

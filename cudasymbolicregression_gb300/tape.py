@@ -26,6 +26,7 @@ class CompiledTapes:
     max_root: int       # largest root + 1
     max_consts: int     # largest number of constants up to the root
     max_operators: int  # largest number of operator nodes (arity >= 1 or NO_OP) up to the root
+    max_live: int = 0   # most operator-node adjoints live at once in a reverse sweep (0: not measured)
     _order: torch.Tensor | None = None
 
     @property
@@ -36,8 +37,11 @@ class CompiledTapes:
         return self._order
 
 
-def compile_tapes(ops_bm: torch.Tensor, ch_bm: torch.Tensor, n_vars: int, validate_only: bool = False):
-    """Validate (and stage) tapes given as (B, M) / (B, M, 2) int64 CUDA views.
+def compile_tapes(ops_bm: torch.Tensor, ch_bm: torch.Tensor, n_vars: int, validate_only: bool = False,
+                  live: bool = False):
+    """Validate (and stage) tapes given as (B, M) / (B, M, 2) int64 CUDA views; live
+    also measures the fit kernel's live adjoint rows (``sr_tape_live_rows``), read with
+    the same single host synchronisation.
 
     Raises RuntimeError("Error during input validation: ...") on an invalid tape.
     """
@@ -60,8 +64,10 @@ def compile_tapes(ops_bm: torch.Tensor, ch_bm: torch.Tensor, n_vars: int, valida
     rc = L.sr_tape_compile(_lib.ptr(ops_bm), _lib.ptr(ch_bm), B, M, sb, sm, cb, cm, ci, int(n_vars),
                            _lib.ptr(desc), _lib.ptr(meta), _lib.ptr(stats), st)
     _lib.check(rc, "sr_tape_compile")
+    if live:
+        _lib.check(L.sr_tape_live_rows(_lib.ptr(desc), _lib.ptr(meta), B, M, _lib.ptr(stats), st), "sr_tape_live_rows")
     s = stats.tolist()
     if s[0]:
         raise RuntimeError(error_message(s[0], "input validation"))
     return CompiledTapes(desc=desc, meta=meta, B=B, M=M, max_len=s[1], max_root=s[2], max_consts=s[3],
-                         max_operators=s[4])
+                         max_operators=s[4], max_live=s[5] if live else 0)

@@ -139,7 +139,20 @@ typedef struct sr_fit_options {
   int32_t max_operators;        /* largest number of operator nodes (arity >= 1 or NO_OP) up to a
                                    root, stats[4] of sr_tape_compile; sizes the node tables
                                    (0 = max_len) */
+  int32_t max_live;             /* largest number of operator-node adjoints live at once in a
+                                   reverse sweep, stats[5] after sr_tape_live_rows; sizes the
+                                   adjoint tables (0 = max_operators) */
 } sr_fit_options;
+
+/* The fit kernel keeps the adjoint of an operator node in a table row only from the
+ * moment its first parent is swept until the node itself is: rows are assigned by
+ * liveness.  This writes into stats_dev[5] (atomic max) the largest number of rows a
+ * tape of the batch needs (exact for tapes of up to 128 nodes to the root, else its
+ * operator-node count, a bound), to be passed as sr_fit_options.max_live.  desc_dev
+ * and meta_dev as written by sr_tape_compile.  No counterpart in the reference.
+ * Returns 0 or an error code. */
+int sr_tape_live_rows(const uint32_t *desc_dev, const int32_t *meta_dev, int64_t B, int64_t M, int32_t *stats_dev,
+                      void *stream);
 
 /*
  * Evaluation with K constant sets per tape (the reference's

@@ -124,6 +124,10 @@ def test_fit_option_checks(L):
                                  None), SR_ERR_INVALID_ARGUMENT, "status")
     _rejected(L, L.sr_fit_lbfgs(None, 16, 1, None, None, None, 8, 32, None, None, 32, 1, None, None, None, None, None,
                                 -1, 4, None, None, 0, ctypes.byref(st), None), SR_ERR_INVALID_ARGUMENT, "negative")
+    _rejected(L, L.sr_tape_live_rows(None, None, -1, 32, None, None), SR_ERR_INVALID_ARGUMENT, "negative")
+    _rejected(L, L.sr_tape_live_rows(None, None, 4, MAX_NODES + 1, None, None), SR_ERR_UNSUPPORTED)
+    _rejected(L, L.sr_tape_live_rows(None, None, 4, 32, None, None), SR_ERR_INVALID_ARGUMENT, "null pointer")
+    assert L.sr_tape_live_rows(None, None, 0, 32, None, None) == 0
     shape = (ctypes.c_int32 * 3)()
     _rejected(L, L.sr_fit_launch_shape(8, 16, 1, 32, 4, 4, None, None), SR_ERR_INVALID_ARGUMENT, "shape")
     _rejected(L, L.sr_fit_launch_shape(-8, 16, 1, 32, 4, 4, None, ctypes.cast(shape, ctypes.c_void_p)),

@@ -429,3 +429,87 @@ def test_tape_longer_than_the_launch_is_reported_not_fitted(golden):
         assert (itn[~over] != -_lib.TAPE_EXCEEDS_LAUNCH).all()
         np.testing.assert_array_equal(Cout.cpu().numpy()[over], g["C"][over])
         assert np.isnan(loss.cpu().numpy()[over]).all()
+
+
+def _live_rows(ops, ch):
+    """Restatement of the fit kernel's liveness assignment count for one tape: a row is
+    taken at the first parent's sweep (the root's from the start, a node without a
+    parent at its own sweep) and freed after the node's own sweep."""
+    root = max(int((ops != 0).sum()) - 1, 0)
+    isop = lambda k: ops[k] == 0 or 10 <= ops[k] <= 31 or 40 <= ops[k] <= 44  # noqa: E731
+    held, cur, best = set(), 0, 0
+    if isop(root):
+        held.add(root)
+        cur = best = 1
+    for k in range(root, -1, -1):
+        if not isop(k):
+            continue
+        if k not in held:
+            held.add(k)
+            cur += 1
+            best = max(best, cur)
+        cur -= 1
+        ar = 1 if 10 <= ops[k] <= 31 else (2 if 40 <= ops[k] <= 44 else 0)
+        for c in ch[k][:ar]:
+            if isop(c) and c not in held:
+                held.add(c)
+                cur += 1
+                best = max(best, cur)
+    return best
+
+
+def test_live_adjoint_rows_and_their_limit():
+    """sr_tape_live_rows counts the rows the fit's liveness assignment needs (here
+    against a restatement, with a shared child and an operator node no root uses); the
+    fit gives the same bits with rows for every operator node (max_live = 0) as with
+    the counted number, and with one row too few the tapes that need them all report
+    602 while every other problem is fitted as before."""
+    import ctypes
+    from cudasymbolicregression_gb300 import _lib, tapes
+    from cudasymbolicregression_gb300.tape import compile_tapes
+    rng = np.random.default_rng(12)
+    B, M, N = 300, 40, 70
+    X = rng.uniform(-2, 2, (N, 2)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    tb = tapes.generate(B, M, seed=13, lengths=rng.integers(1, M + 1, size=B), const_counts=rng.integers(0, 5, size=B),
+                        n_vars=2, X_screen=X, C_screen=C)
+    ops, ch = tb.ops.copy(), tb.ch.copy()
+    # tape 0: C, sin(C) (no parent: the root does not use it), C, cos(2), cos(3) * cos(3) (a shared child)
+    ops[0] = 0
+    ch[0] = -1
+    ops[0, :6] = [1, 10, 1, 11, 11, 42]
+    ch[0, 1, 0], ch[0, 3, 0], ch[0, 4, 0] = 0, 2, 3
+    ch[0, 5] = (4, 4)
+    Y = rng.standard_normal((B, N)).astype(np.float32)
+    X_, Y_, O_, Ch_, C_ = (cuda(a) for a in (X, Y, ops, ch, C))
+    tp = compile_tapes(O_, Ch_, 2, live=True)
+    want = [_live_rows(ops[b], ch[b]) for b in range(B)]
+    assert tp.max_live == max(want)
+    L = _lib.lib()
+
+    def fit(max_live):
+        o = _lib.FitOptions(max_iter=30, history_size=10, tolerance_grad=1e-7, line_search=0, line_search_max_iter=10,
+                            eps=1e-10, max_operators=tp.max_operators, max_live=max_live)
+        wsb = L.sr_fit_workspace_bytes(B, N, M, tp.max_root, tp.max_consts, ctypes.byref(o))
+        ws = torch.empty(int(wsb), dtype=torch.uint8, device="cuda")
+        Co, Yf = torch.empty(B, M, device="cuda"), torch.empty(B, N, device="cuda")
+        it, ls, ev = (torch.empty(B, dtype=torch.int32, device="cuda"), torch.empty(B, device="cuda"),
+                      torch.empty(B, dtype=torch.int32, device="cuda"))
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _lib.check(L.sr_fit_lbfgs(_lib.ptr(X_), N, 2, _lib.ptr(Y_), _lib.ptr(tp.desc), _lib.ptr(tp.meta), B, M,
+                                  _lib.ptr(C_), _lib.ptr(Co), M, 1, _lib.ptr(Yf), _lib.ptr(it), _lib.ptr(ls), _lib.ptr(ev),
+                                  None, tp.max_root, tp.max_consts, ctypes.byref(o), _lib.ptr(ws), ws.numel(),
+                                  _lib.ptr(st), _lib.stream_ptr(X_.device)), "sr_fit_lbfgs")
+        torch.cuda.synchronize()
+        return [t.cpu().numpy() for t in (Co, Yf, it, ls, ev, st)]
+
+    every = fit(0)
+    counted = fit(tp.max_live)
+    for a, b in zip(every[:5], counted[:5]):
+        np.testing.assert_array_equal(np.nan_to_num(a, nan=7.0), np.nan_to_num(b, nan=7.0))
+    short = fit(tp.max_live - 1)
+    over = np.array(want) > tp.max_live - 1
+    assert over.any() and (~over).any() and short[5][0] == _lib.TAPE_EXCEEDS_LAUNCH
+    assert (short[2][over] == -_lib.TAPE_EXCEEDS_LAUNCH).all()
+    for a, b in zip(short[:5], counted[:5]):
+        np.testing.assert_array_equal(np.nan_to_num(a[~over], nan=7.0), np.nan_to_num(b[~over], nan=7.0))
