@@ -34,8 +34,8 @@ def sources():
 
 
 def _deps():
-    return sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + [os.path.join(ROOT, "include", "sr_gb300.h"),
-                                                                    os.path.abspath(__file__)]
+    return sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + [
+        os.path.join(ROOT, "include", "sr_gb300.h"), os.path.abspath(__file__)]
 
 
 def up_to_date() -> bool:

@@ -10,10 +10,11 @@
 //               is summed per lane in float, over the lanes by a butterfly and over
 //               the warps in a fixed order, so results are bit-reproducible run to
 //               run and the same in every warp.
-//   direction   two-loop recursion over the last `history_size` (s, y) pairs held in
-//               warp 0's slice of the workspace, broadcast to the CTA through shared
-//               memory; dots, rho, alpha, beta, gamma as normalised float pairs
-//               (Dekker), vectors in float (one slot per lane).
+//   direction   H g over the last `history_size` (s, y) pairs by warp 0, broadcast to
+//               the CTA through shared memory: the compact representation (R^-1 and
+//               Y^T Y kept up to date as pairs arrive, one lane per pair) for histories
+//               of at most 32 pairs, the two-loop recursion for longer ones; scalars as
+//               normalised float pairs (Dekker), vectors in float (one slot per lane).
 //   line search strong Wolfe (bracket + bisection zoom) or Armijo backtracking, with
 //               the reference's acceptance rules and float32 scalar arithmetic.
 //
@@ -65,9 +66,8 @@ struct FitArgs {
   int Imax;         // rows of the per-warp node tables: largest count of operator nodes
   int Amax;         // rows of the per-warp adjoint tables: most operator-node adjoints live at once
   int VR;           // rows of the per-warp table for variables (distinct variables of a tape)
-  float* ws_vec;    // per CTA: 2 * hist * SPL*32 floats (s and y rings), when not in shared memory
-  double* ws_scal;  // per CTA: 2 * hist 8-byte words (alpha, rho of each pair, float pairs), likewise
-  int ring_off;     // > 0: the rings and scalars sit in shared memory at this byte offset
+  unsigned char* ws_hist;  // per CTA: the L-BFGS history block (hist_block_bytes), when not in shared memory
+  int ring_off;            // > 0: the history block sits in shared memory at this byte offset
   int* counter;
   int32_t* status;
 };
@@ -203,7 +203,7 @@ __device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
 // The total of a float pair (see F2).
 __device__ __forceinline__ float f2_val(F2 a) { return isfinite(a.hi) ? __fadd_rn(a.hi, a.lo) : a.hi; }
 
-// Normalised float pairs for the two-loop recursion (Dekker's double-float
+// Normalised float pairs for the search direction (Dekker's double-float
 // arithmetic on the FP32 pipe, about 44 significant bits): hi is the rounded value,
 // lo the remainder.  f2_norm turns a cascaded sum (see F2) into one (TwoSum of its
 // parts); products use FMA for the exact product of the high parts.
@@ -307,8 +307,8 @@ __device__ __forceinline__ F2 dot_pair(const Problem<SPL>& P, const Slots<SPL>& 
 // Dot product of two slot vectors with float-pair accumulation (TwoProduct by
 // FMA, then pair sums: Ogita, Rump and Oishi's Dot2), as accurate as a dot in twice
 // the precision on the FP32 pipe, rounded to float.  Used for the line-search slope
-// g.p and the gradient norm; the curvature dots of the two-loop recursion are kept as
-// normalised pairs (dot_pair).
+// g.p and the gradient norm; the curvature dots of the direction are kept as
+// normalised pairs (dot_pair, f2_madf).
 template <int SPL>
 __device__ __forceinline__ float dot_f2(const Problem<SPL>& P, const Slots<SPL>& a, const Slots<SPL>& b) {
   F2 acc{0.f, 0.f};
@@ -341,6 +341,268 @@ __device__ __forceinline__ Slots<SPL> axpy(const Slots<SPL>& x, float a, const S
 // reference's tensor arithmetic does.
 __device__ __forceinline__ float armijo(float phi0, float c, float a, float dphi0) {
   return __fadd_rn(phi0, __fmul_rn(__fmul_rn(c, a), dphi0));
+}
+
+// ---- L-BFGS history of one CTA ----
+//
+// Rings of the s and y vectors (hist rows of SPL*32 + 1 floats: the odd row stride
+// keeps a lane per row free of bank conflicts), then float-pair words: alpha and rho
+// per pair (two-loop recursion), and for histories of at most 32 pairs the compact
+// representation's per-pair curvature c = s.y + eps and two hist x MS matrices (MS odd)
+// indexed by ring slot: R^-1 (upper triangular in the age order) and Y^T Y.
+__host__ __device__ __forceinline__ int hist_ring_stride(int SPL) { return SPL * 32 + 1; }
+__host__ __device__ __forceinline__ bool hist_compact(int hist) { return hist <= 32; }
+__host__ __device__ __forceinline__ int hist_mat_stride(int hist) { return hist | 1; }
+__host__ __device__ __forceinline__ size_t hist_vec_bytes(int hist, int SPL) {
+  return fit_align16((size_t)2 * hist * hist_ring_stride(SPL) * sizeof(float));
+}
+__host__ __device__ __forceinline__ size_t hist_block_bytes(int hist, int SPL) {
+  const size_t words = (size_t)2 * hist + (hist_compact(hist) ? (size_t)hist + 2 * (size_t)hist * hist_mat_stride(hist) : 0);
+  return hist_vec_bytes(hist, SPL) + fit_align16(words * 8);
+}
+
+struct History {
+  float* S;       // [hist][RS]
+  float* Y;       // [hist][RS]
+  float2* alph;   // [hist] alpha of the current direction, by position (two-loop)
+  float2* rho;    // [hist] 1 / c, by slot
+  float2* c;      // [hist] s.y + eps, by slot (compact)
+  float2* Rinv;   // [hist][MS] (compact)
+  float2* YY;     // [hist][MS] (compact)
+  int hist, RS, MS;
+  bool compact;
+};
+
+template <int SPL>
+__device__ __forceinline__ History history_at(unsigned char* base, int hist) {
+  History H;
+  H.hist = hist;
+  H.RS = hist_ring_stride(SPL);
+  H.MS = hist_mat_stride(hist);
+  H.compact = hist_compact(hist);
+  H.S = reinterpret_cast<float*>(base);
+  H.Y = H.S + (size_t)hist * H.RS;
+  H.alph = reinterpret_cast<float2*>(base + hist_vec_bytes(hist, SPL));
+  H.rho = H.alph + hist;
+  H.c = H.rho + hist;
+  H.Rinv = H.c + hist;
+  H.YY = H.Rinv + (size_t)hist * H.MS;
+  return H;
+}
+
+// Ring slot of position j (j < hist) for the oldest pair at head (head < hist).
+__device__ __forceinline__ int ring_slot(int head, int j, int hist) {
+  const int s = head + j;
+  return s >= hist ? s - hist : s;
+}
+
+__device__ __forceinline__ F2 ld2(const float2* p) {
+  const float2 v = *p;
+  return F2{v.x, v.y};
+}
+__device__ __forceinline__ void st2(float2* p, F2 v) { *p = make_float2(v.hi, v.lo); }
+__device__ __forceinline__ F2 shfl2(F2 v, int src) {
+  return F2{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+// acc + a * b for float pairs: the exact product of the high parts (FMA) plus the
+// cross terms, added as a cascaded pair sum (normalise the total with f2_norm).
+__device__ __forceinline__ F2 f2_mad(F2 acc, F2 a, F2 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return f2_add(acc, F2{p, e});
+}
+
+// acc + a * b for floats (TwoProduct by FMA), as a cascaded pair sum.
+__device__ __forceinline__ F2 f2_madf(F2 acc, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return f2_add(acc, F2{p, __fmaf_rn(a, b, -p)});
+}
+
+// Compact representation of the L-BFGS inverse Hessian (Byrd, Nocedal and Schnabel,
+// "Representations of quasi-Newton matrices and their use in limited memory methods",
+// Math. Programming 63, 1994): with the pairs (s_i, y_i) oldest first, R upper
+// triangular with R_ij = s_i.y_j (i < j) and R_ii = c_i = s_i.y_i + eps, C = diag(c),
+// gamma = s.y / (y.y + eps) of the newest pair,
+//   H g = gamma g + S z - gamma Y t,   t = R^-1 S^T g,   z = R^-T (C t + gamma Y^T Y t - gamma Y^T g),
+// which equals the two-loop recursion with rho_i = 1 / c_i.  R^-1 is kept instead of R:
+// appending a pair adds the column -R^-1 r / c_new (r_i = s_i.y_new), and dropping the
+// oldest pair keeps the trailing block, which is the inverse of R's trailing block.  Lane i
+// of warp 0 works on the pair at position i, so every dot and every product with R^-1 or
+// Y^T Y is a chain of float-pair multiply-adds on one lane, without cross-lane reductions;
+// the vector is formed per slot in float.  Positions j < h, ring slot (head + j) % hist.
+
+// The sums below run over blocks of 4 terms: the block's shared-memory loads and
+// shuffles are issued first, then its 4 multiply-adds in order, masked by selects (no
+// branch), so that the latencies of the loads overlap; the order of the terms, and so the
+// result, is that of one sequential sum.
+
+// Appends the newest pair (already in its ring slot, at position h - 1): its dots with
+// every pair in the ring, c and rho of the new pair, its row and column of Y^T Y and its
+// column of R^-1.  Returns s.y and y.y of the new pair in *sy, *yy (every lane).
+template <int SPL>
+__device__ __forceinline__ void compact_push(const History& H, int head, int h, int slot, int nslots, F2 eps2,
+                                             int lane, F2* sy, F2* yy) {
+  __syncwarp();
+  const bool mine = lane < h;
+  const int sl = mine ? ring_slot(head, lane, H.hist) : 0;
+  const float* si = H.S + (size_t)sl * H.RS;
+  const float* yi = H.Y + (size_t)sl * H.RS;
+  const float* yn = H.Y + (size_t)slot * H.RS;
+  F2 r{0.f, 0.f}, q{0.f, 0.f};
+  for (int j0 = 0; j0 < nslots; j0 += 4) {
+    float a[4], b[4], c[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int j = min(j0 + k, nslots - 1);
+      a[k] = si[j];
+      b[k] = yi[j];
+      c[k] = yn[j];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const F2 nr = f2_madf(r, a[k], c[k]), nq = f2_madf(q, b[k], c[k]);
+      const bool ok = j0 + k < nslots;
+      r = ok ? nr : r;
+      q = ok ? nq : q;
+    }
+  }
+  r = f2_norm(r);
+  q = f2_norm(q);
+  *sy = shfl2(r, h - 1);
+  *yy = shfl2(q, h - 1);
+  const F2 cn = f2_norm(f2_add(*sy, eps2));
+  const F2 rho = f2_div(F2{1.f, 0.f}, cn);
+  F2 acc{0.f, 0.f};
+  const float2* rrow = H.Rinv + (size_t)sl * H.MS;
+  for (int j0 = 0; j0 < h - 1; j0 += 4) {
+    F2 rj[4], m[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int j = min(j0 + k, h - 2);
+      rj[k] = shfl2(r, j);
+      m[k] = ld2(rrow + ring_slot(head, j, H.hist));
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const F2 n = f2_mad(acc, m[k], rj[k]);
+      acc = (lane <= j0 + k && j0 + k < h - 1) ? n : acc;
+    }
+  }
+  if (mine) {
+    st2(H.YY + (size_t)sl * H.MS + slot, q);
+    st2(H.YY + (size_t)slot * H.MS + sl, q);
+    const F2 col = f2_mul(rho, f2_norm(acc));
+    st2(H.Rinv + (size_t)sl * H.MS + slot, lane == h - 1 ? rho : F2{-col.hi, -col.lo});
+  }
+  if (lane == 0) {
+    st2(H.rho + slot, rho);
+    st2(H.c + slot, cn);
+  }
+  __syncwarp();
+}
+
+// Lane i (mine): sum over the positions j < h (kUpper: j >= i, kLower: j <= i) of
+// M(i, j) x_j, x_j from lane j; M(i, j) at base + slot(j) * stride.
+template <bool kUpper, bool kLower>
+__device__ __forceinline__ F2 compact_matvec(const float2* base, int stride, int head, int h, int hist, F2 x,
+                                             bool mine, int lane) {
+  F2 acc{0.f, 0.f};
+  for (int j0 = 0; j0 < h; j0 += 4) {
+    F2 xj[4], m[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int j = min(j0 + k, h - 1);
+      xj[k] = shfl2(x, j);
+      m[k] = ld2(base + (size_t)ring_slot(head, j, hist) * stride);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int j = j0 + k;
+      const F2 n = f2_mad(acc, m[k], xj[k]);
+      acc = (mine && j < h && (!kUpper || lane <= j) && (!kLower || j <= lane)) ? n : acc;
+    }
+  }
+  return f2_norm(acc);
+}
+
+// q = H g by the compact representation (h >= 1 pairs), every slot of every lane.
+template <int SPL>
+__device__ __forceinline__ void compact_direction(const History& H, int head, int h, int nslots, F2 gam,
+                                                  const Slots<SPL>& g, Slots<SPL>& q, int lane) {
+  const bool mine = lane < h;
+  const int sl = mine ? ring_slot(head, lane, H.hist) : 0;
+  const float* si = H.S + (size_t)sl * H.RS;
+  const float* yi = H.Y + (size_t)sl * H.RS;
+  // u_i = s_i.g and w_i = y_i.g
+  F2 u{0.f, 0.f}, w{0.f, 0.f};
+#pragma unroll
+  for (int s = 0; s < SPL; ++s) {
+    const int top = min(32, nslots - s * 32);
+    for (int l0 = 0; l0 < top; l0 += 4) {
+      float gj[4], a[4], b[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int l = min(l0 + k, top - 1);
+        gj[k] = __shfl_sync(0xffffffffu, g.v[s], l);
+        a[k] = si[s * 32 + l];
+        b[k] = yi[s * 32 + l];
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const F2 nu = f2_madf(u, a[k], gj[k]), nw = f2_madf(w, b[k], gj[k]);
+        const bool ok = l0 + k < top;
+        u = ok ? nu : u;
+        w = ok ? nw : w;
+      }
+    }
+  }
+  u = f2_norm(u);
+  w = f2_norm(w);
+  // t = R^-1 u (positions j >= i), Y^T Y t, v = c t + gamma (Y^T Y t - w), z = R^-T v (j <= i)
+  const F2 t = compact_matvec<true, false>(H.Rinv + (size_t)sl * H.MS, 1, head, h, H.hist, u, mine, lane);
+  const F2 yt = compact_matvec<false, false>(H.YY + (size_t)sl * H.MS, 1, head, h, H.hist, t, mine, lane);
+  const F2 v = f2_norm(f2_add(f2_mul(ld2(H.c + sl), t), f2_mul(gam, f2_sub(yt, w))));
+  const F2 z = compact_matvec<false, true>(H.Rinv + sl, H.MS, head, h, H.hist, v, mine, lane);
+  const F2 b = f2_mul(gam, t);
+  // q = gamma g + sum_i z_i s_i - sum_i (gamma t_i) y_i, per slot in float
+  Slots<SPL> qs, qy;
+#pragma unroll
+  for (int s = 0; s < SPL; ++s) {
+    qs.v[s] = __fmaf_rn(g.v[s], gam.lo, __fmul_rn(g.v[s], gam.hi));
+    qy.v[s] = 0.f;
+  }
+  for (int i0 = 0; i0 < h; i0 += 4) {
+    F2 zi[4], bi[4];
+    float sv[4][SPL], yv[4][SPL];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = min(i0 + k, h - 1);
+      zi[k] = shfl2(z, i);
+      bi[k] = shfl2(b, i);
+      const int sli = ring_slot(head, i, H.hist);
+#pragma unroll
+      for (int s = 0; s < SPL; ++s) {
+        sv[k][s] = H.S[(size_t)sli * H.RS + s * 32 + lane];
+        yv[k][s] = H.Y[(size_t)sli * H.RS + s * 32 + lane];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool ok = i0 + k < h;
+#pragma unroll
+      for (int s = 0; s < SPL; ++s) {
+        const float ns = __fmaf_rn(zi[k].lo, sv[k][s], __fmaf_rn(zi[k].hi, sv[k][s], qs.v[s]));
+        const float ny = __fmaf_rn(bi[k].lo, yv[k][s], __fmaf_rn(bi[k].hi, yv[k][s], qy.v[s]));
+        qs.v[s] = ok ? ns : qs.v[s];
+        qy.v[s] = ok ? ny : qy.v[s];
+      }
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < SPL; ++s) q.v[s] = __fsub_rn(qs.v[s], qy.v[s]);
 }
 
 constexpr int kMaxRegVars = 4;  // X rows of up to this many variables are held in registers
@@ -825,15 +1087,9 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const WarpSmem S = carve(smem, A.Lmax, A.Imax, A.Amax, A.Kmax, V, W, A.VR, warp);
-  // history rings and two-loop scalars of this CTA (used by warp 0)
-  float* ringS = A.ring_off ? reinterpret_cast<float*>(smem + A.ring_off)
-                            : A.ws_vec + (int64_t)blockIdx.x * 2 * A.hist * SPL * 32;
-  float* ringY = ringS + (int64_t)A.hist * SPL * 32;
-  // per history pair: alpha of the current direction and rho = 1 / (s.y + eps), each a
-  // normalised float pair in one 8-byte word
-  float2* alph = A.ring_off ? reinterpret_cast<float2*>(ringY + (int64_t)A.hist * SPL * 32)
-                            : reinterpret_cast<float2*>(A.ws_scal + (int64_t)blockIdx.x * 2 * A.hist);
-  float2* rhos = alph + A.hist;
+  // the L-BFGS history of this CTA (used by warp 0)
+  const History H = history_at<SPL>(
+      A.ring_off ? smem + A.ring_off : A.ws_hist + (int64_t)blockIdx.x * (int64_t)hist_block_bytes(A.hist, SPL), A.hist);
   const float c1 = 1e-4f, c2 = 0.9f, amax = 20.0f;
 
   while (true) {
@@ -1065,15 +1321,16 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
 #pragma unroll
           for (int s = 0; s < SPL; ++s) {
             yv.v[s] = P.active(s) ? __fsub_rn(nxt.g.v[s], g.v[s]) : 0.f;
-            ringS[slot * SPL * 32 + s * 32 + lane] = sv.v[s];
-            ringY[slot * SPL * 32 + s * 32 + lane] = yv.v[s];
+            H.S[(size_t)slot * H.RS + s * 32 + lane] = sv.v[s];
+            H.Y[(size_t)slot * H.RS + s * 32 + lane] = yv.v[s];
           }
-          // curvature of the new pair, computed once: rho of its slot, and s.y, y.y for gamma
-          last_sy = dot_pair(P, yv, sv);
-          last_yy = dot_pair(P, yv, yv);
-          if (lane == 0) {
-            const F2 r = f2_div(F2{1.f, 0.f}, f2_norm(f2_add(last_sy, eps2)));
-            rhos[slot] = make_float2(r.hi, r.lo);
+          if (H.compact) {
+            compact_push<SPL>(H, head, h, slot, P.nslots, eps2, lane, &last_sy, &last_yy);
+          } else {
+            // curvature of the new pair, computed once: rho of its slot, and s.y, y.y for gamma
+            last_sy = dot_pair(P, yv, sv);
+            last_yy = dot_pair(P, yv, yv);
+            if (lane == 0) st2(H.rho + slot, f2_div(F2{1.f, 0.f}, f2_norm(f2_add(last_sy, eps2))));
           }
         }
         __syncwarp();
@@ -1100,45 +1357,45 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
         if (it >= A.max_iter || __fsqrt_rn(dot_f2(P, g, g)) < tolf) {
           phase = PH_DONE;
         } else {
-          // two-loop recursion (lbfgs_batch.py:65-103), by warp 0 for the CTA
+          // direction q = H g (lbfgs_batch.py:65-103), by warp 0 for the CTA
           Slots<SPL> q = g;
           if (warp == 0 && h > 0) {
-            for (int i = h - 1; i >= 0; --i) {
-              const int sl = (head + i) % A.hist;
-              Slots<SPL> si, yi;
+            const F2 gam = f2_div(last_sy, f2_norm(f2_add(last_yy, eps2)));
+            if (H.compact) {
+              compact_direction<SPL>(H, head, h, P.nslots, gam, g, q, lane);
+            } else {
+              // two-loop recursion for long histories
+              for (int i = h - 1; i >= 0; --i) {
+                const int sl = (head + i) % A.hist;
+                Slots<SPL> si, yi;
 #pragma unroll
-              for (int s = 0; s < SPL; ++s) {
-                si.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
-                yi.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
+                for (int s = 0; s < SPL; ++s) {
+                  si.v[s] = H.S[(size_t)sl * H.RS + s * 32 + lane];
+                  yi.v[s] = H.Y[(size_t)sl * H.RS + s * 32 + lane];
+                }
+                // alpha = rho (s.q) and q -= alpha y: float pairs on the FP32 pipe (GB300's
+                // FP64 pipe runs a warp instruction at a small fraction of the FP32 rate)
+                const F2 a = f2_mul(ld2(H.rho + sl), dot_pair(P, si, q));
+#pragma unroll
+                for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(-a.lo, yi.v[s], __fmaf_rn(-a.hi, yi.v[s], q.v[s]));
+                if (lane == 0) st2(H.alph + i, a);
               }
-              // alpha = rho (s.q) and q -= alpha y: float pairs on the FP32 pipe (GB300's
-              // FP64 pipe runs a warp instruction at a small fraction of the FP32 rate)
-              const float2 r2 = rhos[sl];
-              const F2 a = f2_mul(F2{r2.x, r2.y}, dot_pair(P, si, q));
-#pragma unroll
-              for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(-a.lo, yi.v[s], __fmaf_rn(-a.hi, yi.v[s], q.v[s]));
-              if (lane == 0) alph[i] = make_float2(a.hi, a.lo);
-            }
-            __syncwarp();
-            {
-              const F2 gam = f2_div(last_sy, f2_norm(f2_add(last_yy, eps2)));
+              __syncwarp();
 #pragma unroll
               for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(q.v[s], gam.lo, __fmul_rn(q.v[s], gam.hi));
-            }
-            for (int i = 0; i < h; ++i) {
-              const int sl = (head + i) % A.hist;
-              Slots<SPL> si, yi;
+              for (int i = 0; i < h; ++i) {
+                const int sl = (head + i) % A.hist;
+                Slots<SPL> si, yi;
 #pragma unroll
-              for (int s = 0; s < SPL; ++s) {
-                si.v[s] = ringS[sl * SPL * 32 + s * 32 + lane];
-                yi.v[s] = ringY[sl * SPL * 32 + s * 32 + lane];
+                for (int s = 0; s < SPL; ++s) {
+                  si.v[s] = H.S[(size_t)sl * H.RS + s * 32 + lane];
+                  yi.v[s] = H.Y[(size_t)sl * H.RS + s * 32 + lane];
+                }
+                const F2 be = f2_mul(ld2(H.rho + sl), dot_pair(P, yi, q));
+                const F2 coef = f2_sub(ld2(H.alph + i), be);
+#pragma unroll
+                for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(coef.lo, si.v[s], __fmaf_rn(coef.hi, si.v[s], q.v[s]));
               }
-              const float2 r2 = rhos[sl];
-              const F2 be = f2_mul(F2{r2.x, r2.y}, dot_pair(P, yi, q));
-              const float2 al = alph[i];
-              const F2 coef = f2_sub(F2{al.x, al.y}, be);
-#pragma unroll
-              for (int s = 0; s < SPL; ++s) q.v[s] = __fmaf_rn(coef.lo, si.v[s], __fmaf_rn(coef.hi, si.v[s], q.v[s]));
             }
           }
           if (warp == 0) {
@@ -1333,13 +1590,9 @@ static int spl_for(int Kmax) {
 struct FitShape {
   int V, SPL, warps, blocks, Imax, Amax, VR;
   size_t smem;
-  size_t ring_off;  // > 0: the history rings sit in shared memory from this byte offset
+  size_t ring_off;  // > 0: the L-BFGS history sits in shared memory from this byte offset
 };
 
-// Bytes of one CTA's history rings and two-loop scalars.
-static size_t ring_bytes(int hist, int SPL) {
-  return fit_align16((size_t)2 * hist * SPL * 32 * sizeof(float)) + fit_align16((size_t)2 * hist * sizeof(double));
-}
 
 template <int V, int SPL>
 static void* fit_kernel_ptr() {
@@ -1430,11 +1683,11 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
   sh.V = bestV;
   sh.warps = W;
   sh.smem = fit_cta_bytes(Lmax, Imax, Amax, Kmax, bestV, W, sh.VR);
-  // Warp 0's two-loop recursion reads the history at every step: keep it in shared
-  // memory when that costs no resident CTA, else in the workspace.
+  // Warp 0 reads the L-BFGS history for every direction: keep it in shared memory
+  // when that costs no resident CTA, else in the workspace.
   sh.ring_off = 0;
   {
-    const size_t off = fit_align16(sh.smem), with = off + ring_bytes(o.history_size, sh.SPL);
+    const size_t off = fit_align16(sh.smem), with = off + hist_block_bytes(o.history_size, sh.SPL);
     int per_sm = 0;
     if (with <= (size_t)optin &&
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_kernel(bestV, sh.SPL), W * 32, with) ==
@@ -1451,13 +1704,11 @@ static int fit_shape(int64_t B, int64_t N, int64_t n_x, int Lmax, int Kmax, cons
   return SR_OK;
 }
 
-// Workspace of a launch: the work counter, and the history rings unless they sit in
-// shared memory (rings_anyway: the size with the rings, an upper bound for any n_x).
+// Workspace of a launch: the work counter, and the L-BFGS history unless it sits in
+// shared memory (rings_anyway: the size with the history, an upper bound for any n_x).
 static int64_t ws_bytes_for(const FitShape& sh, int hist, bool rings_anyway = false) {
   if (sh.ring_off && !rings_anyway) return 256;
-  const int64_t vec = (int64_t)sh.blocks * 2LL * hist * sh.SPL * 32 * (int64_t)sizeof(float);
-  const int64_t scal = (int64_t)sh.blocks * 2LL * hist * (int64_t)sizeof(double);
-  return 256 + fit_align16((size_t)vec) + fit_align16((size_t)scal);
+  return 256 + (int64_t)sh.blocks * (int64_t)hist_block_bytes(hist, sh.SPL);
 }
 
 }  // namespace sr
@@ -1606,9 +1857,7 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
   A.objective = o.objective; A.tol = o.tolerance_grad; A.eps = o.eps;
   A.Lmax = Lmax; A.Kmax = max_consts; A.Imax = sh.Imax; A.Amax = sh.Amax; A.VR = sh.VR;
   A.counter = reinterpret_cast<int*>(ws);
-  const int64_t vec = (int64_t)sh.blocks * 2LL * o.history_size * sh.SPL * 32 * (int64_t)sizeof(float);
-  A.ws_vec = sh.ring_off ? nullptr : reinterpret_cast<float*>(ws + 256);
-  A.ws_scal = sh.ring_off ? nullptr : reinterpret_cast<double*>(ws + 256 + fit_align16((size_t)vec));
+  A.ws_hist = sh.ring_off ? nullptr : ws + 256;
   A.ring_off = (int)sh.ring_off;
   A.status = status;
   rc = cuda_check(cudaMemsetAsync(ws, 0, 256, st), "work counter reset");
@@ -1628,7 +1877,7 @@ int sr_fit_lbfgs(const float* X, int64_t N, int64_t n_x, const float* Y, const u
 // memory is owned entirely by its own pool allocator and which forbids any other
 // cudaMalloc (cudaMalloc synchronises the device and may fail under the pool's
 // budget), or a latency-bound service that must not allocate on its request path.
-// For them the fit's scratch (work counter, per-warp L-BFGS history rings) lives in
+// For them the fit's scratch (work counter, per-CTA L-BFGS history) lives in
 // a file-scope device array of fixed size instead of a caller buffer.
 // ---------------------------------------------------------------------------------
 namespace sr {
@@ -1665,7 +1914,7 @@ extern "C" int sr_fit_lbfgs_static_scratch(const float* X, int64_t N, int64_t n_
                                             iters_out, loss_out, evals_out, order, max_len, max_consts, &o, nullptr,
                                             0, status, stream);
   // Persistent grid: fewer CTAs only lengthen the work queue per warp, so shrink the
-  // grid until its history rings fit in the static array.
+  // grid until its L-BFGS history fits in the static array.
   FitShape sh;
   const int Lmax = (max_len > 0 && max_len < M) ? max_len : (int)M;
   rc = fit_shape(B, N, n_x, Lmax, max_consts, o, sh);

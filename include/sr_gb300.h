@@ -213,8 +213,8 @@ int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t ma
 /*
  * Fused batched L-BFGS fit of the learnable constants of every tape: one
  * persistent kernel in which each CTA owns one problem at a time (its warps split
- * the data points) and runs the whole optimisation (closure = forward + adjoint over all N points, two-loop
- * recursion, strong-Wolfe or backtracking line search, history update) on chip.
+ * the data points) and runs the whole optimisation (closure = forward + adjoint over all N points, the
+ * L-BFGS direction, strong-Wolfe or backtracking line search, history update) on chip.
  * Follows optimize() and LBFGS_batch per problem (reference
  * symbolic_torch/optimization.py:9-112, symbolic_torch/lbfgs_batch.py:61-326).
  * C_init/C_out (B, M) use (c_sb, c_sm) strides; Y and Y_final (B, N) are
@@ -242,7 +242,7 @@ int sr_fit_lbfgs(const float *X_dev, int64_t N, int64_t n_x, const float *Y_dev,
  * for callers that cannot allocate device memory for this library (a host whose
  * device memory is all owned by its own pool and forbids other cudaMalloc calls,
  * or a service that must not allocate on its request path).  The scratch (work
- * counter and L-BFGS history rings) is a fixed 16 MiB device array inside the
+ * counter and the L-BFGS history of each CTA) is a fixed 16 MiB device array inside the
  * library, present on every device that loads it until the process exits.  The
  * persistent grid is shrunk until its history fits; when even one CTA does not fit
  * (very large history_size) the call fails with SR_ERR_WORKSPACE.  Every call looks

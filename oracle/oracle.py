@@ -209,8 +209,9 @@ def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_gra
     the fused kernel's (double dots and two-loop scalars, where the kernel uses
     float pairs); dot_mode=2 is the fused kernel's arithmetic exactly for a launch
     shape of `warps` warps per problem and `points_per_lane` points per lane (its
-    per-lane sums, lane and warp reduction order, float-pair dots and two-loop
-    scalars, slot vectors and closure count; slot_registers defaults to the batch's
+    per-lane sums, lane and warp reduction order, float-pair dots, its direction --
+    the compact representation up to 32 pairs of history, the two-loop recursion
+    beyond -- slot vectors and closure count; slot_registers defaults to the batch's
     own, as the kernel derives it).
     Returns dict(C, Y, iters, evals, loss, err); iters[b] = -code for a problem
     whose closures raised an error.  Y=None selects the raw

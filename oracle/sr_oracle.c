@@ -374,8 +374,10 @@ void sro_node_fwd_kf32(int64_t n, const int64_t *op, const float *a, const float
  * dot_mode 2 is the fused kernel's arithmetic exactly (see "the fused kernel's
  * arithmetic" below): its slot vectors (the real constants and one virtual slot
  * for all other slots), its per-lane point sums and lane/warp reduction order for a
- * given launch shape, its float-pair (Sum2/Dot2, Dekker) dots and two-loop scalars,
- * and the closures it evaluates (it reuses points the reference evaluates twice).
+ * given launch shape, its float-pair (Sum2/Dot2, Dekker) dots and direction (the
+ * compact representation of the inverse Hessian for histories of at most 32 pairs,
+ * the two-loop recursion for longer ones, both with float-pair scalars), and the
+ * closures it evaluates (it reuses points the reference evaluates twice).
  * Its sin, cos, exp and log are the kernels' own (sr_fmath.h), so on tapes over
  * the IEEE-exact operators (+ - * /, square, sqrt, neg, inv, cube, fourth, fifth)
  * and sin, cos, exp, log this mode and the kernel give the same bits; the other
@@ -594,6 +596,8 @@ typedef struct {
     int hist, h, head;
     float *ringS, *ringY;           /* (hist, D) */
     f2_t *rho, *alph;               /* (hist) rho per ring slot, alpha per position */
+    int compact;                    /* hist <= 32: the compact representation (else the two-loop) */
+    f2_t *cd, *Rinv, *YY;           /* (hist), (hist, hist), (hist, hist): c = s.y + eps, R^-1, Y^T Y by slot */
     f2_t last_sy, last_yy, eps2;
     int poison;
 } kern_t;
@@ -799,12 +803,119 @@ static f2_t kdot_pair(const kern_t *k, const float *a, const float *b)
     return f2_norm(acc[0]);
 }
 
-/* The kernel's two-loop recursion over its history ring (oldest pair at `head`). */
+/* acc + a b for float pairs and for floats, as cascaded pair sums (the kernel's f2_mad
+ * and f2_madf). */
+static f2_t f2_mad(f2_t acc, f2_t a, f2_t b)
+{
+    float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return f2_add(acc, f2_mk(p, e));
+}
+
+static f2_t f2_madf(f2_t acc, float a, float b)
+{
+    float p = a * b;
+    return f2_add(acc, f2_mk(p, fmaf(a, b, -p)));
+}
+
+/* The kernel's compact_push (sr_fit.cu): the newest pair, in ring slot `slot` at
+ * position h - 1, gets its dots with every pair (one sequential float-pair sum over
+ * the slots per pair), c and rho, its row and column of Y^T Y and its column of R^-1
+ * (-rho times R^-1 r over the older pairs; rho on the diagonal).  The dropped pair's
+ * slot is the new one, so what R^-1 keeps of the others is the inverse of R's trailing
+ * block (Byrd, Nocedal and Schnabel 1994). */
+static void kpush_compact(kern_t *k, int slot)
+{
+    const int h = k->h, hs = k->hist, D = k->D, head = k->head;
+    const float *yn = k->ringY + (int64_t)slot * D;
+    f2_t r[32], q[32];
+    for (int i = 0; i < h; ++i) {
+        int sl = (head + i) % hs;
+        const float *si = k->ringS + (int64_t)sl * D, *yi = k->ringY + (int64_t)sl * D;
+        f2_t a = f2_mk(0.0f, 0.0f), b = f2_mk(0.0f, 0.0f);
+        for (int j = 0; j < k->nslots; ++j) {
+            a = f2_madf(a, si[j], yn[j]);
+            b = f2_madf(b, yi[j], yn[j]);
+        }
+        r[i] = f2_norm(a);
+        q[i] = f2_norm(b);
+    }
+    k->last_sy = r[h - 1];
+    k->last_yy = q[h - 1];
+    f2_t cn = f2_norm(f2_add(k->last_sy, k->eps2));
+    f2_t rho = f2_div(f2_mk(1.0f, 0.0f), cn);
+    for (int i = 0; i < h; ++i) {
+        int sl = (head + i) % hs;
+        f2_t acc = f2_mk(0.0f, 0.0f);
+        for (int j = i; j < h - 1; ++j) acc = f2_mad(acc, k->Rinv[sl * hs + (head + j) % hs], r[j]);
+        k->YY[sl * hs + slot] = q[i];
+        k->YY[slot * hs + sl] = q[i];
+        f2_t col = f2_mul(rho, f2_norm(acc));
+        k->Rinv[sl * hs + slot] = i == h - 1 ? rho : f2_mk(-col.hi, -col.lo);
+    }
+    k->rho[slot] = rho;
+    k->cd[slot] = cn;
+}
+
+/* The kernel's compact_direction: q = gamma g + S z - gamma Y t with u = S^T g,
+ * w = Y^T g, t = R^-1 u, v = c t + gamma (Y^T Y t - w), z = R^-T v; each entry of u, w,
+ * t, v, z one sequential float-pair sum, the vector formed per slot in float. */
+static void kdirection_compact(kern_t *k, const float *g, float *q)
+{
+    const int h = k->h, hs = k->hist, D = k->D, head = k->head;
+    f2_t u[32], w[32], t[32], z[32], bb[32], v[32];
+    int sl[32];
+    for (int i = 0; i < h; ++i) {
+        sl[i] = (head + i) % hs;
+        const float *si = k->ringS + (int64_t)sl[i] * D, *yi = k->ringY + (int64_t)sl[i] * D;
+        f2_t a = f2_mk(0.0f, 0.0f), b = f2_mk(0.0f, 0.0f);
+        for (int j = 0; j < k->nslots; ++j) {
+            a = f2_madf(a, si[j], g[j]);
+            b = f2_madf(b, yi[j], g[j]);
+        }
+        u[i] = f2_norm(a);
+        w[i] = f2_norm(b);
+    }
+    for (int i = 0; i < h; ++i) {
+        f2_t acc = f2_mk(0.0f, 0.0f);
+        for (int j = i; j < h; ++j) acc = f2_mad(acc, k->Rinv[sl[i] * hs + sl[j]], u[j]);
+        t[i] = f2_norm(acc);
+    }
+    f2_t gam = f2_div(k->last_sy, f2_norm(f2_add(k->last_yy, k->eps2)));
+    for (int i = 0; i < h; ++i) {
+        f2_t acc = f2_mk(0.0f, 0.0f);
+        for (int j = 0; j < h; ++j) acc = f2_mad(acc, k->YY[sl[i] * hs + sl[j]], t[j]);
+        f2_t yt = f2_norm(acc);
+        v[i] = f2_norm(f2_add(f2_mul(k->cd[sl[i]], t[i]), f2_mul(gam, f2_sub(yt, w[i]))));
+    }
+    for (int i = 0; i < h; ++i) {
+        f2_t acc = f2_mk(0.0f, 0.0f);
+        for (int j = 0; j <= i; ++j) acc = f2_mad(acc, k->Rinv[sl[j] * hs + sl[i]], v[j]);
+        z[i] = f2_norm(acc);
+        bb[i] = f2_mul(gam, t[i]);
+    }
+    for (int j = 0; j < D; ++j) {
+        float qs = fmaf(g[j], gam.lo, g[j] * gam.hi), qy = 0.0f;
+        for (int i = 0; i < h; ++i) {
+            float sv = k->ringS[(int64_t)sl[i] * D + j], yv = k->ringY[(int64_t)sl[i] * D + j];
+            qs = fmaf(z[i].lo, sv, fmaf(z[i].hi, sv, qs));
+            qy = fmaf(bb[i].lo, yv, fmaf(bb[i].hi, yv, qy));
+        }
+        q[j] = qs - qy;
+    }
+}
+
+/* The kernel's direction over its history ring (oldest pair at `head`): the compact
+ * representation for histories of at most 32 pairs, else the two-loop recursion. */
 static void kdirection(kern_t *k, const float *g, float *q, float *p)
 {
     const int D = k->D;
     for (int j = 0; j < D; ++j) q[j] = g[j];
-    if (k->h > 0) {
+    if (k->h > 0 && k->compact) {
+        kdirection_compact(k, g, q);
+    } else if (k->h > 0) {
         for (int i = k->h - 1; i >= 0; --i) {
             int sl = (k->head + i) % k->hist;
             const float *si = k->ringS + (int64_t)sl * D, *yi = k->ringY + (int64_t)sl * D;
@@ -1105,9 +1216,13 @@ static void fit_problem_kernel(problem_t *P, fit_t *F, const float *C_init, int 
         for (int j = 0; j < D; ++j) yv[j] = j < k->nslots ? gn[j] - g[j] : 0.0f;
         memcpy(k->ringS + (int64_t)slot * D, sv, vb);
         memcpy(k->ringY + (int64_t)slot * D, yv, vb);
-        k->last_sy = kdot_pair(k, yv, sv);
-        k->last_yy = kdot_pair(k, yv, yv);
-        k->rho[slot] = f2_div(f2_mk(1.0f, 0.0f), f2_norm(f2_add(k->last_sy, k->eps2)));
+        if (k->compact) {
+            kpush_compact(k, slot);
+        } else {
+            k->last_sy = kdot_pair(k, yv, sv);
+            k->last_yy = kdot_pair(k, yv, yv);
+            k->rho[slot] = f2_div(f2_mk(1.0f, 0.0f), f2_norm(f2_add(k->last_sy, k->eps2)));
+        }
         memcpy(g, gn, vb);
         f = fn;
         ++it;
@@ -1182,6 +1297,10 @@ int sro_optimize_shape_f32(const float *X, int64_t N, int64_t nx, const float *Y
             K.ringY = calloc((size_t)history * K.D, sizeof(float));
             K.rho = calloc((size_t)history, sizeof(f2_t));
             K.alph = calloc((size_t)history, sizeof(f2_t));
+            K.compact = history <= 32;
+            K.cd = calloc((size_t)history, sizeof(f2_t));
+            K.Rinv = K.compact ? calloc((size_t)history * history, sizeof(f2_t)) : NULL;
+            K.YY = K.compact ? calloc((size_t)history * history, sizeof(f2_t)) : NULL;
             K.eps2 = f2_of_double(F.eps);
             F.k = &K; F.D = K.D;
             if (K.nslots <= K.D)
@@ -1191,6 +1310,7 @@ int sro_optimize_shape_f32(const float *X, int64_t N, int64_t nx, const float *Y
             for (int t = 0; t < 32 * K.W; ++t) if (K.lane_err[t] > P.err) P.err = K.lane_err[t];
             free(K.slot_of); free(K.slot_node); free(K.vals); free(K.adjs); free(K.gl); free(K.red_g);
             free(K.red_l); free(K.lane_err); free(K.ringS); free(K.ringY); free(K.rho); free(K.alph);
+            free(K.cd); free(K.Rinv); free(K.YY);
         } else {
             fit_problem_ref(&P, &F, C_init + b * M, max_iter, history, tol, ls_kind, ls_max, cout, &it, &f);
         }

@@ -4,7 +4,8 @@ The oracle's dot_mode 2 runs the reference's control flow (lbfgs_batch.py:61-326
 optimization.py:72-99, restated in oracle/sr_oracle.c and pinned against the
 reference's own fits by tests/test_oracle_golden.py) with the fused kernel's
 arithmetic: its per-lane point sums, lane and warp reduction order for a launch
-shape, float-pair dots and two-loop scalars, and slot vectors.  On tapes whose
+shape, float-pair dots, its direction (the compact representation for histories of
+at most 32 pairs, the two-loop recursion for longer ones), and slot vectors.  On tapes whose
 operators are IEEE-exact (+ - * /, square, neg) the kernel and this oracle must give
 the same bits for every problem: constants, root values, loss, iterations and
 closure counts, at 200 iterations, for every launch shape.  A state-machine
@@ -110,18 +111,22 @@ def test_bit_identical_point_counts(N):
         assert_bit_identical(r, o, f"N={N} V={ppl} W={wpb}")
 
 
-def test_bit_identical_history_wraps_and_many_constants():
-    """A short history ring (3 pairs, wrapping every few iterations) and tapes with up to
-    40 constants (two slot registers per lane), both line searches."""
+@pytest.mark.parametrize("history", [3, 32, 40])
+def test_bit_identical_history_wraps_and_many_constants(history):
+    """History rings that wrap (3 pairs: every few iterations; 32: the most pairs of the
+    compact representation, one lane each; 40: the two-loop recursion) and tapes with
+    up to 40 constants (two slot registers per lane), both line searches."""
     sr = _sr()
     X, Y, ops, ch, C = exact_batch(64, 96, 64, seed=41, max_consts=40, min_len=60)
     assert oracle.kernel_slot_registers(ops) == 2
     for ls in ("strong_wolfe", "backtracking"):
-        r = sr.optimize_ex(cuda(X), cuda(Y), cuda(ops), cuda(ch), cuda(C), max_iter=150, history_size=3,
+        r = sr.optimize_ex(cuda(X), cuda(Y), cuda(ops), cuda(ch), cuda(C), max_iter=150, history_size=history,
                            line_search_fn=ls, points_per_lane=1, warps_per_block=2, raise_errors=False)
-        o = oracle.optimize(X, Y, ops, ch, C, max_iter=150, history_size=3, line_search_fn=ls, dot_mode=2,
+        o = oracle.optimize(X, Y, ops, ch, C, max_iter=150, history_size=history, line_search_fn=ls, dot_mode=2,
                             warps=2, points_per_lane=1)
-        assert_bit_identical(r, o, f"history 3, up to 40 constants, {ls}")
+        assert_bit_identical(r, o, f"history {history}, up to 40 constants, {ls}")
+        if history > 3:
+            assert r.iters.cpu().numpy().max() > history, "the ring never wrapped"
 
 
 def test_bit_identical_raw_objective_rosenbrock(golden):

@@ -44,6 +44,22 @@ def rel_close(a, b, rtol):
     return (r <= rtol) | (np.isnan(a) & np.isnan(b)) | (a == b)
 
 
+def assert_no_systematic_loss(m_dev, m_ref, diff):
+    """Paired quality check over the problems whose final MSEs differ (finite in both).
+    Two fits of one ill-conditioned problem that part by a rounding end in unrelated
+    local minima: the log ratio of their MSEs has a spread of several units, so a
+    fixed bound on its mean is noise at any affordable sample size.  Instead: the
+    device is worse on no more problems than a fair coin gives within two standard
+    deviations (sign test), and the mean log ratio lies within two standard errors of
+    zero or below it."""
+    if diff.sum() < 2:
+        return
+    lr = np.log(np.maximum(m_dev[diff], 1e-30) / np.maximum(m_ref[diff], 1e-30))
+    n = lr.size
+    assert (lr > 0).sum() <= n / 2 + np.sqrt(n) + 1, f"device worse on {(lr > 0).sum()} of {n}"
+    assert lr.mean() <= 2 * lr.std(ddof=1) / np.sqrt(n), f"mean log ratio {lr.mean():.3f} over {n}"
+
+
 def test_linear_known_answer(golden):
     """reference tests/test_optimization.py:10-80."""
     sr = _sr()
@@ -65,10 +81,10 @@ def test_linear_known_answer(golden):
 def test_matches_reference_golden(golden, name, ls, min_frac):
     """Final MSE against the reference's own fits: within 1e-4 relative on at least
     min_frac of the problems (the reference's own reruns reach 0.977 and 0.958 on the
-    first and last set and cannot run the second).  Quality, paired: among the
-    problems finite in both whose MSE differs by more than 1e-4, the geometric mean of
-    the ratio device / reference is at most 1.1 (no systematic loss), and the device
-    leaves at most 2 more problems non-finite than the reference."""
+    first and last set and cannot run the second).  Quality, paired over the problems
+    finite in both whose MSE differs by more than 1e-4: no systematic loss (sign test
+    and mean log ratio, assert_no_systematic_loss), and the device leaves at most 2
+    more problems non-finite than the reference."""
     sr = _sr()
     g = golden(name)
     r = sr.optimize_ex(cuda(g["X"]), cuda(g["Y"]), cuda(g["ops"]), cuda(g["ch"]), cuda(g["C"]),
@@ -80,14 +96,50 @@ def test_matches_reference_golden(golden, name, ls, min_frac):
     close = rel_close(m_gpu, m_ref, 1e-4)
     assert close[ok].mean() >= min_frac
     fin = ok & np.isfinite(m_gpu) & np.isfinite(m_ref)
-    diff = fin & ~close
-    if diff.any():
-        assert np.exp(np.mean(np.log(np.maximum(m_gpu[diff], 1e-30) / np.maximum(m_ref[diff], 1e-30)))) <= 1.1
+    assert_no_systematic_loss(m_gpu, m_ref, fin & ~close)
     assert (ok & ~np.isfinite(m_gpu) & np.isfinite(m_ref)).sum() <= (ok & np.isfinite(m_gpu) & ~np.isfinite(m_ref)).sum() + 2
     # NaN placement of the constants: NaN expressions end with every slot NaN
     nan_ref = np.isnan(g["C_final"]).all(1)
     nan_gpu = np.isnan(r.C.cpu().numpy()).all(1)
     assert (nan_ref == nan_gpu)[ok].mean() >= min_frac
+
+
+def _ragged_problems(seed, B, N=64, M=32):
+    """Problems of the fixture's kind (tests/golden/make_golden.py case_optimize_ragged):
+    ragged tapes of 3..M nodes with 0..8 constants over 2 variables, targets from hidden
+    random tapes plus noise, evaluated by the oracle."""
+    from cudasymbolicregression_gb300 import tapes
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-3, 3, (N, 2)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    tb = tapes.generate(B, M, seed=seed + 1, lengths=rng.integers(3, M + 1, size=B),
+                        const_counts=rng.integers(0, 9, size=B), n_vars=2, X_screen=X, C_screen=C)
+    hid = tapes.generate(B, M, seed=seed + 2, lengths=rng.integers(3, 16, size=B),
+                         const_counts=rng.integers(0, 4, size=B), n_vars=2, X_screen=X, C_screen=C)
+    yh = oracle.eval_fwd(X, hid.ops, hid.ch, rng.standard_normal((B, M)).astype(np.float32))
+    Y = yh[np.arange(B), np.maximum((hid.ops != 0).sum(1) - 1, 0)] + 0.01 * rng.standard_normal((B, N))
+    return X, np.where(np.isfinite(Y), Y, 0.0).astype(np.float32), tb.ops, tb.ch, C
+
+
+@pytest.mark.parametrize("ls,max_iter", [("strong_wolfe", 40), ("backtracking", 30)])
+def test_quality_against_reference_arithmetic_large_sample(ls, max_iter):
+    """2048 problems of the fixtures' kind, fitted by the device and by the oracle in
+    the reference's float32 arithmetic (pinned to the reference's own fits by
+    tests/test_oracle_golden.py): at least 90% within 1e-4 relative, no systematic loss
+    over the rest, and at most 1% more problems left non-finite."""
+    sr = _sr()
+    X, Y, ops, ch, C = _ragged_problems(11, 2048)
+    r = sr.optimize_ex(cuda(X), cuda(Y), cuda(ops), cuda(ch), cuda(C), max_iter=max_iter, line_search_fn=ls,
+                       raise_errors=False)
+    o = oracle.optimize(X, Y, ops, ch, C, max_iter=max_iter, line_search_fn=ls, dot_mode=0)
+    ok = (r.iters.cpu().numpy() >= 0) & (o["iters"] >= 0)
+    assert ok.mean() >= 0.97
+    with np.errstate(over="ignore"):
+        m_gpu, m_ref = mse(r.Y.cpu().numpy(), Y), mse(o["Y"], Y)
+    close = rel_close(m_gpu, m_ref, 1e-4)
+    assert close[ok].mean() >= 0.9
+    assert_no_systematic_loss(m_gpu, m_ref, ok & np.isfinite(m_gpu) & np.isfinite(m_ref) & ~close)
+    assert (ok & ~np.isfinite(m_gpu) & np.isfinite(m_ref)).sum() <= (ok & np.isfinite(m_gpu) & ~np.isfinite(m_ref)).sum() + 20
 
 
 @pytest.mark.parametrize("ls", ["strong_wolfe", "backtracking"])
