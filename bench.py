@@ -88,13 +88,13 @@ SAMPLE_METRIC = "expressions sampled from a grammar, parsed to postfix and linke
 # The fit kernel's traffic per problem is set by N, M and the history, not by the
 # operator set, so the warm-start line's held-out problems (same lengths, M and N)
 # scale the same B=4096 ragged capture.
-FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10579200 + 3840),
-                     ("warmstart", 65536, 512): 16 * (10579200 + 3840)}
+FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10744832 + 2560),
+                     ("warmstart", 65536, 512): 16 * (10744832 + 2560)}
 # Pipe and issue utilisation of the fit kernel (percent of peak, active cycles) from the
-# same capture, the kernel of commit 9a52c77 (profiles/fit_lbfgs_ragged_B16384_N512.txt):
+# same capture, the kernel of commit 2ddf7f6 (profiles/fit_lbfgs_ragged_B16384_N512.txt):
 # an interpreter whose instructions are mostly integer and control work.
-FIT_PROFILE = {"commit": "9a52c77", "issue_active_pct": 50.1, "fp32_pipe_pct": 13.9, "xu_pipe_pct": 1.75,
-               "alu_pipe_pct": 43.9, "lsu_pipe_pct": 23.4, "fp64_pipe_pct": 1.71, "warps_active_pct": 23.3,
+FIT_PROFILE = {"commit": "2ddf7f6", "issue_active_pct": 53.8, "fp32_pipe_pct": 14.7, "xu_pipe_pct": 1.74,
+               "alu_pipe_pct": 48.5, "lsu_pipe_pct": 25.3, "fp64_pipe_pct": 1.68, "warps_active_pct": 23.1,
                "capture": "ncu --set full, ragged B=4096, N=512"}
 # The adjoint call: its three length-class grids and the concurrent padding check.
 EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000),
