@@ -666,8 +666,9 @@ def run_eval(args, rank, world, local):
 
     def bwd_k():
         _lib.check(L.sr_eval_backward_f32(_lib.ptr(Xd), N, Xd.shape[1], _lib.ptr(tapes.desc), _lib.ptr(tapes.meta),
-                                          _lib.ptr(tapes.order), B, M, tapes.max_len, _lib.ptr(Cp), M, 1, _lib.ptr(G),
-                                          _lib.ptr(gCk), None, _lib.ptr(status), st), "sr_eval_backward_f32")
+                                          _lib.ptr(tapes.order), B, M, tapes.max_len, _lib.ptr(Cp), M, 1,
+                                          _lib.ptr(cache), _lib.ptr(G), _lib.ptr(gCk), None, _lib.ptr(status), st),
+                   "sr_eval_backward_f32")
 
     ktimes = {}
     for name, fn in (("eval_forward_kernel", fwd_k), ("eval_backward_kernel", bwd_k)):

@@ -71,18 +71,18 @@ _SIGS = {
     "sr_tape_compile": ([vp, vp, i64, i64, i64, i64, i64, i64, i64, i32, vp, vp, vp, vp], ctypes.c_int),
     "sr_eval_forward_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp], ctypes.c_int),
     "sr_eval_forward_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp], ctypes.c_int),
-    "sr_eval_backward_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp],
+    "sr_eval_backward_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp, vp],
                              ctypes.c_int),
-    "sr_eval_backward_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp],
+    "sr_eval_backward_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, vp, vp, vp, vp, vp, vp],
                              ctypes.c_int),
     "sr_eval_forward_multi_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp],
                                   ctypes.c_int),
     "sr_eval_forward_multi_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp],
                                   ctypes.c_int),
     "sr_eval_backward_multi_f32": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp, vp, vp,
-                                    vp], ctypes.c_int),
+                                    vp, vp], ctypes.c_int),
     "sr_eval_backward_multi_f64": ([vp, i64, i64, vp, vp, vp, i64, i64, i32, vp, i64, i64, i64, i64, vp, vp, vp, vp,
-                                    vp], ctypes.c_int),
+                                    vp, vp], ctypes.c_int),
     "sr_fit_workspace_bytes": ([i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions)], i64),
     "sr_tape_live_rows": ([vp, vp, i64, i64, vp, vp], ctypes.c_int),
     "sr_fit_launch_shape": ([i64, i64, i64, i64, i32, i32, ctypes.POINTER(FitOptions), vp], ctypes.c_int),

@@ -435,6 +435,46 @@ __device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N,
   cp_async_commit();
 }
 
+// Copies the value rows of this chunk from the forward cache Cc (node k, point n at
+// Cc[k * rs + n * es]) into vals[k][32 V] for the operator nodes (rows at byte offsets
+// prow[0..nop) from vals_off) and the variable leaves lvar[0..nvar); the rows of the
+// learnable leaves hold their gradient partial sums and are not touched.  Same copy
+// shapes as stage_rows.
+template <typename T, int V>
+__device__ __forceinline__ void stage_value_rows(T* vals, const T* Cc, const uint32_t* prow, uint32_t vals_off,
+                                                 int nop, const int* lvar, int nvar, int64_t N, int64_t rs,
+                                                 int64_t es, int64_t base, int lane, bool vec16) {
+  constexpr int RW = 32 * V;
+  constexpr uint32_t RB = RW * (uint32_t)sizeof(T);
+  const int nrows = nop + nvar;
+  auto node_of = [&](int r) -> int { return r < nop ? (int)((prow[r] - vals_off) / RB) : lvar[r - nop]; };
+  if (vec16) {
+    constexpr int E = 16 / sizeof(T);
+    constexpr int kLanesPerRow = RW / E;
+    constexpr int kRowsPerStep = 32 / kLanesPerRow;
+    const int r0 = lane / kLanesPerRow, p = (lane % kLanesPerRow) * E;
+    const int64_t left = N - (base + p);
+    const int bytes = left >= E ? 16 : (left > 0 ? (int)left * (int)sizeof(T) : 0);
+    for (int r = r0; r < nrows; r += kRowsPerStep) {
+      const int k = node_of(r);
+      const T* src = bytes ? Cc + (size_t)k * rs + base + p : Cc;
+      cp_async(vals + k * RW + p, src, 16, bytes);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int64_t n = base + v * 32 + lane;
+      const int bytes = n < N ? (int)sizeof(T) : 0;
+      for (int r = 0; r < nrows; ++r) {
+        const int k = node_of(r);
+        const T* src = bytes ? Cc + (size_t)k * rs + n * es : Cc;
+        cp_async(vals + k * RW + v * 32 + lane, src, (int)sizeof(T), bytes);
+      }
+    }
+  }
+  cp_async_commit();
+}
+
 // ------------------------------------------------------------------------------------
 // Adjoint.  One warp per tape, 32 V points per chunk (V points per lane: the per-node
 // decode and dispatch serve V points).  The host launches one persistent grid per
@@ -448,8 +488,11 @@ __device__ __forceinline__ void stage_rows(T* buf, const T* G, int L, int64_t N,
 //                 or the broadcast entry of any other leaf (stride 0);
 //   adjoint destination = byte offset of the child's adjoint row.
 // Every node has an adjoint row.  Per chunk the output-gradient rows are staged into
-// them with cp.async while the operator nodes are recomputed (the saved cache is never
-// read); the reverse sweep then adds the contributions into the children's rows in the
+// them with cp.async.  With the forward cache (kCached: the reference's backward reads
+// it too) the value rows of the operator nodes and variables are staged from it in the
+// same way, the cache holding exactly the values the forward kernel computed; without
+// it the operator nodes are recomputed while the copies are in flight.  The reverse
+// sweep then adds the contributions into the children's rows in the
 // reference's order (parents from the last to the first, child 0 before child 1), and
 // the leaves are reduced afterwards.  A learnable constant's operand is a broadcast
 // entry, so its value row is free and holds its per-lane gradient sums over the
@@ -480,12 +523,13 @@ __host__ __device__ __forceinline__ BwdLayout backward_layout(int Lmax) {
   return l;
 }
 
-template <typename T, bool kMulti, int V>
+template <typename T, bool kMulti, int V, bool kCached>
 __global__ void __launch_bounds__(256, 4) eval_backward_kernel(
     const T* __restrict__ X, int64_t N, int64_t n_x, const uint32_t* __restrict__ desc,
     const int32_t* __restrict__ meta, const int32_t* __restrict__ order, int64_t B, int64_t M, int Llo, int Lhi,
-    const T* __restrict__ C, int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K_, const T* __restrict__ gout,
-    T* __restrict__ gC, T* __restrict__ gX, int32_t* __restrict__ status, bool vec16) {
+    const T* __restrict__ C, int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K_, const T* __restrict__ cache,
+    const T* __restrict__ gout, T* __restrict__ gC, T* __restrict__ gX, int32_t* __restrict__ status, bool vec16,
+    bool cvec16) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t K = kMulti ? K_ : 1;  // one constant set: the strides fold at compile time
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -573,6 +617,7 @@ __global__ void __launch_bounds__(256, 4) eval_backward_kernel(
         for (int v = 0; v < V; ++v) vals[lcon[j] * RW + v * 32 + lane] = T(0);
       }
       const T* G = gout + (size_t)b * M * N * K + kk;
+      const T* Cc = kCached ? cache + (size_t)b * M * N * K + kk : nullptr;
       const int64_t rs = N * K;
       __syncwarp();
       for (int64_t c = 0; c < nchunks; ++c) {
@@ -590,25 +635,29 @@ __global__ void __launch_bounds__(256, 4) eval_backward_kernel(
         // (the reference's zeros_like(cache).add_(grad_output)) can only flip the sign
         // of a zero seed, which no output can see: a zero adjoint contributes nothing
         stage_rows<T, V>(adj, G, L, N, rs, K, base, lane, vec16);
-        for (int j = 0; j < nvar; ++j) {
-          const int k = lvar[j];
-          const int var = child0(tape[k]);
+        if constexpr (kCached) {
+          stage_value_rows<T, V>(vals, Cc, prow, ly.vals, nop, lvar, nvar, N, rs, K, base, lane, cvec16);
+        } else {
+          for (int j = 0; j < nvar; ++j) {
+            const int k = lvar[j];
+            const int var = child0(tape[k]);
 #pragma unroll
-          for (int v = 0; v < V; ++v) vals[k * RW + v * 32 + lane] = __ldg(X + nn[v] * n_x + var);
-        }
-        __syncwarp();
-        for (int i = 0; i < nop; ++i) {
-          const int code = (int)pcode[i];
-          const uint32_t sa = psa[i], sb = psb[i], pr = prow[i];
-          T a[V], bb[V], r[V];
-#pragma unroll
-          for (int v = 0; v < V; ++v) {
-            a[v] = lds_operand<T>(wb, sa, v * 32 + lane);
-            bb[v] = lds_operand<T>(wb, sb, v * 32 + lane);
+            for (int v = 0; v < V; ++v) vals[k * RW + v * 32 + lane] = __ldg(X + nn[v] * n_x + var);
           }
-          op_value_v<T, V>(code, a, bb, r);
+          __syncwarp();
+          for (int i = 0; i < nop; ++i) {
+            const int code = (int)pcode[i];
+            const uint32_t sa = psa[i], sb = psb[i], pr = prow[i];
+            T a[V], bb[V], r[V];
 #pragma unroll
-          for (int v = 0; v < V; ++v) *row_at<T>(wb, pr, v * 32 + lane) = r[v];
+            for (int v = 0; v < V; ++v) {
+              a[v] = lds_operand<T>(wb, sa, v * 32 + lane);
+              bb[v] = lds_operand<T>(wb, sb, v * 32 + lane);
+            }
+            op_value_v<T, V>(code, a, bb, r);
+#pragma unroll
+            for (int v = 0; v < V; ++v) *row_at<T>(wb, pr, v * 32 + lane) = r[v];
+          }
         }
         cp_async_wait<0>();
         __syncwarp();
@@ -861,20 +910,20 @@ static int launch_forward(const T* X, int64_t N, int64_t n_x, const uint32_t* de
   return rc ? rc : rw;
 }
 
-template <typename T, bool kMulti, int V>
+template <typename T, bool kMulti, int V, bool kCached>
 static int launch_backward_v(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                              const int32_t* order, int64_t B, int64_t M, int Llo, int Lhi, const T* C, int64_t c_sb,
-                             int64_t c_sm, int64_t c_sk, int64_t K, const T* gout, T* gC, T* gX, int32_t* status,
-                             bool vec16, cudaStream_t st) {
+                             int64_t c_sm, int64_t c_sk, int64_t K, const T* cache, const T* gout, T* gC, T* gX,
+                             int32_t* status, bool vec16, bool cvec16, cudaStream_t st) {
   const size_t per_warp = backward_layout<T, V>(Lhi).bytes;
   Shape sh;
-  auto kern = eval_backward_kernel<T, kMulti, V>;
+  auto kern = eval_backward_kernel<T, kMulti, V, kCached>;
   if (!pick_shape(reinterpret_cast<const void*>(kern), per_warp, B, sh)) {
     set_error("tape of %d nodes does not fit in shared memory", Lhi);
     return SR_ERR_UNSUPPORTED;
   }
   kern<<<(unsigned)sh.blocks, sh.warps * 32, sh.smem, st>>>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb,
-                                                           c_sm, c_sk, K, gout, gC, gX, status, vec16);
+                                                           c_sm, c_sk, K, cache, gout, gC, gX, status, vec16, cvec16);
   return launch_check("eval_backward_kernel");
 }
 
@@ -885,20 +934,21 @@ static int launch_backward_v(const T* X, int64_t N, int64_t n_x, const uint32_t*
 template <typename T>
 static int launch_backward_class(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                                  const int32_t* order, int64_t B, int64_t M, int Llo, int Lhi, const T* C,
-                                 int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const T* gout, T* gC, T* gX,
-                                 int32_t* status, bool vec16, cudaStream_t st) {
+                                 int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const T* cache, const T* gout,
+                                 T* gC, T* gX, int32_t* status, bool vec16, bool cvec16, cudaStream_t st) {
+#define SR_BWD_ARGS X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K, cache, gout, gC, gX, status, \
+                    vec16, cvec16, st
   if (K == 1)
-    return launch_backward_v<T, false, 1>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K, gout,
-                                          gC, gX, status, vec16, st);
-  return launch_backward_v<T, true, 1>(X, N, n_x, desc, meta, order, B, M, Llo, Lhi, C, c_sb, c_sm, c_sk, K, gout, gC,
-                                       gX, status, vec16, st);
+    return cache ? launch_backward_v<T, false, 1, true>(SR_BWD_ARGS) : launch_backward_v<T, false, 1, false>(SR_BWD_ARGS);
+  return cache ? launch_backward_v<T, true, 1, true>(SR_BWD_ARGS) : launch_backward_v<T, true, 1, false>(SR_BWD_ARGS);
+#undef SR_BWD_ARGS
 }
 
 template <typename T>
 static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                            const int32_t* order, int64_t B, int64_t M, int32_t max_len, const T* C, int64_t c_sb,
-                           int64_t c_sm, int64_t c_sk, int64_t K, const T* gout, T* gC, T* gX, int32_t* status,
-                           void* stream) {
+                           int64_t c_sm, int64_t c_sk, int64_t K, const T* cache, const T* gout, T* gC, T* gX,
+                           int32_t* status, void* stream) {
   int rc = check_tape_args(B, M);
   if (rc) return rc;
   if (N < 0 || n_x < 0 || K < 0) { set_error("negative size"); return SR_ERR_INVALID_ARGUMENT; }
@@ -921,6 +971,8 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
   // 16-byte staging needs every (tape, row, chunk) start 16-byte aligned
   const bool vec16 =
       K == 1 && (reinterpret_cast<uintptr_t>(gout) % 16 == 0) && (N % (16 / (int64_t)sizeof(T)) == 0);
+  const bool cvec16 =
+      K == 1 && (reinterpret_cast<uintptr_t>(cache) % 16 == 0) && (N % (16 / (int64_t)sizeof(T)) == 0);
   // one persistent grid per class of tape lengths (Llo, Lhi]: (32, Lmax], (16, 32],
   // [0, 16], as far as Lmax reaches
   int cls[3][2], nc = 0;
@@ -929,7 +981,7 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
   cls[nc][0] = -1; cls[nc][1] = Lmax < 16 ? Lmax : 16; ++nc;
   for (int ci = 0; ci < nc; ++ci) {
     rc = launch_backward_class<T>(X, N, n_x, desc, meta, order, B, M, cls[ci][0], cls[ci][1], C, c_sb, c_sm, c_sk, K,
-                                  gout, gC, gX, status, vec16, st);
+                                  cache, gout, gC, gX, status, vec16, cvec16, st);
     if (rc) break;
     if (ci == 0) {
       // enqueued after the first adjoint grid, so that grid's CTAs are placed first and
@@ -985,16 +1037,18 @@ int sr_eval_forward_f64(const double* X, int64_t N, int64_t n_x, const uint32_t*
 
 int sr_eval_backward_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                          const int32_t* order, int64_t B, int64_t M, int32_t max_len, const float* C, int64_t c_sb,
-                         int64_t c_sm, const float* gout, float* gC, float* gX, int32_t* status, void* stream) {
-  return sr::launch_backward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, 0, 1, gout, gC, gX,
-                                    status, stream);
+                         int64_t c_sm, const float* cache, const float* gout, float* gC, float* gX, int32_t* status,
+                         void* stream) {
+  return sr::launch_backward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, 0, 1, cache, gout, gC,
+                                    gX, status, stream);
 }
 
 int sr_eval_backward_f64(const double* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                          const int32_t* order, int64_t B, int64_t M, int32_t max_len, const double* C, int64_t c_sb,
-                         int64_t c_sm, const double* gout, double* gC, double* gX, int32_t* status, void* stream) {
-  return sr::launch_backward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, 0, 1, gout, gC, gX,
-                                     status, stream);
+                         int64_t c_sm, const double* cache, const double* gout, double* gC, double* gX,
+                         int32_t* status, void* stream) {
+  return sr::launch_backward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, 0, 1, cache, gout, gC,
+                                     gX, status, stream);
 }
 
 int sr_eval_forward_multi_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
@@ -1012,18 +1066,18 @@ int sr_eval_forward_multi_f64(const double* X, int64_t N, int64_t n_x, const uin
 
 int sr_eval_backward_multi_f32(const float* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                                const int32_t* order, int64_t B, int64_t M, int32_t max_len, const float* C,
-                               int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const float* gout, float* gC,
-                               float* gX, int32_t* status, void* stream) {
-  return sr::launch_backward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, c_sk, K, gout, gC, gX,
-                                    status, stream);
+                               int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const float* cache,
+                               const float* gout, float* gC, float* gX, int32_t* status, void* stream) {
+  return sr::launch_backward<float>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, c_sk, K, cache, gout,
+                                    gC, gX, status, stream);
 }
 
 int sr_eval_backward_multi_f64(const double* X, int64_t N, int64_t n_x, const uint32_t* desc, const int32_t* meta,
                                const int32_t* order, int64_t B, int64_t M, int32_t max_len, const double* C,
-                               int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const double* gout, double* gC,
-                               double* gX, int32_t* status, void* stream) {
-  return sr::launch_backward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, c_sk, K, gout, gC,
-                                     gX, status, stream);
+                               int64_t c_sb, int64_t c_sm, int64_t c_sk, int64_t K, const double* cache,
+                               const double* gout, double* gC, double* gX, int32_t* status, void* stream) {
+  return sr::launch_backward<double>(X, N, n_x, desc, meta, order, B, M, max_len, C, c_sb, c_sm, c_sk, K, cache, gout,
+                                     gC, gX, status, stream);
 }
 
 }  // extern "C"

@@ -85,12 +85,13 @@ class _Evaluate(torch.autograd.Function):
                 tapes.max_len, _lib.ptr(C_bm), cb, cm, _lib.ptr(cache), _lib.stream_ptr(Xc.device))
         _lib.check(rc, "sr_eval_forward")
         ctx.tapes = tapes
-        ctx.save_for_backward(Xc, C_bm)
+        # the adjoint reads the node values from the cache, as the reference's backward does
+        ctx.save_for_backward(Xc, C_bm, cache)
         return cache
 
     @staticmethod
     def backward(ctx, grad):
-        Xc, C_bm = ctx.saved_tensors
+        Xc, C_bm, cache = ctx.saved_tensors
         tapes: CompiledTapes = ctx.tapes
         B, M = tapes.B, tapes.M
         N, nx = Xc.shape
@@ -102,7 +103,7 @@ class _Evaluate(torch.autograd.Function):
         fn = L.sr_eval_backward_f32 if Xc.dtype == torch.float32 else L.sr_eval_backward_f64
         cb, cm = C_bm.stride()
         rc = fn(_lib.ptr(Xc), N, nx, _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), _lib.ptr(tapes.order), B, M,
-                tapes.max_len, _lib.ptr(C_bm), cb, cm, _lib.ptr(grad), _lib.ptr(gC), _lib.ptr(gX),
+                tapes.max_len, _lib.ptr(C_bm), cb, cm, _lib.ptr(cache), _lib.ptr(grad), _lib.ptr(gC), _lib.ptr(gX),
                 _lib.ptr(status), _lib.stream_ptr(Xc.device))
         _lib.check(rc, "sr_eval_backward")
         code = int(status.item())
@@ -192,12 +193,12 @@ class _EvaluateMultiple(torch.autograd.Function):
                 tapes.max_len, _lib.ptr(C_bmk), cb, cm, ck, K, _lib.ptr(cache), _lib.stream_ptr(Xc.device))
         _lib.check(rc, "sr_eval_forward_multi")
         ctx.tapes = tapes
-        ctx.save_for_backward(Xc, C_bmk)
+        ctx.save_for_backward(Xc, C_bmk, cache)
         return cache
 
     @staticmethod
     def backward(ctx, grad):
-        Xc, C_bmk = ctx.saved_tensors
+        Xc, C_bmk, cache = ctx.saved_tensors
         tapes: CompiledTapes = ctx.tapes
         B, M = tapes.B, tapes.M
         K = C_bmk.shape[2]
@@ -210,7 +211,8 @@ class _EvaluateMultiple(torch.autograd.Function):
         fn = L.sr_eval_backward_multi_f32 if Xc.dtype == torch.float32 else L.sr_eval_backward_multi_f64
         cb, cm, ck = C_bmk.stride()
         rc = fn(_lib.ptr(Xc), N, nx, _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), _lib.ptr(tapes.order), B, M,
-                tapes.max_len, _lib.ptr(C_bmk), cb, cm, ck, K, _lib.ptr(grad), _lib.ptr(gC), _lib.ptr(gX),
+                tapes.max_len, _lib.ptr(C_bmk), cb, cm, ck, K, _lib.ptr(cache), _lib.ptr(grad), _lib.ptr(gC),
+                _lib.ptr(gX),
                 _lib.ptr(status), _lib.stream_ptr(Xc.device))
         _lib.check(rc, "sr_eval_backward_multi")
         code = int(status.item())

@@ -101,7 +101,10 @@ int sr_eval_forward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint3
 
 /*
  * Adjoint of the forward evaluation for a dense output gradient grad_out (B, M, N).
- * Node values are recomputed from X and C (the cache is not read).  Writes
+ * Node values are read from cache_dev, the (B, M, N) output of sr_eval_forward_f32 for
+ * the same X, tapes and C, as the reference's backward reads its saved cache; with
+ * cache_dev NULL they are recomputed from X and C (the same bits, more instructions).
+ * Writes
  * grad_C (B, M) (zero at non-constant nodes) and, when grad_X_dev is not NULL,
  * accumulates into grad_X (N, n_x), which the caller zeroes first.  status_dev
  * is zeroed and then receives 201 (nonzero gradient on a NO_OP node) or 204
@@ -115,12 +118,12 @@ int sr_eval_forward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint3
 int sr_eval_backward_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                          const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
                          int32_t max_len, const float *C_dev, int64_t c_sb, int64_t c_sm,
-                         const float *grad_out_dev, float *grad_C_dev, float *grad_X_dev,
+                         const float *cache_dev, const float *grad_out_dev, float *grad_C_dev, float *grad_X_dev,
                          int32_t *status_dev, void *stream);
 int sr_eval_backward_f64(const double *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                          const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
                          int32_t max_len, const double *C_dev, int64_t c_sb, int64_t c_sm,
-                         const double *grad_out_dev, double *grad_C_dev, double *grad_X_dev,
+                         const double *cache_dev, const double *grad_out_dev, double *grad_C_dev, double *grad_X_dev,
                          int32_t *status_dev, void *stream);
 
 /* Options of sr_fit_lbfgs; mirrors optimize()/LBFGS_batch's arguments
@@ -159,9 +162,10 @@ int sr_tape_live_rows(const uint32_t *desc_dev, const int32_t *meta_dev, int64_t
  * evaluate_multiple_constant_backend, src/symbolic_evaluation.cpp:171-305, with the
  * per-position kernels src/evaluation_kernels_cuda.cu:761-1343, here one launch):
  * C (B, M, K) through (b, m, set) strides; cache (B, M, N, K) contiguous, NO_OP rows
- * NaN.  The adjoint takes grad_out (B, M, N, K) contiguous and writes grad_C
- * (B, M, K) contiguous and, if not NULL, adds into grad_X (N, n_x) summed over the
- * sets; status as for sr_eval_backward_f32.
+ * NaN.  The adjoint takes grad_out (B, M, N, K) contiguous and the forward's cache
+ * (B, M, N, K), or NULL to recompute the values, and writes grad_C (B, M, K)
+ * contiguous and, if not NULL, adds into grad_X (N, n_x) summed over the sets; status
+ * as for sr_eval_backward_f32.
  */
 int sr_eval_forward_multi_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                               const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
@@ -174,12 +178,14 @@ int sr_eval_forward_multi_f64(const double *X_dev, int64_t N, int64_t n_x, const
 int sr_eval_backward_multi_f32(const float *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                                const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
                                int32_t max_len, const float *C_dev, int64_t c_sb, int64_t c_sm, int64_t c_sk,
-                               int64_t K, const float *grad_out_dev, float *grad_C_dev, float *grad_X_dev,
+                               int64_t K, const float *cache_dev, const float *grad_out_dev, float *grad_C_dev,
+                               float *grad_X_dev,
                                int32_t *status_dev, void *stream);
 int sr_eval_backward_multi_f64(const double *X_dev, int64_t N, int64_t n_x, const uint32_t *desc_dev,
                                const int32_t *meta_dev, const int32_t *order_dev, int64_t B, int64_t M,
                                int32_t max_len, const double *C_dev, int64_t c_sb, int64_t c_sm, int64_t c_sk,
-                               int64_t K, const double *grad_out_dev, double *grad_C_dev, double *grad_X_dev,
+                               int64_t K, const double *cache_dev, const double *grad_out_dev, double *grad_C_dev,
+                               double *grad_X_dev,
                                int32_t *status_dev, void *stream);
 
 /* Bytes of device workspace sr_fit_lbfgs needs for this problem set

@@ -494,8 +494,8 @@ def test_forward_and_adjoint_replay_in_a_cuda_graph():
         _lib.check(L.sr_eval_forward_f32(_lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), _lib.ptr(tp.order),
                                          B, M, tp.max_len, _lib.ptr(C), M, 1, _lib.ptr(cache), st), "forward")
         _lib.check(L.sr_eval_backward_f32(_lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), _lib.ptr(tp.order),
-                                          B, M, tp.max_len, _lib.ptr(C), M, 1, _lib.ptr(gout), _lib.ptr(gC), None,
-                                          _lib.ptr(status), st), "backward")
+                                          B, M, tp.max_len, _lib.ptr(C), M, 1, _lib.ptr(cache), _lib.ptr(gout),
+                                          _lib.ptr(gC), None, _lib.ptr(status), st), "backward")
 
     ref = (torch.empty((B, M, N), device="cuda"), torch.empty((B, M), device="cuda"),
            torch.zeros(1, dtype=torch.int32, device="cuda"))
@@ -553,7 +553,69 @@ def test_tape_longer_than_max_len_is_nan_and_reported():
     gC = torch.zeros((B, M), device="cuda")
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     _lib.check(L.sr_eval_backward_f32(_lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), None, B, M, max_len,
-                                      _lib.ptr(C), M, 1, _lib.ptr(gout), _lib.ptr(gC), None, _lib.ptr(status), st),
-               "backward")
+                                      _lib.ptr(C), M, 1, None, _lib.ptr(gout), _lib.ptr(gC), None, _lib.ptr(status),
+                                      st), "backward")
     torch.cuda.synchronize()
     assert int(status.item()) == _lib.TAPE_EXCEEDS_LAUNCH
+
+
+@pytest.mark.parametrize("dtype,K", [(torch.float32, 0), (torch.float64, 0), (torch.float32, 3), (torch.float64, 2)])
+def test_adjoint_from_cache_equals_recomputed(dtype, K):
+    """The adjoint reading the node values from the forward's cache (as autograd calls
+    it) and the adjoint recomputing them (cache_dev NULL) give the same grad_C bit for
+    bit and the same status; grad_X, an atomic sum, agrees to rounding.  K = 0: the
+    single-set entry points (16-byte staging when N is a multiple of 4), else
+    evaluate_multiple's (strided staging); N = 1001 leaves a ragged last chunk."""
+    from cudasymbolicregression_gb300 import _lib, tapes as tg
+    from cudasymbolicregression_gb300.tape import compile_tapes
+    rng = np.random.default_rng(41 + K)
+    B, M, nx = 700, 64, 3
+    npdt = np.float32 if dtype == torch.float32 else np.float64
+    tb = tg.generate(B, M, seed=42 + K, mean_length=24.0, n_vars=nx, p_const_leaf=0.3, binary=(40, 41, 42))
+    tp = compile_tapes(cuda(tb.ops), cuda(tb.ch), nx)
+    L = _lib.lib()
+    st = _lib.stream_ptr(torch.device("cuda"))
+    sfx = "f32" if dtype == torch.float32 else "f64"
+    for N in (1000, 1001):
+        X = cuda(rng.uniform(-2, 2, (N, nx)).astype(npdt))
+        kk = max(K, 1)
+        C = cuda(rng.standard_normal((B, M, kk)).astype(npdt))
+        cache = torch.empty((B, M, N, kk), dtype=dtype, device="cuda")
+        gout = torch.as_tensor(rng.standard_normal((B, M, N, kk)), dtype=dtype).cuda()
+        if K == 0:
+            _lib.check(getattr(L, "sr_eval_forward_" + sfx)(
+                _lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), _lib.ptr(tp.order), B, M, tp.max_len,
+                _lib.ptr(C), M, 1, _lib.ptr(cache), st), "forward")
+        else:
+            _lib.check(getattr(L, "sr_eval_forward_multi_" + sfx)(
+                _lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), _lib.ptr(tp.order), B, M, tp.max_len,
+                _lib.ptr(C), M * kk, kk, 1, kk, _lib.ptr(cache), st), "forward")
+        gout[torch.isnan(cache)] = 0.0  # the padding rows (NaN) and NO_OP values take no gradient
+        out = []
+        for cp in (cache, None):
+            gC = torch.full((B, M, kk), 7.0, dtype=dtype, device="cuda")
+            gX = torch.zeros((N, nx), dtype=dtype, device="cuda")
+            status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+            cptr = None if cp is None else _lib.ptr(cp)
+            if K == 0:
+                _lib.check(getattr(L, "sr_eval_backward_" + sfx)(
+                    _lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), _lib.ptr(tp.order), B, M, tp.max_len,
+                    _lib.ptr(C), M, 1, cptr, _lib.ptr(gout), _lib.ptr(gC), _lib.ptr(gX), _lib.ptr(status), st),
+                    "backward")
+            else:
+                _lib.check(getattr(L, "sr_eval_backward_multi_" + sfx)(
+                    _lib.ptr(X), N, nx, _lib.ptr(tp.desc), _lib.ptr(tp.meta), _lib.ptr(tp.order), B, M, tp.max_len,
+                    _lib.ptr(C), M * kk, kk, 1, kk, cptr, _lib.ptr(gout), _lib.ptr(gC), _lib.ptr(gX),
+                    _lib.ptr(status), st), "backward")
+            torch.cuda.synchronize()
+            out.append((gC.cpu().numpy(), gX.cpu().numpy(), int(status.item())))
+        (gc1, gx1, s1), (gc2, gx2, s2) = out
+        assert s1 == s2 == 0
+        assert np.array_equal(gc1.view(np.uint64 if dtype == torch.float64 else np.uint32),
+                              gc2.view(np.uint64 if dtype == torch.float64 else np.uint32)), f"N={N}"
+        fin = np.isfinite(gx2)
+        assert np.array_equal(np.isfinite(gx1), fin) and np.array_equal(np.isnan(gx1), np.isnan(gx2))
+        assert np.array_equal(gx1[np.isinf(gx2)], gx2[np.isinf(gx2)])
+        tol = 1e-4 if dtype == torch.float32 else 1e-10
+        if fin.any():
+            np.testing.assert_allclose(gx1[fin], gx2[fin], rtol=tol, atol=tol * np.abs(gx2[fin]).max())
