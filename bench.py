@@ -96,9 +96,10 @@ FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10744832 + 2560),
 FIT_PROFILE = {"commit": "2ddf7f6", "issue_active_pct": 53.8, "fp32_pipe_pct": 14.7, "xu_pipe_pct": 1.74,
                "alu_pipe_pct": 48.5, "lsu_pipe_pct": 25.3, "fp64_pipe_pct": 1.68, "warps_active_pct": 23.1,
                "capture": "ncu --set full, ragged B=4096, N=512"}
-# The adjoint call: its three length-class grids and the concurrent padding check.
+# The adjoint call: its three length-class grids (which stage the cached value rows of
+# the real nodes beside the grad_out rows) and the concurrent padding check.
 EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000),
-                      ("eval_backward_kernel", 65536, 1024): 16 * (1075467264 + 10125312)}
+                      ("eval_backward_kernel", 65536, 1024): 16 * (1364424192 + 13661696)}
 
 
 def peaks():
