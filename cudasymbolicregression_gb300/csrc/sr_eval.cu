@@ -973,12 +973,24 @@ static int launch_backward(const T* X, int64_t N, int64_t n_x, const uint32_t* d
       K == 1 && (reinterpret_cast<uintptr_t>(gout) % 16 == 0) && (N % (16 / (int64_t)sizeof(T)) == 0);
   const bool cvec16 =
       K == 1 && (reinterpret_cast<uintptr_t>(cache) % 16 == 0) && (N % (16 / (int64_t)sizeof(T)) == 0);
-  // one persistent grid per class of tape lengths (Llo, Lhi]: (32, Lmax], (16, 32],
-  // [0, 16], as far as Lmax reaches
-  int cls[3][2], nc = 0;
-  if (Lmax > 32) { cls[nc][0] = 32; cls[nc][1] = Lmax; ++nc; }
-  if (Lmax > 16) { cls[nc][0] = 16; cls[nc][1] = Lmax < 32 ? Lmax : 32; ++nc; }
-  cls[nc][0] = -1; cls[nc][1] = Lmax < 16 ? Lmax : 16; ++nc;
+  // one persistent grid per class of tape lengths (Llo, Lhi]: (48, Lmax], (32, 48],
+  // (16, 32], [0, 16], as far as Lmax reaches.  The longest class is bound by the
+  // warps its shared memory lets reside (1.5x its tables cost 23% of the adjoint's time
+  // on a GB300, the same for the middle class 5%, the shortest nothing): splitting it at
+  // 48 gained 2%, further splits at 40, 56 or 24 lost more to the extra grids' tails.
+  const int bound[3] = {48, 32, 16};
+  int cls[4][2], nc = 0, hi = Lmax;
+  for (int j = 0; j < 3; ++j) {
+    if (hi > bound[j]) {
+      cls[nc][0] = bound[j];
+      cls[nc][1] = hi;
+      ++nc;
+      hi = bound[j];
+    }
+  }
+  cls[nc][0] = -1;
+  cls[nc][1] = hi;
+  ++nc;
   for (int ci = 0; ci < nc; ++ci) {
     rc = launch_backward_class<T>(X, N, n_x, desc, meta, order, B, M, cls[ci][0], cls[ci][1], C, c_sb, c_sm, c_sk, K,
                                   cache, gout, gC, gX, status, vec16, cvec16, st);

@@ -439,71 +439,6 @@ __device__ __forceinline__ F2 f2_madf(F2 acc, float a, float b) {
 // branch), so that the latencies of the loads overlap; the order of the terms, and so the
 // result, is that of one sequential sum.
 
-// Appends the newest pair (already in its ring slot, at position h - 1): its dots with
-// every pair in the ring, c and rho of the new pair, its row and column of Y^T Y and its
-// column of R^-1.  Returns s.y and y.y of the new pair in *sy, *yy (every lane).
-template <int SPL>
-__device__ __forceinline__ void compact_push(const History& H, int head, int h, int slot, int nslots, F2 eps2,
-                                             int lane, F2* sy, F2* yy) {
-  __syncwarp();
-  const bool mine = lane < h;
-  const int sl = mine ? ring_slot(head, lane, H.hist) : 0;
-  const float* si = H.S + (size_t)sl * H.RS;
-  const float* yi = H.Y + (size_t)sl * H.RS;
-  const float* yn = H.Y + (size_t)slot * H.RS;
-  F2 r{0.f, 0.f}, q{0.f, 0.f};
-  for (int j0 = 0; j0 < nslots; j0 += 4) {
-    float a[4], b[4], c[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int j = min(j0 + k, nslots - 1);
-      a[k] = si[j];
-      b[k] = yi[j];
-      c[k] = yn[j];
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const F2 nr = f2_madf(r, a[k], c[k]), nq = f2_madf(q, b[k], c[k]);
-      const bool ok = j0 + k < nslots;
-      r = ok ? nr : r;
-      q = ok ? nq : q;
-    }
-  }
-  r = f2_norm(r);
-  q = f2_norm(q);
-  *sy = shfl2(r, h - 1);
-  *yy = shfl2(q, h - 1);
-  const F2 cn = f2_norm(f2_add(*sy, eps2));
-  const F2 rho = f2_div(F2{1.f, 0.f}, cn);
-  F2 acc{0.f, 0.f};
-  const float2* rrow = H.Rinv + (size_t)sl * H.MS;
-  for (int j0 = 0; j0 < h - 1; j0 += 4) {
-    F2 rj[4], m[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int j = min(j0 + k, h - 2);
-      rj[k] = shfl2(r, j);
-      m[k] = ld2(rrow + ring_slot(head, j, H.hist));
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const F2 n = f2_mad(acc, m[k], rj[k]);
-      acc = (lane <= j0 + k && j0 + k < h - 1) ? n : acc;
-    }
-  }
-  if (mine) {
-    st2(H.YY + (size_t)sl * H.MS + slot, q);
-    st2(H.YY + (size_t)slot * H.MS + sl, q);
-    const F2 col = f2_mul(rho, f2_norm(acc));
-    st2(H.Rinv + (size_t)sl * H.MS + slot, lane == h - 1 ? rho : F2{-col.hi, -col.lo});
-  }
-  if (lane == 0) {
-    st2(H.rho + slot, rho);
-    st2(H.c + slot, cn);
-  }
-  __syncwarp();
-}
-
 // Lane i (mine): sum over the positions j < h (kUpper: j >= i, kLower: j <= i) of
 // M(i, j) x_j, x_j from lane j; M(i, j) at base + slot(j) * stride.
 template <bool kUpper, bool kLower>
@@ -528,41 +463,98 @@ __device__ __forceinline__ F2 compact_matvec(const float2* base, int stride, int
   return f2_norm(acc);
 }
 
-// q = H g by the compact representation (h >= 1 pairs), every slot of every lane.
+// The history update for the newest pair (already in its ring slot, at position h - 1)
+// and the direction q = H g that follows it, by the compact representation (h >= 1).
+// The update is done here, not when the pair is stored: the next direction is the only
+// reader, so its dots share one pass over the ring with the direction's (four chains on
+// the same loads: s_i.y_new, y_i.y_new, s_i.g, y_i.g) and the new column of R^-1 shares
+// the loop of t = R^-1 u.  Every sum keeps the order of its terms.  Writes c, rho, the
+// row and column of Y^T Y and the column of R^-1 of the new pair, and returns s.y and
+// y.y of the new pair in sy, yy (every lane).
 template <int SPL>
-__device__ __forceinline__ void compact_direction(const History& H, int head, int h, int nslots, F2 gam,
-                                                  const Slots<SPL>& g, Slots<SPL>& q, int lane) {
+__device__ __forceinline__ void compact_update_direction(const History& H, int head, int h, int nslots, F2 eps2,
+                                                         const Slots<SPL>& g, Slots<SPL>& q, F2& sy, F2& yy,
+                                                         int lane) {
+  __syncwarp();  // the new pair's ring rows, written by every lane
   const bool mine = lane < h;
   const int sl = mine ? ring_slot(head, lane, H.hist) : 0;
+  const int slot = ring_slot(head, h - 1, H.hist);
   const float* si = H.S + (size_t)sl * H.RS;
   const float* yi = H.Y + (size_t)sl * H.RS;
-  // u_i = s_i.g and w_i = y_i.g
-  F2 u{0.f, 0.f}, w{0.f, 0.f};
+  const float* yn = H.Y + (size_t)slot * H.RS;
+  // r_i = s_i.y_new, e_i = y_i.y_new (update); u_i = s_i.g, w_i = y_i.g (direction)
+  F2 r{0.f, 0.f}, e{0.f, 0.f}, u{0.f, 0.f}, w{0.f, 0.f};
 #pragma unroll
   for (int s = 0; s < SPL; ++s) {
     const int top = min(32, nslots - s * 32);
     for (int l0 = 0; l0 < top; l0 += 4) {
-      float gj[4], a[4], b[4];
+      float gj[4], a[4], b[4], c[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int l = min(l0 + k, top - 1);
         gj[k] = __shfl_sync(0xffffffffu, g.v[s], l);
         a[k] = si[s * 32 + l];
         b[k] = yi[s * 32 + l];
+        c[k] = yn[s * 32 + l];
       }
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
+        const F2 nr = f2_madf(r, a[k], c[k]), ne = f2_madf(e, b[k], c[k]);
         const F2 nu = f2_madf(u, a[k], gj[k]), nw = f2_madf(w, b[k], gj[k]);
         const bool ok = l0 + k < top;
+        r = ok ? nr : r;
+        e = ok ? ne : e;
         u = ok ? nu : u;
         w = ok ? nw : w;
       }
     }
   }
+  r = f2_norm(r);
+  e = f2_norm(e);
   u = f2_norm(u);
   w = f2_norm(w);
-  // t = R^-1 u (positions j >= i), Y^T Y t, v = c t + gamma (Y^T Y t - w), z = R^-T v (j <= i)
-  const F2 t = compact_matvec<true, false>(H.Rinv + (size_t)sl * H.MS, 1, head, h, H.hist, u, mine, lane);
+  sy = shfl2(r, h - 1);
+  yy = shfl2(e, h - 1);
+  const F2 cn = f2_norm(f2_add(sy, eps2));
+  const F2 rho = f2_div(F2{1.f, 0.f}, cn);
+  // over the older pairs (i <= j < h - 1): the new column's sum R^-1 r and t = R^-1 u
+  F2 acc{0.f, 0.f}, t{0.f, 0.f};
+  const float2* rrow = H.Rinv + (size_t)sl * H.MS;
+  for (int j0 = 0; j0 < h - 1; j0 += 4) {
+    F2 rj[4], uj[4], m[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int j = min(j0 + k, h - 2);
+      rj[k] = shfl2(r, j);
+      uj[k] = shfl2(u, j);
+      m[k] = ld2(rrow + ring_slot(head, j, H.hist));
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const F2 na = f2_mad(acc, m[k], rj[k]), nt = f2_mad(t, m[k], uj[k]);
+      const bool ok = lane <= j0 + k && j0 + k < h - 1;
+      acc = ok ? na : acc;
+      t = ok ? nt : t;
+    }
+  }
+  // the new pair's column of R^-1 (rho on the diagonal), and the last term of t
+  const F2 col = f2_mul(rho, f2_norm(acc));
+  const F2 rnew = lane == h - 1 ? rho : F2{-col.hi, -col.lo};
+  const F2 ulast = shfl2(u, h - 1);
+  t = mine ? f2_mad(t, rnew, ulast) : t;
+  t = f2_norm(t);
+  if (mine) {
+    st2(H.YY + (size_t)sl * H.MS + slot, e);
+    st2(H.YY + (size_t)slot * H.MS + sl, e);
+    st2(H.Rinv + (size_t)sl * H.MS + slot, rnew);
+  }
+  if (lane == 0) {
+    st2(H.rho + slot, rho);
+    st2(H.c + slot, cn);
+  }
+  __syncwarp();
+  const F2 gam = f2_div(sy, f2_norm(f2_add(yy, eps2)));
+  // Y^T Y t, v = c t + gamma (Y^T Y t - w), z = R^-T v (positions j <= i)
   const F2 yt = compact_matvec<false, false>(H.YY + (size_t)sl * H.MS, 1, head, h, H.hist, t, mine, lane);
   const F2 v = f2_norm(f2_add(f2_mul(ld2(H.c + sl), t), f2_mul(gam, f2_sub(yt, w))));
   const F2 z = compact_matvec<false, true>(H.Rinv + sl, H.MS, head, h, H.hist, v, mine, lane);
@@ -1324,9 +1316,7 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
             H.S[(size_t)slot * H.RS + s * 32 + lane] = sv.v[s];
             H.Y[(size_t)slot * H.RS + s * 32 + lane] = yv.v[s];
           }
-          if (H.compact) {
-            compact_push<SPL>(H, head, h, slot, P.nslots, eps2, lane, &last_sy, &last_yy);
-          } else {
+          if (!H.compact) {  // the compact form updates its history with the next direction
             // curvature of the new pair, computed once: rho of its slot, and s.y, y.y for gamma
             last_sy = dot_pair(P, yv, sv);
             last_yy = dot_pair(P, yv, yv);
@@ -1360,10 +1350,10 @@ __global__ void __launch_bounds__(256, 2) fit_lbfgs_kernel(FitArgs A) {
           // direction q = H g (lbfgs_batch.py:65-103), by warp 0 for the CTA
           Slots<SPL> q = g;
           if (warp == 0 && h > 0) {
-            const F2 gam = f2_div(last_sy, f2_norm(f2_add(last_yy, eps2)));
             if (H.compact) {
-              compact_direction<SPL>(H, head, h, P.nslots, gam, g, q, lane);
+              compact_update_direction<SPL>(H, head, h, P.nslots, eps2, g, q, last_sy, last_yy, lane);
             } else {
+              const F2 gam = f2_div(last_sy, f2_norm(f2_add(last_yy, eps2)));
               // two-loop recursion for long histories
               for (int i = h - 1; i >= 0; --i) {
                 const int sl = (head + i) % A.hist;
