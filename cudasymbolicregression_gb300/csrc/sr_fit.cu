@@ -371,6 +371,7 @@ struct History {
   float2* YY;     // [hist][MS] (compact)
   int hist, RS, MS;
   bool compact;
+  bool split;     // two lanes per pair (histories of at most 16 pairs, one slot register)
 };
 
 template <int SPL>
@@ -380,6 +381,7 @@ __device__ __forceinline__ History history_at(unsigned char* base, int hist) {
   H.RS = hist_ring_stride(SPL);
   H.MS = hist_mat_stride(hist);
   H.compact = hist_compact(hist);
+  H.split = SPL == 1 && hist <= 16;
   H.S = reinterpret_cast<float*>(base);
   H.Y = H.S + (size_t)hist * H.RS;
   H.alph = reinterpret_cast<float2*>(base + hist_vec_bytes(hist, SPL));
@@ -436,31 +438,51 @@ __device__ __forceinline__ F2 f2_madf(F2 acc, float a, float b) {
 
 // The sums below run over blocks of 4 terms: the block's shared-memory loads and
 // shuffles are issued first, then its 4 multiply-adds in order, masked by selects (no
-// branch), so that the latencies of the loads overlap; the order of the terms, and so the
-// result, is that of one sequential sum.
+// branch), so that the latencies of the loads overlap.  For histories of at most 16 pairs
+// (and one slot register) two lanes work on each pair, lane i and lane i + 16 for the
+// pair at position i: a sum over n terms is split into its first (n + 1) / 2 terms, summed
+// in order by the lower lane, and the rest, summed in order by the upper lane, and the
+// two partial sums are added (f2_add, the same in both lanes); otherwise lane i sums all
+// n terms in order.
 
-// Lane i (mine): sum over the positions j < h (kUpper: j >= i, kLower: j <= i) of
-// M(i, j) x_j, x_j from lane j; M(i, j) at base + slot(j) * stride.
+// The lane's part of a sum over n terms: terms [lo, hi), trips = loop length (the same
+// in every lane).
+struct SumPart {
+  int lo, hi, trips;
+};
+__device__ __forceinline__ SumPart sum_part(bool split, int grp, int n) {
+  if (!split) return SumPart{0, n, n};
+  const int mid = (n + 1) >> 1;
+  return grp ? SumPart{mid, n, mid} : SumPart{0, mid, mid};
+}
+__device__ __forceinline__ F2 join_parts(bool split, F2 a) {
+  if (!split) return a;
+  return f2_add(a, F2{__shfl_xor_sync(0xffffffffu, a.hi, 16), __shfl_xor_sync(0xffffffffu, a.lo, 16)});
+}
+
+// Pair position i of the lane (mine: i < h): sum over the positions j < h (kUpper:
+// j >= i, kLower: j <= i) of M(i, j) x_j, x_j from lane j; M(i, j) at base + slot(j) * stride.
 template <bool kUpper, bool kLower>
 __device__ __forceinline__ F2 compact_matvec(const float2* base, int stride, int head, int h, int hist, F2 x,
-                                             bool mine, int lane) {
+                                             bool mine, int i, bool split, int grp) {
   F2 acc{0.f, 0.f};
-  for (int j0 = 0; j0 < h; j0 += 4) {
+  const SumPart sp = sum_part(split, grp, h);
+  for (int j0 = 0; j0 < sp.trips; j0 += 4) {
     F2 xj[4], m[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const int j = min(j0 + k, h - 1);
+      const int j = min(sp.lo + j0 + k, h - 1);
       xj[k] = shfl2(x, j);
       m[k] = ld2(base + (size_t)ring_slot(head, j, hist) * stride);
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const int j = j0 + k;
+      const int j = sp.lo + j0 + k;
       const F2 n = f2_mad(acc, m[k], xj[k]);
-      acc = (mine && j < h && (!kUpper || lane <= j) && (!kLower || j <= lane)) ? n : acc;
+      acc = (mine && j < sp.hi && (!kUpper || i <= j) && (!kLower || j <= i)) ? n : acc;
     }
   }
-  return f2_norm(acc);
+  return f2_norm(join_parts(split, acc));
 }
 
 // The history update for the newest pair (already in its ring slot, at position h - 1)
@@ -476,8 +498,11 @@ __device__ __forceinline__ void compact_update_direction(const History& H, int h
                                                          const Slots<SPL>& g, Slots<SPL>& q, F2& sy, F2& yy,
                                                          int lane) {
   __syncwarp();  // the new pair's ring rows, written by every lane
-  const bool mine = lane < h;
-  const int sl = mine ? ring_slot(head, lane, H.hist) : 0;
+  const bool split = H.split;
+  const int grp = split ? lane >> 4 : 0;
+  const int i = split ? lane & 15 : lane;  // the lane's pair position
+  const bool mine = i < h;
+  const int sl = mine ? ring_slot(head, i, H.hist) : 0;
   const int slot = ring_slot(head, h - 1, H.hist);
   const float* si = H.S + (size_t)sl * H.RS;
   const float* yi = H.Y + (size_t)sl * H.RS;
@@ -487,11 +512,12 @@ __device__ __forceinline__ void compact_update_direction(const History& H, int h
 #pragma unroll
   for (int s = 0; s < SPL; ++s) {
     const int top = min(32, nslots - s * 32);
-    for (int l0 = 0; l0 < top; l0 += 4) {
+    const SumPart sp = sum_part(split, grp, top);  // split only with one slot register
+    for (int l0 = 0; l0 < sp.trips; l0 += 4) {
       float gj[4], a[4], b[4], c[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const int l = min(l0 + k, top - 1);
+        const int l = min(sp.lo + l0 + k, top - 1);
         gj[k] = __shfl_sync(0xffffffffu, g.v[s], l);
         a[k] = si[s * 32 + l];
         b[k] = yi[s * 32 + l];
@@ -501,7 +527,7 @@ __device__ __forceinline__ void compact_update_direction(const History& H, int h
       for (int k = 0; k < 4; ++k) {
         const F2 nr = f2_madf(r, a[k], c[k]), ne = f2_madf(e, b[k], c[k]);
         const F2 nu = f2_madf(u, a[k], gj[k]), nw = f2_madf(w, b[k], gj[k]);
-        const bool ok = l0 + k < top;
+        const bool ok = sp.lo + l0 + k < sp.hi;
         r = ok ? nr : r;
         e = ok ? ne : e;
         u = ok ? nu : u;
@@ -509,10 +535,10 @@ __device__ __forceinline__ void compact_update_direction(const History& H, int h
       }
     }
   }
-  r = f2_norm(r);
-  e = f2_norm(e);
-  u = f2_norm(u);
-  w = f2_norm(w);
+  r = f2_norm(join_parts(split, r));
+  e = f2_norm(join_parts(split, e));
+  u = f2_norm(join_parts(split, u));
+  w = f2_norm(join_parts(split, w));
   sy = shfl2(r, h - 1);
   yy = shfl2(e, h - 1);
   const F2 cn = f2_norm(f2_add(sy, eps2));
@@ -520,30 +546,34 @@ __device__ __forceinline__ void compact_update_direction(const History& H, int h
   // over the older pairs (i <= j < h - 1): the new column's sum R^-1 r and t = R^-1 u
   F2 acc{0.f, 0.f}, t{0.f, 0.f};
   const float2* rrow = H.Rinv + (size_t)sl * H.MS;
-  for (int j0 = 0; j0 < h - 1; j0 += 4) {
+  const SumPart tp = sum_part(split, grp, h - 1);
+  for (int j0 = 0; j0 < tp.trips; j0 += 4) {
     F2 rj[4], uj[4], m[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const int j = min(j0 + k, h - 2);
+      const int j = min(tp.lo + j0 + k, h - 2);
       rj[k] = shfl2(r, j);
       uj[k] = shfl2(u, j);
       m[k] = ld2(rrow + ring_slot(head, j, H.hist));
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
+      const int j = tp.lo + j0 + k;
       const F2 na = f2_mad(acc, m[k], rj[k]), nt = f2_mad(t, m[k], uj[k]);
-      const bool ok = lane <= j0 + k && j0 + k < h - 1;
+      const bool ok = i <= j && j < tp.hi;
       acc = ok ? na : acc;
       t = ok ? nt : t;
     }
   }
+  acc = join_parts(split, acc);
+  t = join_parts(split, t);
   // the new pair's column of R^-1 (rho on the diagonal), and the last term of t
   const F2 col = f2_mul(rho, f2_norm(acc));
-  const F2 rnew = lane == h - 1 ? rho : F2{-col.hi, -col.lo};
+  const F2 rnew = i == h - 1 ? rho : F2{-col.hi, -col.lo};
   const F2 ulast = shfl2(u, h - 1);
   t = mine ? f2_mad(t, rnew, ulast) : t;
   t = f2_norm(t);
-  if (mine) {
+  if (mine && grp == 0) {
     st2(H.YY + (size_t)sl * H.MS + slot, e);
     st2(H.YY + (size_t)slot * H.MS + sl, e);
     st2(H.Rinv + (size_t)sl * H.MS + slot, rnew);
@@ -555,9 +585,10 @@ __device__ __forceinline__ void compact_update_direction(const History& H, int h
   __syncwarp();
   const F2 gam = f2_div(sy, f2_norm(f2_add(yy, eps2)));
   // Y^T Y t, v = c t + gamma (Y^T Y t - w), z = R^-T v (positions j <= i)
-  const F2 yt = compact_matvec<false, false>(H.YY + (size_t)sl * H.MS, 1, head, h, H.hist, t, mine, lane);
+  const F2 yt =
+      compact_matvec<false, false>(H.YY + (size_t)sl * H.MS, 1, head, h, H.hist, t, mine, i, split, grp);
   const F2 v = f2_norm(f2_add(f2_mul(ld2(H.c + sl), t), f2_mul(gam, f2_sub(yt, w))));
-  const F2 z = compact_matvec<false, true>(H.Rinv + sl, H.MS, head, h, H.hist, v, mine, lane);
+  const F2 z = compact_matvec<false, true>(H.Rinv + sl, H.MS, head, h, H.hist, v, mine, i, split, grp);
   const F2 b = f2_mul(gam, t);
   // q = gamma g + sum_i z_i s_i - sum_i (gamma t_i) y_i, per slot in float
   Slots<SPL> qs, qy;

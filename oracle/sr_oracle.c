@@ -597,7 +597,10 @@ typedef struct {
     float *ringS, *ringY;           /* (hist, D) */
     f2_t *rho, *alph;               /* (hist) rho per ring slot, alpha per position */
     int compact;                    /* hist <= 32: the compact representation (else the two-loop) */
+    int pending;                    /* ring slot of the pair whose compact update is pending */
+    int split;                      /* compact with hist <= 16 and one slot register: two lanes per pair */
     f2_t *cd, *Rinv, *YY;           /* (hist), (hist, hist), (hist, hist): c = s.y + eps, R^-1, Y^T Y by slot */
+    f2_t u[32], w[32], tpart[32];   /* by position: S^T g, Y^T g, t over the older pairs */
     f2_t last_sy, last_yy, eps2;
     int poison;
 } kern_t;
@@ -820,80 +823,92 @@ static f2_t f2_madf(f2_t acc, float a, float b)
     return f2_add(acc, f2_mk(p, fmaf(a, b, -p)));
 }
 
-/* The kernel's compact_push (sr_fit.cu): the newest pair, in ring slot `slot` at
- * position h - 1, gets its dots with every pair (one sequential float-pair sum over
- * the slots per pair), c and rho, its row and column of Y^T Y and its column of R^-1
- * (-rho times R^-1 r over the older pairs; rho on the diagonal).  The dropped pair's
- * slot is the new one, so what R^-1 keeps of the others is the inverse of R's trailing
- * block (Byrd, Nocedal and Schnabel 1994). */
-static void kpush_compact(kern_t *k, int slot)
+/* Sums of the compact form as the kernel splits them (sr_fit.cu sum_part, join_parts):
+ * with two lanes per pair (split: histories of at most 16 pairs, one slot register) a
+ * sum over n terms is the f2_add of the in-order sum of its first (n + 1) / 2 terms and
+ * the in-order sum of the rest; otherwise one in-order sum.  Terms outside the
+ * predicate are skipped in place.  term_f / term_p give the j-th product (floats / pairs). */
+static f2_t ksplit_dot(int split, int n, const float *a, const float *b)
 {
-    const int h = k->h, hs = k->hist, D = k->D, head = k->head;
+    int mid = split ? (n + 1) >> 1 : n;
+    f2_t p0 = f2_mk(0.0f, 0.0f), p1 = f2_mk(0.0f, 0.0f);
+    for (int j = 0; j < mid; ++j) p0 = f2_madf(p0, a[j], b[j]);
+    if (!split) return p0;
+    for (int j = mid; j < n; ++j) p1 = f2_madf(p1, a[j], b[j]);
+    return f2_add(p0, p1);
+}
+
+/* sum over positions j < n of M[j] x[j] where take(j); M[j], x[j] pairs. */
+static f2_t ksplit_matvec(int split, int n, const f2_t *m, const f2_t *x, int lo_ok, int hi_ok)
+{
+    int mid = split ? (n + 1) >> 1 : n;
+    f2_t p0 = f2_mk(0.0f, 0.0f), p1 = f2_mk(0.0f, 0.0f);
+    for (int j = 0; j < mid; ++j)
+        if (j >= lo_ok && j <= hi_ok) p0 = f2_mad(p0, m[j], x[j]);
+    if (!split) return p0;
+    for (int j = mid; j < n; ++j)
+        if (j >= lo_ok && j <= hi_ok) p1 = f2_mad(p1, m[j], x[j]);
+    return f2_add(p0, p1);
+}
+
+/* The kernel's history update for the newest pair (ring slot `slot`, position h - 1),
+ * done in compact_update_direction (sr_fit.cu) just before the direction: its dots with
+ * every pair in the ring, c and rho, its row and column of Y^T Y and its column of R^-1
+ * (-rho times R^-1 r over the older pairs; rho on the diagonal).  The dropped pair's slot
+ * is the new one, so what R^-1 keeps of the others is the inverse of R's trailing block
+ * (Byrd, Nocedal and Schnabel 1994).  The partial sum of t over the older pairs is kept
+ * in k->tpart for the direction (the kernel forms both in one loop). */
+static void kpush_compact(kern_t *k, int slot, const float *g)
+{
+    const int h = k->h, hs = k->hist, D = k->D, head = k->head, split = k->split;
     const float *yn = k->ringY + (int64_t)slot * D;
-    f2_t r[32], q[32];
+    f2_t r[32], q[32], m[32];
+    int sl[32];
     for (int i = 0; i < h; ++i) {
-        int sl = (head + i) % hs;
-        const float *si = k->ringS + (int64_t)sl * D, *yi = k->ringY + (int64_t)sl * D;
-        f2_t a = f2_mk(0.0f, 0.0f), b = f2_mk(0.0f, 0.0f);
-        for (int j = 0; j < k->nslots; ++j) {
-            a = f2_madf(a, si[j], yn[j]);
-            b = f2_madf(b, yi[j], yn[j]);
-        }
-        r[i] = f2_norm(a);
-        q[i] = f2_norm(b);
+        sl[i] = (head + i) % hs;
+        const float *si = k->ringS + (int64_t)sl[i] * D, *yi = k->ringY + (int64_t)sl[i] * D;
+        r[i] = f2_norm(ksplit_dot(split, k->nslots, si, yn));
+        q[i] = f2_norm(ksplit_dot(split, k->nslots, yi, yn));
+        k->u[i] = f2_norm(ksplit_dot(split, k->nslots, si, g));
+        k->w[i] = f2_norm(ksplit_dot(split, k->nslots, yi, g));
     }
     k->last_sy = r[h - 1];
     k->last_yy = q[h - 1];
     f2_t cn = f2_norm(f2_add(k->last_sy, k->eps2));
     f2_t rho = f2_div(f2_mk(1.0f, 0.0f), cn);
     for (int i = 0; i < h; ++i) {
-        int sl = (head + i) % hs;
-        f2_t acc = f2_mk(0.0f, 0.0f);
-        for (int j = i; j < h - 1; ++j) acc = f2_mad(acc, k->Rinv[sl * hs + (head + j) % hs], r[j]);
-        k->YY[sl * hs + slot] = q[i];
-        k->YY[slot * hs + sl] = q[i];
+        for (int j = 0; j < h - 1; ++j) m[j] = k->Rinv[sl[i] * hs + sl[j]];
+        f2_t acc = ksplit_matvec(split, h - 1, m, r, i, h - 1);
+        k->tpart[i] = ksplit_matvec(split, h - 1, m, k->u, i, h - 1);
+        k->YY[sl[i] * hs + slot] = q[i];
+        k->YY[slot * hs + sl[i]] = q[i];
         f2_t col = f2_mul(rho, f2_norm(acc));
-        k->Rinv[sl * hs + slot] = i == h - 1 ? rho : f2_mk(-col.hi, -col.lo);
+        k->Rinv[sl[i] * hs + slot] = i == h - 1 ? rho : f2_mk(-col.hi, -col.lo);
     }
     k->rho[slot] = rho;
     k->cd[slot] = cn;
 }
 
-/* The kernel's compact_direction: q = gamma g + S z - gamma Y t with u = S^T g,
- * w = Y^T g, t = R^-1 u, v = c t + gamma (Y^T Y t - w), z = R^-T v; each entry of u, w,
- * t, v, z one sequential float-pair sum, the vector formed per slot in float. */
+/* The kernel's compact direction (after kpush_compact): q = gamma g + S z - gamma Y t
+ * with u = S^T g, w = Y^T g, t = R^-1 u, v = c t + gamma (Y^T Y t - w), z = R^-T v;
+ * every sum split as the kernel splits it, the vector formed per slot in float. */
 static void kdirection_compact(kern_t *k, const float *g, float *q)
 {
-    const int h = k->h, hs = k->hist, D = k->D, head = k->head;
-    f2_t u[32], w[32], t[32], z[32], bb[32], v[32];
+    const int h = k->h, hs = k->hist, D = k->D, head = k->head, split = k->split;
+    f2_t t[32], z[32], bb[32], v[32], m[32];
     int sl[32];
-    for (int i = 0; i < h; ++i) {
-        sl[i] = (head + i) % hs;
-        const float *si = k->ringS + (int64_t)sl[i] * D, *yi = k->ringY + (int64_t)sl[i] * D;
-        f2_t a = f2_mk(0.0f, 0.0f), b = f2_mk(0.0f, 0.0f);
-        for (int j = 0; j < k->nslots; ++j) {
-            a = f2_madf(a, si[j], g[j]);
-            b = f2_madf(b, yi[j], g[j]);
-        }
-        u[i] = f2_norm(a);
-        w[i] = f2_norm(b);
-    }
-    for (int i = 0; i < h; ++i) {
-        f2_t acc = f2_mk(0.0f, 0.0f);
-        for (int j = i; j < h; ++j) acc = f2_mad(acc, k->Rinv[sl[i] * hs + sl[j]], u[j]);
-        t[i] = f2_norm(acc);
-    }
+    for (int i = 0; i < h; ++i) sl[i] = (head + i) % hs;
+    for (int i = 0; i < h; ++i)
+        t[i] = f2_norm(f2_mad(k->tpart[i], k->Rinv[sl[i] * hs + sl[h - 1]], k->u[h - 1]));
     f2_t gam = f2_div(k->last_sy, f2_norm(f2_add(k->last_yy, k->eps2)));
     for (int i = 0; i < h; ++i) {
-        f2_t acc = f2_mk(0.0f, 0.0f);
-        for (int j = 0; j < h; ++j) acc = f2_mad(acc, k->YY[sl[i] * hs + sl[j]], t[j]);
-        f2_t yt = f2_norm(acc);
-        v[i] = f2_norm(f2_add(f2_mul(k->cd[sl[i]], t[i]), f2_mul(gam, f2_sub(yt, w[i]))));
+        for (int j = 0; j < h; ++j) m[j] = k->YY[sl[i] * hs + sl[j]];
+        f2_t yt = f2_norm(ksplit_matvec(split, h, m, t, 0, h - 1));
+        v[i] = f2_norm(f2_add(f2_mul(k->cd[sl[i]], t[i]), f2_mul(gam, f2_sub(yt, k->w[i]))));
     }
     for (int i = 0; i < h; ++i) {
-        f2_t acc = f2_mk(0.0f, 0.0f);
-        for (int j = 0; j <= i; ++j) acc = f2_mad(acc, k->Rinv[sl[j] * hs + sl[i]], v[j]);
-        z[i] = f2_norm(acc);
+        for (int j = 0; j < h; ++j) m[j] = k->Rinv[sl[j] * hs + sl[i]];
+        z[i] = f2_norm(ksplit_matvec(split, h, m, v, 0, i));
         bb[i] = f2_mul(gam, t[i]);
     }
     for (int j = 0; j < D; ++j) {
@@ -914,6 +929,7 @@ static void kdirection(kern_t *k, const float *g, float *q, float *p)
     const int D = k->D;
     for (int j = 0; j < D; ++j) q[j] = g[j];
     if (k->h > 0 && k->compact) {
+        kpush_compact(k, k->pending, g);
         kdirection_compact(k, g, q);
     } else if (k->h > 0) {
         for (int i = k->h - 1; i >= 0; --i) {
@@ -1217,7 +1233,7 @@ static void fit_problem_kernel(problem_t *P, fit_t *F, const float *C_init, int 
         memcpy(k->ringS + (int64_t)slot * D, sv, vb);
         memcpy(k->ringY + (int64_t)slot * D, yv, vb);
         if (k->compact) {
-            kpush_compact(k, slot);
+            k->pending = slot;  /* the kernel updates the compact history with the next direction */
         } else {
             k->last_sy = kdot_pair(k, yv, sv);
             k->last_yy = kdot_pair(k, yv, yv);
@@ -1298,6 +1314,7 @@ int sro_optimize_shape_f32(const float *X, int64_t N, int64_t nx, const float *Y
             K.rho = calloc((size_t)history, sizeof(f2_t));
             K.alph = calloc((size_t)history, sizeof(f2_t));
             K.compact = history <= 32;
+            K.split = K.compact && history <= 16 && spl == 1;
             K.cd = calloc((size_t)history, sizeof(f2_t));
             K.Rinv = K.compact ? calloc((size_t)history * history, sizeof(f2_t)) : NULL;
             K.YY = K.compact ? calloc((size_t)history * history, sizeof(f2_t)) : NULL;
