@@ -77,6 +77,9 @@ def lib() -> ctypes.CDLL:
         L.sro_node_fwd_f32.restype = None
         L.sro_node_fwd_kf32.argtypes = [i64, vp, vp, vp, vp, vp, vp]
         L.sro_node_fwd_kf32.restype = None
+        L.sro_direction_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp,
+                                        vp, dbl, vp]
+        L.sro_direction_f32.restype = None
         L.sro_fmath_f32.argtypes = [ctypes.c_int, i64, vp, vp]
         L.sro_fmath_f32.restype = None
         L.sro_fmath_error.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp]
@@ -236,6 +239,22 @@ def optimize(X, Y, ops, ch, C_init, max_iter=100, history_size=10, tolerance_gra
                                        int(line_search_max_iter), int(dot_mode), int(warps), int(points_per_lane),
                                        spl, _p(C), _p(Yo), _p(iters), _p(evals), _p(loss))
     return dict(C=C, Y=Yo, iters=iters, evals=evals, loss=loss, err=err)
+
+
+def direction(S, Y, g, history_size, nslots, two_loop=False, eps=1e-10):
+    """The fused kernel's search direction p = -H g after the pairs S, Y (npairs, 32 spl)
+    float32 rows, oldest first) pass through its history ring of history_size pairs:
+    the compact representation (two lanes per pair up to 16 pairs) or, with two_loop or
+    above 32 pairs, the two-loop recursion.  Returns p (32 spl,) float32."""
+    S = _c(S, np.float32)
+    Y = _c(Y, np.float32)
+    g = _c(g, np.float32)
+    n, D = S.shape
+    spl = D // 32
+    p = np.zeros(D, np.float32)
+    lib().sro_direction_f32(int(history_size), int(bool(two_loop)), spl, int(nslots), n, _p(S), _p(Y), _p(g),
+                            float(eps), _p(p))
+    return p
 
 
 def node_fwd(op, a, b, c, x, kernel_math=False):

@@ -952,6 +952,52 @@ static void kdirection(kern_t *k, const float *g, float *q, float *p)
     for (int j = 0; j < D; ++j) p[j] = j < k->nslots ? -q[j] : 0.0f;
 }
 
+/* The fused kernel's search direction for a given history, for tests of its arithmetic:
+ * npairs (s, y) pairs (rows of 32 spl floats, oldest first) go through the kernel's
+ * history ring of `hist` pairs (the oldest dropped when it is full) and its updates,
+ * then p = -H g.  two_loop = 1 forces the two-loop recursion (the kernel's choice for
+ * histories above 32 pairs); otherwise the kernel's choice for `hist`.  nslots slots are
+ * active (the rest of each row is ignored and p is 0 there). */
+void sro_direction_f32(int hist, int two_loop, int spl, int nslots, int npairs, const float *S, const float *Y,
+                       const float *g, double eps, float *p)
+{
+    kern_t K;
+    memset(&K, 0, sizeof(K));
+    K.spl = spl; K.D = 32 * spl; K.nslots = nslots; K.K = nslots; K.hist = hist;
+    K.compact = !two_loop && hist <= 32;
+    K.split = K.compact && hist <= 16 && spl == 1;
+    K.ringS = calloc((size_t)hist * K.D, sizeof(float));
+    K.ringY = calloc((size_t)hist * K.D, sizeof(float));
+    K.rho = calloc((size_t)hist, sizeof(f2_t));
+    K.alph = calloc((size_t)hist, sizeof(f2_t));
+    K.cd = calloc((size_t)hist, sizeof(f2_t));
+    K.Rinv = calloc((size_t)hist * hist, sizeof(f2_t));
+    K.YY = calloc((size_t)hist * hist, sizeof(f2_t));
+    K.eps2 = f2_of_double(eps);
+    float *q = malloc(sizeof(float) * (size_t)K.D);
+    for (int n = 0; n < npairs; ++n) {
+        int slot;
+        if (K.h < K.hist) { slot = (K.head + K.h) % K.hist; K.h++; }
+        else { slot = K.head; K.head = (K.head + 1) % K.hist; }
+        const float *sv = S + (int64_t)n * K.D, *yv = Y + (int64_t)n * K.D;
+        for (int j = 0; j < K.D; ++j) {
+            K.ringS[(int64_t)slot * K.D + j] = j < nslots ? sv[j] : 0.0f;
+            K.ringY[(int64_t)slot * K.D + j] = j < nslots ? yv[j] : 0.0f;
+        }
+        if (K.compact) {
+            /* each pair's update runs before the direction that follows it */
+            K.pending = slot;
+            if (n + 1 < npairs) kpush_compact(&K, slot, g);
+        } else {
+            K.last_sy = kdot_pair(&K, K.ringY + (int64_t)slot * K.D, K.ringS + (int64_t)slot * K.D);
+            K.last_yy = kdot_pair(&K, K.ringY + (int64_t)slot * K.D, K.ringY + (int64_t)slot * K.D);
+            K.rho[slot] = f2_div(f2_mk(1.0f, 0.0f), f2_norm(f2_add(K.last_sy, K.eps2)));
+        }
+    }
+    kdirection(&K, g, q, p);
+    free(q); free(K.ringS); free(K.ringY); free(K.rho); free(K.alph); free(K.cd); free(K.Rinv); free(K.YY);
+}
+
 /* One problem's fit: the closure and dots of the chosen arithmetic behind the
  * reference's control flow.  kevals counts the closures the fused kernel
  * evaluates: it reuses phi(0), phi(alpha_lo) and the accepted trial point, which
