@@ -91,6 +91,97 @@ __global__ void postfix_children_kernel(const int64_t* __restrict__ ops, int64_t
   err[b] = e;
 }
 
+// The same child table for rows of 1..128 tokens and token ids below 32768, with the
+// CTA's rows staged through shared memory: the CTA reads its 128 rows and writes their
+// child tables with coalesced 8-byte accesses (consecutive threads, consecutive
+// elements), and each thread's stack and table sit in shared memory instead of local
+// memory (an M-token row never holds more than M entries on the stack).  Symbols are
+// staged as -1 (negative) or -2 (too large) when they fail the check.
+constexpr int kChildThreads = 128;
+
+__global__ void __launch_bounds__(kChildThreads) postfix_children_staged_kernel(
+    const int64_t* __restrict__ ops, int64_t B, int64_t M, int64_t n_operators, int64_t* __restrict__ ch,
+    int64_t* __restrict__ err) {
+  extern __shared__ int16_t csm[];
+  const int t = threadIdx.x, Mi = (int)M;
+  int16_t* in = csm;                                   // [M][kChildThreads]
+  int16_t* stk = csm + Mi * kChildThreads;             // [M][kChildThreads]
+  int16_t* tab = csm + 2 * Mi * kChildThreads;         // [2 M][kChildThreads]
+  const int64_t b0 = (int64_t)blockIdx.x * kChildThreads;
+  const int rows = (int)(B - b0 < kChildThreads ? B - b0 : kChildThreads);
+  // element j of the block is token j % M of row j / M; (row, token) advance by
+  // (kChildThreads / M, kChildThreads % M) with a carry
+  {
+    const int total = rows * Mi, dr = kChildThreads / Mi, di = kChildThreads % Mi;
+    int r = t / Mi, i = t - r * Mi;
+#pragma unroll 4
+    for (int j = t; j < total; j += kChildThreads) {
+      const int64_t tok = ops[b0 * M + j];
+      in[i * kChildThreads + r] = (int16_t)(tok < 0 ? -1 : (tok >= n_operators ? -2 : tok));
+      r += dr;
+      i += di;
+      if (i >= Mi) {
+        i -= Mi;
+        ++r;
+      }
+    }
+  }
+  for (int i = 0; i < 2 * Mi; ++i) tab[i * kChildThreads + t] = -1;
+  __syncthreads();
+  if (t < rows) {
+    int64_t e = 0;
+    for (int i = 0; i < Mi; ++i) {
+      const int v = in[i * kChildThreads + t];
+      if (v == -1) {
+        e = SYM_NEGATIVE;
+        break;
+      }
+      if (v == -2) e = SYM_TOO_LARGE;
+    }
+    if (!e) {
+      int sp = 0;
+      bool ended = false;
+      for (int i = 0; i < Mi; ++i) {
+        const int tok = in[i * kChildThreads + t];
+        if (tok == NO_OP) {
+          ended = true;
+          continue;
+        }
+        if (ended) { e = PARSE_UNEXPECTED_TOKEN; break; }
+        const int ar = arity_of(tok);
+        if (ar == 1) {
+          if (sp < 1) { e = PARSE_UNARY_MISSING; break; }
+          tab[(2 * i) * kChildThreads + t] = stk[(--sp) * kChildThreads + t];
+        } else if (ar == 2) {
+          if (sp < 2) { e = PARSE_BINARY_MISSING; break; }
+          const int16_t right = stk[(--sp) * kChildThreads + t];
+          const int16_t left = stk[(--sp) * kChildThreads + t];
+          tab[(2 * i) * kChildThreads + t] = left;
+          tab[(2 * i + 1) * kChildThreads + t] = right;
+        }
+        stk[(sp++) * kChildThreads + t] = (int16_t)i;  // sp <= i + 1 <= M <= kStackLimit
+      }
+      if (!e && sp != 1) e = PARSE_MALFORMED;
+    }
+    err[b0 + t] = e;
+  }
+  __syncthreads();
+  {
+    const int M2 = 2 * Mi, total = rows * M2, dr = kChildThreads / M2, di = kChildThreads % M2;
+    int r = t / M2, i = t - r * M2;
+#pragma unroll 4
+    for (int j = t; j < total; j += kChildThreads) {
+      ch[b0 * 2 * M + j] = tab[i * kChildThreads + r];
+      r += dr;
+      i += di;
+      if (i >= M2) {
+        i -= M2;
+        ++r;
+      }
+    }
+  }
+}
+
 // Right-to-left rendering: the output is built backwards from the end of a
 // 3 x 128 buffer.  An operator first emits ")" (and, for (x)^k forms, its own
 // token); once its right operand is complete a binary operator emits itself, once
@@ -384,9 +475,20 @@ int sr_postfix_children(const int64_t* ops, int64_t B, int64_t M, int32_t n_vars
     return SR_ERR_INVALID_ARGUMENT;
   }
   if (B == 0) return SR_OK;
+  const int64_t n_operators = (int64_t)VAR + n_vars;
+  if (M >= 1 && M <= kStackLimit && n_operators <= 32767) {
+    const size_t smem = (size_t)4 * M * kChildThreads * sizeof(int16_t);
+    int rc = cuda_check(cudaFuncSetAttribute(postfix_children_staged_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "smem");
+    if (rc) return rc;
+    postfix_children_staged_kernel<<<(unsigned)((B + kChildThreads - 1) / kChildThreads), kChildThreads, smem,
+                                     as_stream(stream)>>>(ops, B, M, n_operators, ch, err);
+    return launch_check("postfix_children_staged_kernel");
+  }
   const int threads = 128;
   postfix_children_kernel<<<(unsigned)((B + threads - 1) / threads), threads, 0, as_stream(stream)>>>(
-      ops, B, M, (int64_t)VAR + n_vars, ch, err);
+      ops, B, M, n_operators, ch, err);
   return launch_check("postfix_children_kernel");
 }
 

@@ -3,8 +3,9 @@
 // The sampler draws expressions from a probabilistic context-free grammar given as
 // the reference's CSR tables (src/pcfg.cpp:364-451): rules sorted by left-hand
 // side, nt_rule_ptr[s] .. nt_rule_ptr[s + 1] the rules of symbol s, their cumulative
-// probabilities, and the concatenated right-hand sides.  One thread derives one
-// expression (the derivation is sequential), leftmost first with an explicit stack,
+// probabilities, and the concatenated right-hand sides.  A lane derives one expression
+// at a time (the derivation is sequential; persistent warps hand a finished lane the
+// next expression), leftmost first with an explicit stack,
 // exactly as the reference's sample_infix_kernel (src/pcfg_cuda.cu:10-118) does: a
 // try restarts when the stack would exceed 128 symbols or the output would exceed
 // the padded length, and after max_tries failed tries the expression reports 303.
@@ -67,39 +68,65 @@ __global__ void __launch_bounds__(kThreads) sample_infix_kernel(
     const int32_t* __restrict__ nt_ptr, const float* __restrict__ cum, const int32_t* __restrict__ rhs_ptr,
     const int32_t* __restrict__ rhs, int32_t n_symbols, int32_t start, int64_t B, int32_t max_len,
     int32_t max_tries, uint64_t seed, int64_t* __restrict__ out, int64_t* __restrict__ errors) {
+  // Persistent warps: warp w owns expressions [w per, (w + 1) per).  Every lane works on
+  // one expression and advances it by one symbol per loop turn (the same few branches in
+  // every lane); a lane whose expression is finished writes its row and takes the next
+  // expression of the warp's range.  So a warp pays for the sum of its lanes' work, not for
+  // 32 times its longest derivation (its tries included).  The draws of expression b come
+  // from its own stream, so the assignment of expressions to lanes changes no output.
   extern __shared__ int16_t sm[];
-  int16_t* stack = sm;                   // [kHardMax][kThreads]
+  const int t = threadIdx.x, lane = t & 31;
+  int16_t* stack = sm;                      // [kHardMax][kThreads]
   int16_t* buf = sm + kHardMax * kThreads;  // [max_len][kThreads]
-  const int t = threadIdx.x;
-  const int64_t b0 = (int64_t)blockIdx.x * kThreads;
-  const int64_t b = b0 + t;
-  int len = 0;
-  if (b < B) {
-    Stream rng(seed, (uint64_t)b);
-    int err = 0;
-    bool done = false;
-    for (int tr = 0; tr < max_tries && !done && !err; ++tr) {
+  const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
+  const int64_t w = (int64_t)blockIdx.x * (kThreads / 32) + (t >> 5);
+  const int64_t per = (B + nwarps - 1) / nwarps;
+  const int64_t wbeg = w * per < B ? w * per : B, wend = wbeg + per < B ? wbeg + per : B;
+  const unsigned below = (1u << lane) - 1u;
+  int64_t b = wbeg + lane;
+  int64_t next = wbeg + 32;
+  bool active = b < wend;
+  Stream rng(seed, (uint64_t)(active ? b : 0));
+  int tries = 0, sp = 0, len = 0, err = 0;
+  bool fin = false;
+  // a new expression: its first try (or 303 at once when no try is allowed)
+  auto begin = [&]() {
+    rng = Stream(seed, (uint64_t)b);
+    tries = 0;
+    err = 0;
+    len = 0;
+    sp = 0;
+    fin = false;
+    if (max_tries <= 0) {
+      err = GEN_MAX_TRIES;
+      fin = true;
+    } else {
+      stack[t] = (int16_t)start;
+      sp = 1;
+    }
+  };
+  if (active) begin();
+  while (__any_sync(0xffffffffu, active)) {
+    if (active && !fin) {
+      // one symbol of the derivation, leftmost first
       bool restart = false;
-      int sp = 0;
-      len = 0;
-      stack[(sp++) * kThreads + t] = (int16_t)start;
-      while (sp > 0) {
-        const int sym = stack[(--sp) * kThreads + t];
-        const int r0 = sym < n_symbols ? nt_ptr[sym] : 0;
-        const int r1 = sym < n_symbols ? nt_ptr[sym + 1] : 0;
-        if (r0 != r1) {  // a non-terminal: choose a rule, push its right-hand side reversed
-          const float u = rng.uniform();
-          int chosen = -1;
-          for (int r = r0; r < r1; ++r) {
-            if (u <= cum[r]) {
-              chosen = r;
-              break;
-            }
-          }
-          if (chosen < 0) {
-            err = GEN_NO_RULE;
+      const int sym = stack[(--sp) * kThreads + t];
+      const int r0 = sym < n_symbols ? nt_ptr[sym] : 0;
+      const int r1 = sym < n_symbols ? nt_ptr[sym + 1] : 0;
+      if (r0 != r1) {  // a non-terminal: choose a rule, push its right-hand side reversed
+        const float u = rng.uniform();
+        int chosen = -1;
+        for (int r = r0; r < r1; ++r) {
+          if (u <= cum[r]) {
+            chosen = r;
             break;
           }
+        }
+        if (chosen < 0) {
+          err = GEN_NO_RULE;
+          len = 0;
+          fin = true;
+        } else {
           for (int i = rhs_ptr[chosen + 1] - 1; i >= rhs_ptr[chosen]; --i) {
             if (sp >= kHardMax) {
               restart = true;
@@ -107,28 +134,41 @@ __global__ void __launch_bounds__(kThreads) sample_infix_kernel(
             }
             stack[(sp++) * kThreads + t] = (int16_t)rhs[i];
           }
-          if (restart) break;
-        } else {  // a terminal: emit it
-          if (len >= max_len) {
-            restart = true;
-            break;
-          }
-          buf[(len++) * kThreads + t] = (int16_t)sym;
+        }
+      } else if (len >= max_len) {  // a terminal past the padded length
+        restart = true;
+      } else {  // a terminal: emit it
+        buf[(len++) * kThreads + t] = (int16_t)sym;
+      }
+      // a try ends: restarted, or derived completely (an empty derivation fails too)
+      if (!fin && (restart || sp == 0)) {
+        if (!restart && len > 0) {
+          fin = true;
+        } else if (++tries >= max_tries) {
+          err = GEN_MAX_TRIES;
+          len = 0;
+          fin = true;
+        } else {
+          stack[t] = (int16_t)start;
+          sp = 1;
+          len = 0;
         }
       }
-      if (!restart && !err && len > 0) done = true;
     }
-    if (!done && !err) err = GEN_MAX_TRIES;
-    if (!done) len = 0;
-    errors[b] = err;
-  }
-  for (int i = len; i < max_len; ++i) buf[i * kThreads + t] = (int16_t)NO_OP;
-  __syncthreads();
-  // the CTA's rows are one contiguous block of the output
-  const int64_t rows = B - b0 < kThreads ? B - b0 : kThreads;
-  for (int64_t j = t; j < rows * max_len; j += kThreads) {
-    const int64_t r = j / max_len, i = j - r * max_len;
-    out[b0 * max_len + j] = buf[i * kThreads + r];
+    const bool done = active && fin;
+    if (done) {
+      int64_t* row = out + b * max_len;
+      for (int i = 0; i < len; ++i) row[i] = buf[i * kThreads + t];
+      for (int i = len; i < max_len; ++i) row[i] = NO_OP;
+      errors[b] = err;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, done);
+    if (done) {
+      b = next + __popc(m & below);
+      active = b < wend;
+      if (active) begin();
+    }
+    next += __popc(m);
   }
 }
 
@@ -161,14 +201,25 @@ __global__ void __launch_bounds__(kThreads) infix_parse_kernel(const int64_t* __
   const int64_t b0 = (int64_t)blockIdx.x * kThreads;
   const int64_t rows = B - b0 < kThreads ? B - b0 : kThreads;
   const int64_t lp = VAR + n_vars, rp = lp + 1, limit = rp + 1;
-  // tokens outside [0, limit) are staged as -1 (negative) or -2 (too large)
+  // tokens outside [0, limit) are staged as -1 (negative) or -2 (too large).  Element j
+  // of the CTA's block is token i = j % M of row r = j / M; j advances by kThreads, so
+  // (r, i) advance by (kThreads / M, kThreads % M) with a carry (no division per token).
   int bad = 0;
-  for (int64_t j = t; j < rows * M; j += kThreads) {
-    const int64_t r = j / M, i = j - r * M;
+  const int Mi = M > 0 ? (int)M : 1, total = (int)(rows * M);  // M = 0: no element
+  const int dr = kThreads / Mi, di = kThreads % Mi;
+  int r = t / Mi, i = t - (t / Mi) * Mi;
+#pragma unroll 4
+  for (int j = t; j < total; j += kThreads) {
     const int64_t tok = infix[b0 * M + j];
     int16_t v = (int16_t)tok;
     if (tok < 0 || tok >= limit) v = (int16_t)(tok < 0 ? -1 : -2);
     row[i * kThreads + r] = v;
+    r += dr;
+    i += di;
+    if (i >= Mi) {
+      i -= Mi;
+      ++r;
+    }
   }
   __syncthreads();
   const int64_t b = b0 + t;
@@ -263,9 +314,17 @@ __global__ void __launch_bounds__(kThreads) infix_parse_kernel(const int64_t* __
     }
   }
   __syncthreads();
-  for (int64_t j = t; j < rows * M; j += kThreads) {
-    const int64_t r = j / M, i = j - r * M;
+  r = t / Mi;
+  i = t - r * Mi;
+#pragma unroll 4
+  for (int j = t; j < total; j += kThreads) {
     outp[b0 * M + j] = row[i * kThreads + r];
+    r += dr;
+    i += di;
+    if (i >= Mi) {
+      i -= Mi;
+      ++r;
+    }
   }
 }
 
@@ -325,7 +384,17 @@ int sr_pcfg_sample_infix(const int32_t* nt_rule_ptr, const float* nt_rule_cum_pr
   int rc = cuda_check(cudaFuncSetAttribute(sample_infix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                       "smem");
   if (rc) return rc;
-  const int64_t blocks = (B + kThreads - 1) / kThreads;
+  // persistent grid: the CTAs that fit at once, or fewer when B is small
+  int dev = 0, sms = 0, per_sm = 0;
+  rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  if (!rc)
+    rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sample_infix_kernel, kThreads, smem),
+                    "occupancy");
+  if (rc) return rc;
+  int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+  const int64_t need = (B + kThreads - 1) / kThreads;
+  if (blocks > need) blocks = need;
   sample_infix_kernel<<<(unsigned)blocks, kThreads, smem, as_stream(stream)>>>(
       nt_rule_ptr, nt_rule_cum_probs, rhs_ptr, rhs_concat, n_symbols, start_symbol, B, max_length, max_tries, seed,
       out, errors);
