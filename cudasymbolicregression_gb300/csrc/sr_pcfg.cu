@@ -156,13 +156,20 @@ __global__ void __launch_bounds__(kThreads) sample_infix_kernel(
       }
     }
     const bool done = active && fin;
-    if (done) {
-      int64_t* row = out + b * max_len;
-      for (int i = 0; i < len; ++i) row[i] = buf[i * kThreads + t];
-      for (int i = len; i < max_len; ++i) row[i] = NO_OP;
-      errors[b] = err;
-    }
     const unsigned m = __ballot_sync(0xffffffffu, done);
+    // the warp writes the rows finished in this turn together, one row at a time, its
+    // lanes on consecutive tokens (coalesced), while no lane waits on another's row
+    if (m) __syncwarp();  // the finished rows' tokens, written by their lanes
+    for (unsigned mm = m; mm; mm &= mm - 1) {
+      const int src = __ffs(mm) - 1;
+      const int64_t bs = __shfl_sync(0xffffffffu, b, src);
+      const int ls = __shfl_sync(0xffffffffu, len, src);
+      const int es = __shfl_sync(0xffffffffu, err, src);
+      const int ts = (t & ~31) + src;
+      for (int i = lane; i < max_len; i += 32) out[bs * max_len + i] = i < ls ? (int64_t)buf[i * kThreads + ts] : NO_OP;
+      if (lane == 0) errors[bs] = es;
+    }
+    if (m) __syncwarp();  // read before their lanes start the next expressions
     if (done) {
       b = next + __popc(m & below);
       active = b < wend;
