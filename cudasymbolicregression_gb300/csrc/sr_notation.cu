@@ -96,7 +96,9 @@ __global__ void postfix_children_kernel(const int64_t* __restrict__ ops, int64_t
 // child tables with coalesced 8-byte accesses (consecutive threads, consecutive
 // elements), and each thread's stack and table sit in shared memory instead of local
 // memory (an M-token row never holds more than M entries on the stack).  Symbols are
-// staged as -1 (negative) or -2 (too large) when they fail the check.
+// staged as -1 (negative) or -2 (too large) when they fail the check.  The left child of
+// position i replaces its token once the token has been read; positions the scan does
+// not reach (after an error) are set to -1 at the end, as the table starts all -1.
 constexpr int kChildThreads = 128;
 
 __global__ void __launch_bounds__(kChildThreads) postfix_children_staged_kernel(
@@ -104,9 +106,9 @@ __global__ void __launch_bounds__(kChildThreads) postfix_children_staged_kernel(
     int64_t* __restrict__ err) {
   extern __shared__ int16_t csm[];
   const int t = threadIdx.x, Mi = (int)M;
-  int16_t* in = csm;                                   // [M][kChildThreads]
-  int16_t* stk = csm + Mi * kChildThreads;             // [M][kChildThreads]
-  int16_t* tab = csm + 2 * Mi * kChildThreads;         // [2 M][kChildThreads]
+  int16_t* in = csm;                            // [M][kChildThreads]: tokens, then left children
+  int16_t* rt = csm + Mi * kChildThreads;       // [M][kChildThreads]: right children
+  int16_t* stk = csm + 2 * Mi * kChildThreads;  // [M][kChildThreads]
   const int64_t b0 = (int64_t)blockIdx.x * kChildThreads;
   const int rows = (int)(B - b0 < kChildThreads ? B - b0 : kChildThreads);
   // element j of the block is token j % M of row j / M; (row, token) advance by
@@ -126,7 +128,6 @@ __global__ void __launch_bounds__(kChildThreads) postfix_children_staged_kernel(
       }
     }
   }
-  for (int i = 0; i < 2 * Mi; ++i) tab[i * kChildThreads + t] = -1;
   __syncthreads();
   if (t < rows) {
     int64_t e = 0;
@@ -138,30 +139,38 @@ __global__ void __launch_bounds__(kChildThreads) postfix_children_staged_kernel(
       }
       if (v == -2) e = SYM_TOO_LARGE;
     }
+    int stop = 0;  // positions from here on keep no children
     if (!e) {
       int sp = 0;
       bool ended = false;
-      for (int i = 0; i < Mi; ++i) {
+      int i = 0;
+      for (; i < Mi; ++i) {
         const int tok = in[i * kChildThreads + t];
+        int16_t left = -1, right = -1;
         if (tok == NO_OP) {
           ended = true;
-          continue;
+        } else {
+          if (ended) { e = PARSE_UNEXPECTED_TOKEN; break; }
+          const int ar = arity_of(tok);
+          if (ar == 1) {
+            if (sp < 1) { e = PARSE_UNARY_MISSING; break; }
+            left = stk[(--sp) * kChildThreads + t];
+          } else if (ar == 2) {
+            if (sp < 2) { e = PARSE_BINARY_MISSING; break; }
+            right = stk[(--sp) * kChildThreads + t];
+            left = stk[(--sp) * kChildThreads + t];
+          }
+          stk[(sp++) * kChildThreads + t] = (int16_t)i;  // sp <= i + 1 <= M <= kStackLimit
         }
-        if (ended) { e = PARSE_UNEXPECTED_TOKEN; break; }
-        const int ar = arity_of(tok);
-        if (ar == 1) {
-          if (sp < 1) { e = PARSE_UNARY_MISSING; break; }
-          tab[(2 * i) * kChildThreads + t] = stk[(--sp) * kChildThreads + t];
-        } else if (ar == 2) {
-          if (sp < 2) { e = PARSE_BINARY_MISSING; break; }
-          const int16_t right = stk[(--sp) * kChildThreads + t];
-          const int16_t left = stk[(--sp) * kChildThreads + t];
-          tab[(2 * i) * kChildThreads + t] = left;
-          tab[(2 * i + 1) * kChildThreads + t] = right;
-        }
-        stk[(sp++) * kChildThreads + t] = (int16_t)i;  // sp <= i + 1 <= M <= kStackLimit
+        in[i * kChildThreads + t] = left;
+        rt[i * kChildThreads + t] = right;
       }
+      stop = i;
       if (!e && sp != 1) e = PARSE_MALFORMED;
+    }
+    for (int i = stop; i < Mi; ++i) {
+      in[i * kChildThreads + t] = -1;
+      rt[i * kChildThreads + t] = -1;
     }
     err[b0 + t] = e;
   }
@@ -171,7 +180,8 @@ __global__ void __launch_bounds__(kChildThreads) postfix_children_staged_kernel(
     int r = t / M2, i = t - r * M2;
 #pragma unroll 4
     for (int j = t; j < total; j += kChildThreads) {
-      ch[b0 * 2 * M + j] = tab[i * kChildThreads + r];
+      const int16_t* src = (i & 1) ? rt : in;
+      ch[b0 * 2 * M + j] = src[(i >> 1) * kChildThreads + r];
       r += dr;
       i += di;
       if (i >= M2) {
@@ -477,7 +487,7 @@ int sr_postfix_children(const int64_t* ops, int64_t B, int64_t M, int32_t n_vars
   if (B == 0) return SR_OK;
   const int64_t n_operators = (int64_t)VAR + n_vars;
   if (M >= 1 && M <= kStackLimit && n_operators <= 32767) {
-    const size_t smem = (size_t)4 * M * kChildThreads * sizeof(int16_t);
+    const size_t smem = (size_t)3 * M * kChildThreads * sizeof(int16_t);
     int rc = cuda_check(cudaFuncSetAttribute(postfix_children_staged_kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                         "smem");

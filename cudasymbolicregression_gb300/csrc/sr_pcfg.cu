@@ -203,7 +203,12 @@ __global__ void __launch_bounds__(kThreads) infix_parse_kernel(const int64_t* __
   const int cap = (int)M;
   int16_t* row = sm;                    // [M][kThreads]: the input, then the output
   int16_t* ops = sm + M * kThreads;     // [M][kThreads] operator stack
-  int16_t* queue = ops + M * kThreads;  // [M][kThreads] output queue
+  // [M][kThreads] output queue.  To postfix the queue lives in the row itself: every
+  // queued token was read before (operands when read, operators after, parentheses
+  // never), so the queue never holds more tokens than the scan has read and each write
+  // lands on a token already consumed.  To prefix the scan runs from the right end and
+  // the queue from the left, so it has its own array.
+  int16_t* queue = kPrefix ? ops + M * kThreads : row;
   const int t = threadIdx.x;
   const int64_t b0 = (int64_t)blockIdx.x * kThreads;
   const int64_t rows = B - b0 < kThreads ? B - b0 : kThreads;
@@ -353,7 +358,8 @@ static int launch_parse(const int64_t* infix, int64_t B, int64_t M, int32_t n_va
   if (n_vars < 0 || n_vars > SR_MAX_VARS) { set_error("n_vars out of range (%d)", n_vars); return SR_ERR_UNSUPPORTED; }
   if (B == 0) return SR_OK;
   if (!errors || (M > 0 && (!infix || !outp))) { set_error("null pointer argument"); return SR_ERR_INVALID_ARGUMENT; }
-  const size_t smem = (size_t)(3 * M > 0 ? 3 * M : 1) * kThreads * sizeof(int16_t);
+  const int64_t arrays = kPrefix ? 3 : 2;  // row, operator stack (, queue)
+  const size_t smem = (size_t)(arrays * M > 0 ? arrays * M : 1) * kThreads * sizeof(int16_t);
   auto kern = infix_parse_kernel<kPrefix>;
   int rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem");
   if (rc) return rc;
