@@ -6,12 +6,15 @@ src/pcfg.cpp:1006-1061): the constructor parses the grammar text on the host wit
 the reference's symbol table, rules and error messages and builds its CSR tables
 (rules sorted by left-hand side, cumulative probabilities per non-terminal, the
 concatenated right-hand sides), which then live on the device.  ``sample_infix``
-draws expressions with one CUDA thread per expression (``sr_pcfg_sample_infix``);
+draws expressions on the device, each lane deriving one expression at a time
+(``sr_pcfg_sample_infix``);
 ``infix_to_postfix`` / ``infix_to_prefix`` run the shunting-yard on the device
 (``sr_infix_to_postfix`` / ``sr_infix_to_prefix``); ``get_postfix_children`` and
 ``postfix_to_infix`` are the kernels of :mod:`.notation`.  ``sample(B)`` chains
 sampling, parsing and the child table on the device with one host
-synchronisation at the end, which is what a search loop feeds to the fit.
+synchronisation at the end (a two-number summary of the error words per kernel; the
+words themselves are copied only to report an error), which is what a search loop
+feeds to the fit.
 
 Random numbers: one SplitMix64 stream per expression from a 64-bit seed drawn
 from torch's default generator, so ``torch.manual_seed`` fixes the samples (the
@@ -282,6 +285,13 @@ class ProbabilisticContextFreeGrammar:
                 msg += f"  {error_message(code)}: {counts[code]} occurrences.\n"
             raise RuntimeError(msg)
 
+    @staticmethod
+    def _any_error(errs: torch.Tensor) -> bool:
+        """Whether any per-row error word is nonzero, from the smallest and largest word of
+        each row of errs (one small device-to-host copy instead of all B words)."""
+        lo, hi = torch.aminmax(errs, dim=-1)
+        return bool(torch.stack((lo, hi)).ne(0).any().cpu())
+
     def sample_infix(self, B: int) -> torch.Tensor:
         """(B, padded_maximum_length) int64 infix token rows, NO_OP padded."""
         B = int(B)
@@ -289,7 +299,8 @@ class ProbabilisticContextFreeGrammar:
         err = torch.empty(B, dtype=torch.int64, device=self._device)
         if B:
             self._launch_sample(B, out, err)
-            self._generation_error(err.cpu())
+            if self._any_error(err):  # the full words only to report them
+                self._generation_error(err.cpu())
         return out
 
     def sample(self, B: int):
@@ -311,10 +322,11 @@ class ProbabilisticContextFreeGrammar:
                                            _lib.ptr(errs[1]), st), "sr_infix_to_postfix")
         _lib.check(lib.sr_postfix_children(_lib.ptr(post), B, L, self._n_variables, _lib.ptr(ch), _lib.ptr(errs[2]),
                                            st), "sr_postfix_children")
-        e = errs.cpu()
-        self._generation_error(e[0])
-        self._parsing_error(e[1], infix, "postfix parsing", 0, "infix_ops")
-        self._parsing_error(e[2], post, "get postfix children", 0, "postfix_ops")
+        if self._any_error(errs):  # the full words only to report them
+            e = errs.cpu()
+            self._generation_error(e[0])
+            self._parsing_error(e[1], infix, "postfix parsing", 0, "infix_ops")
+            self._parsing_error(e[2], post, "get postfix children", 0, "postfix_ops")
         return post, ch
 
     # ---- parsing and conversions -------------------------------------------------------
