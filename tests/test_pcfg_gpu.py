@@ -65,6 +65,34 @@ def test_sampler_batch_edges():
         np.testing.assert_array_equal(got, want)
 
 
+@pytest.mark.parametrize("length,max_tries,B", [(7, 3, 5000), (7, 0, 777), (32, 64, 33), (12, 2, 100003),
+                                                 (5, 1, 4097)])
+def test_sampler_rows_and_error_codes_through_the_c_abi(length, max_tries, B):
+    """Every row and every error word of the C ABI equal the oracle's, failed expressions
+    included (rows of NO_OP, 303 after max_tries failed tries, 303 at once for
+    max_tries = 0): the sampler's lanes take the expressions of their warp's range one
+    after another, so batch sizes that leave ragged ranges are covered too."""
+    from cudasymbolicregression_gb300 import _lib
+    p = _pcfg(README_GRAMMAR, "E", 1, length, max_tries=max(max_tries, 1))
+    nt, cum, rp, rc = p._tables
+    start = p.get_symbol_id("E")
+    seed = 0x5EED1234ABCDEF
+    out = torch.full((B, length), 77, dtype=torch.int64, device="cuda")
+    err = torch.full((B,), 77, dtype=torch.int64, device="cuda")
+    L = _lib.lib()
+    _lib.check(L.sr_pcfg_sample_infix(_lib.ptr(nt), _lib.ptr(cum), _lib.ptr(rp), _lib.ptr(rc), int(nt.numel() - 1),
+                                      start, B, length, max_tries, seed, _lib.ptr(out), _lib.ptr(err),
+                                      _lib.stream_ptr(torch.device("cuda"))), "sr_pcfg_sample_infix")
+    want, want_err = oracle.pcfg_sample(p._tables_np, start, B, length, max_tries, seed)
+    got_err = err.cpu().numpy()
+    np.testing.assert_array_equal(got_err, want_err)
+    np.testing.assert_array_equal(out.cpu().numpy(), want)
+    if max_tries == 0:
+        assert (got_err == 303).all()
+    elif length == 7:
+        assert 0 < (got_err == 303).sum() < B  # some expressions fail, most do not
+
+
 def test_reference_sampling_patterns(g):
     """tests/test_sampling.py of the reference: one-rule grammars, 50/50 rules, and
     the max_tries error."""
