@@ -51,6 +51,12 @@ wall-clock to the first MSE < 1e-6 and expressions fitted/s over all rounds.
 --workload sample (the grammar object feeding a search): B=1048576 expressions drawn
 from a 17-rule grammar (infix padded to --N=64 tokens), parsed to postfix and linked
 (child table) on the device, one host synchronisation per step; value = expressions/s.
+--workload gemm: the warm-start network's tensor-core GEMM (sr_mlp_gemm) at a size where
+its efficiency shows: D (--B=262144 rows x 256) = A (262144 x --N=4096) . W (256 x 4096)^T
+in bf16 with fp32 accumulation and a bf16 epilogue, 512 of them back to back per step;
+value = TFLOP/s (2 rows n k per GEMM), roofline against the measured bf16 peak (a
+256-wide product reads each A element for 512 flops, so the shape sits at the ridge of
+the bf16 and HBM roofs).
 --impl reference runs only the CPU port (the reference's own CPU path, restated).
 Multi-GPU: one process per GPU; every rank fits its own batch (independent seeds, no
 collective), value = all problems / max time over ranks.
@@ -78,8 +84,11 @@ M_DEFAULT = 64
 MAX_ITER = 200
 EVAL_METRIC = "evaluation forward+adjoint throughput (algorithmic HBM bytes)"
 DEFAULTS = {"warmstart": (65536, 512), "ragged": (16384, 512), "readme": (65536, 100), "eval": (65536, 1024),
-            "search": (262144, 2048), "sample": (1048576, 64)}
+            "search": (262144, 2048), "sample": (1048576, 64), "gemm": (262144, 4096)}
 SAMPLE_METRIC = "expressions sampled from a grammar, parsed to postfix and linked (child table) per second"
+GEMM_METRIC = "warm-start network GEMM throughput on the tensor cores (tcgen05, bf16 operands, fp32 accumulation)"
+GEMM_N = 256  # the network's widest layer
+GEMM_REPS = 512  # GEMMs per step of the gemm workload (a step long enough to sample its clocks)
 
 # DRAM bytes (read + write) of one launch of the dominant kernel on the default
 # workloads, from ncu captures of a 4x / 16x smaller batch scaled by the number of
@@ -232,6 +241,10 @@ def run_reference(args, rank):
     if rank != 0:
         return
     B, N = args.B, args.N
+    if args.workload == "gemm":
+        print(json.dumps({"impl": "reference", "unavailable": "the warm-start network has no counterpart in the "
+                          "reference"}), flush=True)
+        return
     if args.workload == "sample":
         n = min(B, args.cpu_sample_expr)
         vals = []
@@ -995,6 +1008,112 @@ def run_sample(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_gemm(args, rank, world, local):
+    import ctypes
+    from cudasymbolicregression_gb300 import _lib
+
+    dev = torch.device("cuda", local)
+    rows, k, n = args.B, args.N, GEMM_N
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 1000 * rank)
+    A = (torch.randn((rows, k), generator=g, device=dev) * 0.1).to(torch.bfloat16)
+    W = (torch.randn((n, k), generator=g, device=dev) * 0.1).to(torch.bfloat16)
+    out = torch.empty((rows, n), dtype=torch.bfloat16, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    L, st = _lib.lib(), _lib.stream_ptr(dev)
+    epi = _lib.MlpEpilogue()
+    epi.epilogue = _lib.MLP_EPI_LINEAR
+    epi.ld_out = n
+
+    def gemm(a, w, o):
+        epi.out = o.data_ptr()
+        _lib.check(L.sr_mlp_gemm(ctypes.c_void_p(a.data_ptr()), rows, k, k, ctypes.c_void_p(w.data_ptr()), n, k,
+                                 ctypes.byref(epi), ctypes.c_void_p(status.data_ptr()), st), "sr_mlp_gemm")
+
+    for _ in range(args.warmup):
+        for _r in range(GEMM_REPS):
+            gemm(A, W, out)
+    torch.cuda.synchronize()
+    # a block of rows against torch's product of the same bf16 operands (fp32 accumulation;
+    # the outputs are rounded to bf16)
+    ref = A[:1024].float() @ W.float().T
+    rel = float((out[:1024].float() - ref).abs().max() / ref.abs().max())
+    assert int(status.item()) == 0 and rel < 1e-2, (int(status.item()), rel)
+    flops = 2.0 * rows * n * k
+    nbytes = 2.0 * (rows * k + n * k + rows * n)
+    barrier(world)
+    torch.cuda.synchronize()
+    evs = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _r in range(GEMM_REPS):
+                gemm(A, W, out)
+            e1.record()
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+    barrier(world)
+    t_step = max_over_ranks(statistics.mean(a.elapsed_time(b) / 1000.0 for a, b in evs), world, dev)
+    t = t_step / GEMM_REPS  # one GEMM
+    value = flops * world / t / 1e12
+
+    e2e = None
+    if not args.no_e2e:
+        hA, hW = A.cpu().pin_memory(), W.cpu().pin_memory()
+        hO = torch.empty((rows, n), dtype=torch.bfloat16).pin_memory()
+        ts = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            a_d, w_d = hA.to(dev, non_blocking=True), hW.to(dev, non_blocking=True)
+            gemm(a_d, w_d, out)
+            hO.copy_(out, non_blocking=True)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        e2e = {"value": flops * world / statistics.median(ts) / 1e12, "unit": "TFLOP/s",
+               "h2d_bytes_per_step": int(2 * (rows * k + n * k)), "d2h_bytes_per_step": int(2 * rows * n),
+               "path": "one sr_mlp_gemm with A and W copied from pinned host memory and D copied back"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # numpy's float32 matmul (the host BLAS, all cores) of the first 8192 rows
+        m = min(rows, 8192)
+        a32, w32 = A[:m].float().cpu().numpy(), W.float().cpu().numpy()
+        a32 @ w32.T
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 3.0:
+            a32 @ w32.T
+            reps += 1
+        dt = (time.perf_counter() - t0) / reps
+        cpu = {"value": 2.0 * m * n * k / dt / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"numpy float32 matmul of {m} x {k} by {k} x {n} ({reps} repetitions)"}
+
+    if rank == 0:
+        pk, pk_kind = peaks()
+        peak = float(pk["bf16_tflops"])
+        hbm = float(pk["hbm_gbs"])
+        line = {"metric": GEMM_METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+                "config": {"workload": f"D ({rows} x {n}) = A ({rows} x {k}) . W ({n} x {k})^T, bf16 operands, "
+                                       "fp32 accumulation, bf16 output", "rows": rows, "k": k, "n": n,
+                           "l2": f"inputs larger than L2 ({rows * k * 2 / 1e9:.1f} GB of A)",
+                           "gemms_per_step": GEMM_REPS, "ms_per_gemm": t * 1000.0,
+                           "max_rel_err_first_1024_rows": rel},
+                "roofline": {"bound": "tensor", "achieved": value, "peak": peak, "unit": "TFLOP/s",
+                             "frac": value / peak, "traffic": None, "kernel": "mlp::gemm_kernel<256>",
+                             "peak_kind": pk_kind + " (bf16 burst)",
+                             "hbm": {"GB/s": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm}},
+                "gpu_launches": args.steps * GEMM_REPS, "clocks": clk.summary()}
+        if e2e:
+            line["e2e"] = e2e
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1037,6 +1156,8 @@ def main():
         run_search(args, rank, world, local)
     elif args.workload == "sample":
         run_sample(args, rank, world, local)
+    elif args.workload == "gemm":
+        run_gemm(args, rank, world, local)
     else:
         run_fit(args, rank, world, local)
     if world > 1:
