@@ -365,6 +365,26 @@ def fit_quality(r, ref_finite, max_iter, step_s=None):
     return q
 
 
+def paired_quality(r_warm, r_plain):
+    """Per problem, the warm arm's final MSE against the plain arm's: over the problems
+    finite in both, the shares within 1e-4 relative, lower and higher (with the median
+    ratio of those that differ), and the problems finite in one arm only."""
+    a = r_warm.loss.cpu().numpy().astype(np.float64)
+    b = r_plain.loss.cpu().numpy().astype(np.float64)
+    fa, fb = np.isfinite(a) & (r_warm.iters.cpu().numpy() >= 0), np.isfinite(b) & (r_plain.iters.cpu().numpy() >= 0)
+    both = fa & fb
+    aa, bb = a[both], b[both]
+    same = np.abs(aa - bb) <= 1e-4 * np.maximum(np.abs(bb), 1e-30)
+    lower, higher = (aa < bb) & ~same, (aa > bb) & ~same
+    diff = ~same
+    ratio = np.maximum(aa[diff], 1e-30) / np.maximum(bb[diff], 1e-30)
+    n = max(int(both.sum()), 1)
+    return {"finite_in_both": int(both.sum()), "same_within_1e-4": float(same.sum() / n),
+            "warm_lower": float(lower.sum() / n), "warm_higher": float(higher.sum() / n),
+            "median_ratio_where_different": float(np.median(ratio)) if ratio.size else None,
+            "finite_only_warm": int((fa & ~fb).sum()), "finite_only_plain": int((fb & ~fa).sum())}
+
+
 def fp64_check(r, X, Y, ops, ch, sample=4096):
     """The reported final MSE of a sample of finite problems against an FP64
     evaluation of the same constants (the library's float64 forward kernel): the
@@ -559,6 +579,7 @@ def run_fit(args, rank, world, local):
                              "kernel_ms": tk_plain * 1000.0}
             line["warm_vs_plain"] = (B * world / head_t) / (B * world / t_plain)
             line["fixed_final_mse"] = bool(q_head["median_final_mse"] <= q_plain["median_final_mse"] * 1.0001)
+            line["paired_final_mse"] = paired_quality(head_r, r_plain)
             line["warm_start_training"] = train_info
             line["warm_start_candidates"] = ("per problem the lower initial loss of the plain randn start and the "
                                              "network's start, both measured in one launch of the screening kernel")
