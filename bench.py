@@ -97,16 +97,17 @@ GEMM_REPS = 512  # GEMMs per step of the gemm workload (a step long enough to sa
 # The fit kernel's traffic per problem is set by N, M and the history, not by the
 # operator set, so the warm-start line's held-out problems (same lengths, M and N)
 # scale the same B=4096 ragged capture.
-FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10744832 + 2560),
-                     ("warmstart", 65536, 512): 16 * (10744832 + 2560)}
+FIT_TRAFFIC_BYTES = {("ragged", 16384, 512): 4 * (10738176 + 2048),
+                     ("warmstart", 65536, 512): 16 * (10738176 + 2048)}
 # Pipe and issue utilisation of the fit kernel (percent of peak, active cycles) from the
-# same capture, the kernel of commit 2ddf7f6 (profiles/fit_lbfgs_ragged_B16384_N512.txt):
+# same capture, the kernel of commit a0a780f (profiles/fit_lbfgs_ragged_B16384_N512.txt):
 # an interpreter whose instructions are mostly integer and control work.
-FIT_PROFILE = {"commit": "2ddf7f6", "issue_active_pct": 53.8, "fp32_pipe_pct": 14.7, "xu_pipe_pct": 1.74,
-               "alu_pipe_pct": 48.5, "lsu_pipe_pct": 25.3, "fp64_pipe_pct": 1.68, "warps_active_pct": 23.1,
+FIT_PROFILE = {"commit": "a0a780f", "issue_active_pct": 53.9, "fp32_pipe_pct": 14.9, "xu_pipe_pct": 1.73,
+               "alu_pipe_pct": 48.7, "lsu_pipe_pct": 25.1, "fp64_pipe_pct": 1.68, "warps_active_pct": 23.1,
                "capture": "ncu --set full, ragged B=4096, N=512"}
-# The adjoint call: its three length-class grids (which stage the cached value rows of
-# the real nodes beside the grad_out rows) and the concurrent padding check.
+# The adjoint call: its length-class grids (which stage the cached value rows of the real
+# nodes beside the grad_out rows) and the concurrent padding check, captured with three
+# classes; the split of the longest class at 48 nodes moves the same rows.
 EVAL_TRAFFIC_BYTES = {("eval_forward_kernel", 65536, 1024): 16 * (1611520 + 1012199000),
                       ("eval_backward_kernel", 65536, 1024): 16 * (1364424192 + 13661696)}
 
