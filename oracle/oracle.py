@@ -61,7 +61,9 @@ def lib() -> ctypes.CDLL:
             g.restype = ctypes.c_int
         L.sro_eval_fwd_kf32.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp]
         L.sro_eval_fwd_kf32.restype = None
-        L.sro_eval_bwd_gc_kernel_order_f32.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp, vp]
+        L.sro_eval_bwd_kf32.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, vp]
+        L.sro_eval_bwd_kf32.restype = ctypes.c_int
+        L.sro_eval_bwd_gc_kernel_order_f32.argtypes = [vp, i64, i64, vp, vp, vp, i64, i64, vp, vp, vp, vp, vp, vp]
         L.sro_eval_bwd_gc_kernel_order_f32.restype = ctypes.c_int
         L.sro_optimize_f32.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, i64, ctypes.c_int, ctypes.c_int,
                                        dbl, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
@@ -135,10 +137,16 @@ def eval_fwd(X, ops, ch, C, dtype=np.float32, kernel_math=False):
     return out
 
 
-def eval_gc_kernel_order(X, ops, ch, C, gout):
+def eval_gc_kernel_order(X, ops, ch, C, gout, gx_terms=False):
     """grad_C (B, M) of the evaluation adjoint for a dense output gradient, with the
     kernels' own sin/cos/exp/log and in the device kernel's summation order (per lane
-    over the points l, l + 32, ..., then a 32-lane xor butterfly); returns (gC, err)."""
+    over the points l, l + 32, ..., then a 32-lane xor butterfly); returns (gC, err).
+
+    With gx_terms, returns (gC, err, terms): terms describes, per (point, variable), the
+    nonzero variable-node adjoints that the device adds atomically into grad_X (in no
+    fixed order): "sum" (float64 sum of the finite ones), "abs" (sum of their
+    magnitudes), "count" (all of them) and "flags" (bit 0 NaN, bit 1 +inf, bit 2 -inf
+    among them).  check_gx_bound compares a grad_X against them."""
     X = _c(X, np.float32)
     ops = _c(ops, np.int64)
     ch = _c(ch, np.int64)
@@ -147,12 +155,51 @@ def eval_gc_kernel_order(X, ops, ch, C, gout):
     N, nx = X.shape
     B, M = ops.shape
     gC = np.zeros((B, M), np.float32)
-    err = lib().sro_eval_bwd_gc_kernel_order_f32(_p(X), N, nx, _p(ops), _p(ch), _p(C), B, M, _p(gout), _p(gC))
-    return gC, err
+    if not gx_terms:
+        err = lib().sro_eval_bwd_gc_kernel_order_f32(_p(X), N, nx, _p(ops), _p(ch), _p(C), B, M, _p(gout), _p(gC),
+                                                     None, None, None, None)
+        return gC, err
+    assert B * N * nx <= 1 << 26, "gx_terms keeps per-tape partials: keep B * N * n_x small"
+    t = {"sum": np.zeros((N, nx), np.float64), "abs": np.zeros((N, nx), np.float64),
+         "count": np.zeros((N, nx), np.int32), "flags": np.zeros((N, nx), np.int32)}
+    err = lib().sro_eval_bwd_gc_kernel_order_f32(_p(X), N, nx, _p(ops), _p(ch), _p(C), B, M, _p(gout), _p(gC),
+                                                 _p(t["sum"]), _p(t["abs"]), _p(t["count"]), _p(t["flags"]))
+    return gC, err, t
 
 
-def eval_bwd(X, ops, ch, C, gout, dtype=np.float32, want_gx=True):
-    """Adjoint sweep for a dense (B,M,N) output gradient -> (gC (B,M), gX (N,nx), err)."""
+def check_gx_bound(gx, terms):
+    """Whether a float32 grad_X (N, nx) is a float32 sum, in some order, of the terms that
+    eval_gc_kernel_order(..., gx_terms=True) describes, added to a zeroed buffer.
+
+    Non-finite entries: NaN where a term is NaN or both infinities occur, +inf / -inf
+    where only that infinity occurs.  Finite entries: recursive summation of n terms in
+    any order errs by at most gamma(n - 1) = (n - 1) u / (1 - (n - 1) u) times the sum of
+    their magnitudes (u = 2^-24; Higham, Accuracy and Stability of Numerical Algorithms,
+    2nd ed., section 4.2), plus n 2^-125 for subnormal inputs and partial sums flushed to
+    zero (the device's float atomic add flushes them) and n 2^-53 of the magnitudes for
+    the float64 reference sum.  Returns (ok mask, slack = error / bound)."""
+    gx = np.asarray(gx, np.float32).astype(np.float64)
+    s, a, n, f = terms["sum"], terms["abs"], terms["count"].astype(np.float64), terms["flags"]
+    want_nan = (f & 1).astype(bool) | ((f & 6) == 6)
+    want_pinf = ~want_nan & ((f & 6) == 2)
+    want_ninf = ~want_nan & ((f & 6) == 4)
+    fin = ~(want_nan | want_pinf | want_ninf)
+    u = 2.0 ** -24
+    k = np.maximum(n - 1, 0)
+    bound = k * u / (1 - k * u) * a + n * 2.0 ** -125 + n * 2.0 ** -53 * a
+    err = np.abs(gx - s)
+    ok = np.where(want_nan, np.isnan(gx), False)
+    ok |= want_pinf & (gx == np.inf)
+    ok |= want_ninf & (gx == -np.inf)
+    with np.errstate(invalid="ignore"):
+        ok |= fin & np.isfinite(gx) & (err <= bound)
+        slack = np.where(fin & (bound > 0), err / np.where(bound > 0, bound, 1.0), 0.0)
+    return ok, slack
+
+
+def eval_bwd(X, ops, ch, C, gout, dtype=np.float32, want_gx=True, kernel_math=False):
+    """Adjoint sweep for a dense (B,M,N) output gradient -> (gC (B,M), gX (N,nx), err);
+    kernel_math (float32) takes sin, cos, exp and log from the kernels' own functions."""
     X = _c(X, dtype)
     ops = _c(ops, np.int64)
     ch = _c(ch, np.int64)
@@ -163,6 +210,9 @@ def eval_bwd(X, ops, ch, C, gout, dtype=np.float32, want_gx=True):
     gC = np.zeros((B, M), dtype=dtype)
     gX = np.zeros((N, nx), dtype=dtype) if want_gx else None
     fn = lib().sro_eval_bwd_f32 if dtype == np.float32 else lib().sro_eval_bwd_f64
+    if kernel_math:
+        assert dtype == np.float32
+        fn = lib().sro_eval_bwd_kf32
     err = fn(_p(X), N, nx, _p(ops), _p(ch), _p(C), B, M, _p(gout), _p(gC), _p(gX))
     return gC, gX, err
 

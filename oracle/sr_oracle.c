@@ -277,12 +277,31 @@ static int ladj_f32(int64_t op, float g, float a, float b, float v, int *add0, f
  * adjoints as sro_eval_bwd_kf32 forms them; per constant node, lane l (0..31) sums
  * its nonzero adjoints at the points l, l + 32, l + 64, ... in that order, then the 32
  * lane sums are added by an xor butterfly (offsets 16, 8, 4, 2, 1).  gC (B, M) gets
- * the constant nodes' sums and 0 elsewhere; returns the first error code. */
+ * the constant nodes' sums and 0 elsewhere; returns the first error code.
+ *
+ * The variable gradient is an atomic float sum over tapes and variable nodes on the
+ * device, in no fixed order, so it has no single right answer; what it must satisfy is
+ * the error bound of a float sum of its terms in any order.  When gx_sum is not NULL,
+ * the terms are described per (point, variable), each (N, nx): gx_sum the sum of the
+ * nonzero variable-node adjoints (the device's terms, bit for bit) in double, gx_abs the
+ * sum of their magnitudes, gx_cnt their number, gx_flags bit 0 a NaN term, bit 1 a +inf
+ * term, bit 2 a -inf term (non-finite terms are left out of the sums). */
 int sro_eval_bwd_gc_kernel_order_f32(const float *X, int64_t N, int64_t nx, const int64_t *ops, const int64_t *ch,
-                                     const float *C, int64_t B, int64_t M, const float *gout, float *gC)
+                                     const float *C, int64_t B, int64_t M, const float *gout, float *gC,
+                                     double *gx_sum, double *gx_abs, int32_t *gx_cnt, int32_t *gx_flags)
 {
     int err = 0;
     int *errs = (int *)calloc((size_t)(B > 0 ? B : 1), sizeof(int));
+    const int64_t NX = N * nx;
+    /* per tape, then added over the tapes in order below (the threads own whole tapes) */
+    double *tsum = NULL, *tabs = NULL;
+    int32_t *tcnt = NULL, *tflg = NULL;
+    if (gx_sum) {
+        tsum = (double *)calloc((size_t)(B * NX > 0 ? B * NX : 1), sizeof(double));
+        tabs = (double *)calloc((size_t)(B * NX > 0 ? B * NX : 1), sizeof(double));
+        tcnt = (int32_t *)calloc((size_t)(B * NX > 0 ? B * NX : 1), sizeof(int32_t));
+        tflg = (int32_t *)calloc((size_t)(B * NX > 0 ? B * NX : 1), sizeof(int32_t));
+    }
     _Pragma("omp parallel for schedule(dynamic, 1)")
     for (int64_t b = 0; b < B; ++b) {
         float *val = (float *)malloc(sizeof(float) * (size_t)(M > 0 ? M : 1));
@@ -309,6 +328,17 @@ int sro_eval_bwd_gc_kernel_order_f32(const float *X, int64_t N, int64_t nx, cons
                     if (g != 0.0f) *d = *d + g;
                     continue;
                 }
+                if (op >= OP_VAR0 && op < OP_VAR0 + nx && tsum) {
+                    /* every parent has a larger index: adj[k] is this node's whole adjoint */
+                    const float g = adj[k];
+                    const int64_t i = b * NX + n * nx + (op - OP_VAR0);
+                    if (g != 0.0f) {
+                        if (isnan(g)) tflg[i] |= 1;
+                        else if (isinf(g)) tflg[i] |= g > 0.0f ? 2 : 4;
+                        else { tsum[i] += (double)g; tabs[i] += fabs((double)g); }
+                        tcnt[i] += 1;
+                    }
+                }
                 if (op != OP_NO_OP && arity_of(op) == 0) continue;
                 int a0, a1;
                 float o0, o1;
@@ -330,6 +360,19 @@ int sro_eval_bwd_gc_kernel_order_f32(const float *X, int64_t N, int64_t nx, cons
             gC[b * M + k] = o[k] == OP_LEARNABLE ? v[0] : 0.0f;
         }
         free(val); free(adj); free(lanes);
+    }
+    if (gx_sum) {
+        for (int64_t i = 0; i < NX; ++i) {
+            gx_sum[i] = 0.0; gx_abs[i] = 0.0; gx_cnt[i] = 0; gx_flags[i] = 0;
+        }
+        for (int64_t b = 0; b < B; ++b)
+            for (int64_t i = 0; i < NX; ++i) {
+                gx_sum[i] += tsum[b * NX + i];
+                gx_abs[i] += tabs[b * NX + i];
+                gx_cnt[i] += tcnt[b * NX + i];
+                gx_flags[i] |= tflg[b * NX + i];
+            }
+        free(tsum); free(tabs); free(tcnt); free(tflg);
     }
     for (int64_t b = 0; b < B && !err; ++b) err = errs[b];
     free(errs);
