@@ -111,8 +111,10 @@ __global__ void __launch_bounds__(kThreads) sample_infix_kernel(
       // one symbol of the derivation, leftmost first
       bool restart = false;
       const int sym = stack[(--sp) * kThreads + t];
-      const int r0 = sym < n_symbols ? nt_ptr[sym] : 0;
-      const int r1 = sym < n_symbols ? nt_ptr[sym + 1] : 0;
+      // an id outside [0, n_symbols) has no rules (a terminal): no table read for it
+      const bool has_rules = (unsigned)sym < (unsigned)n_symbols;
+      const int r0 = has_rules ? nt_ptr[sym] : 0;
+      const int r1 = has_rules ? nt_ptr[sym + 1] : 0;
       if (r0 != r1) {  // a non-terminal: choose a rule, push its right-hand side reversed
         const float u = rng.uniform();
         int chosen = -1;

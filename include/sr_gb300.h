@@ -309,8 +309,11 @@ int sr_postfix_to_infix(const int64_t *ops_dev, int64_t B, int64_t M, int32_t n_
  * cumulative per symbol, the last of each symbol 1.0; rhs_ptr (rules + 1) int32 and
  * rhs_concat int32, the right-hand sides.  A seed fixes every expression (a
  * SplitMix64 stream per expression).  err (B) int64: 0, 303 (max_tries exceeded) or
- * 304 (no rule for the drawn number).  max_length <= 128.  Replaces sample_infix
- * (reference src/pcfg.cpp:568-628, src/pcfg_cuda.cu:10-146).
+ * 304 (no rule for the drawn number).  max_length <= 128.  Symbol ids (start_symbol
+ * and every rhs_concat entry) lie in [0, 32768); an id at or above n_symbols is a
+ * terminal.  The tables are read as given: nt_rule_ptr nondecreasing within [0, rules]
+ * and rhs_ptr within rhs_concat, as the grammar object builds them.  Replaces
+ * sample_infix (reference src/pcfg.cpp:568-628, src/pcfg_cuda.cu:10-146).
  */
 int sr_pcfg_sample_infix(const int32_t *nt_rule_ptr, const float *nt_rule_cum_probs, const int32_t *rhs_ptr,
                          const int32_t *rhs_concat, int32_t n_symbols, int32_t start_symbol, int64_t B,

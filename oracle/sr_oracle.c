@@ -1503,8 +1503,9 @@ void sro_pcfg_sample(const int32_t *nt_ptr, const float *cum, const int32_t *rhs
             stack[sp++] = start;
             while (sp > 0) {
                 const int sym = stack[--sp];
-                const int r0 = sym < n_symbols ? nt_ptr[sym] : 0;
-                const int r1 = sym < n_symbols ? nt_ptr[sym + 1] : 0;
+                const int has_rules = (unsigned)sym < (unsigned)n_symbols;
+                const int r0 = has_rules ? nt_ptr[sym] : 0;
+                const int r1 = has_rules ? nt_ptr[sym + 1] : 0;
                 if (r0 != r1) {
                     const float u = sro_uniform(&s);
                     int chosen = -1;
