@@ -526,6 +526,9 @@ def run_fit(args, rank, world, local):
     if not args.no_e2e:
         hX, hY, hO, hCh, hC = (torch.tensor(a).pin_memory() for a in (wl.X, wl.Y, wl.ops, wl.ch, wl.C))
         h2d = sum(t.numel() * t.element_size() for t in (hX, hY, hO, hCh, hC))
+        # the results come back into pinned host buffers, as the inputs go out of them
+        Cf_h = torch.empty(tuple(wl.C.shape), dtype=torch.float32).pin_memory()
+        Yf_h = torch.empty(tuple(wl.Y.shape), dtype=torch.float32).pin_memory()
         e2e_times = []
         for _ in range(max(1, args.steps)):
             flush.fill_(1.0)
@@ -535,7 +538,9 @@ def run_fit(args, rank, world, local):
             if warm:
                 C_ = warmstart.gated_warm_start(net, X_, Y_, O_, Ch_, C_)
             re = sr.optimize_ex(X_, Y_, O_, Ch_, C_, max_iter=max_iter, raise_errors=False)
-            Cf_h, Yf_h = re.C.cpu(), re.Y.cpu()
+            Cf_h.copy_(re.C, non_blocking=True)
+            Yf_h.copy_(re.Y, non_blocking=True)
+            torch.cuda.current_stream(dev).synchronize()
             e2e_times.append(time.perf_counter() - t0)
         d2h = Cf_h.numel() * 4 + Yf_h.numel() * 4
         e2e = {"value": B * world / statistics.median(e2e_times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -730,6 +735,8 @@ def run_eval(args, rank, world, local):
         hCh = torch.tensor(wl.ch).pin_memory()
         hC = torch.tensor(wl.C).pin_memory()
         h2d = sum(t.numel() * t.element_size() for t in (hX, hO, hCh, hC))
+        gC_h = torch.empty(tuple(wl.C.shape), dtype=torch.float32).pin_memory()
+        loss_h = torch.empty((), dtype=torch.float32).pin_memory()
         ts = []
         for _ in range(max(1, args.steps)):
             torch.cuda.synchronize()
@@ -740,7 +747,9 @@ def run_eval(args, rank, world, local):
             rt = (Oh != 0).sum(1) - 1
             loss = out.gather(1, rt.clamp(min=0).view(-1, 1, 1).expand(-1, 1, N)).sum()
             loss.backward()
-            gC_h, loss_h = Ch_.grad.cpu(), loss.detach().cpu()
+            gC_h.copy_(Ch_.grad, non_blocking=True)
+            loss_h.copy_(loss.detach(), non_blocking=True)
+            torch.cuda.current_stream(dev).synchronize()
             ts.append(time.perf_counter() - t0)
             del out, loss
         d2h = gC_h.numel() * 4 + loss_h.numel() * 4
