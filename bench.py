@@ -369,11 +369,25 @@ def fit_quality(r, ref_finite, max_iter, step_s=None):
 def paired_quality(r_warm, r_plain):
     """Per problem, the warm arm's final MSE against the plain arm's: over the problems
     finite in both, the shares within 1e-4 relative, lower and higher (with the median
-    ratio of those that differ), and the problems finite in one arm only."""
+    ratio of those that differ), and the problems finite in one arm only.
+
+    Also the median final MSE of each arm over the problems finite in either arm
+    (non-finite results count as +inf).  The median over the plain arm's finite problems
+    (fit_quality) charges the warm arm +inf for every problem that only the plain start
+    fits and ignores the ones that only the warm start fits; over the union both arms
+    are charged alike."""
     a = r_warm.loss.cpu().numpy().astype(np.float64)
     b = r_plain.loss.cpu().numpy().astype(np.float64)
     fa, fb = np.isfinite(a) & (r_warm.iters.cpu().numpy() >= 0), np.isfinite(b) & (r_plain.iters.cpu().numpy() >= 0)
+    return paired_stats(a, b, fa, fb)
+
+
+def paired_stats(a, b, fa, fb):
+    """paired_quality on arrays: final MSEs a (warm) and b (plain), finite masks fa, fb."""
     both = fa & fb
+    either = fa | fb
+    ua = np.where(fa, a, np.inf)[either]
+    ub = np.where(fb, b, np.inf)[either]
     aa, bb = a[both], b[both]
     same = np.abs(aa - bb) <= 1e-4 * np.maximum(np.abs(bb), 1e-30)
     lower, higher = (aa < bb) & ~same, (aa > bb) & ~same
@@ -383,7 +397,10 @@ def paired_quality(r_warm, r_plain):
     return {"finite_in_both": int(both.sum()), "same_within_1e-4": float(same.sum() / n),
             "warm_lower": float(lower.sum() / n), "warm_higher": float(higher.sum() / n),
             "median_ratio_where_different": float(np.median(ratio)) if ratio.size else None,
-            "finite_only_warm": int((fa & ~fb).sum()), "finite_only_plain": int((fb & ~fa).sum())}
+            "finite_only_warm": int((fa & ~fb).sum()), "finite_only_plain": int((fb & ~fa).sum()),
+            "finite_in_either": int(either.sum()),
+            "median_final_mse_either_finite": {"warm": float(np.median(ua)) if ua.size else None,
+                                               "plain": float(np.median(ub)) if ub.size else None}}
 
 
 def fp64_check(r, X, Y, ops, ch, sample=4096):
@@ -586,6 +603,9 @@ def run_fit(args, rank, world, local):
             line["warm_vs_plain"] = (B * world / head_t) / (B * world / t_plain)
             line["fixed_final_mse"] = bool(q_head["median_final_mse"] <= q_plain["median_final_mse"] * 1.0001)
             line["paired_final_mse"] = paired_quality(head_r, r_plain)
+            med = line["paired_final_mse"]["median_final_mse_either_finite"]
+            line["fixed_final_mse_either_finite"] = bool(med["warm"] is not None and med["plain"] is not None
+                                                         and med["warm"] <= med["plain"] * 1.0001)
             line["warm_start_training"] = train_info
             line["warm_start_candidates"] = ("per problem the lower initial loss of the plain randn start and the "
                                              "network's start, both measured in one launch of the screening kernel")

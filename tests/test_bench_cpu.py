@@ -53,3 +53,19 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def test_paired_statistics_charge_both_arms_alike():
+    """The union median charges +inf to whichever arm leaves a problem non-finite; the
+    plain-conditioned one would charge only the warm arm."""
+    import numpy as np
+    import bench
+    inf = np.inf
+    a = np.array([1.0, 2.0, 3.0, inf, 5.0, 0.5, 0.7])      # warm
+    b = np.array([1.0, 2.5, inf, 4.0, inf, inf, 0.7])      # plain
+    p = bench.paired_stats(a, b, np.isfinite(a), np.isfinite(b))
+    assert p["finite_in_both"] == 3 and p["finite_only_warm"] == 3 and p["finite_only_plain"] == 1
+    assert p["finite_in_either"] == 7
+    assert p["warm_lower"] == 1 / 3 and p["warm_higher"] == 0 and p["same_within_1e-4"] == 2 / 3
+    med = p["median_final_mse_either_finite"]
+    assert med["warm"] == 2.0 and med["plain"] == 4.0
