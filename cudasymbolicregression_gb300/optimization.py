@@ -94,7 +94,7 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
          objective: int = 0, line_search_max_iter: int = 10, eps: float = 1e-10,
          warps_per_block: int = 0, points_per_lane: int = 0, grid_blocks: int = 0,
          order: Optional[torch.Tensor] = None, want_y: bool = True, raise_errors: bool = True,
-         class_width: int = 0, kernel_events=None, autotune: bool = False) -> FitResult:
+         class_width: int = 0, kernel_events=None, autotune: bool = False, consts_floor: int = 0) -> FitResult:
     # the reference's order: unpack Ops' shape (ValueError for another rank), permute C_init
     # and Ops (torch's error for a wrong rank), build the optimizer (line search name),
     # then the evaluation's own checks
@@ -110,6 +110,10 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
     if Y is not None:
         Y = _targets(Y, B, N, dev)
     tapes = compile_tapes(Ops, Ch, nx, live=True)
+    # the constant slots are laid out for the most constants of any tape (at least
+    # consts_floor): 1, 2 or 4 slot registers per lane, which fixes the order of the
+    # direction's sums
+    kmax = max(int(tapes.max_consts), int(consts_floor))
     Xc = X.contiguous()
     if autotune and warps_per_block == 0 and points_per_lane == 0:
         key = (N, nx, tapes.max_root, tapes.max_consts, line_search_fn, objective)
@@ -149,15 +153,15 @@ def _fit(X, Y, Ops, Ch, C_init, max_iter, history_size, tolerance_grad, line_sea
         # one launch per class of tape lengths: the per-warp shared memory is sized
         # for the class, so short tapes run with more resident warps
         max_len = min(max_len, M)
-        wsb = L.sr_fit_workspace_bytes(count, N, M, max_len, tapes.max_consts, opts)
+        wsb = L.sr_fit_workspace_bytes(count, N, M, max_len, kmax, opts)
         if wsb < 0:
             _lib.check(-1, "sr_fit_workspace_bytes")
         ws = torch.empty(int(wsb), dtype=torch.uint8, device=dev)
-        shapes.append((order[start:start + count], *_launch_shape(L, count, N, nx, M, max_len, tapes.max_consts, opts)))
+        shapes.append((order[start:start + count], *_launch_shape(L, count, N, nx, M, max_len, kmax, opts)))
         optr = ctypes.c_void_p(order.data_ptr() + 4 * start)
         rc = L.sr_fit_lbfgs(_lib.ptr(Xc), N, nx, _lib.ptr(Y), _lib.ptr(tapes.desc), _lib.ptr(tapes.meta), count, M,
                             _lib.ptr(Cin), _lib.ptr(C_out), M, 1, _lib.ptr(Y_out), _lib.ptr(iters), _lib.ptr(loss),
-                            _lib.ptr(evals), optr, max_len, tapes.max_consts, opts, _lib.ptr(ws), ws.numel(),
+                            _lib.ptr(evals), optr, max_len, kmax, opts, _lib.ptr(ws), ws.numel(),
                             ctypes.c_void_p(status.data_ptr() + 4 * ci), _lib.stream_ptr(dev))
         _lib.check(rc, "sr_fit_lbfgs")
     if kernel_events is not None:
@@ -213,6 +217,24 @@ def _launch_shape(L, B, N, nx, M, max_len, max_consts, opts):
     return int(shape[0]), int(shape[1])
 
 
+def batch_launch_shape(X: torch.Tensor, Ops: torch.Tensor, Ch: torch.Tensor) -> dict:
+    """What fixes the arithmetic of a fit of this whole batch in one launch, as
+    optimize_ex keywords: the launch shape the library picks for it (points per lane,
+    warps per problem: the order of the sums over the points) and its most constants
+    of any tape (the slot registers per lane: the order of the direction's sums).  A
+    slice of the batch fitted with these keywords gives every problem the bits the
+    whole fit gives it; left to itself, a slice can get another shape (the shape
+    depends on the problem count, the longest tape and the most constants)."""
+    B, M = Ops.shape
+    N, nx = X.shape
+    tapes = compile_tapes(Ops, Ch, nx, live=True)
+    opts = _lib.FitOptions(max_iter=1, history_size=1, tolerance_grad=0.0, line_search=0, line_search_max_iter=0,
+                           eps=0.0, objective=0, max_operators=int(max(tapes.max_operators, 1)),
+                           max_live=int(tapes.max_live))
+    V, W = _launch_shape(_lib.lib(), B, N, nx, M, min(max(tapes.max_root, 1), M), tapes.max_consts, opts)
+    return {"points_per_lane": V, "warps_per_block": W, "consts_floor": int(tapes.max_consts)}
+
+
 def _length_classes(lens: torch.Tensor, order: torch.Tensor, width: int):
     """(start, count, max_len) of each class of tape lengths along ``order``
     (longest first); class c holds lengths in ((c-1)*width, c*width].  One host sync."""
@@ -258,7 +280,8 @@ def optimize_ex(X, Y, Ops, Ch, C_init, max_iter=100, history_size=10, tolerance_
 
     Extra keywords: line_search_max_iter, eps, objective (0 = MSE against Y,
     1 = mean of the root value; Y may be None), warps_per_block, points_per_lane,
-    grid_blocks (kernel shape), order (processing order), want_y, class_width
+    grid_blocks (kernel shape), consts_floor (lay the constant slots out for at least
+    this many constants; see batch_launch_shape), order (processing order), want_y, class_width
     (tapes are fitted in launches per class of lengths this many nodes wide, 0 =
     one launch), raise_errors
     (False: problems whose closures hit error 201/204 are reported through

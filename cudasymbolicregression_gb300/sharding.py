@@ -79,21 +79,53 @@ def gather_rows(part: torch.Tensor, total: int) -> torch.Tensor:
     return torch.cat([o[: b - a] for o, (a, b) in zip(out, spans)], dim=0)
 
 
+def fit_shard(X, Y, Ops, Ch, C_init, start: int, stop: int, fit: Optional[Callable] = None,
+              **kw) -> Tuple[torch.Tensor, torch.Tensor]:
+    """(C_final, Y_final) of problems [start, stop) of the batch, fitted alone.  Y is one
+    row per problem (B, N) or a row that serves every problem.  fit(X, Y, Ops, Ch,
+    C_init, **kw) -> (C_final, Y_final) is any fit whose result for a problem does not
+    depend on the rest of the batch.  By default it is this package's optimize, run with
+    the whole batch's launch shape and constant-slot layout (batch_launch_shape), which
+    fix the order of its sums: each problem then gets the bits the whole fit gives it."""
+    B = Ops.shape[0]
+    Ys = Y[start:stop] if (Y is not None and Y.dim() == 2 and Y.shape[0] == B and B > 1) else Y
+    if fit is None:
+        from .optimization import batch_launch_shape, optimize_ex
+        pin = batch_launch_shape(X, Ops, Ch)
+        r = optimize_ex(X, Ys, Ops[start:stop], Ch[start:stop], C_init[start:stop], **kw, **pin)
+        return r.C, r.Y
+    return fit(X, Ys, Ops[start:stop], Ch[start:stop], C_init[start:stop], **kw)
+
+
 def fit_sharded(X, Y, Ops, Ch, C_init, fit: Optional[Callable] = None, **kw) -> Tuple[torch.Tensor, torch.Tensor]:
     """``optimize`` of one batch on every rank of the process group: rank r fits the
-    contiguous share shard_range(B, r, world) of the problems with X (and a target row
-    that serves every problem) replicated, then C_final (B, M) and Y_final (B, N) are
-    gathered on every rank in batch order.  The only collective is that gather: the
-    problems are independent, so the result equals the unsharded fit's.  fit(X, Y, Ops,
-    Ch, C_init, **kw) -> (C_final, Y_final) defaults to this package's ``optimize``.
+    contiguous share shard_range(B, r, world) of the problems (fit_shard) with X (and a
+    target row that serves every problem) replicated, then C_final (B, M) and Y_final
+    (B, N) are gathered on every rank in batch order.  The problems are independent and
+    every shard is fitted with the whole batch's launch shape, so the result equals the
+    unsharded fit's bit for bit.  A fit that raises on any rank raises on every rank
+    (the others learn of it in an all_gather of the error, before the gather of the
+    results, so no rank waits for a share that will not come).  fit(X, Y, Ops, Ch,
+    C_init, **kw) -> (C_final, Y_final) defaults to this package's ``optimize``.
     Without an initialised process group it is one plain fit."""
     import torch.distributed as dist
-    if fit is None:
-        from .optimization import optimize as fit
     B = Ops.shape[0]
     if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        if fit is None:
+            from .optimization import optimize as fit
         return fit(X, Y, Ops, Ch, C_init, **kw)
-    start, stop = shard_range(B, dist.get_rank(), dist.get_world_size())
-    Ys = Y[start:stop] if (Y is not None and Y.dim() == 2 and Y.shape[0] == B and B > 1) else Y
-    C_part, Y_part = fit(X, Ys, Ops[start:stop], Ch[start:stop], C_init[start:stop], **kw)
+    rank, world = dist.get_rank(), dist.get_world_size()
+    start, stop = shard_range(B, rank, world)
+    failure = None
+    try:
+        C_part, Y_part = fit_shard(X, Y, Ops, Ch, C_init, start, stop, fit=fit, **kw)
+    except Exception as e:  # reported to every rank below, then raised here
+        failure = e
+    errors = [None] * world
+    dist.all_gather_object(errors, None if failure is None else f"{type(failure).__name__}: {failure}")
+    if failure is not None:
+        raise failure
+    failed = [(r, e) for r, e in enumerate(errors) if e is not None]
+    if failed:
+        raise RuntimeError(f"the fit failed on rank {failed[0][0]}: {failed[0][1]}")
     return gather_rows(C_part, B), gather_rows(Y_part, B)

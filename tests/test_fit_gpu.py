@@ -565,3 +565,47 @@ def test_live_adjoint_rows_and_their_limit():
     assert (short[2][over] == -_lib.TAPE_EXCEEDS_LAUNCH).all()
     for a, b in zip(short[:5], counted[:5]):
         np.testing.assert_array_equal(np.nan_to_num(a[~over], nan=7.0), np.nan_to_num(b[~over], nan=7.0))
+
+
+def test_shards_fitted_with_the_batch_launch_shape_equal_the_whole_fit():
+    """sharding.fit_shard, the per-rank part of fit_sharded: each slice of a batch fitted
+    alone with the whole batch's launch shape and constant-slot layout gives every
+    problem the bits of the whole fit (constants, root values, loss, iterations).  The
+    batch is chosen so that a slice left to itself gets another shape: 1200 problems
+    at N = 200 run 4 warps each, 600 would run 8, and only the first half has a tape
+    with 40 constants (two slot registers per lane)."""
+    from cudasymbolicregression_gb300 import sharding, tapes
+    from cudasymbolicregression_gb300.operators import Operator as Op
+    sr = _sr()
+    rng = np.random.default_rng(71)
+    B, M, N = 1200, 96, 200
+    exact_bin = (int(Op.ADD), int(Op.SUB), int(Op.MUL), int(Op.DIV))
+    X = rng.uniform(-3, 3, (N, 2)).astype(np.float32)
+    C = rng.standard_normal((B, M)).astype(np.float32)
+    consts = rng.integers(0, 5, size=B)
+    lens = rng.integers(3, 40, size=B)
+    consts[7], lens[7] = 40, 96
+    tb = tapes.generate(B, M, seed=72, lengths=lens, const_counts=consts, n_vars=2, binary=exact_bin,
+                        unary=(int(Op.SQUARE), int(Op.NEG)), X_screen=X, C_screen=C)
+    Y = (np.sin(X[:, 0]) * X[:, 1]).astype(np.float32)[None, :] + 0.1 * rng.standard_normal((B, N)).astype(np.float32)
+    Xd, Yd, Od, Chd, Cd = (cuda(a) for a in (X, Y, tb.ops, tb.ch, C))
+    kw = dict(max_iter=60, raise_errors=False)
+    whole = sr.optimize_ex(Xd, Yd, Od, Chd, Cd, **kw)
+    pin = sr.optimization.batch_launch_shape(Xd, Od, Chd)
+    assert pin["warps_per_block"] == 4 and pin["consts_floor"] >= 32
+    parts, alone = [], []
+    for start, stop in (sharding.shard_range(B, r, 2) for r in range(2)):
+        parts.append(sharding.fit_shard(Xd, Yd, Od, Chd, Cd, start, stop, **kw))
+        alone.append(sr.optimize_ex(Xd, Yd[start:stop], Od[start:stop], Chd[start:stop], Cd[start:stop], **kw))
+    Cs = torch.cat([p[0] for p in parts]).cpu().numpy()
+    Ys = torch.cat([p[1] for p in parts]).cpu().numpy()
+
+    def bits(a):
+        a = np.ascontiguousarray(a, np.float32)
+        return np.where(np.isnan(a), np.uint32(0x7fc00000), a.view(np.uint32))
+    assert np.array_equal(bits(Cs), bits(whole.C.cpu().numpy()))
+    assert np.array_equal(bits(Ys), bits(whole.Y.cpu().numpy()))
+    # left to itself the second half runs 8 warps per problem and one slot register
+    assert alone[1].shapes[0][2] == 8 and whole.shapes[0][2] == 4
+    C_alone = torch.cat([a.C for a in alone]).cpu().numpy()
+    assert not np.array_equal(bits(C_alone), bits(whole.C.cpu().numpy()))

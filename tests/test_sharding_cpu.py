@@ -136,3 +136,45 @@ def test_sharded_fit_equals_the_whole_batch_fit():
     # without a process group it is one plain fit
     Cs, Ys = sharding.fit_sharded(X, Y, O, Ch, C, fit=_oracle_fit)
     assert torch.equal(torch.nan_to_num(Cs, nan=7.0), torch.nan_to_num(Cw, nan=7.0))
+
+
+def _failing_fit(X, Y, Ops, Ch, C_init):
+    """A fit that raises on the second rank's share (18 problems) only."""
+    if Ops.shape[0] == 18:
+        raise RuntimeError("Error during symbolic evaluation backward pass: planted on this share")
+    return _oracle_fit(X, Y, Ops, Ch, C_init, max_iter=2)
+
+
+def _failing_worker(rank, world, port, results):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        X, Y, O, Ch, C = _fit_batch()
+        try:
+            sharding.fit_sharded(X, Y, O, Ch, C, fit=_failing_fit)
+            results[rank] = "returned"
+        except RuntimeError as e:
+            results[rank] = str(e)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_fit_raises_on_every_rank_when_one_share_fails():
+    """A share whose fit raises (the failure made on the host, in the fit function)
+    makes fit_sharded raise on every rank, the failing rank with its own exception and
+    the other with the failing rank's message, instead of leaving it waiting in the
+    gather for a share that never comes."""
+    ctx = mp.get_context("spawn")
+    manager = ctx.Manager()
+    results = manager.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_failing_worker, args=(r, 2, port, results)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=180)
+        assert p.exitcode == 0
+    assert results[1] == "Error during symbolic evaluation backward pass: planted on this share"
+    assert results[0].startswith("the fit failed on rank 1: RuntimeError: Error during symbolic evaluation")
