@@ -232,7 +232,12 @@ int sr_fit_launch_shape(int64_t B, int64_t N, int64_t n_x, int64_t M, int32_t ma
  * problem is not fitted (C_out = C_init, Y_final and loss NaN).
  * order_dev (B) int32 gives the processing order (NULL = 0..B-1).
  * max_len: largest root + 1 (stats[2] of sr_tape_compile; 0 = M); max_consts:
- * largest meta[2] (stats[3]).  workspace_dev must hold sr_fit_workspace_bytes(...)
+ * largest meta[2] (stats[3]) or more.  max_consts also sets the constant-slot layout
+ * (1, 2 or 4 slot registers per lane for up to 31, 63 or 127 constants), which with
+ * the launch shape fixes the order of the direction's sums: slices of one batch
+ * fitted separately give each problem the bits of the whole fit when each gets the
+ * whole batch's max_consts and, through opt, its warps and points per lane
+ * (sr_fit_launch_shape).  workspace_dev must hold sr_fit_workspace_bytes(...)
  * bytes; it is initialised by the call.
  */
 int sr_fit_lbfgs(const float *X_dev, int64_t N, int64_t n_x, const float *Y_dev,
