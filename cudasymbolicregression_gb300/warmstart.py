@@ -9,11 +9,17 @@ and predicts the first ``N_OUT`` learnable constants of the tape (row-major orde
     x0 --W1,b1,ReLU--> h1 (256) --W2,b2,ReLU--> h2 --W3,b3,ReLU--> h3 --W4,b4--> out (8, padded to 64)
 
 Weights and activations are bf16, every GEMM accumulates in fp32 on the tensor
-cores (``sr_mlp_gemm``), master weights and Adam moments are fp32.  Training
-minimises the squared error against the constants that ``optimize`` itself found,
-on the problems it fitted well.  ``warm_start_constants`` puts the predictions in
-the first learnable slots of C and keeps the plain ``create_constants``-style draw
-everywhere else, so the plain initialisation stays the fallback.
+cores (``sr_mlp_gemm``), master weights and Adam moments are fp32.  Training runs in
+two stages: ``train`` minimises the squared error against the constants that
+``optimize`` itself found, on the problems it fitted well; ``train_fit_objective``
+then back-propagates the fit's own objective (the normalised MSE of each expression at
+the predicted constants, through the library's forward and adjoint kernels) into the
+network.  ``warm_start_constants`` puts the predictions in the first learnable slots of
+C and keeps the plain ``create_constants``-style draw everywhere else;
+``gated_warm_start`` (``candidate_starts`` + ``screened_start``) scores that start and
+the plain one in one launch of the screening kernel and keeps, per problem, the one
+with the lower initial loss (the plain start on ties), so the plain initialisation
+stays the fallback and the judge.
 
 There is no counterpart in the reference; everything here runs on the library's
 own kernels (declared in include/sr_gb300.h).
