@@ -178,3 +178,20 @@ def test_sharded_fit_raises_on_every_rank_when_one_share_fails():
         assert p.exitcode == 0
     assert results[1] == "Error during symbolic evaluation backward pass: planted on this share"
     assert results[0].startswith("the fit failed on rank 1: RuntimeError: Error during symbolic evaluation")
+
+
+def test_fit_shard_slices_per_problem_targets_only():
+    """fit_shard hands the fit the shard's rows of Ops, Ch, C_init and of a per-problem
+    Y (B, N); a target row that serves every problem ((N,) or (1, N)) goes unchanged."""
+    seen = []
+
+    def fit(X, Y, Ops, Ch, C_init, **kw):
+        seen.append((tuple(Y.shape), tuple(Ops.shape), tuple(Ch.shape), tuple(C_init.shape), kw))
+        return C_init.clone(), torch.zeros(Ops.shape[0], X.shape[0])
+    B, M, N = 10, 6, 4
+    X = torch.zeros(N, 1)
+    Ops, Ch, C = torch.zeros(B, M, dtype=torch.int64), torch.zeros(B, M, 2, dtype=torch.int64), torch.randn(B, M)
+    for Y, want in ((torch.randn(B, N), (3, N)), (torch.randn(1, N), (1, N)), (torch.randn(N), (N,))):
+        Cp, Yp = sharding.fit_shard(X, Y, Ops, Ch, C, 4, 7, fit=fit, max_iter=5)
+        assert seen[-1] == (want, (3, M), (3, M, 2), (3, M), {"max_iter": 5})
+        assert torch.equal(Cp, C[4:7]) and tuple(Yp.shape) == (3, N)
